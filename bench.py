@@ -1,0 +1,435 @@
+"""Benchmark: pressure-correction PCG solves/s on GB300 (one JSON line).
+
+Workload (one "step"): one Jacobi-PCG solve of the pressure-correction (p')
+system of a jittered mixed triangle/quad mesh of the unit square,
+1672 x 1672 quads of which a seeded half are split (4,19x,xxx cells), nodes
+jittered by uniform +-20% of the edge (seed 1234), RCM-ordered, assembled
+on the GPU (CellibPressure.f coefficients, one cell pinned), stored CSRD
+(the reference's matriz 1), RHS uniform[-1,1] (seed 42), x0 = 0, solved to
+||b - A x||2 / ||b||2 <= 1e-8 (recomputed in FP64).
+
+value   solves/s of the mixed-precision path (FP32 CG inside FP64 defect
+        correction), inputs resident in HBM, CUDA events on the solve stream.
+e2e     the same solve through the public host API (solver(), the
+        reference's argument list) with pinned host arrays: matrix values,
+        b and x copied in and x copied out inside the timed region.
+Also reported: the plain FP64 persistent PCG (same stopping rule) solves/s,
+the FP64 SpMV GB/s, and the CPU restatement of the reference's OpenMP PCG
+(pcg_omp + matvec_csrd_omp + dot_ompL4) timed on this host's cores.
+
+--impl reference times only that CPU restatement (the reference is Fortran
+and cannot be built here), on the same workload and metric.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+TOL = 1e-8
+NX_DEFAULT = 1672
+L2_BYTES = 129 * 1024 * 1024
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.samples = []
+        self._stop = threading.Event()
+        self._proc = None
+
+    def start(self):
+        try:
+            self._proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self._proc = None
+            return
+        self._t = threading.Thread(target=self._read, daemon=True)
+        self._t.start()
+
+    def _read(self):
+        for line in self._proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.samples.append(parts)
+            if self._stop.is_set():
+                break
+
+    def stop(self) -> dict:
+        self._stop.set()
+        if self._proc:
+            self._proc.terminate()
+            try:
+                self._proc.wait(timeout=5)
+            except Exception:
+                self._proc.kill()
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        smax = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4)
+                          if s[5 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": reasons,
+                "samples": len(self.samples)}
+
+
+def build_mesh(nx: int):
+    from fortranfvcell_gb300 import mesh
+    return mesh.square_mesh(nx, kind="mixed", jitter=0.2, seed=1234)
+
+
+def build_system_gpu(nx: int):
+    """Product setup chain: host C++ graph tools + GPU assembly."""
+    from fortranfvcell_gb300 import mesh
+    t0 = time.time()
+    m = build_mesh(nx)
+    s = mesh.pressure_system(m, matriz=1, unsym=True, pin_cell=1)
+    b = np.random.default_rng(42).uniform(-1.0, 1.0, s.neq)
+    log(f"setup: {s.neq} cells, nad {s.nad}, {time.time() - t0:.1f} s")
+    return s, b
+
+
+def pcg_bytes_fp64(n, nnz):
+    # SpMV (12 B per true off-diagonal + 24 B per row) + 11 vector streams
+    return 12 * nnz + 24 * n + 11 * 8 * n
+
+
+def cg_bytes_fp32(n, nnz):
+    # FP32 inner CG on the Jacobi-scaled matrix (unit diagonal implicit):
+    # SpMV 8 B per off-diagonal + p read + q write; update pass reads
+    # e, p, r, q and writes e, r; direction pass reads r, p, writes p
+    return 8 * nnz + 8 * n + 24 * n + 12 * n
+
+
+def refine_bytes(n, nnz):
+    # FP64 residual sweep (SpMV + b read + scaled residual write) and the
+    # FP64 correction pass (x, D^-1/2, e read; x written)
+    return 12 * nnz + 24 * n + 8 * n + 4 * n + 28 * n
+
+
+def cpu_sample(s, b, its_per_solve, target_s=10.0, threads=None):
+    """The CPU restatement of the reference's OpenMP PCG on this host."""
+    from oracle import oracle
+    threads = threads or os.cpu_count() or 1
+    n = s.neq
+    x = np.zeros(n)
+    # calibrate on a few iterations, then one bounded sample of ~target_s
+    t0 = time.perf_counter()
+    oracle.pcg_omp_sample(s.ad, s.au, x, b.copy(), s.ia, s.ja, n, s.nad, 1e-30, 5, 1, threads)
+    dt = (time.perf_counter() - t0) / 5
+    iters = int(max(10, min(20000, target_s / max(dt, 1e-6))))
+    x[:] = 0
+    t0 = time.perf_counter()
+    oracle.pcg_omp_sample(s.ad, s.au, x, b.copy(), s.ia, s.ja, n, s.nad, 1e-30, iters, 1,
+                          threads)
+    el = time.perf_counter() - t0
+    per_it = el / iters
+    return {"value": 1.0 / (per_it * its_per_solve), "unit": "solves/s", "cores": threads,
+            "kind": "port",
+            "sample": f"{iters} pcg_omp iterations (matvec_csrd_omp, dot_ompL4) on the full "
+                      f"{n}-row system in {el:.1f} s; solves/s = 1/(s per iteration x "
+                      f"{its_per_solve} iterations per solve)",
+            "s_per_iteration": per_it}
+
+
+def run_ours(args):
+    import torch
+    import fortranfvcell_gb300 as fvc
+    from fortranfvcell_gb300 import Context, make_opts
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    s, b = build_system_gpu(args.nx)
+    n = s.neq
+    stream = torch.cuda.Stream()
+    ctx = Context(device=local, stream=stream)
+    ctx.set_matrix(1, True, n, s.nad, s.ad, s.au, s.au, s.ia, s.ja)
+    info = ctx.info()
+    nnz = info["nnz_off"]
+    bd = torch.from_numpy(b).cuda()
+    xd = torch.zeros(n, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    o_mixed = make_opts("mixed", init=1, refine_tol=TOL, inner_tol=args.inner_tol)
+    o_fp64 = make_opts("fp64", init=1, stop_rule=1)
+
+    def solve(opts, which):
+        with torch.cuda.stream(stream):
+            st = ctx.solve(1, bd, xd, TOL, 200000, opts)
+        return st
+
+    # warm-up
+    for _ in range(args.warmup):
+        st_m = solve(o_mixed, "mixed")
+    A_rel = None
+
+    def true_rel():
+        x = xd.cpu().numpy()
+        import scipy.sparse as sp
+        r = np.repeat(np.arange(n), np.diff(s.ia))
+        A = sp.csr_matrix((s.au, (r, s.ja - 1)), shape=(n, n)) + sp.diags(s.ad)
+        return float(np.linalg.norm(b - A @ x) / np.linalg.norm(b))
+
+    # timed region: mixed precision (the headline)
+    launches0 = fvc.kernel_launches()
+    clk = ClockSampler(local)
+    clk.start()
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    stats = []
+    for _ in range(args.steps):
+        stats.append(solve(o_mixed, "mixed"))
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    clocks = clk.stop()
+    launches = fvc.kernel_launches() - launches0
+    ms_total = ev0.elapsed_time(ev1)
+    if ws > 1:
+        t = torch.tensor([ms_total], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_total = float(t.item())
+    ms_step = ms_total / args.steps
+    rel_mixed = true_rel()
+    st = stats[-1]
+    kernel_ms = statistics.mean(x.solve_ms for x in stats)
+    inner = st.inner_iterations
+    sweeps = st.refinements
+    alg_bytes = inner * cg_bytes_fp32(n, nnz) + (sweeps + 1) * refine_bytes(n, nnz)
+    hbm, peak_kind = peaks()
+    achieved = alg_bytes / (kernel_ms * 1e-3) / 1e9
+
+    # plain FP64 persistent PCG, same stopping rule
+    st64 = solve(o_fp64, "fp64")
+    rel64 = true_rel()
+    t64 = [solve(o_fp64, "fp64").solve_ms for _ in range(max(1, min(2, args.steps)))]
+    ms64 = statistics.mean(t64)
+    fp64_bytes = st64.iterations * pcg_bytes_fp64(n, nnz)
+
+    # FP64 SpMV GB/s (reference summation order, bit-identical to Matvec.f)
+    y = torch.empty_like(bd)
+    for _ in range(3):
+        ctx.spmv(bd, y)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    reps = 20
+    e0.record(stream)
+    for _ in range(reps):
+        ctx.spmv(bd, y)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    spmv_ms = e0.elapsed_time(e1) / reps
+    spmv_bytes = 12 * nnz + 24 * n
+    spmv_gbs = spmv_bytes / (spmv_ms * 1e-3) / 1e9
+
+    # end to end through the public host API, pinned host arrays
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+    h_ad, h_au, h_b = pin(s.ad), pin(s.au), pin(b)
+    h_ia, h_ja = pin(s.ia), pin(s.ja)
+    h_x = pin(np.zeros(n))
+    o_e2e = make_opts("mixed", init=1, refine_tol=TOL, inner_tol=args.inner_tol)
+    fvc.solver(h_ad, h_au, h_au, h_x, h_b, h_ia, h_ja, n, s.nad, True, TOL, 200000, 1, 1,
+               opts=o_e2e)  # structure upload (cached afterwards)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e2e_steps = max(1, min(3, args.steps))
+    for _ in range(e2e_steps):
+        h_x[:] = 0.0
+        fvc.solver(h_ad, h_au, h_au, h_x, h_b, h_ia, h_ja, n, s.nad, True, TOL, 200000, 1, 1,
+                   opts=o_e2e)
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    h2d = h_ad.nbytes + h_au.nbytes + h_b.nbytes + h_x.nbytes
+    d2h = h_x.nbytes
+
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    if rank != 0:
+        return None
+    cpu = None
+    if not args.no_cpu:
+        cpu = cpu_sample(s, b, st64.iterations, target_s=args.cpu_seconds)
+    value = ws * 1000.0 / ms_step
+    line = {
+        "metric": "PCG solves/s to ||b-Ax||/||b||<=1e-8, p' system, mixed FP32/FP64 "
+                  "(plain FP64 and SpMV GB/s alongside)",
+        "value": round(value, 4),
+        "unit": "solves/s",
+        "n_gpus": ws,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(ms_step, 3),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "fp32-inner/f64-refine",
+        "data": "synthetic",
+        "config": {"workload": f"p' Jacobi-PCG, jittered mixed tri/quad unit square, {n} cells "
+                               f"(nx={args.nx}), RCM, CSRD -> SELL-32, b~U[-1,1] seed 42, x0=0",
+                   "cells": n, "nnz_off": nnz, "tol_rel_residual": TOL,
+                   "l2": "inputs larger than L2 (working set > 129 MB), no flush",
+                   "parallelism": f"replicas x{ws}"},
+        "solve": {"mixed": {"solves_per_s": round(1000.0 / ms_step, 4),
+                            "inner_iterations": inner, "refinements": sweeps,
+                            "rel_residual_fp64": rel_mixed, "kernel_ms": round(kernel_ms, 3)},
+                  "fp64": {"solves_per_s": round(1000.0 / ms64, 4),
+                           "iterations": st64.iterations, "rel_residual_fp64": rel64,
+                           "kernel_ms": round(ms64, 3),
+                           "gbs": round(fp64_bytes / (ms64 * 1e-3) / 1e9, 1)},
+                  "mixed_over_fp64": round(ms64 / ms_step, 3)},
+        "spmv": {"gbs": round(spmv_gbs, 1), "ms": round(spmv_ms, 4), "bytes": spmv_bytes,
+                 "frac_of_peak": round(spmv_gbs / hbm, 3)},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm,
+                     "unit": "GB/s", "frac": round(achieved / hbm, 3), "traffic": None,
+                     "kernel": "mixed_cg (persistent, one launch per solve)",
+                     "peak_kind": peak_kind,
+                     "alg_bytes_per_launch": int(alg_bytes)},
+        "e2e": {"value": round(1.0 / e2e_s, 4), "unit": "solves/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": int(launches),
+        "clocks": clocks,
+        "cpu_baseline": cpu,
+    }
+    return line
+
+
+def run_reference(args):
+    """The CPU restatement of the reference's OpenMP path (pcg_omp with
+    matvec_csrd_omp and dot_ompL4), all host threads, same workload."""
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return None
+    from oracle import oracle
+    t0 = time.time()
+    m = build_mesh(args.nx)
+    nelcon = oracle.adjacency_mixed(m.ix, m.nnode, m.nshared)
+    num = oracle.reord(nelcon)
+    ident = oracle.numeq(num, nelcon)
+    ia, ja, nad = oracle.datastruc(ident, 1, True)
+    ad, au = oracle.pform_pressure(m.coor, m.ix, m.nshared, nelcon, num, ia, ja, 1, True,
+                                   pin_cell=1)
+    n = m.numel
+    b = np.random.default_rng(42).uniform(-1.0, 1.0, n)
+    log(f"reference setup {time.time() - t0:.1f} s")
+    threads = os.cpu_count() or 1
+    # iterations to the 1e-8 true relative residual: the reference's test
+    # sqrt(r.M^-1 r) < tol sqrt(r0.M^-1 r0) is tightened until the FP64
+    # residual meets 1e-8 on a one-off full solve (cached per size)
+    cache = os.path.join(ROOT, "_work", f"ref_its_{args.nx}.json")
+    its = None
+    if os.path.exists(cache):
+        its = json.load(open(cache)).get("its")
+    if its is None:
+        import scipy.sparse as sp
+        r = np.repeat(np.arange(n), np.diff(ia))
+        A = sp.csr_matrix((au, (r, ja - 1)), shape=(n, n)) + sp.diags(ad)
+        tol = TOL
+        for _ in range(4):
+            x = np.zeros(n)
+            st, so = oracle.pcg_omp_sample(ad, au, x, b.copy(), ia, ja, n, nad, tol, 200000, 1,
+                                           threads)
+            rel = np.linalg.norm(b - A @ x) / np.linalg.norm(b)
+            its = so.iterations
+            if rel <= TOL:
+                break
+            tol *= 0.1
+        os.makedirs(os.path.dirname(cache), exist_ok=True)
+        json.dump({"its": its}, open(cache, "w"))
+    sample_its = args.ref_sample_its
+    times = []
+    for k in range(args.warmup + args.steps):
+        x = np.zeros(n)
+        t1 = time.perf_counter()
+        oracle.pcg_omp_sample(ad, au, x, b.copy(), ia, ja, n, nad, 1e-30, sample_its, 1, threads)
+        dt = time.perf_counter() - t1
+        if k >= args.warmup:
+            times.append(dt)
+    per_it = statistics.mean(times) / sample_its
+    value = 1.0 / (per_it * its)
+    return {
+        "metric": "PCG solves/s to ||b-Ax||/||b||<=1e-8, p' system, mixed FP32/FP64 "
+                  "(plain FP64 and SpMV GB/s alongside)",
+        "value": round(value, 6), "unit": "solves/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(statistics.mean(times) * 1e3, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "impl": "reference",
+        "config": {"workload": f"p' Jacobi-PCG, jittered mixed tri/quad unit square, {n} cells "
+                               f"(nx={args.nx}), RCM, CSRD, b~U[-1,1] seed 42, x0=0",
+                   "cells": n, "tol_rel_residual": TOL},
+        "cpu_baseline": {"value": round(value, 6), "unit": "solves/s", "cores": threads,
+                         "kind": "port",
+                         "sample": f"{sample_its} pcg_omp iterations per step; "
+                                   f"{its} iterations per solve"},
+        "e2e": {"value": round(value, 6), "unit": "solves/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--nx", type=int, default=NX_DEFAULT)
+    ap.add_argument("--inner-tol", type=float, default=0.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--ref-sample-its", type=int, default=300)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        log("note: the timing rules want >= 3 warm-up steps")
+    line = run_reference(args) if args.impl == "reference" else run_ours(args)
+    if line is not None:
+        print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,679 @@
+// fvc_api.cpp -- C ABI of libfvcgpu: the drop-in `solver` entry, contexts,
+// and the conversion from the reference's matrix layouts to SELL-32.
+//
+// Layout conversion keeps each row's terms in the order the reference's
+// src/Matvec.f routine adds them, so the device SpMV reproduces its sums:
+//   matriz 1 unsym (CSRD, values au)   row terms in ja order, diag first
+//   matriz 1 sym   (CSRD lower, al)    lower terms, then the transposed
+//                                      terms of later rows in row order,
+//                                      diag first (matvec_csrd_sym adds
+//                                      them in exactly that order)
+//   matriz 2       (CSR, values ad)    ja order, diagonal inside, t = 0 start
+//   matriz 3       (CSRC al/au)        as matriz 1 sym with au for the
+//                                      transposed terms (matvec_csrc)
+//   matriz 4       (ELLPACK, au)       the w slots incl. pads, diag last
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/fvcgpu.h"
+#include "fvc_internal.h"
+
+namespace fvc {
+
+static std::atomic<int64_t> g_launches{0};
+void count_launch(int64_t k) { g_launches += k; }
+
+// gather kernel (defined in fvc_gather.cu)
+int32_t launch_gather_values(int64_t slots, const int32_t *src, const double *a1,
+                             const double *a2, double *val, cudaStream_t stream);
+
+}  // namespace fvc
+
+using fvc::DeviceMatrix;
+using fvc::Scratch;
+
+struct fvc_context {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  DeviceMatrix A;
+  Scratch S;
+  // structure description
+  int matriz = 0, unsym = 0, neq = 0, nad = 0;
+  bool has_matrix = false;
+  int32_t *d_src = nullptr;      // slot -> source index code (see encode)
+  double *d_raw1 = nullptr, *d_raw2 = nullptr;  // raw uploaded value arrays
+  size_t raw1_n = 0, raw2_n = 0;
+  int raw1_which = 0, raw2_which = 0;  // 1 ad, 2 au, 3 al
+  std::vector<int32_t> jac_slot;  // matriz 2: slot holding each diagonal
+  int32_t *d_jac_src = nullptr;
+  // host-array solve buffers
+  double *d_b = nullptr, *d_x = nullptr;
+  size_t nvec = 0;
+  // drop-in structure cache key
+  const void *key_iax = nullptr, *key_ja = nullptr;
+  uint64_t key_hash = 0;
+};
+
+namespace {
+
+void free_matrix(fvc_context *c) {
+  DeviceMatrix &A = c->A;
+  cudaFree(A.sptr);
+  cudaFree(A.col);
+  cudaFree(A.val);
+  cudaFree(A.diag);
+  cudaFree(A.jac);
+  cudaFree(A.val32);
+  cudaFree(A.diag32);
+  cudaFree(A.dscale);
+  cudaFree(c->d_src);
+  cudaFree(c->d_raw1);
+  cudaFree(c->d_raw2);
+  cudaFree(c->d_jac_src);
+  A = DeviceMatrix();
+  c->d_src = nullptr;
+  c->d_raw1 = c->d_raw2 = nullptr;
+  c->raw1_n = c->raw2_n = 0;
+  c->d_jac_src = nullptr;
+  c->has_matrix = false;
+}
+
+// Source-slot code: >= 0 index into raw array 1; -1 padding (value 0);
+// <= -2 index (-code-2) into raw array 2.
+struct Entry {
+  int32_t col;  // 0-based
+  int32_t src;
+};
+
+struct RowLists {
+  std::vector<int64_t> start;  // n+1
+  std::vector<Entry> e;
+};
+
+// Build the per-row term lists in reference order.  raw1/raw2 name the
+// host arrays the codes index (1 ad, 2 au, 3 al).
+int32_t build_rows(int matriz, int unsym, int n, int nad, const int32_t *ia, const int32_t *ja,
+                   RowLists &R, int &diag_mode, int &raw1, int &raw2, std::vector<int32_t> &jac_slot) {
+  R.start.assign((size_t)n + 1, 0);
+  R.e.clear();
+  raw1 = raw2 = 0;
+  jac_slot.clear();
+  if (matriz == 4) {
+    const int w = ia[0];
+    if (w < 1 || w > 64 || ia[1] != n + 1) return FVC_ERR_ARG;
+    R.e.resize((size_t)n * w);
+    for (int i = 0; i < n; ++i) {
+      R.start[i + 1] = R.start[i] + w;
+      for (int j = 0; j < w; ++j) {
+        int32_t c = ja[(size_t)i * w + j];
+        if (c < 1 || c > n) return FVC_ERR_ARG;
+        R.e[(size_t)i * w + j] = {c - 1, (int32_t)((size_t)i * w + j)};
+      }
+    }
+    diag_mode = fvc::DIAG_LAST;
+    raw1 = 2;  // au
+    return FVC_OK;
+  }
+  if (ia[0] != 1 || ia[n] - 1 != nad) return FVC_ERR_ARG;
+  for (int64_t k = 0; k < nad; ++k)
+    if (ja[k] < 1 || ja[k] > n) return FVC_ERR_ARG;
+  const bool expand = (matriz == 3) || (matriz == 1 && !unsym);
+  if (!expand) {
+    R.e.resize((size_t)nad);
+    for (int i = 0; i < n; ++i) {
+      R.start[i + 1] = ia[i + 1] - 1;
+      for (int64_t k = ia[i] - 1; k < ia[i + 1] - 1; ++k) R.e[k] = {ja[k] - 1, (int32_t)k};
+    }
+    if (matriz == 2) {
+      diag_mode = fvc::DIAG_NONE;
+      raw1 = 1;  // values live in ad
+      jac_slot.assign((size_t)n, -1);
+      for (int i = 0; i < n; ++i)
+        for (int64_t k = ia[i] - 1; k < ia[i + 1] - 1; ++k)
+          if (ja[k] - 1 == i) {
+            jac_slot[i] = (int32_t)k;
+            break;
+          }
+    } else {
+      diag_mode = fvc::DIAG_FIRST;
+      raw1 = 2;  // au (src/Matvec.f:21 matvec_csrd(ad,a=au,...))
+    }
+    return FVC_OK;
+  }
+  // Expanded symmetric-structure formats: row i = its stored (lower) terms
+  // followed by the transposed terms (r, i) of later rows r in order.
+  std::vector<int64_t> cnt((size_t)n, 0);
+  for (int i = 0; i < n; ++i) {
+    cnt[i] += ia[i + 1] - ia[i];
+    for (int64_t k = ia[i] - 1; k < ia[i + 1] - 1; ++k) {
+      int c = ja[k] - 1;
+      if (c >= i) return FVC_ERR_ARG;  // lower part only
+      cnt[c]++;
+    }
+  }
+  for (int i = 0; i < n; ++i) R.start[i + 1] = R.start[i] + cnt[i];
+  R.e.resize((size_t)R.start[n]);
+  std::vector<int64_t> fill(R.start.begin(), R.start.end() - 1);
+  raw1 = 3;  // al: the stored lower values
+  raw2 = (matriz == 3 && unsym) ? 2 : 3;  // au for CSRC unsym transposed terms
+  for (int i = 0; i < n; ++i)
+    for (int64_t k = ia[i] - 1; k < ia[i + 1] - 1; ++k) R.e[fill[i]++] = {ja[k] - 1, (int32_t)k};
+  for (int r = 0; r < n; ++r)
+    for (int64_t k = ia[r] - 1; k < ia[r + 1] - 1; ++k) {
+      int c = ja[k] - 1;
+      R.e[fill[c]++] = {r, (raw2 == raw1) ? (int32_t)k : (int32_t)(-k - 2)};
+    }
+  // Terms sharing raw1 == raw2 (al) index raw array 1 directly.
+  diag_mode = fvc::DIAG_FIRST;
+  if (raw2 == raw1) raw2 = 0;
+  return FVC_OK;
+}
+
+const double *pick(int which, const double *ad, const double *au, const double *al) {
+  if (which == 1) return ad;
+  if (which == 2) return au ? au : al;
+  if (which == 3) return al ? al : au;
+  return nullptr;
+}
+
+int32_t upload_raw(fvc_context *c, const double *ad, const double *au, const double *al) {
+  const double *h1 = pick(c->raw1_which, ad, au, al);
+  const double *h2 = pick(c->raw2_which, ad, au, al);
+  if (!h1 || (c->raw2_which && !h2) || !ad) return FVC_ERR_ARG;
+  cudaStream_t s = c->stream;
+  if (cudaMemcpyAsync(c->d_raw1, h1, sizeof(double) * c->raw1_n, cudaMemcpyHostToDevice, s) !=
+      cudaSuccess)
+    return FVC_ERR_CUDA;
+  if (c->raw2_which &&
+      cudaMemcpyAsync(c->d_raw2, h2, sizeof(double) * c->raw2_n, cudaMemcpyHostToDevice, s) !=
+          cudaSuccess)
+    return FVC_ERR_CUDA;
+  int32_t rc = fvc::launch_gather_values(c->A.slots, c->d_src, c->d_raw1, c->d_raw2, c->A.val, s);
+  if (rc != FVC_OK) return rc;
+  if (c->matriz == 2) {
+    // Jacobi m = the diagonal entries (slot codes into raw array 1 = ad)
+    rc = fvc::launch_gather_values(c->neq, c->d_jac_src, c->d_raw1, nullptr, c->A.jac, s);
+    if (rc != FVC_OK) return rc;
+  } else {
+    if (cudaMemcpyAsync(c->A.diag, ad, sizeof(double) * c->neq, cudaMemcpyHostToDevice, s) !=
+            cudaSuccess ||
+        cudaMemcpyAsync(c->A.jac, ad, sizeof(double) * c->neq, cudaMemcpyHostToDevice, s) !=
+            cudaSuccess)
+      return FVC_ERR_CUDA;
+  }
+  c->A.have32 = false;  // FP32 copy is rebuilt lazily from the new values
+  return FVC_OK;
+}
+
+int default_init(int code, int matriz) {
+  // src/Solver.f with openmpSolver = .false. (or the OpenMP rule, below)
+  static int omp = -1;
+  if (omp < 0) {
+    const char *e = getenv("FVC_OPENMP_SOLVER");
+    omp = (e && atoi(e) != 0) ? 1 : 0;
+  }
+  if (code == 3) return 1;        // Iterativos.f:288-290
+  if (matriz == 4) return 0;      // Solver.f:159,165,253,260
+  if (code == 1 && matriz == 1) return omp ? 0 : 1;  // Solver.f:104,120 vs :130,134
+  return 1;                       // Solver.f:143,149,207,214,222,236,241
+}
+
+
+}  // namespace
+
+extern "C" {
+
+void fvc_opts_default(fvc_opts *o) {
+  if (!o) return;
+  memset(o, 0, sizeof(*o));
+  o->precision = FVC_PREC_FP64;
+  o->init = -1;
+  o->want_residual = 1;
+}
+
+int64_t fvc_kernel_launches(void) { return fvc::g_launches.load(); }
+
+int32_t fvc_context_create(fvc_context **ctx, int32_t device) {
+  if (!ctx) return FVC_ERR_ARG;
+  *ctx = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0 || device < 0 || device >= ndev)
+    return FVC_ERR_CUDA;
+  if (cudaSetDevice(device) != cudaSuccess) return FVC_ERR_CUDA;
+  fvc_context *c = new fvc_context();
+  c->device = device;
+  *ctx = c;
+  return FVC_OK;
+}
+
+int32_t fvc_context_destroy(fvc_context *c) {
+  if (!c) return FVC_ERR_ARG;
+  cudaSetDevice(c->device);
+  free_matrix(c);
+  for (int i = 0; i < 8; ++i) {
+    cudaFree(c->S.v[i]);
+    cudaFree(c->S.f[i]);
+  }
+  cudaFree(c->S.g);
+  cudaFree(c->S.partials);
+  cudaFree(c->S.sync);
+  cudaFree(c->S.err);
+  cudaFree(c->S.result);
+  cudaFree(c->S.iresult);
+  cudaFree(c->d_b);
+  cudaFree(c->d_x);
+  delete c;
+  return FVC_OK;
+}
+
+int32_t fvc_context_set_stream(fvc_context *c, void *stream) {
+  if (!c) return FVC_ERR_ARG;
+  c->stream = (cudaStream_t)stream;
+  return FVC_OK;
+}
+
+int32_t fvc_matrix_set(fvc_context *c, int32_t matriz, int32_t unsym, int32_t neq, int32_t nad,
+                       const double *ad, const double *au, const double *al, const int32_t *iax,
+                       const int32_t *ja) {
+  if (!c || neq <= 0 || nad < 0 || !ad || !iax || !ja) return FVC_ERR_ARG;
+  if (matriz < 1 || matriz > 4) return FVC_ERR_UNSUPPORTED;
+  cudaSetDevice(c->device);
+  RowLists R;
+  int diag_mode = 0, raw1 = 0, raw2 = 0;
+  std::vector<int32_t> jac_slot;
+  int32_t rc = build_rows(matriz, unsym, neq, nad, iax, ja, R, diag_mode, raw1, raw2, jac_slot);
+  if (rc != FVC_OK) return rc;
+  free_matrix(c);
+  const int n = neq;
+  const int nslices = (n + 31) / 32;
+  std::vector<int64_t> sptr((size_t)nslices + 1, 0);
+  int64_t nnz_true = 0;
+  for (int s = 0; s < nslices; ++s) {
+    int64_t w = 0;
+    for (int r = s * 32; r < std::min(n, s * 32 + 32); ++r)
+      w = std::max<int64_t>(w, R.start[r + 1] - R.start[r]);
+    sptr[s + 1] = sptr[s] + 32 * w;
+  }
+  const int64_t slots = sptr[nslices];
+  std::vector<int32_t> col((size_t)std::max<int64_t>(slots, 1), 0);
+  std::vector<int32_t> src((size_t)std::max<int64_t>(slots, 1), -1);
+  for (int s = 0; s < nslices; ++s) {
+    const int w = (int)((sptr[s + 1] - sptr[s]) / 32);
+    for (int l = 0; l < 32; ++l) {
+      const int r = s * 32 + l;
+      for (int k = 0; k < w; ++k) {
+        int64_t q = sptr[s] + 32 * k + l;
+        if (r < n && R.start[r] + k < R.start[r + 1]) {
+          const Entry &e = R.e[R.start[r] + k];
+          col[q] = e.col;
+          src[q] = e.src;
+          ++nnz_true;
+        } else {
+          col[q] = (r < n) ? r : 0;
+          src[q] = -1;
+        }
+      }
+    }
+  }
+  if (matriz == 4) nnz_true = nad;  // ellPackJa's count of real neighbours
+  DeviceMatrix &A = c->A;
+  A.n = n;
+  A.nslices = nslices;
+  A.slots = slots;
+  A.nnz_off = (matriz == 2) ? nnz_true - n : nnz_true;
+  A.diag_mode = diag_mode;
+  A.matriz = matriz;
+  A.unsym = unsym;
+  A.nad = nad;
+  const size_t sl = (size_t)std::max<int64_t>(slots, 1);
+  bool ok = cudaMalloc(&A.sptr, sizeof(int64_t) * (nslices + 1)) == cudaSuccess &&
+            cudaMalloc(&A.col, sizeof(int32_t) * sl) == cudaSuccess &&
+            cudaMalloc(&A.val, sizeof(double) * sl) == cudaSuccess &&
+            cudaMalloc(&A.jac, sizeof(double) * n) == cudaSuccess &&
+            cudaMalloc(&c->d_src, sizeof(int32_t) * sl) == cudaSuccess;
+  if (ok && diag_mode != fvc::DIAG_NONE) ok = cudaMalloc(&A.diag, sizeof(double) * n) == cudaSuccess;
+  c->raw1_which = raw1;
+  c->raw2_which = raw2;
+  c->raw1_n = (raw1 == 1 && matriz != 2) ? (size_t)n : (size_t)std::max<int64_t>((matriz == 4) ? (int64_t)n * iax[0] : nad, 1);
+  c->raw2_n = raw2 ? (size_t)std::max(nad, 1) : 0;
+  if (ok) ok = cudaMalloc(&c->d_raw1, sizeof(double) * c->raw1_n) == cudaSuccess;
+  if (ok && raw2) ok = cudaMalloc(&c->d_raw2, sizeof(double) * c->raw2_n) == cudaSuccess;
+  if (ok && matriz == 2) {
+    ok = cudaMalloc(&c->d_jac_src, sizeof(int32_t) * n) == cudaSuccess &&
+         cudaMemcpy(c->d_jac_src, jac_slot.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice) ==
+             cudaSuccess;
+  }
+  if (!ok) {
+    free_matrix(c);
+    return FVC_ERR_CUDA;
+  }
+  if (cudaMemcpy(A.sptr, sptr.data(), sizeof(int64_t) * (nslices + 1), cudaMemcpyHostToDevice) !=
+          cudaSuccess ||
+      cudaMemcpy(A.col, col.data(), sizeof(int32_t) * sl, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(c->d_src, src.data(), sizeof(int32_t) * sl, cudaMemcpyHostToDevice) != cudaSuccess) {
+    free_matrix(c);
+    return FVC_ERR_CUDA;
+  }
+  c->matriz = matriz;
+  c->unsym = unsym;
+  c->neq = neq;
+  c->nad = nad;
+  c->has_matrix = true;
+  rc = upload_raw(c, ad, au, al);
+  if (rc != FVC_OK) {
+    free_matrix(c);
+    return rc;
+  }
+  if (cudaStreamSynchronize(c->stream) != cudaSuccess) return FVC_ERR_CUDA;
+  return FVC_OK;
+}
+
+int32_t fvc_matrix_update_values(fvc_context *c, const double *ad, const double *au,
+                                 const double *al) {
+  if (!c || !c->has_matrix) return FVC_ERR_ARG;
+  cudaSetDevice(c->device);
+  int32_t rc = upload_raw(c, ad, au, al);
+  if (rc != FVC_OK) return rc;
+  return cudaStreamSynchronize(c->stream) == cudaSuccess ? FVC_OK : FVC_ERR_CUDA;
+}
+
+int32_t fvc_matrix_info(const fvc_context *c, int64_t *n, int64_t *slots, int64_t *nnz_off,
+                        int64_t *nslices) {
+  if (!c || !c->has_matrix) return FVC_ERR_ARG;
+  if (n) *n = c->A.n;
+  if (slots) *slots = c->A.slots;
+  if (nnz_off) *nnz_off = c->A.nnz_off;
+  if (nslices) *nslices = c->A.nslices;
+  return FVC_OK;
+}
+
+int32_t fvc_spmv(fvc_context *c, const double *d_x, double *d_y) {
+  if (!c || !c->has_matrix || !d_x || !d_y) return FVC_ERR_ARG;
+  return fvc::launch_spmv(c->A, d_x, d_y, c->stream);
+}
+
+int32_t fvc_spmv_f32(fvc_context *c, const float *d_x, float *d_y) {
+  if (!c || !c->has_matrix || !d_x || !d_y) return FVC_ERR_ARG;
+  int32_t rc = fvc::build_f32_copy(c->A, c->stream);
+  if (rc != FVC_OK) return rc;
+  return fvc::launch_spmv_f32(c->A, d_x, d_y, c->stream);
+}
+
+int32_t fvc_solve(fvc_context *c, int32_t code, const double *d_b, double *d_x, double tol,
+                  int32_t maxit, const fvc_opts *opts, fvc_stats *st) {
+  if (!c || !c->has_matrix || !d_b || !d_x || maxit < 1) return FVC_ERR_ARG;
+  fvc_opts o;
+  if (opts)
+    o = *opts;
+  else
+    fvc_opts_default(&o);
+  if (st) memset(st, 0, sizeof(*st));
+  cudaSetDevice(c->device);
+  const int matriz = c->matriz;
+  if (code < 1 || code > 3) return FVC_ERR_UNSUPPORTED;
+  if ((code == 2 || code == 3) && matriz == 2) return FVC_ERR_UNSUPPORTED;  // Solver.f:224,305
+  if (code == 3 && matriz == 4) return FVC_ERR_UNSUPPORTED;  // no GMRES branch for ELLPACK
+  int init = (o.init < 0) ? default_init(code, matriz) : (o.init ? 1 : 0);
+  int32_t rc;
+  if (o.precision == FVC_PREC_MIXED) {
+    rc = fvc::run_mixed(c->A, c->S, code, d_b, d_x, tol, maxit, init, o, c->stream, st);
+  } else if (code == 1) {
+    rc = fvc::run_pcg(c->A, c->S, d_b, d_x, tol, maxit, init, o, c->stream, st);
+  } else if (code == 2) {
+    rc = fvc::run_bicgstab(c->A, c->S, d_b, d_x, tol, maxit, init, o, c->stream, st);
+  } else {
+    rc = fvc::run_gmres(c->A, c->S, d_b, d_x, tol, maxit, o, c->stream, st);
+  }
+  if (st && rc != st->status) st->status = rc;
+  return rc;
+}
+
+}  // extern "C"
+
+namespace {
+
+uint64_t fnv_hash(const int32_t *a, size_t n, uint64_t h) {
+  const uint64_t prime = 1099511628211ull;
+  for (size_t i = 0; i < n; ++i) {
+    h ^= (uint32_t)a[i];
+    h *= prime;
+  }
+  return h;
+}
+
+std::mutex g_mutex;
+fvc_context *g_ctx = nullptr;
+
+int32_t solver_ex_ctx(fvc_context *c, double *ad, double *au, double *al, double *x,
+                          const double *b, const int32_t *iax, const int32_t *ja, int32_t neq,
+                          int32_t nad, int32_t unsym, double tol, int32_t maxit, int32_t code,
+                          int32_t matriz, const fvc_opts *opts, fvc_stats *st) {
+  if (!c || !ad || !x || !b || !iax || !ja || neq <= 0) return FVC_ERR_ARG;
+  if (code < 1 || code > 3 || matriz < 1 || matriz > 4) return FVC_ERR_UNSUPPORTED;
+  if ((code == 2 || code == 3) && matriz == 2) return FVC_ERR_UNSUPPORTED;
+  if (code == 3 && matriz == 4) return FVC_ERR_UNSUPPORTED;
+  // structure cache: same arrays and same contents -> only values move
+  const size_t ialen = (matriz == 4) ? 2 : (size_t)neq + 1;
+  const size_t jalen = (matriz == 4) ? (size_t)neq * (size_t)iax[0] : (size_t)std::max(nad, 0);
+  uint64_t h = fnv_hash(iax, ialen, 1469598103934665603ull);
+  h = fnv_hash(ja, jalen, h);
+  h ^= ((uint64_t)matriz << 56) ^ ((uint64_t)(unsym != 0) << 55) ^ ((uint64_t)neq << 20) ^ (uint64_t)nad;
+  int32_t rc;
+  if (c->has_matrix && c->key_iax == iax && c->key_ja == ja && c->key_hash == h) {
+    rc = fvc_matrix_update_values(c, ad, au, al);
+  } else {
+    rc = fvc_matrix_set(c, matriz, unsym, neq, nad, ad, au, al, iax, ja);
+    c->key_iax = iax;
+    c->key_ja = ja;
+    c->key_hash = h;
+  }
+  if (rc != FVC_OK) {
+    c->key_iax = c->key_ja = nullptr;
+    return rc;
+  }
+  if (c->nvec < (size_t)neq) {
+    cudaFree(c->d_b);
+    cudaFree(c->d_x);
+    c->d_b = c->d_x = nullptr;
+    if (cudaMalloc(&c->d_b, sizeof(double) * neq) != cudaSuccess ||
+        cudaMalloc(&c->d_x, sizeof(double) * neq) != cudaSuccess)
+      return FVC_ERR_CUDA;
+    c->nvec = (size_t)neq;
+  }
+  if (cudaMemcpyAsync(c->d_b, b, sizeof(double) * neq, cudaMemcpyHostToDevice, c->stream) !=
+          cudaSuccess ||
+      cudaMemcpyAsync(c->d_x, x, sizeof(double) * neq, cudaMemcpyHostToDevice, c->stream) !=
+          cudaSuccess)
+    return FVC_ERR_CUDA;
+  rc = fvc_solve(c, code, c->d_b, c->d_x, tol, maxit, opts, st);
+  if (rc == FVC_OK || rc == FVC_ERR_NOCONV || rc == FVC_ERR_NAN || rc == FVC_ERR_BREAKDOWN) {
+    if (cudaMemcpyAsync(x, c->d_x, sizeof(double) * neq, cudaMemcpyDeviceToHost, c->stream) !=
+            cudaSuccess ||
+        cudaStreamSynchronize(c->stream) != cudaSuccess)
+      return FVC_ERR_CUDA;
+  }
+  return rc;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t fvc_solver_ex(double *ad, double *au, double *al, double *x, const double *b,
+                      const int32_t *iax, const int32_t *ja, int32_t neq, int32_t nad,
+                      int32_t unsym, double tol, int32_t maxit, int32_t code, int32_t matriz,
+                      const fvc_opts *opts, fvc_stats *st) {
+  std::lock_guard<std::mutex> lock(g_mutex);
+  if (!g_ctx) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int32_t rc = fvc_context_create(&g_ctx, dev);
+    if (rc != FVC_OK) return rc;
+  }
+  return solver_ex_ctx(g_ctx, ad, au, al, x, b, iax, ja, neq, nad, unsym, tol, maxit, code,
+                           matriz, opts, st);
+}
+
+}  // extern "C"
+
+// ---- drop-in entry: messages and STOP behaviour of the reference ---------
+namespace {
+
+// Fortran Dw.d edit descriptor (gfortran style: 0.ddddddD+ee, right-justified).
+std::string fortran_d(double v, int w, int d) {
+  char buf[64];
+  if (!std::isfinite(v)) {
+    snprintf(buf, sizeof buf, "%*s", w, std::isnan(v) ? "NaN" : (v > 0 ? "Infinity" : "-Infinity"));
+    return buf;
+  }
+  int e = 0;
+  double m = v;
+  if (v != 0.0) {
+    e = (int)std::floor(std::log10(std::fabs(v))) + 1;
+    m = v / std::pow(10.0, e);
+    // rounding may push |m| to 1.0: renormalise
+    double r = std::round(std::fabs(m) * std::pow(10.0, d)) / std::pow(10.0, d);
+    if (r >= 1.0) {
+      e += 1;
+      m = v / std::pow(10.0, e);
+    }
+  }
+  char mant[48];
+  snprintf(mant, sizeof mant, "%.*f", d, std::fabs(m));
+  std::string s = (v < 0 ? "-" : "");
+  s += mant;
+  char ex[16];
+  snprintf(ex, sizeof ex, "D%c%02d", e < 0 ? '-' : '+', std::abs(e));
+  s += ex;
+  if ((int)s.size() < w) s = std::string(w - s.size(), ' ') + s;
+  return s;
+}
+
+bool stop_on_error() {
+  const char *e = getenv("FVC_STOP_ON_ERROR");
+  return !(e && e[0] == '0');
+}
+
+void error_block(const char *func, const char *file, const char *msg) {
+  // include/error.fi format 2000
+  printf(" ***************************************************\n");
+  printf(" Funcao:           %s\n", func);
+  printf(" Arquivo:          %s\n", file);
+  printf(" Messagem de erro: %s\n", msg);
+  printf(" ***************************************************\n");
+  fflush(stdout);
+}
+
+void solvit_log(const char *tag, int it, double energy, double tol) {
+  // the reference's unit-13 line, '(a,a,i9,a,d20.10,a,d20.10)'
+  const char *path = getenv("FVC_SOLVIT_LOG");
+  if (!path || !*path) return;
+  FILE *f = fopen(path, "a");
+  if (!f) return;
+  fprintf(f, "%s%s%9d%s%s%s%s\n", tag, "it", it, " energy norm ", fortran_d(energy, 20, 10).c_str(),
+          " tol ", fortran_d(tol, 20, 10).c_str());
+  fclose(f);
+}
+
+void dropin(double *ad, double *au, double *al, double *x, double *b, const int32_t *iax,
+            const int32_t *ja, const int32_t *neq, const int32_t *nad, const int32_t *unsym,
+            const double *tol, const int32_t *maxit, const int32_t *code, const int32_t *matriz,
+            const int32_t *nlit) {
+  const int cd = *code, mz = *matriz;
+  if (cd < 1 || cd > 3) {
+    error_block("Solver", "Solver.f", "solver nao especificado!!!");
+    if (stop_on_error()) exit(0);
+    return;
+  }
+  if (cd == 2 && mz == 2) {
+    error_block("Solver", "Solver.f", "PBiCGSTAB nao implementado para o CSR");
+    if (stop_on_error()) exit(0);
+    return;
+  }
+  if (cd == 3 && mz == 2) {
+    error_block("Solver", "Solver.f", "PGMRES nao implementado para o CSR");
+    if (stop_on_error()) exit(0);
+    return;
+  }
+  if (cd == 3 && mz == 4) return;  // the reference has no GMRES branch for ELLPACK
+  fvc_opts o;
+  fvc_opts_default(&o);
+  fvc_stats st;
+  int32_t rc = fvc_solver_ex(ad, au, al, x, b, iax, ja, *neq, *nad, *unsym != 0, *tol, *maxit, cd,
+                             mz, &o, &st);
+  if (rc == FVC_ERR_NOCONV || rc == FVC_ERR_NAN) {
+    if (cd == 1)
+      printf(" *** WARNING:  PCG no convergence reached after %9d iterations !%s Res %s Conv\n\n",
+             *maxit, fortran_d(st.final_crit, 20, 6).c_str(), fortran_d(st.conv, 20, 6).c_str());
+    else if (cd == 2)
+      printf(" *** WARNING: BiPCGSTAB no convergence reached after %9d iterations !%s Res %s Conv\n\n",
+             *maxit, fortran_d(st.final_crit, 20, 6).c_str(), fortran_d(st.conv, 20, 6).c_str());
+    else
+      printf(" *** WARNING: no convergence reached for %9d cycles !\n\n", *maxit);
+    fflush(stdout);
+    if (stop_on_error()) exit(0);
+    return;
+  }
+  if (rc != FVC_OK) {
+    fprintf(stderr, "fvcgpu: solver failed with status %d\n", rc);
+    if (stop_on_error()) exit(1);
+    return;
+  }
+  const double secs = st.solve_ms * 1e-3;
+  if (cd == 1 || cd == 2) {
+    if (*nlit == 1) {
+      printf(" (%s) solver:\n", cd == 1 ? "PCG" : "PBICGSTAB");
+      printf("     Solver tol           = %s\n", fortran_d(*tol, 20, 6).c_str());
+      printf("     Number of equations  = %20d\n", *neq);
+      printf("     Nad                  = %20d\n", *nad);
+      printf("     Number of iterations = %20d\n", st.iterations);
+      printf("     Energy norm          = %s\n", fortran_d(st.energy, 20, 10).c_str());
+      printf("     CPU time (s)         = %20.2f\n\n", secs);
+      fflush(stdout);
+    }
+    solvit_log(cd == 1 ? "PCG:       " : "PBICGSTAB: ", st.iterations, st.energy, *tol);
+  } else {
+    if (*nlit == 1) {
+      printf(" (GMRES) solver:\n");
+      printf("     Solver tol           = %s\n", fortran_d(*tol, 20, 6).c_str());
+      printf("     Number of equations  = %20d\n", *neq);
+      printf("     Nad                  = %20d\n", *nad);
+    }
+    printf("     Number of cycles     = %20d\n", st.iterations);
+    printf("     Number of iterations = %20d\n", st.inner_iterations);
+    printf("     Norm                 = %s\n", fortran_d(st.final_crit, 20, 6).c_str());
+    printf("     Energy norm          = %s\n", fortran_d(st.energy, 20, 10).c_str());
+    printf("     CPU time (s)         = %20.2f\n\n", secs);
+    fflush(stdout);
+    solvit_log("GMRES: ", st.iterations, st.energy, *tol);
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+void fvc_solver(double *ad, double *au, double *al, double *x, double *b, const int32_t *iax,
+                const int32_t *ja, const int32_t *neq, const int32_t *nad, const int32_t *unsym,
+                const double *tol, const int32_t *maxit, const int32_t *code,
+                const int32_t *matriz, const int32_t *nlit) {
+  dropin(ad, au, al, x, b, iax, ja, neq, nad, unsym, tol, maxit, code, matriz, nlit);
+}
+
+void solver_(double *ad, double *au, double *al, double *x, double *b, const int32_t *iax,
+             const int32_t *ja, const int32_t *neq, const int32_t *nad, const int32_t *unsym,
+             const double *tol, const int32_t *maxit, const int32_t *code, const int32_t *matriz,
+             const int32_t *nlit) {
+  dropin(ad, au, al, x, b, iax, ja, neq, nad, unsym, tol, maxit, code, matriz, nlit);
+}
+
+}  // extern "C"

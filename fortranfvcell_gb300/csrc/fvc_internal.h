@@ -1,0 +1,77 @@
+// fvc_internal.h -- host-side declarations shared by the translation units
+// of libfvcgpu (not part of the public C ABI).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/fvcgpu.h"
+
+namespace fvc {
+
+// Where the reference's SpMV adds the diagonal term (src/Matvec.f).
+enum DiagMode : int { DIAG_FIRST = 0, DIAG_LAST = 1, DIAG_NONE = 2 };
+
+// Device copy of one matrix in SELL-32 (see fvc_device.cuh).
+struct DeviceMatrix {
+  int n = 0;
+  int nslices = 0;
+  int64_t slots = 0;      // stored slots incl. padding
+  int64_t nnz_off = 0;    // true off-diagonal nonzeros
+  int diag_mode = 0;
+  int64_t *sptr = nullptr;
+  int *col = nullptr;
+  double *val = nullptr;
+  double *diag = nullptr;  // ad (null for DIAG_NONE)
+  double *jac = nullptr;   // Jacobi m (the reference's m = ad)
+  // FP32 Jacobi-scaled copy for mixed precision: S = D^-1/2 A D^-1/2
+  float *val32 = nullptr;
+  float *diag32 = nullptr;  // scaled diagonal (1 except for zero rows)
+  double *dscale = nullptr; // D^-1/2 (FP64)
+  bool have32 = false;
+  // host-side description of the source layout, for value updates
+  int matriz = 0, unsym = 0, nad = 0;
+  int64_t *src_of_slot = nullptr;  // device map: slot -> source value index
+  int8_t *src_arr = nullptr;       // device map: slot -> 0 none,1 ad,2 au,3 al
+};
+
+struct Scratch {
+  size_t n = 0, nf = 0, ngmres = 0;  // capacities of v[], f[], g
+  double *v[8] = {nullptr};     // Krylov vectors
+  float *f[8] = {nullptr};      // FP32 vectors (mixed precision)
+  double *g = nullptr;          // GMRES basis (k+1) x n
+  double *partials = nullptr;   // reduction partials
+  size_t npart = 0;
+  unsigned int *sync = nullptr; // barrier counter + generation
+  int *err = nullptr;
+  double *result = nullptr;     // solver scalars written by block 0
+  int *iresult = nullptr;
+};
+
+struct Launch {
+  int threads = 256;
+  int blocks = 0;
+};
+
+// Kernel launch counter (fvc_kernel_launches).
+void count_launch(int64_t k = 1);
+
+// Krylov drivers (fvc_krylov.cu).  All synchronous on `stream`.
+int32_t run_pcg(const DeviceMatrix &A, Scratch &S, const double *b, double *x,
+                double tol, int maxit, int init, const fvc_opts &o,
+                cudaStream_t stream, fvc_stats *st);
+int32_t run_bicgstab(const DeviceMatrix &A, Scratch &S, const double *b,
+                     double *x, double tol, int maxit, int init,
+                     const fvc_opts &o, cudaStream_t stream, fvc_stats *st);
+int32_t run_gmres(const DeviceMatrix &A, Scratch &S, const double *b, double *x,
+                  double tol, int maxit, const fvc_opts &o, cudaStream_t stream,
+                  fvc_stats *st);
+int32_t run_mixed(const DeviceMatrix &A, Scratch &S, int code, const double *b,
+                  double *x, double tol, int maxit, int init, const fvc_opts &o,
+                  cudaStream_t stream, fvc_stats *st);
+int32_t launch_spmv(const DeviceMatrix &A, const double *x, double *y,
+                    cudaStream_t stream);
+int32_t launch_spmv_f32(const DeviceMatrix &A, const float *x, float *y,
+                        cudaStream_t stream);
+int32_t build_f32_copy(DeviceMatrix &A, cudaStream_t stream);
+
+}  // namespace fvc

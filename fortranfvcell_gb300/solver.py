@@ -1,0 +1,153 @@
+"""Host-side mirror of the reference's ``solver`` call (src/Solver.f:28-29).
+
+``solver(ad, au, al, x, b, iax, ja, neq, nad, unsym, tol, maxit, code,
+matriz, nlit)`` takes the same arguments with the same meaning as the
+Fortran subroutine (numpy host arrays, Fortran 1-based indices, negated
+off-diagonals) and runs the solve on the GPU through libfvcgpu's C ABI.
+``x`` is updated in place.  Where the reference prints a warning and
+executes STOP (non-convergence, an unsupported code/matriz pair), this
+mirror raises :class:`FvcError` with the matching status instead.
+
+:class:`Context` exposes the device-resident path: a matrix uploaded once,
+device vectors (torch tensors used as plain device buffers), FP64 or mixed
+precision, the reference's or the ||r||/||b|| stopping rule.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import FvcError, FvcOpts, FvcStats
+
+CODES = {1: "PCG", 2: "BiCGSTAB", 3: "GMRES"}
+
+
+def _p(a):
+    return None if a is None else np.ascontiguousarray(a).ctypes.data_as(C.c_void_p)
+
+
+def make_opts(precision: str = "fp64", init: int = -1, stop_rule: int = 0,
+              refine_tol: float = 0.0, inner_tol: float = 0.0, max_refine: int = 0,
+              block_threads: int = 0, blocks_per_sm: int = 0) -> FvcOpts:
+    o = FvcOpts()
+    _lib.load().fvc_opts_default(C.byref(o))
+    o.precision = {"fp64": _lib.FVC_PREC_FP64, "mixed": _lib.FVC_PREC_MIXED}[precision]
+    o.init = init
+    o.stop_rule = stop_rule
+    o.refine_tol = refine_tol
+    o.inner_tol = inner_tol
+    o.max_refine = max_refine
+    o.block_threads = block_threads
+    o.blocks_per_sm = blocks_per_sm
+    return o
+
+
+def solver(ad, au, al, x, b, iax, ja, neq, nad, unsym, tol, maxit, code, matriz, nlit=0,
+           opts: FvcOpts | None = None) -> FvcStats:
+    """GPU solve with the reference's argument list; returns the stats.
+
+    Raises FvcError on non-convergence (the reference STOPs) and on the
+    code/matriz pairs Solver.f rejects.
+    """
+    L = _lib.load()
+    if x.dtype != np.float64 or not x.flags.c_contiguous:
+        raise TypeError("x must be a contiguous float64 array (updated in place)")
+    ad = np.ascontiguousarray(ad, np.float64)
+    au = None if au is None else np.ascontiguousarray(au, np.float64)
+    al = None if al is None else np.ascontiguousarray(al, np.float64)
+    b = np.ascontiguousarray(b, np.float64)
+    iax = np.ascontiguousarray(iax, np.int32)
+    ja = np.ascontiguousarray(ja, np.int32)
+    st = FvcStats()
+    o = opts if opts is not None else make_opts()
+    rc = L.fvc_solver_ex(_p(ad), _p(au), _p(al), x.ctypes.data_as(C.c_void_p), _p(b), _p(iax),
+                         _p(ja), int(neq), int(nad), int(bool(unsym)), float(tol), int(maxit),
+                         int(code), int(matriz), C.byref(o), C.byref(st))
+    if rc != _lib.FVC_OK:
+        raise FvcError(rc, f"{CODES.get(code, code)} (matriz {matriz}) ended with status "
+                           f"{_lib.STATUS_NAMES.get(rc, rc)} after {st.iterations} iterations")
+    return st
+
+
+class Context:
+    """A device-resident matrix plus solver scratch (one per host thread)."""
+
+    def __init__(self, device: int = 0, stream=None):
+        self._L = _lib.load()
+        self._h = C.c_void_p()
+        _lib.check(self._L.fvc_context_create(C.byref(self._h), int(device)),
+                   "fvc_context_create")
+        if stream is not None:
+            self.set_stream(stream)
+
+    def close(self):
+        if self._h:
+            self._L.fvc_context_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream) -> None:
+        """stream: a torch.cuda.Stream, a raw cudaStream_t int, or None."""
+        raw = getattr(stream, "cuda_stream", stream)
+        _lib.check(self._L.fvc_context_set_stream(self._h, C.c_void_p(raw or 0)),
+                   "fvc_context_set_stream")
+
+    def set_matrix(self, matriz, unsym, neq, nad, ad, au, al, iax, ja) -> None:
+        self._keep = [np.ascontiguousarray(a) if a is not None else None
+                      for a in (ad, au, al, iax, ja)]
+        ad, au, al, iax, ja = self._keep
+        _lib.check(self._L.fvc_matrix_set(self._h, int(matriz), int(bool(unsym)), int(neq),
+                                          int(nad), _p(ad), _p(au), _p(al), _p(iax), _p(ja)),
+                   "fvc_matrix_set")
+
+    def update_values(self, ad, au=None, al=None) -> None:
+        _lib.check(self._L.fvc_matrix_update_values(self._h, _p(ad), _p(au), _p(al)),
+                   "fvc_matrix_update_values")
+
+    def info(self) -> dict:
+        n, slots, nnz, ns = C.c_int64(), C.c_int64(), C.c_int64(), C.c_int64()
+        _lib.check(self._L.fvc_matrix_info(self._h, C.byref(n), C.byref(slots), C.byref(nnz),
+                                           C.byref(ns)), "fvc_matrix_info")
+        return {"n": n.value, "slots": slots.value, "nnz_off": nnz.value, "nslices": ns.value}
+
+    def solve(self, code: int, b_dev, x_dev, tol: float, maxit: int,
+              opts: FvcOpts | None = None, raise_on_error: bool = True) -> FvcStats:
+        """b_dev, x_dev: device buffers (torch CUDA float64 tensors or raw
+        device addresses).  x_dev is the initial guess and the result."""
+        st = FvcStats()
+        o = opts if opts is not None else make_opts()
+        rc = self._L.fvc_solve(self._h, int(code), C.c_void_p(_addr(b_dev)),
+                               C.c_void_p(_addr(x_dev)), float(tol), int(maxit), C.byref(o),
+                               C.byref(st))
+        if raise_on_error and rc != _lib.FVC_OK:
+            raise FvcError(rc, f"{CODES.get(code, code)} ended with status "
+                               f"{_lib.STATUS_NAMES.get(rc, rc)}")
+        st.status = rc
+        return st
+
+    def spmv(self, x_dev, y_dev) -> None:
+        _lib.check(self._L.fvc_spmv(self._h, C.c_void_p(_addr(x_dev)), C.c_void_p(_addr(y_dev))),
+                   "fvc_spmv")
+
+    def spmv_f32(self, x_dev, y_dev) -> None:
+        _lib.check(self._L.fvc_spmv_f32(self._h, C.c_void_p(_addr(x_dev)),
+                                        C.c_void_p(_addr(y_dev))), "fvc_spmv_f32")
+
+
+def _addr(t) -> int:
+    if hasattr(t, "data_ptr"):
+        if not t.is_cuda or not t.is_contiguous():
+            raise ValueError("device buffers must be contiguous CUDA tensors")
+        return int(t.data_ptr())
+    return int(t)
+
+
+def kernel_launches() -> int:
+    return int(_lib.load().fvc_kernel_launches())

@@ -1,0 +1,212 @@
+/*
+ * fvcgpu.h -- C ABI of the GB300 linear-solver library (libfvcgpu.so).
+ *
+ * This is the drop-in boundary for the linear-solver hot path of the
+ * fortranFVCell finite-volume code: the `solver` subroutine of
+ * src/Solver.f:28-29 and the routines it calls (src/Iterativos.f,
+ * src/Matvec.f).  Plain pointers and sizes only; no C++ or torch types.
+ *
+ * Conventions shared by every entry point (as in the reference):
+ *   - indices (iax, ja, num, nelcon, id) are Fortran 1-based values;
+ *   - off-diagonal matrix values are stored NEGATED (A = diag - neighbours),
+ *     exactly as the reference's assembly writes them (src/Csr.f:172,
+ *     src/EllPack.f:85);
+ *   - matriz: 1 CSRD, 2 CSR, 3 CSRC, 4 ELLPACK (src/Datastruct.f:27-179);
+ *   - code:   1 PCG, 2 BiCGSTAB, 3 GMRES(15)   (src/Solver.f:19-21).
+ */
+#ifndef FVCGPU_H
+#define FVCGPU_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+enum {
+  FVC_OK = 0,
+  FVC_ERR_NOCONV = 1,      /* maxit reached (reference: print + STOP)      */
+  FVC_ERR_BREAKDOWN = 2,   /* a Krylov denominator became exactly zero     */
+  FVC_ERR_NAN = 3,         /* NaN/Inf in the iteration                     */
+  FVC_ERR_UNSUPPORTED = 4, /* code x matriz pair the reference rejects     */
+  FVC_ERR_CUDA = 5,        /* CUDA runtime error or no usable GPU          */
+  FVC_ERR_ARG = 6,         /* invalid argument                             */
+  FVC_ERR_TIMEOUT = 7      /* an on-device wait exceeded its bound         */
+};
+
+/* ---- drop-in solver ---------------------------------------------------- */
+/* Replaces src/Solver.f:28-346 `solver(ad,au,al,x,b,iax,ja,neq,nad,unsym,
+ * tol,maxit,code,matriz,nlit)`.  Every argument is passed by reference as
+ * gfortran passes it; `unsym` is a Fortran LOGICAL (4 bytes, nonzero =
+ * .true.).  All arrays are host arrays owned by the caller.
+ *
+ * Behaviour follows the reference path that Solver.f selects for the same
+ * (code, matriz, unsym) when openmpSolver is .false.: the warm-start rule
+ * (x zeroed or used as the initial guess), the Jacobi preconditioner
+ * m = ad, and the stopping tests of src/Iterativos.f.  Differences:
+ *   - b is left unchanged (the reference overwrites it with p or s);
+ *   - non-convergence prints the reference's warning and, like Fortran
+ *     STOP, ends the process unless FVC_STOP_ON_ERROR=0 is set in the
+ *     environment, in which case the call returns with x = last iterate.
+ * Unsupported pairs (BiCGSTAB/GMRES with matriz 2, src/Solver.f:224-227,
+ * 305-308; unknown code, :337-339) print the reference's message and stop
+ * the same way. */
+void fvc_solver(double *ad, double *au, double *al, double *x, double *b,
+                const int32_t *iax, const int32_t *ja, const int32_t *neq,
+                const int32_t *nad, const int32_t *unsym, const double *tol,
+                const int32_t *maxit, const int32_t *code,
+                const int32_t *matriz, const int32_t *nlit);
+
+/* Same as fvc_solver, under the gfortran-mangled name of the reference
+ * subroutine, so object files compiled from the reference link against this
+ * library unchanged once src/Solver.f is left out of the build. */
+void solver_(double *ad, double *au, double *al, double *x, double *b,
+             const int32_t *iax, const int32_t *ja, const int32_t *neq,
+             const int32_t *nad, const int32_t *unsym, const double *tol,
+             const int32_t *maxit, const int32_t *code, const int32_t *matriz,
+             const int32_t *nlit);
+
+/* ---- extended solver --------------------------------------------------- */
+enum {
+  FVC_PREC_FP64 = 0,  /* reference arithmetic: FP64 everywhere             */
+  FVC_PREC_MIXED = 1  /* FP32 SpMV + Jacobi inside FP64 defect correction  */
+};
+
+typedef struct {
+  int32_t precision;   /* FVC_PREC_*                                       */
+  int32_t init;        /* -1: the reference's rule for (code,matriz); 0: warm
+                          start from x; 1: start from x = 0               */
+  double refine_tol;   /* MIXED: target ||b-Ax||/||b|| (0 -> derived: tol)  */
+  double inner_tol;    /* MIXED: inner FP32 reduction per sweep (0 -> 1e-4)*/
+  int32_t max_refine;  /* MIXED: max outer sweeps (0 -> 30)                */
+  int32_t block_threads; /* 0 -> autotuned                                 */
+  int32_t blocks_per_sm; /* 0 -> autotuned                                 */
+  int32_t stop_rule;   /* 0: the reference's test for the method;
+                          1: ||r||2 <= tol*||b||2 on the recurrence residual */
+  int32_t want_residual; /* 1: recompute ||b-Ax||/||b|| in FP64 at exit   */
+  int32_t reserved[3];
+} fvc_opts;
+
+typedef struct {
+  int32_t status;      /* FVC_*                                            */
+  int32_t iterations;  /* j of the reference loop at exit (GMRES: cycles)  */
+  int32_t inner_iterations; /* GMRES inner steps; MIXED: total FP32 its   */
+  int32_t refinements; /* MIXED: outer sweeps                              */
+  double energy;       /* x.Ax (PCG/BiCGSTAB) or x.b (GMRES), as logged in
+                          the reference's unit-13 line                     */
+  double conv;         /* the stopping threshold                           */
+  double final_crit;   /* the stopped quantity at exit                     */
+  double rel_residual; /* ||b-Ax||/||b|| recomputed in FP64 (if requested) */
+  double solve_ms;     /* device time of the solve                         */
+} fvc_stats;
+
+void fvc_opts_default(fvc_opts *opts);
+
+/* Host-array solve with explicit options; returns an FVC_* status and never
+ * ends the process.  Arguments by value; arrays as in fvc_solver. */
+int32_t fvc_solver_ex(double *ad, double *au, double *al, double *x,
+                      const double *b, const int32_t *iax, const int32_t *ja,
+                      int32_t neq, int32_t nad, int32_t unsym, double tol,
+                      int32_t maxit, int32_t code, int32_t matriz,
+                      const fvc_opts *opts, fvc_stats *stats);
+
+/* ---- device-resident context ------------------------------------------ */
+/* A context owns the device copy of one matrix and its solver scratch, so a
+ * caller that solves the same structure repeatedly (one SIMPLE outer
+ * iteration after another) uploads the structure once.  Not thread-safe;
+ * use one context per host thread. */
+typedef struct fvc_context fvc_context;
+
+int32_t fvc_context_create(fvc_context **ctx, int32_t device);
+int32_t fvc_context_destroy(fvc_context *ctx);
+/* cudaStream_t passed as void*; NULL = the legacy default stream */
+int32_t fvc_context_set_stream(fvc_context *ctx, void *stream);
+
+/* Load a matrix in reference layout from HOST arrays (conversion to the
+ * device layout happens here).  au/al may be NULL where matriz/unsym do not
+ * use them (see src/Datastruct.f). */
+int32_t fvc_matrix_set(fvc_context *ctx, int32_t matriz, int32_t unsym,
+                       int32_t neq, int32_t nad, const double *ad,
+                       const double *au, const double *al, const int32_t *iax,
+                       const int32_t *ja);
+/* Replace only the values (same structure as the last fvc_matrix_set). */
+int32_t fvc_matrix_update_values(fvc_context *ctx, const double *ad,
+                                 const double *au, const double *al);
+
+/* Solve with DEVICE vectors b (not modified) and x (in: guess, out: solution)
+ * on the context's stream.  Synchronous: returns after the solve ends. */
+int32_t fvc_solve(fvc_context *ctx, int32_t code, const double *d_b, double *d_x,
+                  double tol, int32_t maxit, const fvc_opts *opts,
+                  fvc_stats *stats);
+
+/* y = A x with DEVICE vectors, the reference's summation order, FP64
+ * (bit-identical to src/Matvec.f for the loaded format).  Asynchronous on
+ * the context's stream. */
+int32_t fvc_spmv(fvc_context *ctx, const double *d_x, double *d_y);
+/* y = A x with FP32 values (Jacobi-scaled copy kept by MIXED solves),
+ * FP32 vectors; asynchronous. */
+int32_t fvc_spmv_f32(fvc_context *ctx, const float *d_x, float *d_y);
+
+/* Describe the device layout: rows, stored off-diagonal slots (with
+ * padding), true off-diagonal nonzeros, slice count. */
+int32_t fvc_matrix_info(const fvc_context *ctx, int64_t *n, int64_t *slots,
+                        int64_t *nnz_off, int64_t *nslices);
+
+/* Number of kernels this library launched since load (instrumentation). */
+int64_t fvc_kernel_launches(void);
+
+/* ---- mesh -> equation graph (host) ------------------------------------- */
+/* Face-neighbour table.  ix(ld,numel) column-major holds each cell's nodes
+ * (1-based, counter-clockwise) in its first slots; a cell has nsides =
+ * the number of nonzero leading entries (3 or 4, up to nshared).
+ * nelcon(nshared,numel): neighbour cell across side i, -1 on the boundary
+ * or for unused sides.  For one-type meshes this equals
+ * src/Adjacency.f:1-189 (adjtria3/adjquad4).  Returns FVC_* status. */
+int32_t fvc_mesh_adjacency(const int32_t *ix, int32_t ld, int32_t nnode,
+                           int32_t numel, int32_t nshared, int32_t *nelcon);
+
+/* Reverse Cuthill-McKee cell permutation: num(old cell) = new equation.
+ * Same result as src/Reord.f:6-52 (SPARSPAK genrcm/fnroot/rcm with the
+ * reference's tie rules); freord = 0 gives the identity. */
+int32_t fvc_mesh_rcm(const int32_t *nelcon, int32_t numel, int32_t nshared,
+                     int32_t freord, int32_t *num);
+
+/* id(j, num(c)) = num(nelcon(j,c)) or -1 (src/Numeq.f:4-25). */
+int32_t fvc_mesh_numeq(const int32_t *num, const int32_t *nelcon,
+                       int32_t numel, int32_t nshared, int32_t *id);
+
+/* Sparse structure for one system (src/Datastruct.f:27-179, src/Csr.f,
+ * src/EllPack.f, src/Graph.f).  Call with ja == NULL to get nad (and the
+ * ja length: nad for CSR formats, nshared*neq for ELLPACK), then again
+ * with ja sized accordingly.  ia holds neq+1 entries (2 for ELLPACK). */
+int32_t fvc_mesh_datastruc(const int32_t *id, int32_t neq, int32_t nshared,
+                           int32_t matriz, int32_t unsym, int32_t *ia,
+                           int32_t *ja, int32_t *nad, int64_t *ja_len);
+
+/* ---- face-coefficient assembly (GPU) ----------------------------------- */
+/* Pressure-correction (p') diffusion coefficients of
+ * src/CellibPressure.f:476-572 (iws = 1) with the geometry of
+ * src/Celllib.f:695-794 and src/Celllib.f:596-655, computed on the GPU one
+ * thread per cell, scattered into the matrix slots of `matriz`
+ * (src/Csr.f:142-227 / src/EllPack.f:68-93).
+ * Inputs (host): coor(2,nnode); ix(ld,numel) as for fvc_mesh_adjacency;
+ * nelcon(nshared,numel); num(numel); k(numel) the property kf per cell;
+ * d(2,numel) the SIMPLE d per cell; pin_cell (1-based, 0 = none) gets the
+ * 1e60 pressure pin of CellibPressure.f:557; int_vel selects the face
+ * interpolation (1..3 Darwish et al., 5 Ferziger-Peric).
+ * Outputs (host): ad(neq), off-diagonal values into au (CSRD/ELLPACK) in
+ * the slots of (ia, ja) built by fvc_mesh_datastruc. */
+int32_t fvc_assemble_pressure(const double *coor, int32_t nnode,
+                              const int32_t *ix, int32_t ld, int32_t numel,
+                              int32_t nshared, const int32_t *nelcon,
+                              const int32_t *num, const double *kprop,
+                              const double *dsimple, int32_t pin_cell,
+                              int32_t int_vel, int32_t matriz, int32_t unsym,
+                              const int32_t *ia, const int32_t *ja, double *ad,
+                              double *au);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,227 @@
+"""ctypes front end of the CPU restatement (test infrastructure only).
+
+Only tests/, ``__graft_entry__.smoke()`` and the CPU-baseline leg of bench.py
+load this module.  It wraps ``oracle/build/liboracle.so`` (built from
+``fvc_oracle.c`` by ``oracle/Makefile``).  All index arrays carry Fortran
+1-based values, exactly as the reference's Fortran routines see them.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "build", "liboracle.so")
+
+_i32p = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_f64p = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+
+
+class Stats(C.Structure):
+    _fields_ = [
+        ("iterations", C.c_int32),
+        ("inner_its", C.c_int32),
+        ("energy", C.c_double),
+        ("conv", C.c_double),
+        ("final_crit", C.c_double),
+        ("status", C.c_int32),
+    ]
+
+
+OK, NOCONV, UNSUPPORTED = 0, 1, 2
+
+
+def build() -> str:
+    """Compile liboracle.so with the committed Makefile."""
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+    return LIB_PATH
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(
+            os.path.join(HERE, "fvc_oracle.c")
+        ):
+            build()
+        L = C.CDLL(LIB_PATH)
+        I, D = C.c_int32, C.c_double
+        vp = C.c_void_p
+        sig = {
+            "oref_adjtria3": [vp, vp, vp, I, I, I, vp],
+            "oref_adjquad4": [vp, vp, vp, I, I, I, vp],
+            "oref_reord": [vp, vp, I, I, I],
+            "oref_adjacency_mixed": [vp, I, vp, vp, I, I, I],
+            "oref_pform_pressure": [vp, I, vp, I, I, I, vp, vp, vp, vp, I, I, I, I, vp, vp, vp,
+                                    vp],
+            "oref_numeq": [vp, vp, vp, I, I, vp],
+            "oref_datastruc": [vp, vp, vp, I, I, I, I],
+            "oref_banda_csr": [vp, vp, I],
+            "oref_assbly": [vp, vp, vp, vp, vp, vp, vp, D, vp, I, I, I, I, I],
+            "oref_matvec_csrd": [vp] * 7 + [I],
+            "oref_matvec_csr": [vp] * 7 + [I],
+            "oref_matvec_csrc": [vp] * 7 + [I],
+            "oref_matvec_csrc_sym": [vp] * 7 + [I],
+            "oref_matvec_csrd_sym": [vp] * 7 + [I],
+            "oref_matvec_ellpack": [vp] * 7 + [I],
+            "oref_dot": [vp, vp, I],
+            "oref_solver": [vp] * 7 + [I, I, I, D, I, I, I, I, C.POINTER(Stats)],
+            "oref_pcg_omp_sample": [vp] * 7 + [I, I, D, I, I, I, I, C.POINTER(Stats)],
+            "oref_smachn": [],
+            "oref_getres": [vp, vp, vp, I, I, I],
+        }
+        res = {"oref_dot": D, "oref_smachn": D, "oref_banda_csr": I, "oref_datastruc": I,
+               "oref_solver": I, "oref_pcg_omp_sample": I}
+        for name, argt in sig.items():
+            f = getattr(L, name)
+            f.argtypes = argt
+            f.restype = res.get(name, None)
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def adjacency(ix: np.ndarray, nnode: int, nen: int) -> np.ndarray:
+    """nelcon(nen, numel) from ix(nen+1, numel) (Adjacency.f)."""
+    ix = np.ascontiguousarray(ix, dtype=np.int32)
+    numel = ix.shape[0]
+    nelcon = np.zeros((numel, nen), dtype=np.int32)
+    nodcon = np.zeros(nnode, dtype=np.int32)
+    nedge = C.c_int32(0)
+    f = lib().oref_adjquad4 if nen == 4 else lib().oref_adjtria3
+    f(_p(ix), _p(nodcon), _p(nelcon), nnode, numel, nen, C.byref(nedge))
+    return nelcon
+
+
+def adjacency_mixed(ix: np.ndarray, nnode: int, nshared: int) -> np.ndarray:
+    """nelcon for meshes mixing triangles and quads (0 = unused node slot)."""
+    ix = np.ascontiguousarray(ix, dtype=np.int32)
+    numel, ld = ix.shape
+    nelcon = np.zeros((numel, nshared), dtype=np.int32)
+    nodcon = np.zeros(nnode, dtype=np.int32)
+    lib().oref_adjacency_mixed(_p(ix), ld, _p(nodcon), _p(nelcon), nnode, numel, nshared)
+    return nelcon
+
+
+def pform_pressure(coor, ix, nshared, nelcon, num, ia, ja, matriz, unsym=True, kprop=None,
+                   dsim=None, pin_cell=1, int_vel=5):
+    """(ad, au) of the pressure-correction system (CellibPressure.f)."""
+    coor = np.ascontiguousarray(coor, np.float64)
+    ix = np.ascontiguousarray(ix, np.int32)
+    numel = ix.shape[0]
+    kprop = np.ones(numel) if kprop is None else np.ascontiguousarray(kprop, np.float64)
+    dsim = np.ones((numel, 2)) if dsim is None else np.ascontiguousarray(dsim, np.float64)
+    ja = np.ascontiguousarray(ja, np.int32).ravel()
+    ad = np.zeros(numel)
+    au = np.zeros(ja.size)
+    lib().oref_pform_pressure(_p(coor), coor.shape[0], _p(ix), ix.shape[1], numel, nshared,
+                              _p(np.ascontiguousarray(nelcon, np.int32)),
+                              _p(np.ascontiguousarray(num, np.int32)), _p(kprop), _p(dsim),
+                              pin_cell, int_vel, matriz, int(unsym),
+                              _p(np.ascontiguousarray(ia, np.int32)), _p(ja), _p(ad), _p(au))
+    return ad, au
+
+
+def reord(nelcon: np.ndarray, freord: bool = True) -> np.ndarray:
+    """num(old cell) = new equation (Reord.f, RCM)."""
+    nelcon = np.ascontiguousarray(nelcon, dtype=np.int32)
+    numel, nshared = nelcon.shape
+    iperm = np.zeros(numel, dtype=np.int32)
+    lib().oref_reord(_p(nelcon), _p(iperm), numel, nshared, int(freord))
+    return iperm
+
+
+def numeq(num: np.ndarray, nelcon: np.ndarray) -> np.ndarray:
+    nelcon = np.ascontiguousarray(nelcon, dtype=np.int32)
+    numel, nshared = nelcon.shape
+    ident = np.zeros((numel, nshared), dtype=np.int32)
+    neq = C.c_int32(0)
+    lib().oref_numeq(_p(ident), _p(np.ascontiguousarray(num, np.int32)), _p(nelcon), numel,
+                     nshared, C.byref(neq))
+    return ident
+
+
+def datastruc(ident: np.ndarray, matriz: int, unsym: bool):
+    """(ia, ja, nad) for matriz 1..4 (Datastruct.f)."""
+    ident = np.ascontiguousarray(ident, dtype=np.int32)
+    neq, nshared = ident.shape
+    ia = np.zeros(2 if matriz == 4 else neq + 1, dtype=np.int32)
+    n = lib().oref_datastruc(_p(ident), _p(ia), None, neq, nshared, matriz, int(unsym))
+    ja = np.zeros(max(n, 1), dtype=np.int32)
+    nad = lib().oref_datastruc(_p(ident), _p(ia), _p(ja), neq, nshared, matriz, int(unsym))
+    if matriz == 4:
+        ja = ja.reshape(neq, nshared)
+    return ia, ja, nad
+
+
+def banda_csr(ia, ja, neq):
+    return lib().oref_banda_csr(_p(ia), _p(ja), neq)
+
+
+def dot(a, b):
+    a = np.ascontiguousarray(a, np.float64)
+    b = np.ascontiguousarray(b, np.float64)
+    return lib().oref_dot(_p(a), _p(b), a.size)
+
+
+def smachn():
+    return lib().oref_smachn()
+
+
+_MV = {
+    "csrd": "oref_matvec_csrd",
+    "csr": "oref_matvec_csr",
+    "csrc": "oref_matvec_csrc",
+    "csrc_sym": "oref_matvec_csrc_sym",
+    "csrd_sym": "oref_matvec_csrd_sym",
+    "ellpack": "oref_matvec_ellpack",
+}
+
+
+def matvec(kind, ad, au, al, x, ia, ja, neq, y=None):
+    """Call the restated Matvec.f routine with the argument order that
+    Solver.f passes (ad, au, al, x, y, ia, ja, neq)."""
+    if y is None:
+        y = np.zeros(neq, dtype=np.float64)
+    args = {
+        "csrd": (ad, au, al),
+        "csr": (ad, au, al),
+        "csrc": (ad, au, al),
+        "csrc_sym": (ad, au, al),
+        "csrd_sym": (ad, au, al),
+        "ellpack": (ad, au, al),
+    }[kind]
+    getattr(lib(), _MV[kind])(*[_p(a) for a in args], _p(x), _p(y), _p(ia), _p(ja), neq)
+    return y
+
+
+def solver(ad, au, al, x, b, iax, ja, neq, nad, unsym, tol, maxit, code, matriz,
+           omp_threads=0):
+    """Solver.f:28 restated.  x and b are updated in place (b is clobbered
+    as in the reference).  Returns (status, Stats)."""
+    st = Stats()
+    dummy = np.zeros(1, np.float64)
+    au = dummy if au is None else au
+    al = dummy if al is None else al
+    status = lib().oref_solver(_p(ad), _p(au), _p(al), _p(x), _p(b), _p(iax), _p(ja),
+                               neq, nad, int(unsym), tol, maxit, code, matriz,
+                               omp_threads, C.byref(st))
+    return status, st
+
+
+def pcg_omp_sample(ad, au, x, b, iax, ja, neq, nad, tol, maxit, matriz, nthreads,
+                   init=True):
+    st = Stats()
+    status = lib().oref_pcg_omp_sample(_p(ad), _p(au), _p(au), _p(x), _p(b), _p(iax),
+                                       _p(ja), neq, nad, tol, maxit, matriz, nthreads,
+                                       int(init), C.byref(st))
+    return status, st
