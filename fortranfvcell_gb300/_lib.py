@@ -77,6 +77,7 @@ SIGNATURES = {
     "fvc_matrix_update_values": ([P, P, P, P], I32),
     "fvc_solve": ([P, I32, P, P, F64, I32, C.POINTER(FvcOpts), C.POINTER(FvcStats)], I32),
     "fvc_spmv": ([P, P, P], I32),
+    "fvc_spmv_fast": ([P, P, P], I32),
     "fvc_spmv_f32": ([P, P, P], I32),
     "fvc_matrix_info": ([P, C.POINTER(I64), C.POINTER(I64), C.POINTER(I64), C.POINTER(I64)], I32),
     "fvc_kernel_launches": ([], I64),

@@ -72,9 +72,10 @@ void free_matrix(fvc_context *c) {
   cudaFree(A.val);
   cudaFree(A.diag);
   cudaFree(A.jac);
+  cudaFree(A.jinv);
   cudaFree(A.val32);
   cudaFree(A.diag32);
-  cudaFree(A.dscale);
+  cudaFree(A.minv32);
   cudaFree(c->d_src);
   cudaFree(c->d_raw1);
   cudaFree(c->d_raw2);
@@ -210,6 +211,8 @@ int32_t upload_raw(fvc_context *c, const double *ad, const double *au, const dou
             cudaSuccess)
       return FVC_ERR_CUDA;
   }
+  rc = fvc::launch_reciprocal(c->A, s);
+  if (rc != FVC_OK) return rc;
   c->A.have32 = false;  // FP32 copy is rebuilt lazily from the new values
   return FVC_OK;
 }
@@ -259,10 +262,8 @@ int32_t fvc_context_destroy(fvc_context *c) {
   if (!c) return FVC_ERR_ARG;
   cudaSetDevice(c->device);
   free_matrix(c);
-  for (int i = 0; i < 8; ++i) {
-    cudaFree(c->S.v[i]);
-    cudaFree(c->S.f[i]);
-  }
+  for (int i = 0; i < 8; ++i) cudaFree(c->S.v[i]);
+  for (int i = 0; i < 9; ++i) cudaFree(c->S.f[i]);
   cudaFree(c->S.g);
   cudaFree(c->S.partials);
   cudaFree(c->S.sync);
@@ -339,6 +340,7 @@ int32_t fvc_matrix_set(fvc_context *c, int32_t matriz, int32_t unsym, int32_t ne
             cudaMalloc(&A.col, sizeof(int32_t) * sl) == cudaSuccess &&
             cudaMalloc(&A.val, sizeof(double) * sl) == cudaSuccess &&
             cudaMalloc(&A.jac, sizeof(double) * n) == cudaSuccess &&
+            cudaMalloc(&A.jinv, sizeof(double) * n) == cudaSuccess &&
             cudaMalloc(&c->d_src, sizeof(int32_t) * sl) == cudaSuccess;
   if (ok && diag_mode != fvc::DIAG_NONE) ok = cudaMalloc(&A.diag, sizeof(double) * n) == cudaSuccess;
   c->raw1_which = raw1;
@@ -399,6 +401,11 @@ int32_t fvc_matrix_info(const fvc_context *c, int64_t *n, int64_t *slots, int64_
 int32_t fvc_spmv(fvc_context *c, const double *d_x, double *d_y) {
   if (!c || !c->has_matrix || !d_x || !d_y) return FVC_ERR_ARG;
   return fvc::launch_spmv(c->A, d_x, d_y, c->stream);
+}
+
+int32_t fvc_spmv_fast(fvc_context *c, const double *d_x, double *d_y) {
+  if (!c || !c->has_matrix || !d_x || !d_y) return FVC_ERR_ARG;
+  return fvc::launch_spmv(c->A, d_x, d_y, c->stream, true);
 }
 
 int32_t fvc_spmv_f32(fvc_context *c, const float *d_x, float *d_y) {

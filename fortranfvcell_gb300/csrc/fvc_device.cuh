@@ -32,14 +32,21 @@ struct SellView {
   int diag_mode;
 };
 
-// Scalars of one solve that every block computes identically from the
-// same reduction partials.
+// Grid synchronisation state of one persistent launch.  `count` is a
+// monotonically increasing arrival counter (episode e completes when it
+// reaches e * nblocks, so it never needs resetting inside the launch);
+// `flag` holds the last released episode.  Partials and totals rotate over
+// four slots so a block running ahead never overwrites data still read.
 struct GridSync {
-  unsigned int *count;   // arrival counter
-  unsigned int *gen;     // generation
-  int *err;              // sticky error (FVC_ERR_TIMEOUT on a stuck wait)
+  unsigned int *count;
+  unsigned int *flag;
+  int *err;                // sticky error (FVC_ERR_TIMEOUT on a stuck wait)
+  double *partials;        // 4 slots x kMaxNV x nblocks
+  double *totals;          // 4 slots x kMaxNV
   unsigned int nblocks;
 };
+
+constexpr int kMaxNV = 4;
 
 __device__ __forceinline__ uint64_t global_ns() {
   uint64_t t;
@@ -47,52 +54,28 @@ __device__ __forceinline__ uint64_t global_ns() {
   return t;
 }
 
-// Grid-wide barrier for a cooperative (co-resident) launch.  The wait is
-// bounded: after kBarrierTimeoutNs the block records FVC_ERR_TIMEOUT and
-// leaves; every other waiter sees the flag and leaves too, so a broken
-// launch returns an error instead of spinning.  Returns false on error.
-constexpr uint64_t kBarrierTimeoutNs = 4000000000ull;  // 4 s
-
-__device__ __forceinline__ bool grid_barrier(const GridSync &gs) {
-  __syncthreads();
-  __shared__ int s_ok;
-  if (threadIdx.x == 0) {
-    volatile unsigned int *vgen = gs.gen;
-    volatile int *verr = gs.err;
-    unsigned int my_gen = *vgen;
-    __threadfence();
-    unsigned int arrived = atomicAdd(gs.count, 1u);
-    if (arrived == gs.nblocks - 1) {
-      *gs.count = 0;
-      __threadfence();
-      atomicAdd(gs.gen, 1u);
-    } else {
-      uint64_t t0 = global_ns();
-      unsigned int spins = 0;
-      while (*vgen == my_gen) {
-        if (*verr != 0) break;
-        if ((++spins & 63u) == 0 && global_ns() - t0 > kBarrierTimeoutNs) {
-          atomicExch(gs.err, 7 /* FVC_ERR_TIMEOUT */);
-          break;
-        }
-        __nanosleep(64);
-      }
-    }
-    __threadfence();
-    s_ok = (*verr == 0);
-  }
-  __syncthreads();
-  return s_ok != 0;
+__device__ __forceinline__ unsigned int atom_add_acq_rel(unsigned int *p, unsigned int v) {
+  unsigned int old;
+  asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+  return old;
 }
+__device__ __forceinline__ void st_release(unsigned int *p, unsigned int v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ unsigned int ld_acquire(const unsigned int *p) {
+  unsigned int v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Every wait is bounded: after kBarrierTimeoutNs the block records
+// FVC_ERR_TIMEOUT and leaves; the other waiters see the flag and leave too,
+// so a broken launch returns an error instead of spinning.
+constexpr uint64_t kBarrierTimeoutNs = 4000000000ull;  // 4 s
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v = __dadd_rn(v, __shfl_down_sync(0xffffffffu, v, o));
-  return v;
-}
-__device__ __forceinline__ float warp_sum(float v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
   return v;
 }
 
@@ -118,24 +101,69 @@ __device__ __forceinline__ void block_sum(double (&v)[NV], double *red) {
   __syncthreads();
 }
 
-// Sum of the per-block partials of NV reductions, read after a barrier.
-// Every block runs the same fixed-order sum, so all blocks obtain the
-// same bits without a broadcast.  Result valid in all threads.
+// Grid-wide barrier (NV == 0) or deterministic all-reduce of NV doubles
+// per thread.  One arrival atomic per block; the last block to arrive sums
+// the per-block partials in block order (the same order whichever block is
+// last) and releases the others, which then read the NV totals.  Returns
+// false, with gs.err set, when a wait exceeded its bound.
 template <int NV>
-__device__ __forceinline__ void grid_total(const double *partials, int nblocks,
-                                           double (&out)[NV], double *sh) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (warp < NV) {
-    const double *p = partials + (size_t)warp * nblocks;
-    double t = 0.0;
-    for (int b = lane; b < nblocks; b += 32) t = __dadd_rn(t, __ldcg(p + b));
-    t = warp_sum(t);
-    if (lane == 0) sh[warp] = t;
+__device__ __forceinline__ bool grid_allreduce(const GridSync &gs, unsigned int &episode,
+                                               double (&v)[NV > 0 ? NV : 1], double *red) {
+  __shared__ int s_last, s_ok;
+  if (NV > 0) {
+    block_sum<(NV > 0 ? NV : 1)>(v, red);
+  } else {
+    __syncthreads();
+  }
+  const unsigned int ep = ++episode;
+  const unsigned int nb = gs.nblocks;
+  double *part = gs.partials + (size_t)(ep & 3u) * kMaxNV * nb;
+  double *tot = gs.totals + (ep & 3u) * kMaxNV;
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int q = 0; q < NV; ++q) part[(size_t)q * nb + blockIdx.x] = v[q];
+    const unsigned int old = atom_add_acq_rel(gs.count, 1u);
+    s_last = (old == ep * nb - 1u);
+    s_ok = 1;
   }
   __syncthreads();
-#pragma unroll
-  for (int q = 0; q < NV; ++q) out[q] = sh[q];
+  if (s_last) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (NV > 0 && warp < NV) {
+      const double *p = part + (size_t)warp * nb;
+      double t = 0.0;
+      for (unsigned int b = lane; b < nb; b += 32) t = __dadd_rn(t, __ldcg(p + b));
+      t = warp_sum(t);
+      if (lane == 0) __stcg(tot + warp, t);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) st_release(gs.flag, ep);
+  } else if (threadIdx.x == 0) {
+    const uint64_t t0 = global_ns();
+    unsigned int spins = 0;
+    while (ld_acquire(gs.flag) < ep) {
+      if (*(volatile int *)gs.err != 0) {
+        s_ok = 0;
+        break;
+      }
+      if ((++spins & 255u) == 0 && global_ns() - t0 > kBarrierTimeoutNs) {
+        atomicExch(gs.err, 7 /* FVC_ERR_TIMEOUT */);
+        s_ok = 0;
+        break;
+      }
+      __nanosleep(20);
+    }
+  }
   __syncthreads();
+  if (!s_ok) return false;
+#pragma unroll
+  for (int q = 0; q < NV; ++q) v[q] = __ldcg(tot + q);
+  return true;
+}
+
+__device__ __forceinline__ bool grid_barrier(const GridSync &gs, unsigned int &episode) {
+  double none[1];
+  return grid_allreduce<0>(gs, episode, none, nullptr);
 }
 
 // Streaming loads of read-only matrix data (never written by the kernel
@@ -156,8 +184,17 @@ __device__ __forceinline__ float ld_stream(const float *p) {
   return v;
 }
 
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
 // y_row = (A x)_row for the lane's row of slice s, with x supplied by a
-// functor (so callers can form x on the fly, e.g. p = z + beta*p).
+// functor (so callers can form x on the fly, e.g. p = z + beta*p).  Rows
+// of width <= 4 (every cell of a triangle/quad mesh) issue all value and
+// column loads before the gathers, so a warp has 8 independent streaming
+// loads in flight per slice.
 // Reference order: DIAG_FIRST  t = ad*x_i; t = t + a_k*x_k ...  (csrd)
 //                  DIAG_LAST   t = a_1x_1 + ... + a_wx_w + ad*x_i (ellpack)
 //                  DIAG_NONE   t = 0 + a_k*x_k ...                 (csr)
@@ -166,27 +203,109 @@ __device__ __forceinline__ double sell_row_f64(const SellView<double> &A, int s,
                                                int lane, int row, XF xf) {
   const int64_t base = A.sptr[s];
   const int w = (int)((A.sptr[s + 1] - base) >> 5);
-  double t;
-  double xd = 0.0;
-  if (A.diag_mode != DIAG_NONE) xd = __dmul_rn(ld_stream(A.diag + row), xf(row));
-  if (A.diag_mode == DIAG_FIRST) {
-    t = xd;
-  } else {
-    t = 0.0;
-  }
   const int *cp = A.col + base + lane;
   const double *vp = A.val + base + lane;
+  double xd = 0.0;
+  if (A.diag_mode != DIAG_NONE) xd = __dmul_rn(ld_stream(A.diag + row), xf(row));
+  double t = (A.diag_mode == DIAG_FIRST) ? xd : 0.0;
+  if (w <= 4) {
+    int c[4];
+    double a[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      c[k] = (k < w) ? ld_stream(cp + 32 * k) : 0;
+      a[k] = (k < w) ? ld_stream(vp + 32 * k) : 0.0;
+    }
+    if (A.diag_mode == DIAG_LAST) {
+      // the reference's ELLPACK sums t1+t2+...+tw+t_diag left to right
+      if (w > 0) t = __dmul_rn(a[0], xf(c[0]));
+#pragma unroll
+      for (int k = 1; k < 4; ++k)
+        if (k < w) t = __dadd_rn(t, __dmul_rn(a[k], xf(c[k])));
+      return __dadd_rn(t, xd);
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      if (k < w) t = __dadd_rn(t, __dmul_rn(a[k], xf(c[k])));
+    return t;
+  }
   if (A.diag_mode == DIAG_LAST) {
-    // the reference's ELLPACK sums t1+t2+...+tw+t_diag left to right
-    if (w > 0) t = __dmul_rn(ld_stream(vp), xf(ld_stream(cp)));
+    t = __dmul_rn(ld_stream(vp), xf(ld_stream(cp)));
     for (int k = 1; k < w; ++k)
       t = __dadd_rn(t, __dmul_rn(ld_stream(vp + 32 * k), xf(ld_stream(cp + 32 * k))));
-    t = __dadd_rn(t, xd);
-  } else {
-    for (int k = 0; k < w; ++k)
-      t = __dadd_rn(t, __dmul_rn(ld_stream(vp + 32 * k), xf(ld_stream(cp + 32 * k))));
+    return __dadd_rn(t, xd);
   }
+  for (int k = 0; k < w; ++k)
+    t = __dadd_rn(t, __dmul_rn(ld_stream(vp + 32 * k), xf(ld_stream(cp + 32 * k))));
   return t;
+}
+
+// The same row sum with fused multiply-adds (one FP64 instruction per
+// term instead of two; GB300's FP64 pipe, ~1/64 of its FP32 rate, is the
+// bottleneck of the FP64 solvers).  Terms are added in the same order.
+template <typename XF>
+__device__ __forceinline__ double sell_row_fma(const SellView<double> &A, int s, int lane,
+                                               int row, XF xf) {
+  const int64_t base = A.sptr[s];
+  const int w = (int)((A.sptr[s + 1] - base) >> 5);
+  const int *cp = A.col + base + lane;
+  const double *vp = A.val + base + lane;
+  const bool has_diag = A.diag_mode != DIAG_NONE;
+  const double dv = has_diag ? ld_stream(A.diag + row) : 0.0;
+  const double xi = has_diag ? xf(row) : 0.0;
+  double t = (A.diag_mode == DIAG_FIRST) ? dv * xi : 0.0;
+  if (w <= 4) {
+    int c[4];
+    double a[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      c[k] = (k < w) ? ld_stream(cp + 32 * k) : 0;
+      a[k] = (k < w) ? ld_stream(vp + 32 * k) : 0.0;
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      if (k < w) t = fma(a[k], xf(c[k]), t);
+  } else {
+    for (int k = 0; k < w; ++k) t = fma(ld_stream(vp + 32 * k), xf(ld_stream(cp + 32 * k)), t);
+  }
+  if (A.diag_mode == DIAG_LAST) t = fma(dv, xi, t);
+  return t;
+}
+
+// Host side: scratch for the grid synchronisation of a persistent launch.
+inline int32_t ensure_sync(Scratch &S, size_t nblocks) {
+  const size_t need = 4 * kMaxNV * nblocks + 4 * kMaxNV;
+  if (S.npart < need) {
+    if (S.partials) cudaFree(S.partials);
+    S.partials = nullptr;
+    if (cudaMalloc(&S.partials, sizeof(double) * need) != cudaSuccess) return FVC_ERR_CUDA;
+    S.npart = need;
+  }
+  if (!S.sync) {
+    if (cudaMalloc(&S.sync, 64) != cudaSuccess) return FVC_ERR_CUDA;
+    if (cudaMalloc(&S.err, 64) != cudaSuccess) return FVC_ERR_CUDA;
+    if (cudaMalloc(&S.result, 16 * sizeof(double)) != cudaSuccess) return FVC_ERR_CUDA;
+    if (cudaMalloc(&S.iresult, 16 * sizeof(int)) != cudaSuccess) return FVC_ERR_CUDA;
+  }
+  return FVC_OK;
+}
+
+inline GridSync make_sync(const Scratch &S, int nblocks) {
+  GridSync g;
+  g.count = S.sync;
+  g.flag = S.sync + 8;  // separate 32-byte sector from the counter
+  g.err = S.err;
+  g.partials = S.partials;
+  g.totals = S.partials + 4 * kMaxNV * (size_t)nblocks;
+  g.nblocks = (unsigned int)nblocks;
+  return g;
+}
+
+inline void reset_sync(Scratch &S, cudaStream_t stream) {
+  cudaMemsetAsync(S.sync, 0, 64, stream);
+  cudaMemsetAsync(S.err, 0, 64, stream);
+  cudaMemsetAsync(S.iresult, 0, 16 * sizeof(int), stream);
+  cudaMemsetAsync(S.result, 0, 16 * sizeof(double), stream);
 }
 
 }  // namespace fvc

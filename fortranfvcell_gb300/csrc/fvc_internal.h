@@ -23,10 +23,12 @@ struct DeviceMatrix {
   double *val = nullptr;
   double *diag = nullptr;  // ad (null for DIAG_NONE)
   double *jac = nullptr;   // Jacobi m (the reference's m = ad)
-  // FP32 Jacobi-scaled copy for mixed precision: S = D^-1/2 A D^-1/2
-  float *val32 = nullptr;
-  float *diag32 = nullptr;  // scaled diagonal (1 except for zero rows)
-  double *dscale = nullptr; // D^-1/2 (FP64)
+  double *jinv = nullptr;  // 1/m (FP64), computed once per value upload
+  // FP32 operator for mixed precision in difference form:
+  //   (A x)_i = e_i x_i + sum_k w_ik (x_i - x_k),  w = -a_ik, e_i = a_ii - sum w
+  float *val32 = nullptr;   // w per slot (0 on padding and on a diagonal slot)
+  float *diag32 = nullptr;  // e per row (clamped to +-1e30)
+  float *minv32 = nullptr;  // Jacobi 1/m per row (0 for |m| beyond FP32)
   bool have32 = false;
   // host-side description of the source layout, for value updates
   int matriz = 0, unsym = 0, nad = 0;
@@ -37,7 +39,7 @@ struct DeviceMatrix {
 struct Scratch {
   size_t n = 0, nf = 0, ngmres = 0;  // capacities of v[], f[], g
   double *v[8] = {nullptr};     // Krylov vectors
-  float *f[8] = {nullptr};      // FP32 vectors (mixed precision)
+  float *f[9] = {nullptr};      // FP32 vectors (mixed precision)
   double *g = nullptr;          // GMRES basis (k+1) x n
   double *partials = nullptr;   // reduction partials
   size_t npart = 0;
@@ -69,7 +71,8 @@ int32_t run_mixed(const DeviceMatrix &A, Scratch &S, int code, const double *b,
                   double *x, double tol, int maxit, int init, const fvc_opts &o,
                   cudaStream_t stream, fvc_stats *st);
 int32_t launch_spmv(const DeviceMatrix &A, const double *x, double *y,
-                    cudaStream_t stream);
+                    cudaStream_t stream, bool fused = false);
+int32_t launch_reciprocal(const DeviceMatrix &A, cudaStream_t stream);
 int32_t launch_spmv_f32(const DeviceMatrix &A, const float *x, float *y,
                         cudaStream_t stream);
 int32_t build_f32_copy(DeviceMatrix &A, cudaStream_t stream);

@@ -13,9 +13,13 @@
 //   pbicgstab  Iterativos.f:140-234  (5 barriers per iteration)
 //   gmres      Iterativos.f:271-446  (restarted, k = 15, modified
 //              Gram-Schmidt, Givens rotations)
-// Products, sums and divisions of the vector updates are rounded as the
-// Fortran statements round them (no FMA contraction); only the dot
-// products differ, being tree sums in a fixed (deterministic) order.
+// The arithmetic follows the Fortran statements term by term, with two
+// GB300-motivated substitutions: products and sums are fused (FMA), and the
+// Jacobi division r/m is a multiplication by 1/m computed once per matrix.
+// GB300 executes FP64 at ~1/64 of its FP32 rate, and these two changes
+// roughly halve the FP64 instructions per row; they move results only at
+// rounding level, like the dot products, which are tree sums in a fixed
+// (deterministic) order instead of the reference's sequential sums.
 #include <cmath>
 #include <cstdio>
 #include <vector>
@@ -30,11 +34,11 @@ namespace {
 struct KArgs {
   SellView<double> A;
   const double *m;
+  const double *minv;
   const double *b;
   double *x;
   double *v0, *v1, *v2, *v3, *v4, *v5, *v6;
   double *g;  // GMRES basis
-  double *partials;
   GridSync gs;
   double tol;
   int maxit;
@@ -62,36 +66,10 @@ struct Part {
   for (int s_ = (P).sb + (P).warp; s_ < (P).se; s_ += (P).nwarps) \
     for (int row = s_ * 32 + (P).lane, once_ = 1; once_ && row < (P).n; once_ = 0)
 
-constexpr int kMaxNV = 4;
-
-// Rotating partial buffers: reduction r uses slot r % 4, so a block that
-// runs ahead never overwrites partials that a slower block still reads.
-__device__ __forceinline__ double *slot(const KArgs &a, int rot, int q) {
-  return a.partials + ((size_t)(rot & 3) * kMaxNV + q) * gridDim.x;
-}
-
 template <int NV>
-__device__ __forceinline__ bool reduce(const KArgs &a, int &rot, double (&v)[NV],
-                                       double *red, double *tot) {
-  block_sum<NV>(v, red);
-  if (threadIdx.x == 0)
-#pragma unroll
-    for (int q = 0; q < NV; ++q) slot(a, rot, q)[blockIdx.x] = v[q];
-  if (!grid_barrier(a.gs)) return false;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (warp < NV) {
-    const double *p = slot(a, rot, warp);
-    double t = 0.0;
-    for (int b = lane; b < (int)gridDim.x; b += 32) t = __dadd_rn(t, __ldcg(p + b));
-    t = warp_sum(t);
-    if (lane == 0) tot[warp] = t;
-  }
-  __syncthreads();
-#pragma unroll
-  for (int q = 0; q < NV; ++q) v[q] = tot[q];
-  __syncthreads();
-  ++rot;
-  return true;
+__device__ __forceinline__ bool reduce(const KArgs &a, unsigned int &ep, double (&v)[NV],
+                                       double *red) {
+  return grid_allreduce<NV>(a.gs, ep, v, red);
 }
 
 __device__ __forceinline__ void finish(const KArgs &a, int iters, int status,
@@ -107,20 +85,20 @@ __device__ __forceinline__ void finish(const KArgs &a, int iters, int status,
 
 // Energy norm x.Ax and the FP64 residual ||b-Ax||^2, ||b||^2 in one pass
 // (x must be complete at every row: called right after a grid barrier).
-__device__ __forceinline__ bool epilogue(const KArgs &a, int &rot, double *red,
-                                         double *tot, bool energy_xb) {
+__device__ __forceinline__ bool epilogue(const KArgs &a, unsigned int &ep, double *red,
+                                         bool energy_xb) {
   const Part P(a.A.nslices, a.A.n);
   double acc[3] = {0.0, 0.0, 0.0};
   const double *x = a.x;
   FOR_ROWS(P) {
-    double ax = sell_row_f64(a.A, s_, P.lane, row, [&](int k) { return x[k]; });
+    double ax = sell_row_fma(a.A, s_, P.lane, row, [&](int k) { return x[k]; });
     double xi = x[row], bi = a.b[row];
-    double rr = __dsub_rn(bi, ax);
-    acc[0] = __dadd_rn(acc[0], __dmul_rn(xi, energy_xb ? bi : ax));
-    acc[1] = __dadd_rn(acc[1], __dmul_rn(rr, rr));
-    acc[2] = __dadd_rn(acc[2], __dmul_rn(bi, bi));
+    double rr = bi - ax;
+    acc[0] = fma(xi, energy_xb ? bi : ax, acc[0]);
+    acc[1] = fma(rr, rr, acc[1]);
+    acc[2] = fma(bi, bi, acc[2]);
   }
-  if (!reduce<3>(a, rot, acc, red, tot)) return false;
+  if (!reduce<3>(a, ep, acc, red)) return false;
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     a.result[0] = acc[0];
     a.result[3] = acc[1];
@@ -133,13 +111,12 @@ __device__ __forceinline__ bool epilogue(const KArgs &a, int &rot, double *red,
 // PCG (Iterativos.f:29-106).  v0 = r, v1 = z, v2/v3 = p (double buffer),
 // v4 = q (the reference's z = A p).
 // ---------------------------------------------------------------------
-__global__ void __launch_bounds__(256) pcg_f64(KArgs a) {
+__global__ void __launch_bounds__(1024, 1) pcg_f64(KArgs a) {
   __shared__ double red[kMaxNV * 32];
-  __shared__ double tot[kMaxNV];
   const Part P(a.A.nslices, a.A.n);
   double *r = a.v0, *z = a.v1, *q = a.v4, *x = a.x;
-  const double *m = a.m, *b = a.b;
-  int rot = 0;
+  const double *minv = a.minv, *b = a.b;
+  unsigned int ep = 0;
   double acc[2];
 
   // r = b - A x ; z = r/m ; p = z ; d = r.z  (x = 0 when init)
@@ -148,19 +125,19 @@ __global__ void __launch_bounds__(256) pcg_f64(KArgs a) {
   FOR_ROWS(P) {
     double ax;
     if (a.init) {
-      ax = sell_row_f64(a.A, s_, P.lane, row, [&](int) { return 0.0; });
+      ax = 0.0;
       x[row] = 0.0;
     } else {
-      ax = sell_row_f64(a.A, s_, P.lane, row, [&](int k) { return x[k]; });
+      ax = sell_row_fma(a.A, s_, P.lane, row, [&](int k) { return x[k]; });
     }
-    double ri = __dsub_rn(b[row], ax);
-    double zi = __ddiv_rn(ri, m[row]);
+    const double ri = b[row] - ax;
+    const double zi = ri * minv[row];
     r[row] = ri;
     a.v2[row] = zi;
-    acc[0] = __dadd_rn(acc[0], __dmul_rn(ri, zi));
-    acc[1] = __dadd_rn(acc[1], __dmul_rn(b[row], b[row]));
+    acc[0] = fma(ri, zi, acc[0]);
+    acc[1] = fma(b[row], b[row], acc[1]);
   }
-  if (!reduce<2>(a, rot, acc, red, tot)) return;
+  if (!reduce<2>(a, ep, acc, red)) return;
   double d = acc[0];
   const double bnorm2 = acc[1];
   const double conv = (a.stop_rule == 0) ? a.tol * sqrt(fabs(d)) : a.tol * sqrt(bnorm2);
@@ -174,39 +151,38 @@ __global__ void __launch_bounds__(256) pcg_f64(KArgs a) {
     if (j == 1) {
       FOR_ROWS(P) {
         const double *pc = pcur;
-        double qi = sell_row_f64(a.A, s_, P.lane, row, [&](int k) { return pc[k]; });
+        const double qi = sell_row_fma(a.A, s_, P.lane, row, [&](int k) { return pc[k]; });
         q[row] = qi;
-        pq[0] = __dadd_rn(pq[0], __dmul_rn(pc[row], qi));
+        pq[0] = fma(pc[row], qi, pq[0]);
       }
     } else {
       FOR_ROWS(P) {
         const double *pp = pprev;
-        auto pf = [&](int k) { return __dadd_rn(z[k], __dmul_rn(beta, pp[k])); };
-        double pi = pf(row);
+        auto pf = [&](int k) { return fma(beta, pp[k], z[k]); };
+        const double pi = pf(row);
         pcur[row] = pi;
-        double qi = sell_row_f64(a.A, s_, P.lane, row, pf);
+        const double qi = sell_row_fma(a.A, s_, P.lane, row, pf);
         q[row] = qi;
-        pq[0] = __dadd_rn(pq[0], __dmul_rn(pi, qi));
+        pq[0] = fma(pi, qi, pq[0]);
       }
     }
-    if (!reduce<1>(a, rot, pq, red, tot)) return;
-    const double alpha = __ddiv_rn(d, pq[0]);
+    if (!reduce<1>(a, ep, pq, red)) return;
+    const double alpha = d / pq[0];
     // x += alpha p ; r -= alpha q ; z = r/m ; r.z (and r.r for stop_rule 1)
     acc[0] = 0.0;
     acc[1] = 0.0;
     FOR_ROWS(P) {
-      double pi = pcur[row];
-      x[row] = __dadd_rn(x[row], __dmul_rn(alpha, pi));
-      double ri = __dsub_rn(r[row], __dmul_rn(alpha, q[row]));
-      double zi = __ddiv_rn(ri, m[row]);
+      x[row] = fma(alpha, pcur[row], x[row]);
+      const double ri = fma(-alpha, q[row], r[row]);
+      const double zi = ri * minv[row];
       r[row] = ri;
       z[row] = zi;
-      acc[0] = __dadd_rn(acc[0], __dmul_rn(ri, zi));
-      acc[1] = __dadd_rn(acc[1], __dmul_rn(ri, ri));
+      acc[0] = fma(ri, zi, acc[0]);
+      acc[1] = fma(ri, ri, acc[1]);
     }
-    if (!reduce<2>(a, rot, acc, red, tot)) return;
-    beta = __ddiv_rn(acc[0], d);
-    d = __dmul_rn(beta, d);
+    if (!reduce<2>(a, ep, acc, red)) return;
+    beta = acc[0] / d;
+    d = beta * d;
     crit = (a.stop_rule == 0) ? sqrt(fabs(d)) : sqrt(acc[1]);
     if (!(crit == crit) || isinf(d)) {
       status = FVC_ERR_NAN;
@@ -221,21 +197,20 @@ __global__ void __launch_bounds__(256) pcg_f64(KArgs a) {
     status = FVC_ERR_NOCONV;
   }
   finish(a, j, status, conv, crit, 0);
-  epilogue(a, rot, red, tot, false);
+  epilogue(a, ep, red, false);
 }
 
 // ---------------------------------------------------------------------
 // BiCGSTAB (Iterativos.f:140-234).  v0 = r (shadow r0), v1 = s (the
 // reference's b), v2 = p, v3 = z, v4 = v, v5 = t.
 // ---------------------------------------------------------------------
-__global__ void __launch_bounds__(256) bicgstab_f64(KArgs a) {
+__global__ void __launch_bounds__(1024, 1) bicgstab_f64(KArgs a) {
   __shared__ double red[kMaxNV * 32];
-  __shared__ double tot[kMaxNV];
   const Part P(a.A.nslices, a.A.n);
   double *r = a.v0, *sv = a.v1, *p = a.v2, *z = a.v3, *v = a.v4, *t = a.v5;
   double *x = a.x;
-  const double *m = a.m, *b = a.b;
-  int rot = 0;
+  const double *minv = a.minv, *b = a.b;
+  unsigned int ep = 0;
   double acc[2];
 
   acc[0] = 0.0;
@@ -243,21 +218,21 @@ __global__ void __launch_bounds__(256) bicgstab_f64(KArgs a) {
   FOR_ROWS(P) {
     double ax;
     if (a.init) {
-      ax = sell_row_f64(a.A, s_, P.lane, row, [&](int) { return 0.0; });
+      ax = 0.0;
       x[row] = 0.0;
     } else {
-      ax = sell_row_f64(a.A, s_, P.lane, row, [&](int k) { return x[k]; });
+      ax = sell_row_fma(a.A, s_, P.lane, row, [&](int k) { return x[k]; });
     }
-    double ri = __dsub_rn(b[row], ax);
+    const double ri = b[row] - ax;
     r[row] = ri;
     p[row] = ri;
     sv[row] = ri;
-    double zi = __ddiv_rn(ri, m[row]);
+    const double zi = ri * minv[row];
     z[row] = zi;
-    acc[0] = __dadd_rn(acc[0], __dmul_rn(ri, zi));
-    acc[1] = __dadd_rn(acc[1], __dmul_rn(b[row], b[row]));
+    acc[0] = fma(ri, zi, acc[0]);
+    acc[1] = fma(b[row], b[row], acc[1]);
   }
-  if (!reduce<2>(a, rot, acc, red, tot)) return;
+  if (!reduce<2>(a, ep, acc, red)) return;
   const double d = acc[0];
   const double bnorm2 = acc[1];
   const double conv = (a.stop_rule == 0) ? a.tol * sqrt(fabs(d)) : a.tol * sqrt(bnorm2);
@@ -268,68 +243,68 @@ __global__ void __launch_bounds__(256) bicgstab_f64(KArgs a) {
     acc[0] = 0.0;
     acc[1] = 0.0;
     FOR_ROWS(P) {
-      double vi = sell_row_f64(a.A, s_, P.lane, row, [&](int k) { return z[k]; });
+      const double vi = sell_row_fma(a.A, s_, P.lane, row, [&](int k) { return z[k]; });
       v[row] = vi;
-      double ri = r[row];
-      acc[0] = __dadd_rn(acc[0], __dmul_rn(sv[row], ri));
-      acc[1] = __dadd_rn(acc[1], __dmul_rn(vi, ri));
+      const double ri = r[row];
+      acc[0] = fma(sv[row], ri, acc[0]);
+      acc[1] = fma(vi, ri, acc[1]);
     }
-    if (!reduce<2>(a, rot, acc, red, tot)) return;
+    if (!reduce<2>(a, ep, acc, red)) return;
     const double rr0 = acc[0];
-    const double alpha = __ddiv_rn(rr0, acc[1]);
+    const double alpha = rr0 / acc[1];
     // x += alpha z ; s -= alpha v ; z = s/m
     FOR_ROWS(P) {
-      x[row] = __dadd_rn(x[row], __dmul_rn(alpha, z[row]));
-      double si = __dsub_rn(sv[row], __dmul_rn(alpha, v[row]));
+      x[row] = fma(alpha, z[row], x[row]);
+      const double si = fma(-alpha, v[row], sv[row]);
       sv[row] = si;
-      z[row] = __ddiv_rn(si, m[row]);
+      z[row] = si * minv[row];
     }
-    if (!grid_barrier(a.gs)) return;
+    if (!grid_barrier(a.gs, ep)) return;
     // t = A z ; t.s ; t.t
     acc[0] = 0.0;
     acc[1] = 0.0;
     FOR_ROWS(P) {
-      double ti = sell_row_f64(a.A, s_, P.lane, row, [&](int k) { return z[k]; });
+      const double ti = sell_row_fma(a.A, s_, P.lane, row, [&](int k) { return z[k]; });
       t[row] = ti;
-      acc[0] = __dadd_rn(acc[0], __dmul_rn(ti, sv[row]));
-      acc[1] = __dadd_rn(acc[1], __dmul_rn(ti, ti));
+      acc[0] = fma(ti, sv[row], acc[0]);
+      acc[1] = fma(ti, ti, acc[1]);
     }
-    if (!reduce<2>(a, rot, acc, red, tot)) return;
-    const double w = __ddiv_rn(acc[0], acc[1]);
+    if (!reduce<2>(a, ep, acc, red)) return;
+    const double w = acc[0] / acc[1];
     // x += w z ; s -= w t ; s.z ; r.s (and s.s for stop_rule 1)
     double acc3[3] = {0.0, 0.0, 0.0};
     FOR_ROWS(P) {
-      double zi = z[row];
-      x[row] = __dadd_rn(x[row], __dmul_rn(w, zi));
-      double si = __dsub_rn(sv[row], __dmul_rn(w, t[row]));
+      const double zi = z[row];
+      x[row] = fma(w, zi, x[row]);
+      const double si = fma(-w, t[row], sv[row]);
       sv[row] = si;
-      acc3[0] = __dadd_rn(acc3[0], __dmul_rn(si, zi));
-      acc3[1] = __dadd_rn(acc3[1], __dmul_rn(r[row], si));
-      acc3[2] = __dadd_rn(acc3[2], __dmul_rn(si, si));
+      acc3[0] = fma(si, zi, acc3[0]);
+      acc3[1] = fma(r[row], si, acc3[1]);
+      acc3[2] = fma(si, si, acc3[2]);
     }
-    if (!reduce<3>(a, rot, acc3, red, tot)) return;
-    double beta = __ddiv_rn(acc3[0], d);
+    if (!reduce<3>(a, ep, acc3, red)) return;
+    double beta = acc3[0] / d;
     crit = (a.stop_rule == 0) ? sqrt(fabs(beta)) : sqrt(acc3[2]);
     if (!(crit == crit) || !(w == w)) {
       status = FVC_ERR_NAN;
       break;
     }
     if (crit < conv) break;
-    beta = __dmul_rn(__ddiv_rn(acc3[1], rr0), __ddiv_rn(alpha, w));
+    beta = (acc3[1] / rr0) * (alpha / w);
     // p = s + beta (p - w v) ; z = p/m
     FOR_ROWS(P) {
-      double pi = __dadd_rn(sv[row], __dmul_rn(beta, __dsub_rn(p[row], __dmul_rn(w, v[row]))));
+      const double pi = fma(beta, fma(-w, v[row], p[row]), sv[row]);
       p[row] = pi;
-      z[row] = __ddiv_rn(pi, m[row]);
+      z[row] = pi * minv[row];
     }
-    if (!grid_barrier(a.gs)) return;
+    if (!grid_barrier(a.gs, ep)) return;
   }
   if (j > a.maxit) {
     j = a.maxit;
     status = FVC_ERR_NOCONV;
   }
   finish(a, j, status, conv, crit, 0);
-  epilogue(a, rot, red, tot, false);
+  epilogue(a, ep, red, false);
 }
 
 // ---------------------------------------------------------------------
@@ -339,29 +314,28 @@ __global__ void __launch_bounds__(256) bicgstab_f64(KArgs a) {
 // ---------------------------------------------------------------------
 constexpr int kGmresK = 15;
 
-__global__ void __launch_bounds__(256) gmres_f64(KArgs a) {
+__global__ void __launch_bounds__(1024, 1) gmres_f64(KArgs a) {
   __shared__ double red[kMaxNV * 32];
-  __shared__ double tot[kMaxNV];
   __shared__ double h[(kGmresK + 1) * kGmresK];
   __shared__ double cc[kGmresK], ss[kGmresK], e[kGmresK + 1], y[kGmresK];
   const Part P(a.A.nslices, a.A.n);
   const int n = a.A.n;
   const int k = kGmresK;
   double *x = a.x;
-  const double *m = a.m, *b = a.b;
+  const double *minv = a.minv, *b = a.b;
   auto G = [&](int i) { return a.g + (size_t)(i - 1) * n; };  // 1-based column
   auto H = [&](int i, int jj) -> double & { return h[(i - 1) + (jj - 1) * (k + 1)]; };
-  int rot = 0;
+  unsigned int ep = 0;
   double acc[1];
 
   // x = 0 ; econv = tol*||b||
   acc[0] = 0.0;
   FOR_ROWS(P) {
     x[row] = 0.0;
-    acc[0] = __dadd_rn(acc[0], __dmul_rn(b[row], b[row]));
+    acc[0] = fma(b[row], b[row], acc[0]);
   }
-  if (!reduce<1>(a, rot, acc, red, tot)) return;
-  const double econv = __dmul_rn(a.tol, sqrt(acc[0]));
+  if (!reduce<1>(a, ep, acc, red)) return;
+  const double econv = a.tol * sqrt(acc[0]);
   int l, nit = 0, ni = 0, status = FVC_OK;
   double crit = 0.0;
   for (l = 1; l <= a.maxit; ++l) {
@@ -369,19 +343,18 @@ __global__ void __launch_bounds__(256) gmres_f64(KArgs a) {
     acc[0] = 0.0;
     double *g1 = G(1);
     FOR_ROWS(P) {
-      double ax = sell_row_f64(a.A, s_, P.lane, row, [&](int kk) { return x[kk]; });
-      double gi = __ddiv_rn(__dsub_rn(b[row], ax), m[row]);
+      const double ax = sell_row_fma(a.A, s_, P.lane, row, [&](int kk) { return x[kk]; });
+      const double gi = (b[row] - ax) * minv[row];
       g1[row] = gi;
-      acc[0] = __dadd_rn(acc[0], __dmul_rn(gi, gi));
+      acc[0] = fma(gi, gi, acc[0]);
     }
-    if (!reduce<1>(a, rot, acc, red, tot)) return;
+    if (!reduce<1>(a, ep, acc, red)) return;
     if (threadIdx.x == 0) e[0] = sqrt(acc[0]);
     __syncthreads();
-    const double e1 = e[0];
-    FOR_ROWS(P) { g1[row] = __ddiv_rn(g1[row], e1); }
-    if (!grid_barrier(a.gs)) return;
+    const double e1inv = 1.0 / e[0];
+    FOR_ROWS(P) { g1[row] = g1[row] * e1inv; }
+    if (!grid_barrier(a.gs, ep)) return;
     ni = 0;
-    bool done = false;
     for (int i = 1; i <= k; ++i) {
       ++nit;
       ++ni;
@@ -390,12 +363,12 @@ __global__ void __launch_bounds__(256) gmres_f64(KArgs a) {
       acc[0] = 0.0;
       const double *g1c = G(1);
       FOR_ROWS(P) {
-        double av = sell_row_f64(a.A, s_, P.lane, row, [&](int kk) { return gi[kk]; });
-        double vi = __ddiv_rn(av, m[row]);
+        const double av = sell_row_fma(a.A, s_, P.lane, row, [&](int kk) { return gi[kk]; });
+        const double vi = av * minv[row];
         gn[row] = vi;
-        acc[0] = __dadd_rn(acc[0], __dmul_rn(vi, g1c[row]));
+        acc[0] = fma(vi, g1c[row], acc[0]);
       }
-      if (!reduce<1>(a, rot, acc, red, tot)) return;
+      if (!reduce<1>(a, ep, acc, red)) return;
       double beta = acc[0];
       if (threadIdx.x == 0) H(1, i) = beta;
       // modified Gram-Schmidt: subtract, then dot with the next vector
@@ -404,36 +377,36 @@ __global__ void __launch_bounds__(256) gmres_f64(KArgs a) {
         const double *gnext = G(jj + 1);
         acc[0] = 0.0;
         FOR_ROWS(P) {
-          double vi = __dsub_rn(gn[row], __dmul_rn(beta, gj[row]));
+          const double vi = fma(-beta, gj[row], gn[row]);
           gn[row] = vi;
-          acc[0] = __dadd_rn(acc[0], __dmul_rn(vi, (jj < i) ? gnext[row] : vi));
+          acc[0] = fma(vi, (jj < i) ? gnext[row] : vi, acc[0]);
         }
-        if (!reduce<1>(a, rot, acc, red, tot)) return;
+        if (!reduce<1>(a, ep, acc, red)) return;
         beta = acc[0];
         if (jj < i && threadIdx.x == 0) H(jj + 1, i) = beta;
       }
       const double norm = sqrt(beta);
-      FOR_ROWS(P) { gn[row] = __ddiv_rn(gn[row], norm); }
+      const double ninv = 1.0 / norm;
+      FOR_ROWS(P) { gn[row] = gn[row] * ninv; }
       if (threadIdx.x == 0) {
         H(i + 1, i) = norm;
         for (int jj = 1; jj <= i - 1; ++jj) {
-          double aux1 = __dadd_rn(__dmul_rn(cc[jj - 1], H(jj, i)), __dmul_rn(ss[jj - 1], H(jj + 1, i)));
-          double aux2 = __dadd_rn(-__dmul_rn(ss[jj - 1], H(jj, i)), __dmul_rn(cc[jj - 1], H(jj + 1, i)));
+          const double aux1 = cc[jj - 1] * H(jj, i) + ss[jj - 1] * H(jj + 1, i);
+          const double aux2 = -ss[jj - 1] * H(jj, i) + cc[jj - 1] * H(jj + 1, i);
           H(jj, i) = aux1;
           H(jj + 1, i) = aux2;
         }
-        double rr = sqrt(__dadd_rn(__dmul_rn(H(i, i), H(i, i)), __dmul_rn(H(i + 1, i), H(i + 1, i))));
-        cc[i - 1] = __ddiv_rn(H(i, i), rr);
-        ss[i - 1] = __ddiv_rn(H(i + 1, i), rr);
+        const double rr = sqrt(H(i, i) * H(i, i) + H(i + 1, i) * H(i + 1, i));
+        cc[i - 1] = H(i, i) / rr;
+        ss[i - 1] = H(i + 1, i) / rr;
         H(i, i) = rr;
         H(i + 1, i) = 0.0;
-        e[i] = -__dmul_rn(ss[i - 1], e[i - 1]);
-        e[i - 1] = __dmul_rn(cc[i - 1], e[i - 1]);
+        e[i] = -ss[i - 1] * e[i - 1];
+        e[i - 1] = cc[i - 1] * e[i - 1];
       }
-      if (!grid_barrier(a.gs)) return;  // also publishes g(i+1) and h
+      if (!grid_barrier(a.gs, ep)) return;  // also publishes g(i+1) and h
       if (!(e[i] == e[i])) {
         status = FVC_ERR_NAN;
-        done = true;
         break;
       }
       if (fabs(e[i]) <= econv) break;
@@ -441,59 +414,72 @@ __global__ void __launch_bounds__(256) gmres_f64(KArgs a) {
     if (status != FVC_OK) break;
     // back substitution h y = e
     if (threadIdx.x == 0) {
-      y[ni - 1] = __ddiv_rn(e[ni - 1], H(ni, ni));
+      y[ni - 1] = e[ni - 1] / H(ni, ni);
       for (int i = ni - 1; i >= 1; --i) {
         double yi = 0.0;
-        for (int jj = i + 1; jj <= ni; ++jj) yi = __dsub_rn(yi, __dmul_rn(H(i, jj), y[jj - 1]));
-        y[i - 1] = __ddiv_rn(__dadd_rn(yi, e[i - 1]), H(i, i));
+        for (int jj = i + 1; jj <= ni; ++jj) yi = yi - H(i, jj) * y[jj - 1];
+        y[i - 1] = (yi + e[i - 1]) / H(i, i);
       }
     }
     __syncthreads();
     FOR_ROWS(P) {
       double xi = x[row];
-      for (int jj = 1; jj <= ni; ++jj) xi = __dadd_rn(xi, __dmul_rn(y[jj - 1], G(jj)[row]));
+      for (int jj = 1; jj <= ni; ++jj) xi = fma(y[jj - 1], G(jj)[row], xi);
       x[row] = xi;
     }
-    if (!grid_barrier(a.gs)) return;
+    if (!grid_barrier(a.gs, ep)) return;
     crit = fabs(e[ni]);
     if (crit <= econv) break;
-    (void)done;
   }
   if (l > a.maxit) {
     l = a.maxit;
     if (status == FVC_OK) status = FVC_ERR_NOCONV;
   }
   finish(a, l, status, econv, crit, nit);
-  epilogue(a, rot, red, tot, true);
+  epilogue(a, ep, red, true);
 }
 
 // ---------------------------------------------------------------------
 // Plain SpMV kernels (one warp per slice, grid-stride over slices)
 // ---------------------------------------------------------------------
+template <bool kFused>
 __global__ void __launch_bounds__(256) spmv_f64(SellView<double> A, const double *__restrict__ x,
                                                 double *__restrict__ y) {
   const int lane = threadIdx.x & 31;
   const int nw = (gridDim.x * blockDim.x) >> 5;
   for (int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < A.nslices; s += nw) {
     const int row = s * 32 + lane;
-    if (row < A.n) y[row] = sell_row_f64(A, s, lane, row, [&](int k) { return __ldg(x + k); });
+    if (row >= A.n) continue;
+    auto xf = [&](int k) { return __ldg(x + k); };
+    y[row] = kFused ? sell_row_fma(A, s, lane, row, xf) : sell_row_f64(A, s, lane, row, xf);
   }
 }
 
-__global__ void __launch_bounds__(256) spmv_f32(SellView<float> A, const float *__restrict__ x,
-                                                float *__restrict__ y) {
+// FP32 difference form: y_i = e_i x_i + sum_k w_ik (x_i - x_k)
+__global__ void __launch_bounds__(256) spmv_f32(int n, int nslices, const int64_t *__restrict__ sptr,
+                                                const int *__restrict__ col,
+                                                const float *__restrict__ w32,
+                                                const float *__restrict__ e32,
+                                                const float *__restrict__ x, float *__restrict__ y) {
   const int lane = threadIdx.x & 31;
   const int nw = (gridDim.x * blockDim.x) >> 5;
-  for (int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < A.nslices; s += nw) {
+  for (int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < nslices; s += nw) {
     const int row = s * 32 + lane;
-    if (row >= A.n) continue;
-    const int64_t base = A.sptr[s];
-    const int w = (int)((A.sptr[s + 1] - base) >> 5);
-    float t = A.diag ? A.diag[row] * __ldg(x + row) : 0.0f;
+    if (row >= n) continue;
+    const int64_t base = sptr[s];
+    const int w = (int)((sptr[s + 1] - base) >> 5);
+    const float xi = __ldg(x + row);
+    float t = ld_stream(e32 + row) * xi;
     for (int kk = 0; kk < w; ++kk)
-      t = fmaf(ld_stream(A.val + base + 32 * kk + lane), __ldg(x + ld_stream(A.col + base + 32 * kk + lane)), t);
+      t = fmaf(ld_stream(w32 + base + 32 * kk + lane),
+               xi - __ldg(x + ld_stream(col + base + 32 * kk + lane)), t);
     y[row] = t;
   }
+}
+
+__global__ void reciprocal_kernel(int n, const double *__restrict__ m, double *__restrict__ minv) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) minv[i] = 1.0 / m[i];
 }
 
 SellView<double> view64(const DeviceMatrix &A) {
@@ -524,7 +510,7 @@ int sm_count() {
 template <typename K>
 Launch persistent_launch(K kernel, const DeviceMatrix &A, const fvc_opts &o) {
   Launch L;
-  L.threads = (o.block_threads > 0) ? o.block_threads : 256;
+  L.threads = (o.block_threads > 0) ? o.block_threads : 1024;
   int occ = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, L.threads, 0);
   if (occ <= 0) occ = 1;
@@ -551,19 +537,7 @@ int32_t ensure_vectors(Scratch &S, size_t n, int nvec, size_t nblocks, bool gmre
     if (cudaMalloc(&S.g, sizeof(double) * (size_t)(kGmresK + 1) * n) != cudaSuccess) return FVC_ERR_CUDA;
     S.ngmres = n;
   }
-  size_t need = 4 * kMaxNV * nblocks;
-  if (S.npart < need) {
-    if (S.partials) cudaFree(S.partials);
-    if (cudaMalloc(&S.partials, sizeof(double) * need) != cudaSuccess) return FVC_ERR_CUDA;
-    S.npart = need;
-  }
-  if (!S.sync) {
-    if (cudaMalloc(&S.sync, 64) != cudaSuccess) return FVC_ERR_CUDA;
-    if (cudaMalloc(&S.err, 64) != cudaSuccess) return FVC_ERR_CUDA;
-    if (cudaMalloc(&S.result, 16 * sizeof(double)) != cudaSuccess) return FVC_ERR_CUDA;
-    if (cudaMalloc(&S.iresult, 16 * sizeof(int)) != cudaSuccess) return FVC_ERR_CUDA;
-  }
-  return FVC_OK;
+  return ensure_sync(S, nblocks);
 }
 
 template <typename K>
@@ -574,13 +548,11 @@ int32_t run_persistent(K kernel, const DeviceMatrix &A, Scratch &S, const double
   Launch L = persistent_launch(kernel, A, o);
   int32_t rc = ensure_vectors(S, (size_t)A.n, nvec, (size_t)L.blocks, gmres);
   if (rc != FVC_OK) return rc;
-  cudaMemsetAsync(S.sync, 0, 64, stream);
-  cudaMemsetAsync(S.err, 0, 64, stream);
-  cudaMemsetAsync(S.iresult, 0, 16 * sizeof(int), stream);
-  cudaMemsetAsync(S.result, 0, 16 * sizeof(double), stream);
+  reset_sync(S, stream);
   KArgs a{};
   a.A = view64(A);
   a.m = A.jac;
+  a.minv = A.jinv;
   a.b = b;
   a.x = x;
   a.v0 = S.v[0];
@@ -591,11 +563,7 @@ int32_t run_persistent(K kernel, const DeviceMatrix &A, Scratch &S, const double
   a.v5 = S.v[5];
   a.v6 = S.v[6];
   a.g = S.g;
-  a.partials = S.partials;
-  a.gs.count = S.sync;
-  a.gs.gen = S.sync + 1;
-  a.gs.err = S.err;
-  a.gs.nblocks = (unsigned)L.blocks;
+  a.gs = make_sync(S, L.blocks);
   a.tol = tol;
   a.maxit = maxit;
   a.init = init;
@@ -663,30 +631,33 @@ int32_t run_gmres(const DeviceMatrix &A, Scratch &S, const double *b, double *x,
   return run_persistent(gmres_f64, A, S, b, x, tol, maxit, 1, o, stream, st, 0, true);
 }
 
-int32_t launch_spmv(const DeviceMatrix &A, const double *x, double *y, cudaStream_t stream) {
+int32_t launch_spmv(const DeviceMatrix &A, const double *x, double *y, cudaStream_t stream,
+                    bool fused) {
   if (A.n <= 0) return FVC_ERR_ARG;
   const int threads = 256;
   int blocks = (A.nslices + 7) / 8;
   blocks = std::max(1, std::min(blocks, sm_count() * 8));
-  spmv_f64<<<blocks, threads, 0, stream>>>(view64(A), x, y);
+  if (fused)
+    spmv_f64<true><<<blocks, threads, 0, stream>>>(view64(A), x, y);
+  else
+    spmv_f64<false><<<blocks, threads, 0, stream>>>(view64(A), x, y);
   count_launch();
   return cudaPeekAtLastError() == cudaSuccess ? FVC_OK : FVC_ERR_CUDA;
 }
 
 int32_t launch_spmv_f32(const DeviceMatrix &A, const float *x, float *y, cudaStream_t stream) {
   if (A.n <= 0 || !A.have32) return FVC_ERR_ARG;
-  SellView<float> v;
-  v.n = A.n;
-  v.nslices = A.nslices;
-  v.sptr = A.sptr;
-  v.col = A.col;
-  v.val = A.val32;
-  v.diag = A.diag32;
-  v.diag_mode = DIAG_FIRST;
   const int threads = 256;
   int blocks = (A.nslices + 7) / 8;
   blocks = std::max(1, std::min(blocks, sm_count() * 8));
-  spmv_f32<<<blocks, threads, 0, stream>>>(v, x, y);
+  spmv_f32<<<blocks, threads, 0, stream>>>(A.n, A.nslices, A.sptr, A.col, A.val32, A.diag32, x, y);
+  count_launch();
+  return cudaPeekAtLastError() == cudaSuccess ? FVC_OK : FVC_ERR_CUDA;
+}
+
+int32_t launch_reciprocal(const DeviceMatrix &A, cudaStream_t stream) {
+  if (A.n <= 0 || !A.jac || !A.jinv) return FVC_ERR_ARG;
+  reciprocal_kernel<<<(A.n + 255) / 256, 256, 0, stream>>>(A.n, A.jac, A.jinv);
   count_launch();
   return cudaPeekAtLastError() == cudaSuccess ? FVC_OK : FVC_ERR_CUDA;
 }

@@ -1,19 +1,41 @@
-// fvc_mixed.cu -- mixed-precision solves: FP32 Krylov inside an FP64
-// defect-correction (iterative refinement) loop, one persistent launch.
+// fvc_mixed.cu -- mixed-precision solves: FP32 Krylov iterations with the
+// solution and the true residual kept in FP64, one persistent launch.
 //
-//   outer sweep (FP64):  r = b - A x        (FP64 matrix, FP64 vectors)
-//                        stop if ||r||2 <= refine_tol * ||b||2
-//   inner solve (FP32):  S e = D^-1/2 r      S = D^-1/2 A D^-1/2, D = diag(A)
-//                        CG (code 1) or BiCGSTAB (code 2), stopped after a
-//                        relative reduction inner_tol of its own residual
-//   update (FP64):       x = x + D^-1/2 e
+// FP32 operator.  The matrix is stored for the FP32 iterations in
+// difference form
+//     (A x)_i = e_i x_i + sum_k w_ik (x_i - x_k),
+//     w_ik = -a_ik (FP32 per slot),  e_i = a_ii - sum_k w_ik (FP32 per row),
+// an exact identity for any matrix.  For the finite-volume matrices of the
+// reference the rows of a Neumann pressure-correction system sum to zero
+// (e_i = 0) and FP32 rounding of the weights then perturbs the operator only
+// relatively, so its near-null space (the lowest eigenvalues, O(1e-7) at a
+// few million cells) survives; rounding a_ii and a_ik separately would shift
+// those eigenvalues by a comparable absolute amount and stall the solve.
+// The Jacobi preconditioner m = ad (src/Solver.f:84) is applied as an FP32
+// reciprocal.  A row whose m lies beyond FP32 range (the 1e60 pressure pin
+// of src/CellibPressure.f:557) gets 1/m = 0 there and is moved only by the
+// FP64 Jacobi step of each reliable update (fold_correction).
 //
-// The symmetric Jacobi scaling is the reference's Jacobi preconditioner
-// (m = ad, src/Solver.f:84) moved into the matrix, so the inner solver needs
-// no preconditioner pass and S has a unit diagonal that is not stored.  It
-// also keeps the 1e60 pressure pin of src/CellibPressure.f:557 inside the
-// FP32 range (its row of S is O(1e-30) off the diagonal).  Dot products and
-// norms accumulate in FP64.
+// CG (code 1): Jacobi-PCG with reliable updates (residual replacement): the
+// correction e accumulates alpha*p as an unevaluated FP32 pair (hi + lo,
+// products split exactly with FMA, sums by TwoSum), which keeps it as
+// accurate as FP64 with FP32 arithmetic -- rounding it to one FP32 number
+// would add a residual error of order eps32 * cond(A) per update cycle and
+// stall the solve at a few million cells.  Whenever the FP32 residual has
+// dropped by a factor inner_tol (default 0.1) since the last update, or
+// looks converged, x += e in FP64, the true residual b - A x is recomputed
+// with the FP64 matrix, and replaces the FP32 residual.  The search
+// direction survives updates, so the iteration count stays close to the
+// FP64 PCG count while the iterations stream FP32 data.
+// BiCGSTAB (code 2): the reference's Jacobi BiCGSTAB (src/Iterativos.f:
+// 140-234) in FP32 on the correction equation, restarted from the FP64
+// residual (defect correction) after each inner reduction by inner_tol
+// (default 1e-4).
+// Both stop on ||b - A x||2 <= refine_tol * ||b||2 recomputed in FP64.  Dot
+// products and norms: each thread sums its rows with compensated FP32
+// (TwoSum), the per-thread pairs are combined in FP64.  GB300 executes FP64
+// at ~1/64 of its FP32 rate, so the iteration keeps the FP64 pipe idle.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 
@@ -24,47 +46,75 @@ namespace fvc {
 
 namespace {
 
-__global__ void scale_setup(int n, const double *__restrict__ jac, double *__restrict__ ds,
-                            int *__restrict__ bad) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) {
-    double m = jac[i];
-    if (!(m > 0.0)) {
-      atomicExch(bad, 1);
-      ds[i] = 1.0;
-    } else {
-      ds[i] = 1.0 / sqrt(m);
-    }
+constexpr double kF32Clamp = 1.0e30;
+
+// Compensated FP32 sum (TwoSum per term); value() folds it to FP64.  The
+// _rn intrinsics keep the compiler from contracting the error terms.
+struct CSum {
+  float s = 0.0f, c = 0.0f;
+  __device__ __forceinline__ void add(float v) {
+    const float t = __fadd_rn(s, v);
+    const float bp = __fsub_rn(t, s);
+    c = __fadd_rn(c, __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(v, bp)));
+    s = t;
   }
+  __device__ __forceinline__ double value() const { return (double)s + (double)c; }
+};
+
+// (hi, lo) += alpha * p with alpha given as an FP32 pair (ah, al): the
+// product ah*p is split exactly with an FMA, the sum uses TwoSum and a
+// final Fast2Sum renormalisation.
+__device__ __forceinline__ float2 df_axpy(float2 e, float ah, float al, float p) {
+  const float th = __fmul_rn(ah, p);
+  const float terr = fmaf(ah, p, -th);
+  const float tl = fmaf(al, p, terr);
+  const float s = __fadd_rn(e.x, th);
+  const float bp = __fsub_rn(s, e.x);
+  const float err = __fadd_rn(__fsub_rn(e.x, __fsub_rn(s, bp)), __fsub_rn(th, bp));
+  const float lo = __fadd_rn(__fadd_rn(e.y, tl), err);
+  const float hi = __fadd_rn(s, lo);
+  return make_float2(hi, __fsub_rn(lo, __fsub_rn(hi, s)));
 }
 
-__global__ void scale_values(int n, int nslices, const int64_t *__restrict__ sptr,
-                             const int *__restrict__ col, const double *__restrict__ val,
-                             const double *__restrict__ ds, float *__restrict__ val32) {
+// e_i (FP64 sum, rounded once), Jacobi 1/m, and the FP32 weights.
+__global__ void build_f32_operator(int n, int nslices, const int64_t *__restrict__ sptr,
+                                   const int *__restrict__ col, const double *__restrict__ val,
+                                   const double *__restrict__ jac, float *__restrict__ w32,
+                                   float *__restrict__ e32, float *__restrict__ minv32) {
   const int lane = threadIdx.x & 31;
   const int nw = (gridDim.x * blockDim.x) >> 5;
   for (int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < nslices; s += nw) {
     const int row = s * 32 + lane;
     const int64_t base = sptr[s];
-    const int w = (int)((sptr[s + 1] - base) >> 5);
-    const double dr = (row < n) ? ds[row] : 0.0;
-    for (int k = 0; k < w; ++k) {
-      int64_t q = base + 32 * k + lane;
-      val32[q] = (row < n) ? (float)(val[q] * dr * ds[col[q]]) : 0.0f;
+    const int wd = (int)((sptr[s + 1] - base) >> 5);
+    double off = 0.0;  // sum of a_ik over true off-diagonal slots
+    for (int k = 0; k < wd; ++k) {
+      const int64_t q = base + 32 * k + lane;
+      const bool diag_slot = (row < n) && (col[q] == row);
+      const double a = (row < n && !diag_slot) ? val[q] : 0.0;
+      off += a;
+      w32[q] = (float)(-a);
+    }
+    if (row < n) {
+      const double m = jac[row];
+      double e = m + off;
+      e = fmin(fmax(e, -kF32Clamp), kF32Clamp);
+      e32[row] = (float)e;
+      minv32[row] = (fabs(m) > 1.0e37 || m == 0.0) ? 0.0f : (float)(1.0 / m);
     }
   }
 }
 
 struct MArgs {
-  SellView<double> A;   // FP64 matrix (residuals)
-  const float *val32;   // S values (same slots as A)
-  int unit_diag;        // 1: S has an implicit unit diagonal
-  const double *ds;     // D^-1/2
+  SellView<double> A;   // FP64 matrix (true residuals)
+  const float *w32;     // weights per slot
+  const float *e32;     // row excess
+  const float *minv;    // Jacobi 1/m (0 on rows whose m is beyond FP32)
+  const double *jac;    // m in FP64
   const double *b;
   double *x;
-  double *rd;           // FP64 residual scratch (unused slot reserved)
-  float *rs, *pa, *pb, *q, *e, *r0, *v, *t;
-  double *partials;
+  float *rs, *pa, *pb, *q, *r0, *v, *t, *z;
+  float2 *e;            // correction, FP32 pair (hi, lo)
   GridSync gs;
   double target;        // refine tolerance on ||b-Ax||/||b||
   double inner_tol;
@@ -75,46 +125,29 @@ struct MArgs {
   int *iresult;
 };
 
-constexpr int kNV = 4;
-
-__device__ __forceinline__ double *mslot(const MArgs &a, int rot, int q) {
-  return a.partials + ((size_t)(rot & 3) * kNV + q) * gridDim.x;
-}
-
-template <int NV>
-__device__ __forceinline__ bool mreduce(const MArgs &a, int &rot, double (&v)[NV], double *red,
-                                        double *tot) {
-  block_sum<NV>(v, red);
-  if (threadIdx.x == 0)
-#pragma unroll
-    for (int q = 0; q < NV; ++q) mslot(a, rot, q)[blockIdx.x] = v[q];
-  if (!grid_barrier(a.gs)) return false;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (warp < NV) {
-    const double *p = mslot(a, rot, warp);
-    double t = 0.0;
-    for (int b = lane; b < (int)gridDim.x; b += 32) t += __ldcg(p + b);
-    t = warp_sum(t);
-    if (lane == 0) tot[warp] = t;
-  }
-  __syncthreads();
-#pragma unroll
-  for (int q = 0; q < NV; ++q) v[q] = tot[q];
-  __syncthreads();
-  ++rot;
-  return true;
-}
-
-// (S y)_row with y supplied by a functor, FP32 arithmetic.
+// (A y)_row in FP32 difference form, y supplied by a functor.
 template <typename YF>
-__device__ __forceinline__ float srow(const MArgs &a, int s, int lane, int row, YF yf) {
+__device__ __forceinline__ float arow32(const MArgs &a, int s, int lane, int row, YF yf) {
   const int64_t base = a.A.sptr[s];
   const int w = (int)((a.A.sptr[s + 1] - base) >> 5);
-  float t = a.unit_diag ? yf(row) : 0.0f;
   const int *cp = a.A.col + base + lane;
-  const float *vp = a.val32 + base + lane;
-#pragma unroll 4
-  for (int k = 0; k < w; ++k) t = fmaf(ld_stream(vp + 32 * k), yf(ld_stream(cp + 32 * k)), t);
+  const float *vp = a.w32 + base + lane;
+  const float yi = yf(row);
+  float t = ld_stream(a.e32 + row) * yi;
+  if (w <= 4) {
+    int c[4];
+    float v[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      c[k] = (k < w) ? ld_stream(cp + 32 * k) : row;
+      v[k] = (k < w) ? ld_stream(vp + 32 * k) : 0.0f;
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      if (k < w) t = fmaf(v[k], yi - yf(c[k]), t);
+    return t;
+  }
+  for (int k = 0; k < w; ++k) t = fmaf(ld_stream(vp + 32 * k), yi - yf(ld_stream(cp + 32 * k)), t);
   return t;
 }
 
@@ -135,134 +168,168 @@ struct MPart {
   for (int s_ = (P).sb + (P).warp; s_ < (P).se; s_ += (P).nwarps) \
     for (int row = s_ * 32 + (P).lane, once_ = 1; once_ && row < (P).n; once_ = 0)
 
-// FP64 residual sweep: rs = D^-1/2 (b - A x) in FP32, returns ||b-Ax||^2,
-// ||b||^2 and ||rs||^2.
-__device__ __forceinline__ bool residual_sweep(const MArgs &a, int &rot, bool zero_x,
-                                               double (&out)[3], double *red, double *tot) {
+// FP64 residual sweep: rs = b - A x rounded to FP32.  Returns ||b-Ax||^2,
+// ||b||^2, rs.(rs/m) and ||b-Ax||^2 over the rows the FP32 iteration moves
+// (FP64 sums).
+__device__ __forceinline__ bool residual_sweep(const MArgs &a, unsigned int &ep, bool zero_x,
+                                               double (&out)[4], double *red) {
   const MPart P(a.A.nslices, a.A.n);
-  double acc[3] = {0.0, 0.0, 0.0};
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
   const double *x = a.x;
   MFOR_ROWS(P) {
-    double ax = zero_x ? 0.0 : sell_row_f64(a.A, s_, P.lane, row, [&](int k) { return x[k]; });
+    double ax = zero_x ? 0.0 : sell_row_fma(a.A, s_, P.lane, row, [&](int k) { return x[k]; });
     if (zero_x) a.x[row] = 0.0;
-    double bi = a.b[row];
-    double ri = bi - ax;
-    float rsi = (float)(a.ds[row] * ri);
+    const double bi = a.b[row];
+    const double ri = bi - ax;
+    const float rsi = (float)ri;
     a.rs[row] = rsi;
-    acc[0] += ri * ri;
-    acc[1] += bi * bi;
-    acc[2] += (double)rsi * (double)rsi;
+    acc[0] = fma(ri, ri, acc[0]);
+    acc[1] = fma(bi, bi, acc[1]);
+    const float mi = a.minv[row];
+    acc[2] = fma((double)rsi, (double)(rsi * mi), acc[2]);
+    if (mi != 0.0f) acc[3] = fma(ri, ri, acc[3]);
   }
-  if (!mreduce<3>(a, rot, acc, red, tot)) return false;
+  if (!grid_allreduce<4>(a.gs, ep, acc, red)) return false;
   out[0] = acc[0];
   out[1] = acc[1];
   out[2] = acc[2];
+  out[3] = acc[3];
   return true;
 }
 
-// x += D^-1/2 e (FP64), own rows; caller places a barrier after it.
-__device__ __forceinline__ void apply_correction(const MArgs &a) {
+// x += e (FP64) and e = 0, own rows; a barrier must follow.  Rows whose
+// diagonal is beyond FP32 range (1/m = 0: the pressure pin) are frozen in
+// the FP32 iteration; they take one FP64 Jacobi step on their current
+// residual estimate instead, which solves such a row to FP64 accuracy.
+__device__ __forceinline__ void fold_correction(const MArgs &a) {
   const MPart P(a.A.nslices, a.A.n);
-  MFOR_ROWS(P) { a.x[row] = a.x[row] + a.ds[row] * (double)a.e[row]; }
+  MFOR_ROWS(P) {
+    const float2 ev = a.e[row];
+    double dx = (double)ev.x + (double)ev.y;
+    const double m = a.jac[row];
+    if (a.minv[row] == 0.0f && m != 0.0) dx += (double)a.rs[row] / m;
+    a.x[row] = a.x[row] + dx;
+    a.e[row] = make_float2(0.0f, 0.0f);
+  }
 }
 
-__global__ void __launch_bounds__(256) mixed_cg(MArgs a) {
-  __shared__ double red[kNV * 32];
-  __shared__ double tot[kNV];
+__global__ void __launch_bounds__(1024, 1) mixed_cg(MArgs a) {
+  __shared__ double red[kMaxNV * 32];
   const MPart P(a.A.nslices, a.A.n);
-  int rot = 0, sweep = 0, inner_total = 0, status = FVC_ERR_NOCONV;
-  double res[3];
-  double relres = 0.0, bnorm2 = 0.0;
-  bool zero_x = a.init != 0;
-  for (sweep = 0; sweep <= a.max_refine; ++sweep) {
-    if (!residual_sweep(a, rot, zero_x, res, red, tot)) return;
-    zero_x = false;
-    if (sweep == 0) bnorm2 = res[1];
-    relres = (bnorm2 > 0.0) ? sqrt(res[0] / bnorm2) : sqrt(res[0]);
-    if (!(relres == relres)) {
+  unsigned int ep = 0;
+  int status = FVC_ERR_NOCONV, updates = 0, it = 0;
+  double res[4];
+  if (!residual_sweep(a, ep, a.init != 0, res, red)) return;
+  const double bnorm2 = res[1];
+  const double scale = (bnorm2 > 0.0) ? bnorm2 : 1.0;
+  double relres = sqrt(res[0] / scale);
+  double rz = res[2];
+  double rr_upd = res[3];  // ||r||^2 (moving rows) at the last reliable update
+  const double delta2 = a.inner_tol * a.inner_tol;
+  const double target2 = a.target * a.target * scale;
+  float beta = 0.0f;
+  float *pprev = a.pb, *pcur = a.pa;
+  const float *rs = a.rs;
+  const float *minv = a.minv;
+  if (!(relres == relres)) status = FVC_ERR_NAN;
+  else if (relres <= a.target) status = FVC_OK;
+  while (status == FVC_ERR_NOCONV && it < a.maxit) {
+    ++it;
+    // p = z + beta p_prev (z = rs/m), formed on the fly at the neighbours;
+    // q = A p ; p.q
+    CSum cpq;
+    const float *pp = pprev;
+    if (it == 1) {
+      MFOR_ROWS(P) {
+        auto pf = [&](int k) { return rs[k] * minv[k]; };
+        const float pi = pf(row);
+        pcur[row] = pi;
+        a.e[row] = make_float2(0.0f, 0.0f);
+        const float qi = arow32(a, s_, P.lane, row, pf);
+        a.q[row] = qi;
+        cpq.add(pi * qi);
+      }
+    } else {
+      MFOR_ROWS(P) {
+        auto pf = [&](int k) { return fmaf(beta, pp[k], rs[k] * minv[k]); };
+        const float pi = pf(row);
+        pcur[row] = pi;
+        const float qi = arow32(a, s_, P.lane, row, pf);
+        a.q[row] = qi;
+        cpq.add(pi * qi);
+      }
+    }
+    double pq[1] = {cpq.value()};
+    if (!grid_allreduce<1>(a.gs, ep, pq, red)) return;
+    const double alpha_d = rz / pq[0];
+    const float alpha = (float)alpha_d;
+    const float alpha_lo = (float)(alpha_d - (double)alpha);
+    // e += alpha p (FP32 pair) ; rs -= alpha q ; rs.z ; rs.rs
+    CSum crz, crr;
+    MFOR_ROWS(P) {
+      a.e[row] = df_axpy(a.e[row], alpha, alpha_lo, pcur[row]);
+      const float ri = fmaf(-alpha, a.q[row], a.rs[row]);
+      a.rs[row] = ri;
+      const float mi = minv[row];
+      crz.add(ri * (ri * mi));
+      if (mi != 0.0f) crr.add(ri * ri);
+    }
+    double acc[2] = {crz.value(), crr.value()};
+    if (!grid_allreduce<2>(a.gs, ep, acc, red)) return;
+    double rz_new = acc[0];
+    if (!(rz_new == rz_new)) {
       status = FVC_ERR_NAN;
       break;
     }
-    if (relres <= a.target) {
-      status = FVC_OK;
-      break;
-    }
-    if (sweep == a.max_refine || inner_total >= a.maxit) break;
-    // inner CG on S e = rs from e = 0
-    double rz = res[2];
-    const double stop2 = a.inner_tol * a.inner_tol * rz;
-    float beta = 0.0f;
-    float *pprev = a.rs, *pcur = a.pa;
-    int it = 0;
-    for (;;) {
-      ++it;
-      double acc[1] = {0.0};
-      const float *pp = pprev;
-      const float *rr = a.rs;
-      if (it == 1) {
-        MFOR_ROWS(P) {
-          float qi = srow(a, s_, P.lane, row, [&](int k) { return rr[k]; });
-          float pi = rr[row];
-          pcur[row] = pi;
-          a.e[row] = 0.0f;
-          a.q[row] = qi;
-          acc[0] += (double)pi * (double)qi;
-        }
-      } else {
-        MFOR_ROWS(P) {
-          auto pf = [&](int k) { return fmaf(beta, pp[k], rr[k]); };
-          float pi = pf(row);
-          pcur[row] = pi;
-          float qi = srow(a, s_, P.lane, row, pf);
-          a.q[row] = qi;
-          acc[0] += (double)pi * (double)qi;
-        }
+    if (acc[1] <= delta2 * rr_upd || acc[1] <= target2 || it >= a.maxit) {
+      // reliable update: fold e into x, recompute the true residual in FP64
+      fold_correction(a);
+      if (!grid_barrier(a.gs, ep)) return;
+      if (!residual_sweep(a, ep, false, res, red)) return;
+      ++updates;
+      relres = sqrt(res[0] / scale);
+      if (!(relres == relres)) {
+        status = FVC_ERR_NAN;
+        break;
       }
-      if (!mreduce<1>(a, rot, acc, red, tot)) return;
-      const float alpha = (float)(rz / acc[0]);
-      acc[0] = 0.0;
-      MFOR_ROWS(P) {
-        float pi = pcur[row];
-        a.e[row] = fmaf(alpha, pi, a.e[row]);
-        float ri = fmaf(-alpha, a.q[row], a.rs[row]);
-        a.rs[row] = ri;
-        acc[0] += (double)ri * (double)ri;
+      if (relres <= a.target) {
+        status = FVC_OK;
+        break;
       }
-      if (!mreduce<1>(a, rot, acc, red, tot)) return;
-      const double rz_new = acc[0];
-      beta = (float)(rz_new / rz);
-      rz = rz_new;
-      if (!(rz == rz)) break;
-      if (rz <= stop2 || inner_total + it >= a.maxit) break;
-      pprev = pcur;
-      pcur = (pcur == a.pa) ? a.pb : a.pa;
+      rz_new = res[2];
+      rr_upd = res[3];
     }
-    inner_total += it;
-    apply_correction(a);
-    if (!grid_barrier(a.gs)) return;
+    beta = (float)(rz_new / rz);
+    rz = rz_new;
+    float *tmp = pprev;
+    pprev = pcur;
+    pcur = tmp;
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
-    a.iresult[0] = sweep;
+    a.iresult[0] = updates;
     a.iresult[1] = status;
-    a.iresult[2] = inner_total;
+    a.iresult[2] = it;
     a.result[2] = relres;
     a.result[3] = res[0];
     a.result[4] = bnorm2;
   }
 }
 
-// BiCGSTAB inner solver (unpreconditioned, on S).
-__global__ void __launch_bounds__(256) mixed_bicgstab(MArgs a) {
-  __shared__ double red[kNV * 32];
-  __shared__ double tot[kNV];
+// The reference's Jacobi BiCGSTAB (Iterativos.f:140-234) in FP32 on the
+// correction equation A e = r, inside FP64 defect correction.
+__global__ void __launch_bounds__(1024, 1) mixed_bicgstab(MArgs a) {
+  __shared__ double red[kMaxNV * 32];
   const MPart P(a.A.nslices, a.A.n);
-  int rot = 0, sweep = 0, inner_total = 0, status = FVC_ERR_NOCONV;
-  double res[3];
+  unsigned int ep = 0;
+  int sweep = 0, inner_total = 0, status = FVC_ERR_NOCONV;
+  double res[4];
   double relres = 0.0, bnorm2 = 0.0;
   bool zero_x = a.init != 0;
-  float *sv = a.rs, *p = a.pa, *v = a.q, *t = a.t, *r0 = a.r0, *e = a.e;
+  float *sv = a.rs, *p = a.pa, *v = a.q, *t = a.t, *r0 = a.r0, *z = a.z;
+  float2 *e = a.e;
+  const float *minv = a.minv;
   for (sweep = 0; sweep <= a.max_refine; ++sweep) {
-    if (!residual_sweep(a, rot, zero_x, res, red, tot)) return;
+    if (!residual_sweep(a, ep, zero_x, res, red)) return;
     zero_x = false;
     if (sweep == 0) bnorm2 = res[1];
     relres = (bnorm2 > 0.0) ? sqrt(res[0] / bnorm2) : sqrt(res[0]);
@@ -275,60 +342,79 @@ __global__ void __launch_bounds__(256) mixed_bicgstab(MArgs a) {
       break;
     }
     if (sweep == a.max_refine || inner_total >= a.maxit) break;
-    double rho = res[2];
-    const double stop2 = a.inner_tol * a.inner_tol * res[2];
+    const double d = res[2];  // r.z with z = r/m
+    const double stop2 = a.inner_tol * a.inner_tol * fabs(d);
     MFOR_ROWS(P) {
-      float si = sv[row];
+      const float si = sv[row];
       r0[row] = si;
       p[row] = si;
-      e[row] = 0.0f;
+      z[row] = si * minv[row];
+      e[row] = make_float2(0.0f, 0.0f);
     }
-    if (!grid_barrier(a.gs)) return;
+    if (!grid_barrier(a.gs, ep)) return;
     int it = 0;
     for (;;) {
       ++it;
-      double acc1[1] = {0.0};
+      // v = A z ; rr0 = s.r0 ; v.r0
+      CSum c0, c1;
       MFOR_ROWS(P) {
-        float vi = srow(a, s_, P.lane, row, [&](int k) { return p[k]; });
+        const float vi = arow32(a, s_, P.lane, row, [&](int k) { return z[k]; });
         v[row] = vi;
-        acc1[0] += (double)r0[row] * (double)vi;
+        const float r0i = r0[row];
+        c0.add(sv[row] * r0i);
+        c1.add(vi * r0i);
       }
-      if (!mreduce<1>(a, rot, acc1, red, tot)) return;
-      const float alpha = (float)(rho / acc1[0]);
-      double acc[2];
-      MFOR_ROWS(P) { sv[row] = fmaf(-alpha, v[row], sv[row]); }
-      if (!grid_barrier(a.gs)) return;
-      acc[0] = acc[1] = 0.0;
+      double acc[2] = {c0.value(), c1.value()};
+      if (!grid_allreduce<2>(a.gs, ep, acc, red)) return;
+      const double rr0 = acc[0];
+      const float alpha = (float)(rr0 / acc[1]);
+      // e += alpha z ; s -= alpha v ; z = s/m
       MFOR_ROWS(P) {
-        float ti = srow(a, s_, P.lane, row, [&](int k) { return sv[k]; });
+        e[row] = df_axpy(e[row], alpha, 0.0f, z[row]);
+        const float si = fmaf(-alpha, v[row], sv[row]);
+        sv[row] = si;
+        z[row] = si * minv[row];
+      }
+      if (!grid_barrier(a.gs, ep)) return;
+      // t = A z ; t.s ; t.t
+      CSum c2, c3;
+      MFOR_ROWS(P) {
+        const float ti = arow32(a, s_, P.lane, row, [&](int k) { return z[k]; });
         t[row] = ti;
-        acc[0] += (double)ti * (double)sv[row];
-        acc[1] += (double)ti * (double)ti;
+        c2.add(ti * sv[row]);
+        c3.add(ti * ti);
       }
-      if (!mreduce<2>(a, rot, acc, red, tot)) return;
+      acc[0] = c2.value();
+      acc[1] = c3.value();
+      if (!grid_allreduce<2>(a.gs, ep, acc, red)) return;
       const float omega = (acc[1] > 0.0) ? (float)(acc[0] / acc[1]) : 0.0f;
-      double acc2[2] = {0.0, 0.0};
+      // e += w z ; s -= w t ; s.z ; r0.s
+      CSum c4, c5;
       MFOR_ROWS(P) {
-        float si = sv[row];
-        e[row] = fmaf(omega, si, fmaf(alpha, p[row], e[row]));
-        float sn = fmaf(-omega, t[row], si);
+        const float zi = z[row];
+        e[row] = df_axpy(e[row], omega, 0.0f, zi);
+        const float sn = fmaf(-omega, t[row], sv[row]);
         sv[row] = sn;
-        acc2[0] += (double)r0[row] * (double)sn;
-        acc2[1] += (double)sn * (double)sn;
+        c4.add(sn * zi);
+        c5.add(r0[row] * sn);
       }
-      if (!mreduce<2>(a, rot, acc2, red, tot)) return;
-      const double rho_new = acc2[0];
-      if (!(acc2[1] == acc2[1]) || acc2[1] <= stop2 || inner_total + it >= a.maxit || omega == 0.0f ||
-          rho_new == 0.0)
+      double acc2[2] = {c4.value(), c5.value()};
+      if (!grid_allreduce<2>(a.gs, ep, acc2, red)) return;
+      if (!(acc2[0] == acc2[0]) || fabs(acc2[0]) <= stop2 || inner_total + it >= a.maxit ||
+          omega == 0.0f)
         break;
-      const float beta = (float)((rho_new / rho) * ((double)alpha / (double)omega));
-      rho = rho_new;
-      MFOR_ROWS(P) { p[row] = fmaf(beta, fmaf(-omega, v[row], p[row]), sv[row]); }
-      if (!grid_barrier(a.gs)) return;
+      const float beta = (float)((acc2[1] / rr0) * ((double)alpha / (double)omega));
+      // p = s + beta (p - w v) ; z = p/m
+      MFOR_ROWS(P) {
+        const float pi = fmaf(beta, fmaf(-omega, v[row], p[row]), sv[row]);
+        p[row] = pi;
+        z[row] = pi * minv[row];
+      }
+      if (!grid_barrier(a.gs, ep)) return;
     }
     inner_total += it;
-    apply_correction(a);
-    if (!grid_barrier(a.gs)) return;
+    fold_correction(a);
+    if (!grid_barrier(a.gs, ep)) return;
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     a.iresult[0] = sweep;
@@ -355,24 +441,17 @@ int sm_count_m() {
 
 int32_t build_f32_copy(DeviceMatrix &A, cudaStream_t stream) {
   if (A.have32) return FVC_OK;
-  if (!A.val32 && cudaMalloc(&A.val32, sizeof(float) * (size_t)std::max<int64_t>(A.slots, 1)) != cudaSuccess)
+  const size_t sl = (size_t)std::max<int64_t>(A.slots, 1);
+  if (!A.val32 && cudaMalloc(&A.val32, sizeof(float) * sl) != cudaSuccess) return FVC_ERR_CUDA;
+  if (!A.diag32 && cudaMalloc(&A.diag32, sizeof(float) * (size_t)A.n) != cudaSuccess)
     return FVC_ERR_CUDA;
-  if (!A.dscale && cudaMalloc(&A.dscale, sizeof(double) * (size_t)A.n) != cudaSuccess)
+  if (!A.minv32 && cudaMalloc(&A.minv32, sizeof(float) * (size_t)A.n) != cudaSuccess)
     return FVC_ERR_CUDA;
-  int *bad = nullptr;
-  if (cudaMalloc(&bad, sizeof(int)) != cudaSuccess) return FVC_ERR_CUDA;
-  cudaMemsetAsync(bad, 0, sizeof(int), stream);
-  scale_setup<<<(A.n + 255) / 256, 256, 0, stream>>>(A.n, A.jac, A.dscale, bad);
-  count_launch();
   int blocks = std::max(1, std::min((A.nslices + 7) / 8, sm_count_m() * 8));
-  scale_values<<<blocks, 256, 0, stream>>>(A.n, A.nslices, A.sptr, A.col, A.val, A.dscale, A.val32);
+  build_f32_operator<<<blocks, 256, 0, stream>>>(A.n, A.nslices, A.sptr, A.col, A.val, A.jac,
+                                                 A.val32, A.diag32, A.minv32);
   count_launch();
-  int hbad = 0;
-  cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, stream);
-  cudaError_t ce = cudaStreamSynchronize(stream);
-  cudaFree(bad);
-  if (ce != cudaSuccess) return FVC_ERR_CUDA;
-  if (hbad) return FVC_ERR_UNSUPPORTED;  // Jacobi scaling needs ad > 0
+  if (cudaStreamSynchronize(stream) != cudaSuccess) return FVC_ERR_CUDA;
   A.have32 = true;
   return FVC_OK;
 }
@@ -386,38 +465,25 @@ int32_t run_mixed(const DeviceMatrix &A0, Scratch &S, int code, const double *b,
   if (rc != FVC_OK) return rc;
   const size_t n = (size_t)A.n;
   if (S.nf < n) {
-    for (int i = 0; i < 8; ++i) {
+    for (int i = 0; i < 9; ++i) {
       if (S.f[i]) cudaFree(S.f[i]);
       S.f[i] = nullptr;
     }
     S.nf = n;
   }
-  for (int i = 0; i < 8; ++i)
-    if (!S.f[i] && cudaMalloc(&S.f[i], sizeof(float) * (n + 64)) != cudaSuccess) return FVC_ERR_CUDA;
+  for (int i = 0; i < 9; ++i)  // f[4] holds the float2 correction
+    if (!S.f[i] && cudaMalloc(&S.f[i], sizeof(float) * (i == 4 ? 2 : 1) * (n + 64)) != cudaSuccess)
+      return FVC_ERR_CUDA;
   auto kern = (code == 1) ? mixed_cg : mixed_bicgstab;
-  const int threads = (o.block_threads > 0) ? o.block_threads : 256;
+  const int threads = (o.block_threads > 0) ? o.block_threads : 1024;
   int occ = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, threads, 0);
   if (occ <= 0) occ = 1;
   if (o.blocks_per_sm > 0 && o.blocks_per_sm < occ) occ = o.blocks_per_sm;
   const int warps = threads / 32;
   int blocks = std::max(1, std::min(occ * sm_count_m(), (A.nslices + warps - 1) / warps));
-  size_t need = 4 * kNV * (size_t)blocks;
-  if (S.npart < need) {
-    if (S.partials) cudaFree(S.partials);
-    if (cudaMalloc(&S.partials, sizeof(double) * need) != cudaSuccess) return FVC_ERR_CUDA;
-    S.npart = need;
-  }
-  if (!S.sync) {
-    if (cudaMalloc(&S.sync, 64) != cudaSuccess) return FVC_ERR_CUDA;
-    if (cudaMalloc(&S.err, 64) != cudaSuccess) return FVC_ERR_CUDA;
-    if (cudaMalloc(&S.result, 16 * sizeof(double)) != cudaSuccess) return FVC_ERR_CUDA;
-    if (cudaMalloc(&S.iresult, 16 * sizeof(int)) != cudaSuccess) return FVC_ERR_CUDA;
-  }
-  cudaMemsetAsync(S.sync, 0, 64, stream);
-  cudaMemsetAsync(S.err, 0, 64, stream);
-  cudaMemsetAsync(S.iresult, 0, 16 * sizeof(int), stream);
-  cudaMemsetAsync(S.result, 0, 16 * sizeof(double), stream);
+  if (ensure_sync(S, (size_t)blocks) != FVC_OK) return FVC_ERR_CUDA;
+  reset_sync(S, stream);
   MArgs a{};
   a.A.n = A.n;
   a.A.nslices = A.nslices;
@@ -426,26 +492,24 @@ int32_t run_mixed(const DeviceMatrix &A0, Scratch &S, int code, const double *b,
   a.A.val = A.val;
   a.A.diag = A.diag;
   a.A.diag_mode = A.diag_mode;
-  a.val32 = A.val32;
-  a.unit_diag = (A.diag_mode != DIAG_NONE) ? 1 : 0;
-  a.ds = A.dscale;
+  a.w32 = A.val32;
+  a.e32 = A.diag32;
+  a.minv = A.minv32;
+  a.jac = A.jac;
   a.b = b;
   a.x = x;
   a.rs = S.f[0];
   a.pa = S.f[1];
   a.pb = S.f[2];
   a.q = S.f[3];
-  a.e = S.f[4];
+  a.e = reinterpret_cast<float2 *>(S.f[4]);
   a.r0 = S.f[5];
   a.t = S.f[6];
   a.v = S.f[7];
-  a.partials = S.partials;
-  a.gs.count = S.sync;
-  a.gs.gen = S.sync + 1;
-  a.gs.err = S.err;
-  a.gs.nblocks = (unsigned)blocks;
+  a.z = S.f[8];
+  a.gs = make_sync(S, blocks);
   a.target = (o.refine_tol > 0) ? o.refine_tol : tol;
-  a.inner_tol = (o.inner_tol > 0) ? o.inner_tol : 1e-4;
+  a.inner_tol = (o.inner_tol > 0) ? o.inner_tol : (code == 1 ? 0.1 : 1e-4);
   a.max_refine = (o.max_refine > 0) ? o.max_refine : 30;
   a.maxit = maxit;
   a.init = init;
@@ -482,7 +546,7 @@ int32_t run_mixed(const DeviceMatrix &A0, Scratch &S, int code, const double *b,
     st->status = ires[1];
     st->iterations = ires[2];
     st->inner_iterations = ires[2];
-    st->refinements = ires[0];
+    st->refinements = ires[0];  // CG: reliable updates; BiCGSTAB: sweeps
     st->energy = 0.0;
     st->conv = a.target;
     st->final_crit = res[2];

@@ -136,6 +136,10 @@ class Context:
         _lib.check(self._L.fvc_spmv(self._h, C.c_void_p(_addr(x_dev)), C.c_void_p(_addr(y_dev))),
                    "fvc_spmv")
 
+    def spmv_fast(self, x_dev, y_dev) -> None:
+        _lib.check(self._L.fvc_spmv_fast(self._h, C.c_void_p(_addr(x_dev)),
+                                         C.c_void_p(_addr(y_dev))), "fvc_spmv_fast")
+
     def spmv_f32(self, x_dev, y_dev) -> None:
         _lib.check(self._L.fvc_spmv_f32(self._h, C.c_void_p(_addr(x_dev)),
                                         C.c_void_p(_addr(y_dev))), "fvc_spmv_f32")

@@ -144,7 +144,12 @@ int32_t fvc_solve(fvc_context *ctx, int32_t code, const double *d_b, double *d_x
  * (bit-identical to src/Matvec.f for the loaded format).  Asynchronous on
  * the context's stream. */
 int32_t fvc_spmv(fvc_context *ctx, const double *d_x, double *d_y);
-/* y = A x with FP32 values (Jacobi-scaled copy kept by MIXED solves),
+/* y = A x, FP64, the same terms in the same order with fused
+ * multiply-adds (what the FP64 solvers run); within rounding of fvc_spmv.
+ * Asynchronous on the context's stream. */
+int32_t fvc_spmv_fast(fvc_context *ctx, const double *d_x, double *d_y);
+/* y = A x with the FP32 operator of MIXED solves (difference form
+ * y_i = e_i x_i + sum_k w_ik (x_i - x_k), w = -a_ik, e_i = a_ii - sum w),
  * FP32 vectors; asynchronous. */
 int32_t fvc_spmv_f32(fvc_context *ctx, const float *d_x, float *d_y);
 

