@@ -42,7 +42,8 @@ class FvcOpts(C.Structure):
         ("blocks_per_sm", I32),
         ("stop_rule", I32),
         ("want_residual", I32),
-        ("reserved", I32 * 3),
+        ("update_beta", I32),
+        ("reserved", I32 * 2),
     ]
 
 
@@ -81,6 +82,7 @@ SIGNATURES = {
     "fvc_spmv_f32": ([P, P, P], I32),
     "fvc_matrix_info": ([P, C.POINTER(I64), C.POINTER(I64), C.POINTER(I64), C.POINTER(I64)], I32),
     "fvc_kernel_launches": ([], I64),
+    "fvc_solve_trace": ([P, I32, P, P], I32),
     "fvc_mesh_adjacency": ([P, I32, I32, I32, I32, P], I32),
     "fvc_mesh_rcm": ([P, I32, I32, I32, P], I32),
     "fvc_mesh_numeq": ([P, P, I32, I32, P], I32),

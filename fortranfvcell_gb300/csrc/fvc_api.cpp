@@ -263,13 +263,14 @@ int32_t fvc_context_destroy(fvc_context *c) {
   cudaSetDevice(c->device);
   free_matrix(c);
   for (int i = 0; i < 8; ++i) cudaFree(c->S.v[i]);
-  for (int i = 0; i < 9; ++i) cudaFree(c->S.f[i]);
+  for (int i = 0; i < 10; ++i) cudaFree(c->S.f[i]);
   cudaFree(c->S.g);
   cudaFree(c->S.partials);
   cudaFree(c->S.sync);
   cudaFree(c->S.err);
   cudaFree(c->S.result);
   cudaFree(c->S.iresult);
+  cudaFree(c->S.trace);
   cudaFree(c->d_b);
   cudaFree(c->d_x);
   delete c;
@@ -396,6 +397,21 @@ int32_t fvc_matrix_info(const fvc_context *c, int64_t *n, int64_t *slots, int64_
   if (nnz_off) *nnz_off = c->A.nnz_off;
   if (nslices) *nslices = c->A.nslices;
   return FVC_OK;
+}
+
+int32_t fvc_solve_trace(const fvc_context *c, int32_t max, int32_t *its, double *relres) {
+  if (!c || !c->S.trace || !c->S.iresult || max < 0) return -FVC_ERR_ARG;
+  int ires[16];
+  double tr[2 * fvc::kTraceMax];
+  if (cudaMemcpy(ires, c->S.iresult, sizeof(ires), cudaMemcpyDeviceToHost) != cudaSuccess ||
+      cudaMemcpy(tr, c->S.trace, sizeof(tr), cudaMemcpyDeviceToHost) != cudaSuccess)
+    return -FVC_ERR_CUDA;
+  const int n = std::min(std::min(ires[0], fvc::kTraceMax), (int)max);
+  for (int k = 0; k < n; ++k) {
+    if (its) its[k] = (int32_t)tr[2 * k];
+    if (relres) relres[k] = tr[2 * k + 1];
+  }
+  return n;
 }
 
 int32_t fvc_spmv(fvc_context *c, const double *d_x, double *d_y) {

@@ -286,6 +286,7 @@ inline int32_t ensure_sync(Scratch &S, size_t nblocks) {
     if (cudaMalloc(&S.err, 64) != cudaSuccess) return FVC_ERR_CUDA;
     if (cudaMalloc(&S.result, 16 * sizeof(double)) != cudaSuccess) return FVC_ERR_CUDA;
     if (cudaMalloc(&S.iresult, 16 * sizeof(int)) != cudaSuccess) return FVC_ERR_CUDA;
+    if (cudaMalloc(&S.trace, 2 * kTraceMax * sizeof(double)) != cudaSuccess) return FVC_ERR_CUDA;
   }
   return FVC_OK;
 }

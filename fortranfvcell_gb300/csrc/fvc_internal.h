@@ -39,7 +39,7 @@ struct DeviceMatrix {
 struct Scratch {
   size_t n = 0, nf = 0, ngmres = 0;  // capacities of v[], f[], g
   double *v[8] = {nullptr};     // Krylov vectors
-  float *f[9] = {nullptr};      // FP32 vectors (mixed precision)
+  float *f[10] = {nullptr};     // FP32 vectors (mixed precision)
   double *g = nullptr;          // GMRES basis (k+1) x n
   double *partials = nullptr;   // reduction partials
   size_t npart = 0;
@@ -47,7 +47,10 @@ struct Scratch {
   int *err = nullptr;
   double *result = nullptr;     // solver scalars written by block 0
   int *iresult = nullptr;
+  double *trace = nullptr;      // per residual replacement: (iteration, ||r||/||b||)
 };
+
+constexpr int kTraceMax = 256;
 
 struct Launch {
   int threads = 256;

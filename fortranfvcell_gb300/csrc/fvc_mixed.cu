@@ -114,15 +114,18 @@ struct MArgs {
   const double *b;
   double *x;
   float *rs, *pa, *pb, *q, *r0, *v, *t, *z;
+  float *rsl;           // CG: low part of the residual (FP32 pair rs + rsl)
   float2 *e;            // correction, FP32 pair (hi, lo)
   GridSync gs;
   double target;        // refine tolerance on ||b-Ax||/||b||
   double inner_tol;
   int max_refine;
+  int update_beta;      // 1: beta from the recursive residual at updates
   int maxit;            // cap on total inner iterations
   int init;
   double *result;
   int *iresult;
+  double *trace;        // (iteration, relres) per residual replacement
 };
 
 // (A y)_row in FP32 difference form, y supplied by a functor.
@@ -183,9 +186,11 @@ __device__ __forceinline__ bool residual_sweep(const MArgs &a, unsigned int &ep,
     const double ri = bi - ax;
     const float rsi = (float)ri;
     a.rs[row] = rsi;
+    if (a.rsl) a.rsl[row] = (float)(ri - (double)rsi);
     acc[0] = fma(ri, ri, acc[0]);
     acc[1] = fma(bi, bi, acc[1]);
     const float mi = a.minv[row];
+    a.z[row] = rsi * mi;
     acc[2] = fma((double)rsi, (double)(rsi * mi), acc[2]);
     if (mi != 0.0f) acc[3] = fma(ri, ri, acc[3]);
   }
@@ -213,6 +218,152 @@ __device__ __forceinline__ void fold_correction(const MArgs &a) {
   }
 }
 
+// CG phase A: p = z + beta p_prev (formed on the fly at the neighbours),
+// q = A p, returns p.q.  Each warp handles two slices per step and issues
+// every load of both before any arithmetic, so two slices' streams and
+// gathers are in flight per warp (the loop is latency-bound otherwise).
+template <bool kFirst>
+__device__ __forceinline__ double cg_phase_a(const MArgs &a, const MPart &P, float beta,
+                                             const float *__restrict__ z,
+                                             const float *__restrict__ pp,
+                                             float *__restrict__ pcur, float *__restrict__ q,
+                                             float2 *__restrict__ e) {
+  CSum cpq;
+  const int n = P.n;
+  const int64_t *__restrict__ sptr = a.A.sptr;
+  const int *__restrict__ col = a.A.col;
+  const float *__restrict__ w32 = a.w32;
+  const float *__restrict__ e32 = a.e32;
+  for (int s0 = P.sb + P.warp; s0 < P.se; s0 += 2 * P.nwarps) {
+    int row[2], wd[2];
+    bool ok[2];
+    int64_t base[2];
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const int sl = s0 + u * P.nwarps;
+      row[u] = sl * 32 + P.lane;
+      ok[u] = (sl < P.se) && (row[u] < n);
+      base[u] = 0;
+      wd[u] = 0;
+      if (sl < P.se) {
+        base[u] = sptr[sl];
+        wd[u] = (int)((sptr[sl + 1] - base[u]) >> 5);
+      }
+    }
+    if (wd[0] > 4 || wd[1] > 4) {  // wide slices: one row at a time
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        if (!ok[u]) continue;
+        auto pf = [&](int k) { return kFirst ? z[k] : fmaf(beta, pp[k], z[k]); };
+        const float pi = pf(row[u]);
+        const float t = arow32(a, s0 + u * P.nwarps, P.lane, row[u], pf);
+        pcur[row[u]] = pi;
+        q[row[u]] = t;
+        if (kFirst) e[row[u]] = make_float2(0.0f, 0.0f);
+        cpq.add(pi * t);
+      }
+      continue;
+    }
+    int c[2][4];
+    float w[2][4], ex[2], zo[2], po[2];
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const bool use = ok[u] && k < wd[u];
+        c[u][k] = use ? ld_stream(col + base[u] + 32 * k + P.lane) : (ok[u] ? row[u] : 0);
+        w[u][k] = use ? ld_stream(w32 + base[u] + 32 * k + P.lane) : 0.0f;
+      }
+      ex[u] = ok[u] ? ld_stream(e32 + row[u]) : 0.0f;
+      zo[u] = ok[u] ? z[row[u]] : 0.0f;
+      po[u] = (!kFirst && ok[u]) ? pp[row[u]] : 0.0f;
+    }
+    float nb[2][4];
+#pragma unroll
+    for (int u = 0; u < 2; ++u)
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const int ck = c[u][k];
+        nb[u][k] = kFirst ? z[ck] : fmaf(beta, pp[ck], z[ck]);
+      }
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      if (!ok[u]) continue;
+      const float pi = kFirst ? zo[u] : fmaf(beta, po[u], zo[u]);
+      float t = ex[u] * pi;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) t = fmaf(w[u][k], pi - nb[u][k], t);
+      pcur[row[u]] = pi;
+      q[row[u]] = t;
+      if (kFirst) e[row[u]] = make_float2(0.0f, 0.0f);
+      cpq.add(pi * t);
+    }
+  }
+  return cpq.value();
+}
+
+// CG phase B: e += alpha p (FP32 pair), rs -= alpha q, z = rs/m; sums
+// rs.z and rs.rs (over the rows the FP32 iteration moves).  kUB slices
+// per warp step, loads first.  With kPair the residual is carried as an
+// FP32 pair (rs + rsl): rounding the residual recurrence to one FP32
+// number delays the last decades of convergence (the lowest eigenvalues of
+// the Jacobi-scaled matrix approach the FP32 rounding level), so the pair
+// is switched on below kPairFrom relative residual; earlier iterations
+// stream the high part only (the two parts live in separate arrays).
+// Measured (and emulated in numpy): promoting the residual only late does
+// not help -- the lost orthogonality dates from the first iterations -- so
+// the pair runs from the start unless the caller opts out.
+constexpr int kUB = 2;
+constexpr double kPairFrom = 1.0e300;  // always
+template <bool kPair>
+__device__ __forceinline__ void cg_phase_b(const MPart &P, float alpha, float alpha_lo,
+                                           const float *__restrict__ pcur,
+                                           const float *__restrict__ q, float *__restrict__ rs,
+                                           float *__restrict__ rsl, float *__restrict__ z,
+                                           float2 *__restrict__ e,
+                                           const float *__restrict__ minv, CSum &crz,
+                                           CSum &crr) {
+  const int n = P.n;
+  for (int s0 = P.sb + P.warp; s0 < P.se; s0 += kUB * P.nwarps) {
+    int row[kUB];
+    bool ok[kUB];
+    float2 ev[kUB];
+    float pv[kUB], qv[kUB], rv[kUB], rl[kUB], mv[kUB];
+#pragma unroll
+    for (int u = 0; u < kUB; ++u) {
+      const int sl = s0 + u * P.nwarps;
+      row[u] = sl * 32 + P.lane;
+      ok[u] = (sl < P.se) && (row[u] < n);
+      if (ok[u]) {
+        ev[u] = e[row[u]];
+        pv[u] = pcur[row[u]];
+        qv[u] = q[row[u]];
+        rv[u] = rs[row[u]];
+        rl[u] = kPair ? rsl[row[u]] : 0.0f;
+        mv[u] = minv[row[u]];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kUB; ++u) {
+      if (!ok[u]) continue;
+      e[row[u]] = df_axpy(ev[u], alpha, alpha_lo, pv[u]);
+      float r;
+      if (kPair) {
+        const float2 rp = df_axpy(make_float2(rv[u], rl[u]), -alpha, -alpha_lo, qv[u]);
+        r = rp.x;
+        rsl[row[u]] = rp.y;
+      } else {
+        r = fmaf(-alpha, qv[u], rv[u]);
+      }
+      const float zz = r * mv[u];
+      rs[row[u]] = r;
+      z[row[u]] = zz;
+      crz.add(r * zz);
+      if (mv[u] != 0.0f) crr.add(r * r);
+    }
+  }
+}
+
 __global__ void __launch_bounds__(1024, 1) mixed_cg(MArgs a) {
   __shared__ double red[kMaxNV * 32];
   const MPart P(a.A.nslices, a.A.n);
@@ -229,51 +380,27 @@ __global__ void __launch_bounds__(1024, 1) mixed_cg(MArgs a) {
   const double target2 = a.target * a.target * scale;
   float beta = 0.0f;
   float *pprev = a.pb, *pcur = a.pa;
-  const float *rs = a.rs;
-  const float *minv = a.minv;
+  bool pair = relres <= kPairFrom;
   if (!(relres == relres)) status = FVC_ERR_NAN;
   else if (relres <= a.target) status = FVC_OK;
   while (status == FVC_ERR_NOCONV && it < a.maxit) {
     ++it;
-    // p = z + beta p_prev (z = rs/m), formed on the fly at the neighbours;
-    // q = A p ; p.q
-    CSum cpq;
-    const float *pp = pprev;
-    if (it == 1) {
-      MFOR_ROWS(P) {
-        auto pf = [&](int k) { return rs[k] * minv[k]; };
-        const float pi = pf(row);
-        pcur[row] = pi;
-        a.e[row] = make_float2(0.0f, 0.0f);
-        const float qi = arow32(a, s_, P.lane, row, pf);
-        a.q[row] = qi;
-        cpq.add(pi * qi);
-      }
-    } else {
-      MFOR_ROWS(P) {
-        auto pf = [&](int k) { return fmaf(beta, pp[k], rs[k] * minv[k]); };
-        const float pi = pf(row);
-        pcur[row] = pi;
-        const float qi = arow32(a, s_, P.lane, row, pf);
-        a.q[row] = qi;
-        cpq.add(pi * qi);
-      }
-    }
-    double pq[1] = {cpq.value()};
+    // p = z + beta p_prev (formed on the fly at the neighbours); q = A p; p.q
+    double pq[1];
+    if (it == 1)
+      pq[0] = cg_phase_a<true>(a, P, beta, a.z, pprev, pcur, a.q, a.e);
+    else
+      pq[0] = cg_phase_a<false>(a, P, beta, a.z, pprev, pcur, a.q, a.e);
     if (!grid_allreduce<1>(a.gs, ep, pq, red)) return;
     const double alpha_d = rz / pq[0];
     const float alpha = (float)alpha_d;
     const float alpha_lo = (float)(alpha_d - (double)alpha);
-    // e += alpha p (FP32 pair) ; rs -= alpha q ; rs.z ; rs.rs
+    // e += alpha p (FP32 pair) ; rs -= alpha q ; z = rs/m ; rs.z ; rs.rs
     CSum crz, crr;
-    MFOR_ROWS(P) {
-      a.e[row] = df_axpy(a.e[row], alpha, alpha_lo, pcur[row]);
-      const float ri = fmaf(-alpha, a.q[row], a.rs[row]);
-      a.rs[row] = ri;
-      const float mi = minv[row];
-      crz.add(ri * (ri * mi));
-      if (mi != 0.0f) crr.add(ri * ri);
-    }
+    if (pair)
+      cg_phase_b<true>(P, alpha, alpha_lo, pcur, a.q, a.rs, a.rsl, a.z, a.e, a.minv, crz, crr);
+    else
+      cg_phase_b<false>(P, alpha, alpha_lo, pcur, a.q, a.rs, a.rsl, a.z, a.e, a.minv, crz, crr);
     double acc[2] = {crz.value(), crr.value()};
     if (!grid_allreduce<2>(a.gs, ep, acc, red)) return;
     double rz_new = acc[0];
@@ -288,6 +415,10 @@ __global__ void __launch_bounds__(1024, 1) mixed_cg(MArgs a) {
       if (!residual_sweep(a, ep, false, res, red)) return;
       ++updates;
       relres = sqrt(res[0] / scale);
+      if (blockIdx.x == 0 && threadIdx.x == 0 && updates <= kTraceMax) {
+        a.trace[2 * (updates - 1)] = (double)it;
+        a.trace[2 * (updates - 1) + 1] = relres;
+      }
       if (!(relres == relres)) {
         status = FVC_ERR_NAN;
         break;
@@ -296,8 +427,18 @@ __global__ void __launch_bounds__(1024, 1) mixed_cg(MArgs a) {
         status = FVC_OK;
         break;
       }
-      rz_new = res[2];
+      if (relres <= kPairFrom) pair = true;  // the sweep wrote both parts
       rr_upd = res[3];
+      if (a.update_beta) {
+        // beta from the recursive residual, the next alpha from the true one
+        beta = (float)(rz_new / rz);
+        rz = res[2];
+        float *tmp = pprev;
+        pprev = pcur;
+        pcur = tmp;
+        continue;
+      }
+      rz_new = res[2];
     }
     beta = (float)(rz_new / rz);
     rz = rz_new;
@@ -465,13 +606,13 @@ int32_t run_mixed(const DeviceMatrix &A0, Scratch &S, int code, const double *b,
   if (rc != FVC_OK) return rc;
   const size_t n = (size_t)A.n;
   if (S.nf < n) {
-    for (int i = 0; i < 9; ++i) {
+    for (int i = 0; i < 10; ++i) {
       if (S.f[i]) cudaFree(S.f[i]);
       S.f[i] = nullptr;
     }
     S.nf = n;
   }
-  for (int i = 0; i < 9; ++i)  // f[4] holds the float2 correction
+  for (int i = 0; i < 10; ++i)  // f[4] holds the float2 correction
     if (!S.f[i] && cudaMalloc(&S.f[i], sizeof(float) * (i == 4 ? 2 : 1) * (n + 64)) != cudaSuccess)
       return FVC_ERR_CUDA;
   auto kern = (code == 1) ? mixed_cg : mixed_bicgstab;
@@ -507,14 +648,17 @@ int32_t run_mixed(const DeviceMatrix &A0, Scratch &S, int code, const double *b,
   a.t = S.f[6];
   a.v = S.f[7];
   a.z = S.f[8];
+  a.rsl = (code == 1) ? S.f[9] : nullptr;
   a.gs = make_sync(S, blocks);
   a.target = (o.refine_tol > 0) ? o.refine_tol : tol;
   a.inner_tol = (o.inner_tol > 0) ? o.inner_tol : (code == 1 ? 0.1 : 1e-4);
   a.max_refine = (o.max_refine > 0) ? o.max_refine : 30;
+  a.update_beta = o.update_beta;
   a.maxit = maxit;
   a.init = init;
   a.result = S.result;
   a.iresult = S.iresult;
+  a.trace = S.trace;
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);

@@ -30,7 +30,8 @@ def _p(a):
 
 def make_opts(precision: str = "fp64", init: int = -1, stop_rule: int = 0,
               refine_tol: float = 0.0, inner_tol: float = 0.0, max_refine: int = 0,
-              block_threads: int = 0, blocks_per_sm: int = 0) -> FvcOpts:
+              block_threads: int = 0, blocks_per_sm: int = 0,
+              update_beta: int = 0) -> FvcOpts:
     o = FvcOpts()
     _lib.load().fvc_opts_default(C.byref(o))
     o.precision = {"fp64": _lib.FVC_PREC_FP64, "mixed": _lib.FVC_PREC_MIXED}[precision]
@@ -41,6 +42,7 @@ def make_opts(precision: str = "fp64", init: int = -1, stop_rule: int = 0,
     o.max_refine = max_refine
     o.block_threads = block_threads
     o.blocks_per_sm = blocks_per_sm
+    o.update_beta = update_beta
     return o
 
 
@@ -131,6 +133,17 @@ class Context:
                                f"{_lib.STATUS_NAMES.get(rc, rc)}")
         st.status = rc
         return st
+
+    def trace(self, max_records: int = 256):
+        """(iterations, rel. residuals) at the residual replacements of the
+        last mixed-precision CG solve."""
+        its = np.zeros(max_records, np.int32)
+        rel = np.zeros(max_records, np.float64)
+        k = self._L.fvc_solve_trace(self._h, max_records, its.ctypes.data_as(C.c_void_p),
+                                    rel.ctypes.data_as(C.c_void_p))
+        if k < 0:
+            raise FvcError(-k, "fvc_solve_trace failed")
+        return its[:k], rel[:k]
 
     def spmv(self, x_dev, y_dev) -> None:
         _lib.check(self._L.fvc_spmv(self._h, C.c_void_p(_addr(x_dev)), C.c_void_p(_addr(y_dev))),

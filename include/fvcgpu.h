@@ -85,7 +85,10 @@ typedef struct {
   int32_t stop_rule;   /* 0: the reference's test for the method;
                           1: ||r||2 <= tol*||b||2 on the recurrence residual */
   int32_t want_residual; /* 1: recompute ||b-Ax||/||b|| in FP64 at exit   */
-  int32_t reserved[3];
+  int32_t update_beta; /* MIXED CG: beta = (r.z)/(r_old.z_old) at a residual
+                          replacement taken from 0: the replaced (true)
+                          residual; 1: the recursive one                 */
+  int32_t reserved[2];
 } fvc_opts;
 
 typedef struct {
@@ -152,6 +155,13 @@ int32_t fvc_spmv_fast(fvc_context *ctx, const double *d_x, double *d_y);
  * y_i = e_i x_i + sum_k w_ik (x_i - x_k), w = -a_ik, e_i = a_ii - sum w),
  * FP32 vectors; asynchronous. */
 int32_t fvc_spmv_f32(fvc_context *ctx, const float *d_x, float *d_y);
+
+/* Convergence record of the last MIXED CG solve on this context: for each
+ * residual replacement (at most max, and at most 256) the inner iteration
+ * and the recomputed FP64 ||b-Ax||/||b||.  Returns the number of records,
+ * or a negative FVC_* status. */
+int32_t fvc_solve_trace(const fvc_context *ctx, int32_t max, int32_t *its,
+                        double *relres);
 
 /* Describe the device layout: rows, stored off-diagonal slots (with
  * padding), true off-diagonal nonzeros, slice count. */
