@@ -83,6 +83,8 @@ SIGNATURES = {
     "fvc_matrix_info": ([P, C.POINTER(I64), C.POINTER(I64), C.POINTER(I64), C.POINTER(I64)], I32),
     "fvc_kernel_launches": ([], I64),
     "fvc_solve_trace": ([P, I32, P, P], I32),
+    "fvc_pcg_csrd_noalloc": ([P, P, P, P, I32, P, P, F64, I32, I32, I32, P,
+                              C.POINTER(FvcStats)], I32),
     "fvc_mesh_adjacency": ([P, I32, I32, I32, I32, P], I32),
     "fvc_mesh_rcm": ([P, I32, I32, I32, P], I32),
     "fvc_mesh_numeq": ([P, P, I32, I32, P], I32),

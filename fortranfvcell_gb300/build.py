@@ -19,7 +19,7 @@ LIBDIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIBDIR, "libfvcgpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["fvc_krylov.cu", "fvc_mixed.cu", "fvc_gather.cu", "fvc_assembly.cu",
-           "fvc_api.cpp", "fvc_mesh.cpp"]
+           "fvc_noalloc.cu", "fvc_api.cpp", "fvc_mesh.cpp"]
 
 
 def nvcc() -> str:

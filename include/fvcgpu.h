@@ -171,6 +171,29 @@ int32_t fvc_matrix_info(const fvc_context *ctx, int64_t *n, int64_t *slots,
 /* Number of kernels this library launched since load (instrumentation). */
 int64_t fvc_kernel_launches(void);
 
+/* ---- allocation-free solve --------------------------------------------- */
+/* No counterpart in the reference.  FP64 Jacobi-PCG (the method of
+ * fvc_solve with code 1) on a CSRD matrix (matriz 1, unsym: ad(neq), au(nad),
+ * 1-based ia(neq+1)/ja(nad)) that the caller already holds in DEVICE memory,
+ * with b, x also device pointers (x: initial guess unless init, then the
+ * solution).  For callers that cannot allocate device memory at solve time
+ * (a fixed device budget handed out at start-up, allocations owned by a
+ * pool outside the caller, or a time step that must not synchronise on a
+ * cudaMalloc): it calls no cudaMalloc/cudaFree.  Its scratch is one static
+ * device array of about 5.0 MiB that every GPU loading this library holds
+ * until exit; neq above 131072 is rejected with FVC_ERR_ARG and a message.
+ * The first call on each device looks up that array's device address; make
+ * that first call before any stream capture.  All calls share the array, so
+ * calls that overlap on the GPU (two streams, two host threads) race; the
+ * call is synchronous on `stream` (a cudaStream_t, NULL = default stream).
+ * stop_rule as in fvc_opts.  Returns an FVC_* status; stats may be NULL. */
+int32_t fvc_pcg_csrd_noalloc(const double *d_ad, const double *d_au,
+                             const int32_t *d_ia, const int32_t *d_ja,
+                             int32_t neq, const double *d_b, double *d_x,
+                             double tol, int32_t maxit, int32_t init,
+                             int32_t stop_rule, void *stream,
+                             fvc_stats *stats);
+
 /* ---- mesh -> equation graph (host) ------------------------------------- */
 /* Face-neighbour table.  ix(ld,numel) column-major holds each cell's nodes
  * (1-based, counter-clockwise) in its first slots; a cell has nsides =
