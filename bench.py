@@ -135,10 +135,19 @@ def pcg_bytes_fp64(n, nnz):
 
 
 def cg_bytes_fp32(n, nnz):
-    # FP32 inner CG on the Jacobi-scaled matrix (unit diagonal implicit):
-    # SpMV 8 B per off-diagonal + p read + q write; update pass reads
-    # e, p, r, q and writes e, r; direction pass reads r, p, writes p
-    return 8 * nnz + 8 * n + 24 * n + 12 * n
+    # one mixed-precision CG iteration: FP32 weights + columns (8 B per true
+    # off-diagonal); phase A reads z, p_prev, e_i and writes p, q (20 B per
+    # row); phase B reads the FP32-pair correction (8) and residual (8), p,
+    # q, 1/m and writes correction (8), residual (8) and z (48 B per row)
+    return 8 * nnz + 68 * n
+
+
+# DRAM bytes per mixed-CG iteration measured with ncu on the profiling case
+# of this workload (bench.py --profile-its 200: dram__bytes_read.sum +
+# dram__bytes_write.sum of mixed_cg, less its one residual sweep, / 200);
+# used to report roofline.traffic, scaled by the iterations of a launch.
+MEASURED_BYTES_PER_ITERATION = {4192598: 413.0e6}
+MEASURED_BYTES_PER_SWEEP = {4192598: 0.33e9}
 
 
 def refine_bytes(n, nnz):
@@ -243,6 +252,10 @@ def run_ours(args):
     inner = st.inner_iterations
     sweeps = st.refinements
     alg_bytes = inner * cg_bytes_fp32(n, nnz) + (sweeps + 1) * refine_bytes(n, nnz)
+    traffic = None
+    if n in MEASURED_BYTES_PER_ITERATION:
+        traffic = int(inner * MEASURED_BYTES_PER_ITERATION[n]
+                      + (sweeps + 1) * MEASURED_BYTES_PER_SWEEP[n])
     hbm, peak_kind = peaks()
     achieved = alg_bytes / (kernel_ms * 1e-3) / 1e9
 
@@ -333,7 +346,7 @@ def run_ours(args):
                  "frac_of_peak": round(spmv_gbs / hbm, 3),
                  "ref_rounding_gbs": round(spmv_bytes / (spmv_ref_ms * 1e-3) / 1e9, 1)},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm,
-                     "unit": "GB/s", "frac": round(achieved / hbm, 3), "traffic": None,
+                     "unit": "GB/s", "frac": round(achieved / hbm, 3), "traffic": traffic,
                      "kernel": "mixed_cg (persistent, one launch per solve)",
                      "peak_kind": peak_kind,
                      "alg_bytes_per_launch": int(alg_bytes)},
@@ -344,6 +357,33 @@ def run_ours(args):
         "cpu_baseline": cpu,
     }
     return line
+
+
+def run_profile_case(args):
+    """Profiling case for ncu: the bench workload, each solver run once for
+    a fixed number of iterations (no convergence wait), plus one SpMV."""
+    import torch
+    from fortranfvcell_gb300 import Context, make_opts
+    s, b = build_system_gpu(args.nx)
+    n = s.neq
+    ctx = Context()
+    ctx.set_matrix(1, True, n, s.nad, s.ad, s.au, s.au, s.ia, s.ja)
+    bd = torch.from_numpy(b).cuda()
+    xd = torch.zeros(n, dtype=torch.float64, device="cuda")
+    y = torch.empty_like(bd)
+    torch.cuda.synchronize()
+    ctx.spmv_fast(bd, y)
+    ctx.spmv(bd, y)
+    out = {}
+    for name, opts in (("mixed", make_opts("mixed", init=1)),
+                       ("fp64", make_opts("fp64", init=1, stop_rule=1))):
+        st = ctx.solve(1, bd, xd, 1e-30, args.profile_its, opts, raise_on_error=False)
+        out[name] = {"iterations": st.iterations, "ms": round(st.solve_ms, 3),
+                     "us_per_iteration": round(st.solve_ms * 1e3 / max(st.iterations, 1), 2)}
+    torch.cuda.synchronize()
+    out["cells"] = n
+    out["nnz_off"] = ctx.info()["nnz_off"]
+    return out
 
 
 def run_reference(args):
@@ -429,7 +469,12 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--ref-sample-its", type=int, default=300)
+    ap.add_argument("--profile-its", type=int, default=0,
+                    help="profiling case: run each solver once for this many iterations")
     args = ap.parse_args()
+    if args.profile_its > 0:
+        print(json.dumps(run_profile_case(args)), flush=True)
+        return
     if args.warmup < 3:
         log("note: the timing rules want >= 3 warm-up steps")
     line = run_reference(args) if args.impl == "reference" else run_ours(args)
