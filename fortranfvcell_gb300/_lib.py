@@ -43,7 +43,8 @@ class FvcOpts(C.Structure):
         ("stop_rule", I32),
         ("want_residual", I32),
         ("update_beta", I32),
-        ("reserved", I32 * 2),
+        ("staging", I32),
+        ("reserved", I32),
     ]
 
 
@@ -83,6 +84,7 @@ SIGNATURES = {
     "fvc_matrix_info": ([P, C.POINTER(I64), C.POINTER(I64), C.POINTER(I64), C.POINTER(I64)], I32),
     "fvc_kernel_launches": ([], I64),
     "fvc_solve_trace": ([P, I32, P, P], I32),
+    "fvc_solve_history": ([P, I32, P], I32),
     "fvc_pcg_csrd_noalloc": ([P, P, P, P, I32, P, P, F64, I32, I32, I32, P,
                               C.POINTER(FvcStats)], I32),
     "fvc_mesh_adjacency": ([P, I32, I32, I32, I32, P], I32),

@@ -7,6 +7,7 @@ the same recipe runs on the x86_64 build host and on the aarch64 GPU host.
 from __future__ import annotations
 
 import concurrent.futures as cf
+import fcntl
 import os
 import shutil
 import subprocess
@@ -68,14 +69,19 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> str:
         return LIB
     os.makedirs(BUILD, exist_ok=True)
     os.makedirs(LIBDIR, exist_ok=True)
-    with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 2)) as ex:
-        objs = list(ex.map(lambda s: _compile(s, verbose_ptxas), sources()))
-    tmp = LIB + ".tmp"
-    cmd = [nvcc(), "-shared", "-o", tmp, *objs, *ARCH, "-Xcompiler", "-fPIC"]
-    res = subprocess.run(cmd, capture_output=True, text=True)
-    if res.returncode != 0:
-        raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")
-    os.replace(tmp, LIB)
+    # one build at a time: processes started together wait for the first
+    with open(os.path.join(BUILD, ".lock"), "w") as lock:
+        fcntl.flock(lock, fcntl.LOCK_EX)
+        if not force and not needs_build():
+            return LIB
+        with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 2)) as ex:
+            objs = list(ex.map(lambda s: _compile(s, verbose_ptxas), sources()))
+        tmp = f"{LIB}.{os.getpid()}.tmp"
+        cmd = [nvcc(), "-shared", "-o", tmp, *objs, *ARCH, "-Xcompiler", "-fPIC"]
+        res = subprocess.run(cmd, capture_output=True, text=True)
+        if res.returncode != 0:
+            raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")
+        os.replace(tmp, LIB)
     return LIB
 
 

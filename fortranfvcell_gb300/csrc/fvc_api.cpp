@@ -76,6 +76,8 @@ void free_matrix(fvc_context *c) {
   cudaFree(A.val32);
   cudaFree(A.diag32);
   cudaFree(A.minv32);
+  cudaFree(A.col16);
+  cudaFree(A.sflag);
   cudaFree(c->d_src);
   cudaFree(c->d_raw1);
   cudaFree(c->d_raw2);
@@ -271,6 +273,7 @@ int32_t fvc_context_destroy(fvc_context *c) {
   cudaFree(c->S.result);
   cudaFree(c->S.iresult);
   cudaFree(c->S.trace);
+  cudaFree(c->S.history);
   cudaFree(c->d_b);
   cudaFree(c->d_x);
   delete c;
@@ -411,6 +414,18 @@ int32_t fvc_solve_trace(const fvc_context *c, int32_t max, int32_t *its, double 
     if (its) its[k] = (int32_t)tr[2 * k];
     if (relres) relres[k] = tr[2 * k + 1];
   }
+  return n;
+}
+
+int32_t fvc_solve_history(const fvc_context *c, int32_t max, float *relres) {
+  if (!c || !c->S.history || !c->S.iresult || max < 0 || !relres) return -FVC_ERR_ARG;
+  int ires[16];
+  if (cudaMemcpy(ires, c->S.iresult, sizeof(ires), cudaMemcpyDeviceToHost) != cudaSuccess)
+    return -FVC_ERR_CUDA;
+  const int n = std::min(std::min(ires[2], fvc::kHistoryMax), (int)max);
+  if (n > 0 && cudaMemcpy(relres, c->S.history, sizeof(float) * n, cudaMemcpyDeviceToHost) !=
+                   cudaSuccess)
+    return -FVC_ERR_CUDA;
   return n;
 }
 

@@ -59,6 +59,9 @@ __device__ __forceinline__ unsigned int atom_add_acq_rel(unsigned int *p, unsign
   asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
   return old;
 }
+__device__ __forceinline__ void red_add_release(unsigned int *p, unsigned int v) {
+  asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
 __device__ __forceinline__ void st_release(unsigned int *p, unsigned int v) {
   asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
@@ -178,6 +181,11 @@ __device__ __forceinline__ double ld_stream(const double *p) {
   asm volatile("ld.global.nc.L1::no_allocate.f64 %0, [%1];" : "=d"(v) : "l"(p));
   return v;
 }
+__device__ __forceinline__ int16_t ld_stream16(const int16_t *p) {
+  short v;
+  asm volatile("ld.global.nc.L1::no_allocate.s16 %0, [%1];" : "=h"(v) : "l"(p));
+  return v;
+}
 __device__ __forceinline__ float ld_stream(const float *p) {
   float v;
   asm volatile("ld.global.nc.L1::no_allocate.f32 %0, [%1];" : "=f"(v) : "l"(p));
@@ -287,6 +295,7 @@ inline int32_t ensure_sync(Scratch &S, size_t nblocks) {
     if (cudaMalloc(&S.result, 16 * sizeof(double)) != cudaSuccess) return FVC_ERR_CUDA;
     if (cudaMalloc(&S.iresult, 16 * sizeof(int)) != cudaSuccess) return FVC_ERR_CUDA;
     if (cudaMalloc(&S.trace, 2 * kTraceMax * sizeof(double)) != cudaSuccess) return FVC_ERR_CUDA;
+    if (cudaMalloc(&S.history, kHistoryMax * sizeof(float)) != cudaSuccess) return FVC_ERR_CUDA;
   }
   return FVC_OK;
 }

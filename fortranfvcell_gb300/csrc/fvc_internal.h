@@ -29,6 +29,9 @@ struct DeviceMatrix {
   float *val32 = nullptr;   // w per slot (0 on padding and on a diagonal slot)
   float *diag32 = nullptr;  // e per row (clamped to +-1e30)
   float *minv32 = nullptr;  // Jacobi 1/m per row (0 for |m| beyond FP32)
+  int16_t *col16 = nullptr; // column - row per slot (when every one fits)
+  uint8_t *sflag = nullptr; // per slice: 1 if some row has e_i != 0
+  bool col16_ok = false;
   bool have32 = false;
   // host-side description of the source layout, for value updates
   int matriz = 0, unsym = 0, nad = 0;
@@ -48,9 +51,11 @@ struct Scratch {
   double *result = nullptr;     // solver scalars written by block 0
   int *iresult = nullptr;
   double *trace = nullptr;      // per residual replacement: (iteration, ||r||/||b||)
+  float *history = nullptr;     // per iteration: recursive ||r||/||b|| (first kHistoryMax)
 };
 
 constexpr int kTraceMax = 256;
+constexpr int kHistoryMax = 16384;
 
 struct Launch {
   int threads = 256;

@@ -41,6 +41,7 @@
 
 #include "fvc_device.cuh"
 #include "fvc_internal.h"
+#include "fvc_tma.cuh"
 
 namespace fvc {
 
@@ -61,6 +62,111 @@ struct CSum {
   __device__ __forceinline__ double value() const { return (double)s + (double)c; }
 };
 
+// (s, c) += (s2, c2) for unevaluated FP32 pairs: TwoSum of the leading
+// parts, the trailing parts added to the error, Fast2Sum renormalisation.
+__device__ __forceinline__ void ff_add(float &s, float &c, float s2, float c2) {
+  const float t = __fadd_rn(s, s2);
+  const float bp = __fsub_rn(t, s);
+  const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(s2, bp));
+  const float cc = __fadd_rn(__fadd_rn(c, c2), err);
+  s = __fadd_rn(t, cc);
+  c = __fsub_rn(cc, __fsub_rn(s, t));
+}
+
+// Grid-wide deterministic sum of NV compensated FP32 partials per thread.
+// Warps reduce their pairs with an FP32 butterfly (FP32 pair arithmetic,
+// not FP64: GB300 runs FP64 at ~2 lanes per clock per SM, and a block of
+// 1024 threads each doing FP64 shuffles and divisions costs microseconds
+// per reduction); warp 0 combines the warps, converts the block's pair to
+// FP64 once, publishes it and arrives on the grid counter (release), waits
+// for every block's arrival (acquire) and sums all partials in block order
+// itself, so every block holds identical totals after two trips to L2.
+// Lane 0 of warp 0 then calls f(totals) -- the place for the iteration's scalar FP64
+// work, which it publishes through shared memory -- and one __syncthreads
+// hands the results to the block.  Returns false when a wait exceeded its
+// bound (gs.err set).
+template <int NV, typename F>
+__device__ __forceinline__ bool grid_allreduce_ff(const GridSync &gs, unsigned int &episode,
+                                                  const CSum (&v)[NV], float2 *red2, F &&f) {
+  __shared__ int s_ok;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nwarps = blockDim.x >> 5;
+#pragma unroll
+  for (int q = 0; q < NV; ++q) {
+    float s = v[q].s, c = v[q].c;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const float s2 = __shfl_xor_sync(0xffffffffu, s, o);
+      const float c2 = __shfl_xor_sync(0xffffffffu, c, o);
+      ff_add(s, c, s2, c2);
+    }
+    if (lane == 0) red2[q * 32 + warp] = make_float2(s, c);
+  }
+  if (threadIdx.x == 0) s_ok = 1;
+  __syncthreads();
+  const unsigned int ep = ++episode;
+  if (warp == 0) {
+    const unsigned int nb = gs.nblocks;
+    double *part = gs.partials + (size_t)(ep & 3u) * kMaxNV * nb;
+    double bsum[NV];
+#pragma unroll
+    for (int q = 0; q < NV; ++q) {
+      const float2 w = (lane < nwarps) ? red2[q * 32 + lane] : make_float2(0.0f, 0.0f);
+      float s = w.x, c = w.y;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const float s2 = __shfl_xor_sync(0xffffffffu, s, o);
+        const float c2 = __shfl_xor_sync(0xffffffffu, c, o);
+        ff_add(s, c, s2, c2);
+      }
+      bsum[q] = (double)s + (double)c;
+    }
+    // publish the block's partials, then wait until every block has
+    bool ok = true;
+    if (lane == 0) {
+#pragma unroll
+      for (int q = 0; q < NV; ++q) part[(size_t)q * nb + blockIdx.x] = bsum[q];
+      red_add_release(gs.count, 1u);
+      const unsigned int target = ep * nb;
+      const uint64_t t0 = global_ns();
+      unsigned int spins = 0;
+      while (ld_acquire(gs.count) < target) {
+        if (*(volatile int *)gs.err != 0) {
+          ok = false;
+          break;
+        }
+        if ((++spins & 255u) == 0 && global_ns() - t0 > kBarrierTimeoutNs) {
+          atomicExch(gs.err, 7 /* FVC_ERR_TIMEOUT */);
+          ok = false;
+          break;
+        }
+        __nanosleep(20);
+      }
+    }
+    ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+    // every block sums the partials itself, in block order (identical
+    // totals everywhere; no second round trip through a release flag)
+    double t[NV];
+#pragma unroll
+    for (int q = 0; q < NV; ++q) {
+      double u = 0.0;
+      if (ok) {
+        const double *pp = part + (size_t)q * nb;
+        for (unsigned int b = lane; b < nb; b += 32) u = __dadd_rn(u, __ldcg(pp + b));
+      }
+      t[q] = warp_sum(u);
+    }
+    if (lane == 0) {
+      if (ok)
+        f(t);
+      else
+        s_ok = 0;
+    }
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
 // (hi, lo) += alpha * p with alpha given as an FP32 pair (ah, al): the
 // product ah*p is split exactly with an FMA, the sum uses TwoSum and a
 // final Fast2Sum renormalisation.
@@ -76,11 +182,14 @@ __device__ __forceinline__ float2 df_axpy(float2 e, float ah, float al, float p)
   return make_float2(hi, __fsub_rn(lo, __fsub_rn(hi, s)));
 }
 
-// e_i (FP64 sum, rounded once), Jacobi 1/m, and the FP32 weights.
+// e_i (FP64 sum, rounded once), Jacobi 1/m, the FP32 weights, the 16-bit
+// column offsets (col - row) and the per-slice "has excess" flags.
 __global__ void build_f32_operator(int n, int nslices, const int64_t *__restrict__ sptr,
                                    const int *__restrict__ col, const double *__restrict__ val,
                                    const double *__restrict__ jac, float *__restrict__ w32,
-                                   float *__restrict__ e32, float *__restrict__ minv32) {
+                                   float *__restrict__ e32, float *__restrict__ minv32,
+                                   int16_t *__restrict__ col16, uint8_t *__restrict__ sflag,
+                                   int *__restrict__ col16_overflow) {
   const int lane = threadIdx.x & 31;
   const int nw = (gridDim.x * blockDim.x) >> 5;
   for (int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < nslices; s += nw) {
@@ -88,20 +197,29 @@ __global__ void build_f32_operator(int n, int nslices, const int64_t *__restrict
     const int64_t base = sptr[s];
     const int wd = (int)((sptr[s + 1] - base) >> 5);
     double off = 0.0;  // sum of a_ik over true off-diagonal slots
+    bool wide = false;
     for (int k = 0; k < wd; ++k) {
       const int64_t q = base + 32 * k + lane;
       const bool diag_slot = (row < n) && (col[q] == row);
       const double a = (row < n && !diag_slot) ? val[q] : 0.0;
       off += a;
       w32[q] = (float)(-a);
+      const int d = (row < n) ? col[q] - row : 0;
+      if (d < -32768 || d > 32767) wide = true;
+      col16[q] = (int16_t)d;
     }
+    float ev = 0.0f;
     if (row < n) {
       const double m = jac[row];
       double e = m + off;
       e = fmin(fmax(e, -kF32Clamp), kF32Clamp);
-      e32[row] = (float)e;
+      ev = (float)e;
+      e32[row] = ev;
       minv32[row] = (fabs(m) > 1.0e37 || m == 0.0) ? 0.0f : (float)(1.0 / m);
     }
+    const bool any_e = __any_sync(0xffffffffu, ev != 0.0f);
+    if (lane == 0) sflag[s] = any_e ? 1 : 0;
+    if (__any_sync(0xffffffffu, wide) && lane == 0) atomicExch(col16_overflow, 1);
   }
 }
 
@@ -110,6 +228,8 @@ struct MArgs {
   const float *w32;     // weights per slot
   const float *e32;     // row excess
   const float *minv;    // Jacobi 1/m (0 on rows whose m is beyond FP32)
+  const int16_t *col16; // column offsets (col - row), when col16_ok
+  const uint8_t *sflag; // per slice: some row has e_i != 0
   const double *jac;    // m in FP64
   const double *b;
   double *x;
@@ -126,6 +246,7 @@ struct MArgs {
   double *result;
   int *iresult;
   double *trace;        // (iteration, relres) per residual replacement
+  float *history;       // recursive relres per iteration
 };
 
 // (A y)_row in FP32 difference form, y supplied by a functor.
@@ -202,17 +323,25 @@ __device__ __forceinline__ bool residual_sweep(const MArgs &a, unsigned int &ep,
   return true;
 }
 
-// x += e (FP64) and e = 0, own rows; a barrier must follow.  Rows whose
+// x += e (+ a deferred alpha*p) in FP64 and e = 0, own rows; a barrier
+// must follow.  Rows whose
 // diagonal is beyond FP32 range (1/m = 0: the pressure pin) are frozen in
 // the FP32 iteration; they take one FP64 Jacobi step on their current
 // residual estimate instead, which solves such a row to FP64 accuracy.
-__device__ __forceinline__ void fold_correction(const MArgs &a) {
+__device__ __forceinline__ void fold_correction(const MArgs &a, const float *ppend = nullptr,
+                                                double apend = 0.0) {
   const MPart P(a.A.nslices, a.A.n);
   MFOR_ROWS(P) {
     const float2 ev = a.e[row];
     double dx = (double)ev.x + (double)ev.y;
+    if (ppend) dx = fma(apend, (double)ppend[row], dx);  // a deferred alpha*p
     const double m = a.jac[row];
-    if (a.minv[row] == 0.0f && m != 0.0) dx += (double)a.rs[row] / m;
+    if (a.minv[row] == 0.0f && m != 0.0) {
+      // the frozen row's residual grows to the size of the neighbours' x
+      // over a cycle; the Jacobi step needs all of it (both pair parts)
+      const double rr = (double)a.rs[row] + (a.rsl ? (double)a.rsl[row] : 0.0);
+      dx += rr / m;
+    }
     a.x[row] = a.x[row] + dx;
     a.e[row] = make_float2(0.0f, 0.0f);
   }
@@ -222,8 +351,8 @@ __device__ __forceinline__ void fold_correction(const MArgs &a) {
 // q = A p, returns p.q.  Each warp handles two slices per step and issues
 // every load of both before any arithmetic, so two slices' streams and
 // gathers are in flight per warp (the loop is latency-bound otherwise).
-template <bool kFirst>
-__device__ __forceinline__ double cg_phase_a(const MArgs &a, const MPart &P, float beta,
+template <bool kFirst, bool kCol16>
+__device__ __forceinline__ CSum cg_phase_a(const MArgs &a, const MPart &P, float beta,
                                              const float *__restrict__ z,
                                              const float *__restrict__ pp,
                                              float *__restrict__ pcur, float *__restrict__ q,
@@ -236,7 +365,7 @@ __device__ __forceinline__ double cg_phase_a(const MArgs &a, const MPart &P, flo
   const float *__restrict__ e32 = a.e32;
   for (int s0 = P.sb + P.warp; s0 < P.se; s0 += 2 * P.nwarps) {
     int row[2], wd[2];
-    bool ok[2];
+    bool ok[2], hase[2];
     int64_t base[2];
 #pragma unroll
     for (int u = 0; u < 2; ++u) {
@@ -245,9 +374,11 @@ __device__ __forceinline__ double cg_phase_a(const MArgs &a, const MPart &P, flo
       ok[u] = (sl < P.se) && (row[u] < n);
       base[u] = 0;
       wd[u] = 0;
+      hase[u] = false;
       if (sl < P.se) {
         base[u] = sptr[sl];
         wd[u] = (int)((sptr[sl + 1] - base[u]) >> 5);
+        hase[u] = a.sflag[sl] != 0;
       }
     }
     if (wd[0] > 4 || wd[1] > 4) {  // wide slices: one row at a time
@@ -271,10 +402,14 @@ __device__ __forceinline__ double cg_phase_a(const MArgs &a, const MPart &P, flo
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
         const bool use = ok[u] && k < wd[u];
-        c[u][k] = use ? ld_stream(col + base[u] + 32 * k + P.lane) : (ok[u] ? row[u] : 0);
+        if (kCol16)
+          c[u][k] = use ? row[u] + (int)ld_stream16(a.col16 + base[u] + 32 * k + P.lane)
+                        : (ok[u] ? row[u] : 0);
+        else
+          c[u][k] = use ? ld_stream(col + base[u] + 32 * k + P.lane) : (ok[u] ? row[u] : 0);
         w[u][k] = use ? ld_stream(w32 + base[u] + 32 * k + P.lane) : 0.0f;
       }
-      ex[u] = ok[u] ? ld_stream(e32 + row[u]) : 0.0f;
+      ex[u] = (ok[u] && hase[u]) ? ld_stream(e32 + row[u]) : 0.0f;
       zo[u] = ok[u] ? z[row[u]] : 0.0f;
       po[u] = (!kFirst && ok[u]) ? pp[row[u]] : 0.0f;
     }
@@ -299,7 +434,7 @@ __device__ __forceinline__ double cg_phase_a(const MArgs &a, const MPart &P, flo
       cpq.add(pi * t);
     }
   }
-  return cpq.value();
+  return cpq;
 }
 
 // CG phase B: e += alpha p (FP32 pair), rs -= alpha q, z = rs/m; sums
@@ -315,9 +450,13 @@ __device__ __forceinline__ double cg_phase_a(const MArgs &a, const MPart &P, flo
 // the pair runs from the start unless the caller opts out.
 constexpr int kUB = 2;
 constexpr double kPairFrom = 1.0e300;  // always
-template <bool kPair>
-__device__ __forceinline__ void cg_phase_b(const MPart &P, float alpha, float alpha_lo,
-                                           const float *__restrict__ pcur,
+// With kUpdE the correction takes the two pending steps at once,
+// e += a1 p_prev + a2 p_cur (both p buffers are intact in phase B), so the
+// correction is read and written every second iteration only.
+template <bool kPair, bool kUpdE>
+__device__ __forceinline__ void cg_phase_b(const MPart &P, float a1, float a1_lo,
+                                           const float *__restrict__ pprev, float alpha,
+                                           float alpha_lo, const float *__restrict__ pcur,
                                            const float *__restrict__ q, float *__restrict__ rs,
                                            float *__restrict__ rsl, float *__restrict__ z,
                                            float2 *__restrict__ e,
@@ -328,15 +467,18 @@ __device__ __forceinline__ void cg_phase_b(const MPart &P, float alpha, float al
     int row[kUB];
     bool ok[kUB];
     float2 ev[kUB];
-    float pv[kUB], qv[kUB], rv[kUB], rl[kUB], mv[kUB];
+    float p1[kUB], pv[kUB], qv[kUB], rv[kUB], rl[kUB], mv[kUB];
 #pragma unroll
     for (int u = 0; u < kUB; ++u) {
       const int sl = s0 + u * P.nwarps;
       row[u] = sl * 32 + P.lane;
       ok[u] = (sl < P.se) && (row[u] < n);
       if (ok[u]) {
-        ev[u] = e[row[u]];
-        pv[u] = pcur[row[u]];
+        if (kUpdE) {
+          ev[u] = e[row[u]];
+          p1[u] = pprev[row[u]];
+          pv[u] = pcur[row[u]];
+        }
         qv[u] = q[row[u]];
         rv[u] = rs[row[u]];
         rl[u] = kPair ? rsl[row[u]] : 0.0f;
@@ -346,7 +488,7 @@ __device__ __forceinline__ void cg_phase_b(const MPart &P, float alpha, float al
 #pragma unroll
     for (int u = 0; u < kUB; ++u) {
       if (!ok[u]) continue;
-      e[row[u]] = df_axpy(ev[u], alpha, alpha_lo, pv[u]);
+      if (kUpdE) e[row[u]] = df_axpy(df_axpy(ev[u], a1, a1_lo, p1[u]), alpha, alpha_lo, pv[u]);
       float r;
       if (kPair) {
         const float2 rp = df_axpy(make_float2(rv[u], rl[u]), -alpha, -alpha_lo, qv[u]);
@@ -364,97 +506,536 @@ __device__ __forceinline__ void cg_phase_b(const MPart &P, float alpha, float al
   }
 }
 
-__global__ void __launch_bounds__(1024, 1) mixed_cg(MArgs a) {
+// ---------------------------------------------------------------------
+// Staged phases.  Each block walks its slice range in chunks of 32 slices
+// (1024 rows: one slice per warp in phase A, one row per thread in phase
+// B).  Warp 0 keeps bulk copies (TMA) running ahead into shared memory,
+// so the streams arrive without occupying registers or warps:
+//  * phase A keeps a window of z and p_prev around the chunk it works on
+//    -- chunks i-3 .. i+3 of the block's rows, reaching into the
+//    neighbouring blocks' rows -- in a ring of kWinSlots chunk slots, so
+//    the neighbour gathers of q = A p read shared memory (under the RCM
+//    numbering of a 2-D mesh with up to ~3000 rows per level, every
+//    neighbour lies in the window; one outside it is read from global
+//    memory), and stages each chunk's weights and column offsets in
+//    kAStages buffers;
+//  * phase B stages all of its row vectors in kBStages buffers.
+// The two phases reuse the same shared memory (a grid barrier separates
+// them).  A chunk with more than kStSlotCap slots (mean row width above 5)
+// reads its weights and offsets from global memory instead.
+constexpr int kStChunkSlices = 32;
+constexpr int kStRows = kStChunkSlices * kSlice;  // = threads per block
+constexpr int kStSlotCap = kStRows * 5;
+constexpr int kWinHalo = 3;                      // window: chunks i-3 .. i+3
+constexpr int kWinSlots = 10;                    // window + 3 chunks in flight
+constexpr int kWinSpan = (2 * kWinHalo + 1) * kStRows;
+constexpr int kAStages = 4;
+constexpr int kBStages = 6;
+// window slot: z[1024] | pp[1024]
+constexpr uint32_t kWinSlotBytes = 2 * kStRows * 4;
+// phase-A stage (after the window): w32[kStSlotCap] | col16[kStSlotCap]
+constexpr uint32_t kA_Base = kWinSlots * kWinSlotBytes;
+constexpr uint32_t kA_C = kStSlotCap * 4;
+constexpr uint32_t kA_Bytes = kA_C + kStSlotCap * 2;
+// phase-B stage: q | rs | rsl | minv | pprev | pcur (1024 floats each) | e[1024] float2
+constexpr uint32_t kB_Q = 0, kB_RS = kStRows * 4, kB_RSL = 2 * kStRows * 4,
+                   kB_MINV = 3 * kStRows * 4, kB_PPREV = 4 * kStRows * 4,
+                   kB_PCUR = 5 * kStRows * 4, kB_E = 6 * kStRows * 4;
+constexpr uint32_t kB_Bytes = kB_E + kStRows * 8;
+constexpr uint32_t kRegionA = kA_Base + kAStages * kA_Bytes;
+constexpr uint32_t kRegionB = kBStages * kB_Bytes;
+constexpr uint32_t kStHeader = 256;
+constexpr size_t kStSmem = kStHeader + (kRegionA > kRegionB ? kRegionA : kRegionB);
+static_assert(kA_Bytes % 128 == 0 && kB_Bytes % 128 == 0 && kA_Base % 128 == 0, "alignment");
+static_assert(kStSmem + 2048 <= 227 * 1024, "shared memory per block");
+
+struct StHdr {
+  uint64_t win[kWinSlots];  // window chunk landed
+  uint64_t sa[kAStages];    // phase-A stage landed
+  uint64_t sb[kBStages];    // phase-B stage landed
+  int64_t base[kAStages];   // first slot of the chunk in each phase-A stage
+  int ok[kAStages];         // 1: its weights and offsets are staged
+};
+static_assert(sizeof(StHdr) <= kStHeader, "stage header");
+
+// Running counts of the copies issued into each ring (the same in every
+// thread): ring slot = count % size, mbarrier parity = (count / size) & 1.
+struct StCount {
+  uint32_t win = 0, sa = 0, sb = 0;
+};
+
+__device__ __forceinline__ unsigned char *st_region(unsigned char *smem) {
+  return smem + kStHeader;
+}
+
+// Chunk boundaries sptr[min(se, sb + 32 j)], cached 32 at a time in the
+// lanes of warp 0 (every lane calls with the same j).
+struct Bounds {
+  int64_t v;
+  int jb;
+};
+__device__ __forceinline__ int64_t bounds_get(Bounds &B, const MArgs &a, const MPart &P, int j) {
+  if (j < B.jb || j >= B.jb + 32) {
+    B.jb = j;
+    const int s = min(P.se, P.sb + kStChunkSlices * (j + P.lane));
+    B.v = a.A.sptr[s];
+  }
+  return __shfl_sync(0xffffffffu, B.v, j - B.jb);
+}
+
+__device__ __forceinline__ int st_chunks(const MPart &P) {
+  return (P.se > P.sb) ? (P.se - P.sb + kStChunkSlices - 1) / kStChunkSlices : 0;
+}
+
+// Lane 0 of warp 0: window chunk j (rows R0 + 1024 j .., clipped to the
+// padded row range [0, nrows)) of z and p_prev into its ring slot.
+template <bool kFirst>
+__device__ __forceinline__ void issue_win(const MPart &P, unsigned char *smem, uint32_t seq,
+                                          int j, int nrows, const float *z, const float *pp) {
+  StHdr *H = reinterpret_cast<StHdr *>(smem);
+  const uint32_t slot = seq % kWinSlots;
+  const int c0 = P.sb * kSlice + j * kStRows;
+  const int lo = max(c0, 0), hi = min(c0 + kStRows, nrows);
+  uint64_t *bar = &H->win[slot];
+  if (hi <= lo) {
+    mbar_arrive_expect_tx(bar, 0);
+    return;
+  }
+  const uint32_t bytes = (uint32_t)(hi - lo) * 4u;
+  unsigned char *dst = st_region(smem) + slot * kWinSlotBytes + (uint32_t)(lo - c0) * 4u;
+  mbar_arrive_expect_tx(bar, kFirst ? bytes : 2u * bytes);
+  bulk_g2s(dst, z + lo, bytes, bar);
+  if (!kFirst) bulk_g2s(dst + kStRows * 4, pp + lo, bytes, bar);
+}
+
+// Warp 0: weights and column offsets of chunk j into phase-A stage seq.
+__device__ __forceinline__ void issue_slots(const MArgs &a, const MPart &P, unsigned char *smem,
+                                            Bounds &B, uint32_t seq, int j) {
+  StHdr *H = reinterpret_cast<StHdr *>(smem);
+  const int64_t s0 = bounds_get(B, a, P, j);
+  const int64_t s1 = bounds_get(B, a, P, j + 1);
+  if (P.lane != 0) return;
+  const uint32_t stg = seq % kAStages;
+  const int64_t nsl = s1 - s0;
+  const bool ok = nsl <= kStSlotCap;
+  H->base[stg] = s0;
+  H->ok[stg] = ok ? 1 : 0;
+  uint64_t *bar = &H->sa[stg];
+  unsigned char *b = st_region(smem) + kA_Base + stg * kA_Bytes;
+  mbar_arrive_expect_tx(bar, (ok && nsl > 0) ? (uint32_t)nsl * 6u : 0u);
+  if (ok && nsl > 0) {
+    bulk_g2s(b, a.w32 + s0, (uint32_t)nsl * 4u, bar);
+    bulk_g2s(b + kA_C, a.col16 + s0, (uint32_t)nsl * 2u, bar);
+  }
+}
+
+// Staged phase A: p = z + beta p_prev, q = A p, returns p.q.  Same
+// arithmetic, in the same order, as cg_phase_a.
+template <bool kFirst>
+__device__ __forceinline__ CSum cg_phase_a_st(const MArgs &a, const MPart &P, float beta,
+                                             const float *__restrict__ z,
+                                             const float *__restrict__ pp,
+                                             float *__restrict__ pcur, float *__restrict__ q,
+                                             float2 *__restrict__ e, unsigned char *smem,
+                                             StCount &cnt) {
+  StHdr *H = reinterpret_cast<StHdr *>(smem);
+  CSum cpq;
+  const int nch = st_chunks(P);
+  if (nch == 0) return cpq;
+  const int nrows = a.A.nslices * kSlice;
+  const int jlast = nch - 1 + kWinHalo;  // last window chunk any row needs
+  const uint32_t w0 = cnt.win + kWinHalo;  // sequence number of window chunk 0
+  Bounds B;
+  B.jb = -64;
+  B.v = 0;
+  if (P.warp == 0) {
+    if (P.lane == 0) {
+      fence_proxy_async_global();
+      fence_proxy_async_smem();
+      for (int j = -kWinHalo; j <= jlast && j < kWinSlots - kWinHalo - 1; ++j)
+        issue_win<kFirst>(P, smem, w0 + j, j, nrows, z, pp);
+    }
+    for (int j = 0; j < kAStages - 1 && j < nch; ++j) issue_slots(a, P, smem, B, cnt.sa + j, j);
+  }
+  // this warp's slice bounds and its rows' excess e_i, one chunk ahead
+  int64_t my0 = 0, my1 = 0;
+  float myex = 0.0f;
+  {
+    const int s = P.sb + P.warp;
+    if (s < P.se) {
+      my0 = a.A.sptr[s];
+      my1 = a.A.sptr[s + 1];
+      if (a.sflag[s] && s * kSlice + P.lane < P.n) myex = ld_stream(a.e32 + s * kSlice + P.lane);
+    }
+  }
+  const float *ring = reinterpret_cast<const float *>(st_region(smem));
+  for (int i = 0; i < nch; ++i) {
+    if (P.warp == 0) {
+      const int jw = i + kWinSlots - kWinHalo - 1;
+      if (P.lane == 0 && jw <= jlast) issue_win<kFirst>(P, smem, w0 + jw, jw, nrows, z, pp);
+      if (i + kAStages - 1 < nch)
+        issue_slots(a, P, smem, B, cnt.sa + i + kAStages - 1, i + kAStages - 1);
+    }
+    const int s = P.sb + kStChunkSlices * i + P.warp;
+    // next chunk's slice bounds, loaded while this chunk is processed
+    int64_t n0 = 0, n1 = 0;
+    float nex = 0.0f;
+    if (s + kStChunkSlices < P.se) {
+      const int sn = s + kStChunkSlices, rn = sn * kSlice + P.lane;
+      n0 = a.A.sptr[sn];
+      n1 = a.A.sptr[sn + 1];
+      if (a.sflag[sn] && rn < P.n) nex = ld_stream(a.e32 + rn);
+    }
+    // window chunks i-3 .. i+3 (all of them before the first chunk)
+    for (int j = (i == 0 ? -kWinHalo : i + kWinHalo); j <= i + kWinHalo && j <= jlast; ++j) {
+      const uint32_t sq = w0 + j;
+      mbar_wait(&H->win[sq % kWinSlots], (sq / kWinSlots) & 1u, a.gs.err);
+    }
+    const uint32_t ga = cnt.sa + i, stg = ga % kAStages;
+    mbar_wait(&H->sa[stg], (ga / kAStages) & 1u, a.gs.err);
+    if (s < P.se) {
+      const int row = s * kSlice + P.lane;
+      const int wlo = P.sb * kSlice + (i - kWinHalo) * kStRows;  // first window row
+      const uint32_t slot0 = (w0 + i - kWinHalo) % kWinSlots;   // its ring slot
+      const int wd = (int)((my1 - my0) >> 5);
+      const float *ws;
+      const int16_t *cs;
+      if (H->ok[stg]) {
+        const unsigned char *b = st_region(smem) + kA_Base + stg * kA_Bytes;
+        const int64_t off = my0 - H->base[stg];
+        ws = reinterpret_cast<const float *>(b) + off + P.lane;
+        cs = reinterpret_cast<const int16_t *>(b + kA_C) + off + P.lane;
+      } else {
+        ws = a.w32 + my0 + P.lane;
+        cs = a.col16 + my0 + P.lane;
+      }
+      // p at row k: from the window when it holds k, else global memory
+      auto pat = [&](int k) -> float {
+        const int rel = k - wlo;
+        if ((unsigned)rel < (unsigned)kWinSpan) {
+          uint32_t sl = slot0 + (uint32_t)(rel >> 10);
+          if (sl >= kWinSlots) sl -= kWinSlots;
+          const float *w = ring + sl * (kWinSlotBytes / 4) + (rel & (kStRows - 1));
+          return kFirst ? w[0] : fmaf(beta, w[kStRows], w[0]);
+        }
+        return kFirst ? z[k] : fmaf(beta, pp[k], z[k]);
+      };
+      if (row < P.n) {
+        const float pi = pat(row);
+        float t = myex * pi;
+        if (wd <= 4) {
+          int c[4];
+          float w[4], nb[4];
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            c[k] = (k < wd) ? row + (int)cs[32 * k] : row;
+            w[k] = (k < wd) ? ws[32 * k] : 0.0f;
+          }
+#pragma unroll
+          for (int k = 0; k < 4; ++k) nb[k] = pat(c[k]);
+#pragma unroll
+          for (int k = 0; k < 4; ++k) t = fmaf(w[k], pi - nb[k], t);
+        } else {
+          for (int k = 0; k < wd; ++k) t = fmaf(ws[32 * k], pi - pat(row + (int)cs[32 * k]), t);
+        }
+        pcur[row] = pi;
+        q[row] = t;
+        if (kFirst) e[row] = make_float2(0.0f, 0.0f);
+        cpq.add(pi * t);
+      }
+    }
+    my0 = n0;
+    my1 = n1;
+    myex = nex;
+    __syncthreads();
+  }
+  cnt.win = w0 + (uint32_t)(jlast + 1);
+  cnt.sa += (uint32_t)nch;
+  return cpq;
+}
+
+// Lane 0 of warp 0: bulk copies of phase-B chunk j into stage seq.
+template <bool kPair, bool kUpdE>
+__device__ __forceinline__ void issue_b(const MArgs &a, const MPart &P, unsigned char *smem,
+                                        uint32_t seq, int j, const float *pprev,
+                                        const float *pcur) {
+  StHdr *H = reinterpret_cast<StHdr *>(smem);
+  const uint32_t stg = seq % kBStages;
+  const int c0 = P.sb + kStChunkSlices * j;
+  const int c1 = min(P.se, c0 + kStChunkSlices);
+  const uint32_t rows = (uint32_t)(c1 - c0) * kSlice;
+  const size_t r0 = (size_t)c0 * kSlice;
+  unsigned char *b = st_region(smem) + stg * kB_Bytes;
+  const uint32_t bytes = rows * 4u * (kPair ? 4u : 3u) + (kUpdE ? rows * 16u : 0u);
+  uint64_t *bar = &H->sb[stg];
+  mbar_arrive_expect_tx(bar, bytes);
+  bulk_g2s(b + kB_Q, a.q + r0, rows * 4u, bar);
+  bulk_g2s(b + kB_RS, a.rs + r0, rows * 4u, bar);
+  if (kPair) bulk_g2s(b + kB_RSL, a.rsl + r0, rows * 4u, bar);
+  bulk_g2s(b + kB_MINV, a.minv + r0, rows * 4u, bar);
+  if (kUpdE) {
+    bulk_g2s(b + kB_PPREV, pprev + r0, rows * 4u, bar);
+    bulk_g2s(b + kB_PCUR, pcur + r0, rows * 4u, bar);
+    bulk_g2s(b + kB_E, a.e + r0, rows * 8u, bar);
+  }
+}
+
+// Staged phase B: the arithmetic of cg_phase_b, one row per thread.
+template <bool kPair, bool kUpdE>
+__device__ __forceinline__ void cg_phase_b_st(const MArgs &a, const MPart &P, float a1,
+                                           float a1_lo, const float *__restrict__ pprev,
+                                           float alpha, float alpha_lo,
+                                           const float *__restrict__ pcur, CSum &crz,
+                                           CSum &crr, unsigned char *smem, StCount &cnt) {
+  StHdr *H = reinterpret_cast<StHdr *>(smem);
+  const int nch = st_chunks(P);
+  if (P.warp == 0 && P.lane == 0) {
+    fence_proxy_async_global();
+    fence_proxy_async_smem();
+    for (int j = 0; j < kBStages - 1 && j < nch; ++j)
+      issue_b<kPair, kUpdE>(a, P, smem, cnt.sb + j, j, pprev, pcur);
+  }
+  float *__restrict__ rs = a.rs;
+  float *__restrict__ rsl = a.rsl;
+  float *__restrict__ z = a.z;
+  float2 *__restrict__ e = a.e;
+  for (int i = 0; i < nch; ++i) {
+    if (P.warp == 0 && P.lane == 0 && i + kBStages - 1 < nch)
+      issue_b<kPair, kUpdE>(a, P, smem, cnt.sb + i + kBStages - 1, i + kBStages - 1, pprev,
+                            pcur);
+    const uint32_t gi = cnt.sb + i, stg = gi % kBStages;
+    mbar_wait(&H->sb[stg], (gi / kBStages) & 1u, a.gs.err);
+    const int s = P.sb + kStChunkSlices * i + P.warp;
+    const int row = s * kSlice + P.lane;
+    if (s < P.se && row < P.n) {
+      const unsigned char *b = st_region(smem) + stg * kB_Bytes;
+      const int t = threadIdx.x;
+      const float qv = reinterpret_cast<const float *>(b + kB_Q)[t];
+      const float rv = reinterpret_cast<const float *>(b + kB_RS)[t];
+      const float mv = reinterpret_cast<const float *>(b + kB_MINV)[t];
+      if (kUpdE) {
+        const float2 ev = reinterpret_cast<const float2 *>(b + kB_E)[t];
+        const float p1 = reinterpret_cast<const float *>(b + kB_PPREV)[t];
+        const float pv = reinterpret_cast<const float *>(b + kB_PCUR)[t];
+        e[row] = df_axpy(df_axpy(ev, a1, a1_lo, p1), alpha, alpha_lo, pv);
+      }
+      float r;
+      if (kPair) {
+        const float rl = reinterpret_cast<const float *>(b + kB_RSL)[t];
+        const float2 rp = df_axpy(make_float2(rv, rl), -alpha, -alpha_lo, qv);
+        r = rp.x;
+        rsl[row] = rp.y;
+      } else {
+        r = fmaf(-alpha, qv, rv);
+      }
+      const float zz = r * mv;
+      rs[row] = r;
+      z[row] = zz;
+      crz.add(r * zz);
+      if (mv != 0.0f) crr.add(r * r);
+    }
+    __syncthreads();
+  }
+  cnt.sb += (uint32_t)nch;
+}
+
+template <bool kStaged>
+__device__ __forceinline__ void mixed_cg_body(const MArgs &a) {
   __shared__ double red[kMaxNV * 32];
+  extern __shared__ __align__(128) unsigned char st_smem[];
   const MPart P(a.A.nslices, a.A.n);
+  StCount gch;  // staged copies issued so far, per ring
+  if (kStaged) {
+    if (threadIdx.x == 0) {
+      StHdr *H = reinterpret_cast<StHdr *>(st_smem);
+      for (int i = 0; i < kWinSlots; ++i) mbar_init(&H->win[i], 1);
+      for (int i = 0; i < kAStages; ++i) mbar_init(&H->sa[i], 1);
+      for (int i = 0; i < kBStages; ++i) mbar_init(&H->sb[i], 1);
+      mbar_init_fence();
+    }
+    __syncthreads();
+  }
+  // FP64 scalars of the recurrence: kept by lane 0 of warp 0 in shared
+  // memory (it runs all scalar FP64 work inside the all-reduces), read by
+  // every thread after the all-reduce's closing __syncthreads
+  __shared__ struct {
+    double rz, rr_upd, relres, pend_alpha, alpha, rz_new;
+    double bnorm2, scale, delta2, target2, res0;
+    float alpha_f, alpha_lo, a1, a1_lo, beta;
+    int action, status, updates, pair;
+  } sh;
+  __shared__ float2 red2[kMaxNV * 32];
+  enum { kContinue = 0, kUpdate = 1, kStop = 2 };
   unsigned int ep = 0;
-  int status = FVC_ERR_NOCONV, updates = 0, it = 0;
+  int it = 0;
   double res[4];
   if (!residual_sweep(a, ep, a.init != 0, res, red)) return;
-  const double bnorm2 = res[1];
-  const double scale = (bnorm2 > 0.0) ? bnorm2 : 1.0;
-  double relres = sqrt(res[0] / scale);
-  double rz = res[2];
-  double rr_upd = res[3];  // ||r||^2 (moving rows) at the last reliable update
-  const double delta2 = a.inner_tol * a.inner_tol;
-  const double target2 = a.target * a.target * scale;
+  if (threadIdx.x == 0) {
+    const double scale = (res[1] > 0.0) ? res[1] : 1.0;
+    sh.bnorm2 = res[1];
+    sh.scale = scale;
+    sh.delta2 = a.inner_tol * a.inner_tol;
+    sh.target2 = a.target * a.target * scale;
+    sh.res0 = res[0];
+    sh.relres = sqrt(res[0] / scale);
+    sh.rz = res[2];
+    sh.rr_upd = res[3];  // ||r||^2 (moving rows) at the last reliable update
+    sh.pend_alpha = 0.0;
+    sh.beta = 0.0f;
+    sh.updates = 0;
+    sh.pair = sh.relres <= kPairFrom;
+    sh.status = !(sh.relres == sh.relres) ? FVC_ERR_NAN
+                : (sh.relres <= a.target) ? FVC_OK
+                                          : FVC_ERR_NOCONV;
+  }
+  __syncthreads();
+  int status = sh.status;
+  bool pair = sh.pair != 0;
   float beta = 0.0f;
   float *pprev = a.pb, *pcur = a.pa;
-  bool pair = relres <= kPairFrom;
-  if (!(relres == relres)) status = FVC_ERR_NAN;
-  else if (relres <= a.target) status = FVC_OK;
+  bool pending = false;  // an alpha*p not yet added to e
   while (status == FVC_ERR_NOCONV && it < a.maxit) {
     ++it;
     // p = z + beta p_prev (formed on the fly at the neighbours); q = A p; p.q
-    double pq[1];
-    if (it == 1)
-      pq[0] = cg_phase_a<true>(a, P, beta, a.z, pprev, pcur, a.q, a.e);
-    else
-      pq[0] = cg_phase_a<false>(a, P, beta, a.z, pprev, pcur, a.q, a.e);
-    if (!grid_allreduce<1>(a.gs, ep, pq, red)) return;
-    const double alpha_d = rz / pq[0];
-    const float alpha = (float)alpha_d;
-    const float alpha_lo = (float)(alpha_d - (double)alpha);
-    // e += alpha p (FP32 pair) ; rs -= alpha q ; z = rs/m ; rs.z ; rs.rs
-    CSum crz, crr;
-    if (pair)
-      cg_phase_b<true>(P, alpha, alpha_lo, pcur, a.q, a.rs, a.rsl, a.z, a.e, a.minv, crz, crr);
-    else
-      cg_phase_b<false>(P, alpha, alpha_lo, pcur, a.q, a.rs, a.rsl, a.z, a.e, a.minv, crz, crr);
-    double acc[2] = {crz.value(), crr.value()};
-    if (!grid_allreduce<2>(a.gs, ep, acc, red)) return;
-    double rz_new = acc[0];
-    if (!(rz_new == rz_new)) {
-      status = FVC_ERR_NAN;
-      break;
+    CSum pq[1];
+    if (kStaged) {
+      pq[0] = (it == 1)
+                  ? cg_phase_a_st<true>(a, P, beta, a.z, pprev, pcur, a.q, a.e, st_smem, gch)
+                  : cg_phase_a_st<false>(a, P, beta, a.z, pprev, pcur, a.q, a.e, st_smem, gch);
+    } else if (a.col16) {
+      pq[0] = (it == 1) ? cg_phase_a<true, true>(a, P, beta, a.z, pprev, pcur, a.q, a.e)
+                        : cg_phase_a<false, true>(a, P, beta, a.z, pprev, pcur, a.q, a.e);
+    } else {
+      pq[0] = (it == 1) ? cg_phase_a<true, false>(a, P, beta, a.z, pprev, pcur, a.q, a.e)
+                        : cg_phase_a<false, false>(a, P, beta, a.z, pprev, pcur, a.q, a.e);
     }
-    if (acc[1] <= delta2 * rr_upd || acc[1] <= target2 || it >= a.maxit) {
-      // reliable update: fold e into x, recompute the true residual in FP64
-      fold_correction(a);
+    if (!grid_allreduce_ff<1>(a.gs, ep, pq, red2, [&](const double *t) {
+          const double alpha_d = sh.rz / t[0];
+          sh.alpha = alpha_d;
+          sh.alpha_f = (float)alpha_d;
+          sh.alpha_lo = (float)(alpha_d - (double)sh.alpha_f);
+          sh.a1 = (float)sh.pend_alpha;
+          sh.a1_lo = (float)(sh.pend_alpha - (double)sh.a1);
+        }))
+      return;
+    const float alpha = sh.alpha_f, alpha_lo = sh.alpha_lo;
+    const float a1 = sh.a1, a1_lo = sh.a1_lo;
+    // rs -= alpha q ; z = rs/m ; rs.z ; rs.rs ; every second iteration also
+    // e += a_prev p_prev + alpha p (FP32 pair)
+    CSum acc[2];
+    if (kStaged) {
+      if (pending) {
+        if (pair)
+          cg_phase_b_st<true, true>(a, P, a1, a1_lo, pprev, alpha, alpha_lo, pcur, acc[0],
+                                    acc[1], st_smem, gch);
+        else
+          cg_phase_b_st<false, true>(a, P, a1, a1_lo, pprev, alpha, alpha_lo, pcur, acc[0],
+                                     acc[1], st_smem, gch);
+      } else {
+        if (pair)
+          cg_phase_b_st<true, false>(a, P, a1, a1_lo, pprev, alpha, alpha_lo, pcur, acc[0],
+                                     acc[1], st_smem, gch);
+        else
+          cg_phase_b_st<false, false>(a, P, a1, a1_lo, pprev, alpha, alpha_lo, pcur, acc[0],
+                                      acc[1], st_smem, gch);
+      }
+    } else if (pending) {
+      if (pair)
+        cg_phase_b<true, true>(P, a1, a1_lo, pprev, alpha, alpha_lo, pcur, a.q, a.rs, a.rsl,
+                               a.z, a.e, a.minv, acc[0], acc[1]);
+      else
+        cg_phase_b<false, true>(P, a1, a1_lo, pprev, alpha, alpha_lo, pcur, a.q, a.rs, a.rsl,
+                                a.z, a.e, a.minv, acc[0], acc[1]);
+    } else {
+      if (pair)
+        cg_phase_b<true, false>(P, a1, a1_lo, pprev, alpha, alpha_lo, pcur, a.q, a.rs, a.rsl,
+                                a.z, a.e, a.minv, acc[0], acc[1]);
+      else
+        cg_phase_b<false, false>(P, a1, a1_lo, pprev, alpha, alpha_lo, pcur, a.q, a.rs, a.rsl,
+                                 a.z, a.e, a.minv, acc[0], acc[1]);
+    }
+    const bool was_pending = pending;
+    pending = !pending;
+    if (!grid_allreduce_ff<2>(a.gs, ep, acc, red2, [&](const double *t) {
+          // the alpha*p of an iteration that did not update e is added later
+          if (!was_pending) sh.pend_alpha = sh.alpha;
+          const double rz_new = t[0];
+          sh.rz_new = rz_new;
+          if (blockIdx.x == 0 && it <= kHistoryMax) a.history[it - 1] = (float)sqrt(t[1] / sh.scale);
+          if (!(rz_new == rz_new)) {
+            sh.status = FVC_ERR_NAN;
+            sh.action = kStop;
+          } else if (t[1] <= sh.delta2 * sh.rr_upd || t[1] <= sh.target2 || it >= a.maxit) {
+            sh.action = kUpdate;
+          } else {
+            sh.beta = (float)(rz_new / sh.rz);
+            sh.rz = rz_new;
+            sh.action = kContinue;
+          }
+        }))
+      return;
+    int action = sh.action;
+    if (action == kUpdate) {
+      // reliable update: fold e (and a deferred alpha p) into x, recompute
+      // the true residual in FP64
+      fold_correction(a, pending ? pcur : nullptr, sh.pend_alpha);
+      pending = false;
       if (!grid_barrier(a.gs, ep)) return;
       if (!residual_sweep(a, ep, false, res, red)) return;
-      ++updates;
-      relres = sqrt(res[0] / scale);
-      if (blockIdx.x == 0 && threadIdx.x == 0 && updates <= kTraceMax) {
-        a.trace[2 * (updates - 1)] = (double)it;
-        a.trace[2 * (updates - 1) + 1] = relres;
+      if (threadIdx.x == 0) {
+        const int u = ++sh.updates;
+        const double relres = sqrt(res[0] / sh.scale);
+        sh.res0 = res[0];
+        sh.relres = relres;
+        if (blockIdx.x == 0 && u <= kTraceMax) {
+          a.trace[2 * (u - 1)] = (double)it;
+          a.trace[2 * (u - 1) + 1] = relres;
+        }
+        sh.action = kContinue;
+        if (!(relres == relres)) {
+          sh.status = FVC_ERR_NAN;
+          sh.action = kStop;
+        } else if (relres <= a.target) {
+          sh.status = FVC_OK;
+          sh.action = kStop;
+        } else {
+          if (relres <= kPairFrom) sh.pair = 1;  // the sweep wrote both parts
+          sh.rr_upd = res[3];
+          // beta from the replaced (true) residual, or with update_beta from
+          // the recursive one; the next alpha uses the true r.z
+          sh.beta = (float)((a.update_beta ? sh.rz_new : res[2]) / sh.rz);
+          sh.rz = res[2];
+        }
+        sh.pend_alpha = 0.0;
       }
-      if (!(relres == relres)) {
-        status = FVC_ERR_NAN;
-        break;
-      }
-      if (relres <= a.target) {
-        status = FVC_OK;
-        break;
-      }
-      if (relres <= kPairFrom) pair = true;  // the sweep wrote both parts
-      rr_upd = res[3];
-      if (a.update_beta) {
-        // beta from the recursive residual, the next alpha from the true one
-        beta = (float)(rz_new / rz);
-        rz = res[2];
-        float *tmp = pprev;
-        pprev = pcur;
-        pcur = tmp;
-        continue;
-      }
-      rz_new = res[2];
+      __syncthreads();
+      action = sh.action;
+      pair = sh.pair != 0;
     }
-    beta = (float)(rz_new / rz);
-    rz = rz_new;
+    if (action == kStop) {
+      status = sh.status;
+      break;
+    }
+    beta = sh.beta;
     float *tmp = pprev;
     pprev = pcur;
     pcur = tmp;
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
-    a.iresult[0] = updates;
-    a.iresult[1] = status;
+    a.iresult[0] = sh.updates;
+    a.iresult[1] = (status == FVC_ERR_NOCONV) ? sh.status : status;
     a.iresult[2] = it;
-    a.result[2] = relres;
-    a.result[3] = res[0];
-    a.result[4] = bnorm2;
+    a.result[2] = sh.relres;
+    a.result[3] = sh.res0;
+    a.result[4] = sh.bnorm2;
   }
 }
+
+__global__ void __launch_bounds__(1024, 1) mixed_cg(MArgs a) { mixed_cg_body<false>(a); }
+
+// Staged form: 1024 threads, kStSmem bytes of dynamic shared memory, and
+// the 16-bit column offsets (col16) present.
+__global__ void __launch_bounds__(1024, 1) mixed_cg_staged(MArgs a) { mixed_cg_body<true>(a); }
 
 // The reference's Jacobi BiCGSTAB (Iterativos.f:140-234) in FP32 on the
 // correction equation A e = r, inside FP64 defect correction.
@@ -584,15 +1165,28 @@ int32_t build_f32_copy(DeviceMatrix &A, cudaStream_t stream) {
   if (A.have32) return FVC_OK;
   const size_t sl = (size_t)std::max<int64_t>(A.slots, 1);
   if (!A.val32 && cudaMalloc(&A.val32, sizeof(float) * sl) != cudaSuccess) return FVC_ERR_CUDA;
-  if (!A.diag32 && cudaMalloc(&A.diag32, sizeof(float) * (size_t)A.n) != cudaSuccess)
+  // row arrays cover whole slices (the staged loops copy 32-row units)
+  const size_t nrow = (size_t)A.nslices * kSlice + 64;
+  if (!A.diag32 && cudaMalloc(&A.diag32, sizeof(float) * nrow) != cudaSuccess)
     return FVC_ERR_CUDA;
-  if (!A.minv32 && cudaMalloc(&A.minv32, sizeof(float) * (size_t)A.n) != cudaSuccess)
+  if (!A.minv32 && cudaMalloc(&A.minv32, sizeof(float) * nrow) != cudaSuccess)
     return FVC_ERR_CUDA;
+  if (!A.col16 && cudaMalloc(&A.col16, sizeof(int16_t) * sl) != cudaSuccess) return FVC_ERR_CUDA;
+  if (!A.sflag && cudaMalloc(&A.sflag, (size_t)A.nslices + 1) != cudaSuccess) return FVC_ERR_CUDA;
+  int *ovf = nullptr;
+  if (cudaMalloc(&ovf, sizeof(int)) != cudaSuccess) return FVC_ERR_CUDA;
+  cudaMemsetAsync(ovf, 0, sizeof(int), stream);
   int blocks = std::max(1, std::min((A.nslices + 7) / 8, sm_count_m() * 8));
   build_f32_operator<<<blocks, 256, 0, stream>>>(A.n, A.nslices, A.sptr, A.col, A.val, A.jac,
-                                                 A.val32, A.diag32, A.minv32);
+                                                 A.val32, A.diag32, A.minv32, A.col16, A.sflag,
+                                                 ovf);
   count_launch();
-  if (cudaStreamSynchronize(stream) != cudaSuccess) return FVC_ERR_CUDA;
+  int hovf = 1;
+  cudaMemcpyAsync(&hovf, ovf, sizeof(int), cudaMemcpyDeviceToHost, stream);
+  const cudaError_t ce = cudaStreamSynchronize(stream);
+  cudaFree(ovf);
+  if (ce != cudaSuccess) return FVC_ERR_CUDA;
+  A.col16_ok = (hovf == 0);
   A.have32 = true;
   return FVC_OK;
 }
@@ -615,10 +1209,21 @@ int32_t run_mixed(const DeviceMatrix &A0, Scratch &S, int code, const double *b,
   for (int i = 0; i < 10; ++i)  // f[4] holds the float2 correction
     if (!S.f[i] && cudaMalloc(&S.f[i], sizeof(float) * (i == 4 ? 2 : 1) * (n + 64)) != cudaSuccess)
       return FVC_ERR_CUDA;
-  auto kern = (code == 1) ? mixed_cg : mixed_bicgstab;
   const int threads = (o.block_threads > 0) ? o.block_threads : 1024;
+  // CG streams through shared-memory stages when its layout allows
+  const bool staged = code == 1 && threads == kStRows && A.col16_ok && o.staging == 0;
+  auto kern = (code == 1) ? (staged ? mixed_cg_staged : mixed_cg) : mixed_bicgstab;
+  const size_t dsmem = staged ? kStSmem : 0;
+  if (staged) {
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsmem) !=
+        cudaSuccess)
+      return FVC_ERR_CUDA;
+  } else {
+    // the plain-load kernels gather through L1: keep it at its largest
+    cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
+  }
   int occ = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, threads, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, threads, dsmem);
   if (occ <= 0) occ = 1;
   if (o.blocks_per_sm > 0 && o.blocks_per_sm < occ) occ = o.blocks_per_sm;
   const int warps = threads / 32;
@@ -636,6 +1241,8 @@ int32_t run_mixed(const DeviceMatrix &A0, Scratch &S, int code, const double *b,
   a.w32 = A.val32;
   a.e32 = A.diag32;
   a.minv = A.minv32;
+  a.col16 = A.col16_ok ? A.col16 : nullptr;
+  a.sflag = A.sflag;
   a.jac = A.jac;
   a.b = b;
   a.x = x;
@@ -659,13 +1266,14 @@ int32_t run_mixed(const DeviceMatrix &A0, Scratch &S, int code, const double *b,
   a.result = S.result;
   a.iresult = S.iresult;
   a.trace = S.trace;
+  a.history = S.history;
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   cudaEventRecord(e0, stream);
   void *args[] = {&a};
   cudaError_t ce =
-      cudaLaunchCooperativeKernel((const void *)kern, dim3(blocks), dim3(threads), args, 0, stream);
+      cudaLaunchCooperativeKernel((const void *)kern, dim3(blocks), dim3(threads), args, dsmem, stream);
   count_launch();
   cudaEventRecord(e1, stream);
   if (ce != cudaSuccess) {

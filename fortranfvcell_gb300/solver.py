@@ -31,7 +31,7 @@ def _p(a):
 def make_opts(precision: str = "fp64", init: int = -1, stop_rule: int = 0,
               refine_tol: float = 0.0, inner_tol: float = 0.0, max_refine: int = 0,
               block_threads: int = 0, blocks_per_sm: int = 0,
-              update_beta: int = 0) -> FvcOpts:
+              update_beta: int = 0, staging: int = 0) -> FvcOpts:
     o = FvcOpts()
     _lib.load().fvc_opts_default(C.byref(o))
     o.precision = {"fp64": _lib.FVC_PREC_FP64, "mixed": _lib.FVC_PREC_MIXED}[precision]
@@ -43,6 +43,7 @@ def make_opts(precision: str = "fp64", init: int = -1, stop_rule: int = 0,
     o.block_threads = block_threads
     o.blocks_per_sm = blocks_per_sm
     o.update_beta = update_beta
+    o.staging = staging
     return o
 
 
@@ -144,6 +145,15 @@ class Context:
         if k < 0:
             raise FvcError(-k, "fvc_solve_trace failed")
         return its[:k], rel[:k]
+
+    def history(self, max_values: int = 16384) -> np.ndarray:
+        """Recursive ||r||/||b|| after each iteration of the last
+        mixed-precision CG solve."""
+        out = np.zeros(max_values, np.float32)
+        k = self._L.fvc_solve_history(self._h, max_values, out.ctypes.data_as(C.c_void_p))
+        if k < 0:
+            raise FvcError(-k, "fvc_solve_history failed")
+        return out[:k]
 
     def spmv(self, x_dev, y_dev) -> None:
         _lib.check(self._L.fvc_spmv(self._h, C.c_void_p(_addr(x_dev)), C.c_void_p(_addr(y_dev))),

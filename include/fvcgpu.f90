@@ -28,7 +28,8 @@ module fvcgpu
      integer(c_int32_t) :: stop_rule
      integer(c_int32_t) :: want_residual
      integer(c_int32_t) :: update_beta
-     integer(c_int32_t) :: reserved(2)
+     integer(c_int32_t) :: staging
+     integer(c_int32_t) :: reserved
   end type fvc_opts
 
   type, bind(C) :: fvc_stats

@@ -88,7 +88,11 @@ typedef struct {
   int32_t update_beta; /* MIXED CG: beta = (r.z)/(r_old.z_old) at a residual
                           replacement taken from 0: the replaced (true)
                           residual; 1: the recursive one                 */
-  int32_t reserved[2];
+  int32_t staging;     /* MIXED CG: 0 streams the iteration's arrays through
+                          shared memory with bulk asynchronous copies when
+                          the layout allows (1024 threads, 16-bit column
+                          offsets); 1: plain loads                        */
+  int32_t reserved;
 } fvc_opts;
 
 typedef struct {
@@ -162,6 +166,11 @@ int32_t fvc_spmv_f32(fvc_context *ctx, const float *d_x, float *d_y);
  * or a negative FVC_* status. */
 int32_t fvc_solve_trace(const fvc_context *ctx, int32_t max, int32_t *its,
                         double *relres);
+
+/* Convergence history of the last MIXED CG solve on this context: the
+ * recursive ||r||/||b|| after each iteration (the first 16384 iterations,
+ * at most max).  Returns the number of values or a negative FVC_* status. */
+int32_t fvc_solve_history(const fvc_context *ctx, int32_t max, float *relres);
 
 /* Describe the device layout: rows, stored off-diagonal slots (with
  * padding), true off-diagonal nonzeros, slice count. */
