@@ -235,6 +235,7 @@ struct MArgs {
   double *x;
   float *rs, *pa, *pb, *q, *r0, *v, *t, *z;
   float *rsl;           // CG: low part of the residual (FP32 pair rs + rsl)
+  float *pal, *pbl;     // CG: low parts of the search directions in pa, pb
   float2 *e;            // correction, FP32 pair (hi, lo)
   GridSync gs;
   double target;        // refine tolerance on ||b-Ax||/||b||
@@ -329,12 +330,14 @@ __device__ __forceinline__ bool residual_sweep(const MArgs &a, unsigned int &ep,
 // the FP32 iteration; they take one FP64 Jacobi step on their current
 // residual estimate instead, which solves such a row to FP64 accuracy.
 __device__ __forceinline__ void fold_correction(const MArgs &a, const float *ppend = nullptr,
+                                                const float *ppend_lo = nullptr,
                                                 double apend = 0.0) {
   const MPart P(a.A.nslices, a.A.n);
   MFOR_ROWS(P) {
     const float2 ev = a.e[row];
     double dx = (double)ev.x + (double)ev.y;
-    if (ppend) dx = fma(apend, (double)ppend[row], dx);  // a deferred alpha*p
+    if (ppend)  // a deferred alpha*p (p an FP32 pair)
+      dx = fma(apend, (double)ppend[row] + (double)ppend_lo[row], dx);
     const double m = a.jac[row];
     if (a.minv[row] == 0.0f && m != 0.0) {
       // the frozen row's residual grows to the size of the neighbours' x
@@ -347,162 +350,109 @@ __device__ __forceinline__ void fold_correction(const MArgs &a, const float *ppe
   }
 }
 
-// CG phase A: p = z + beta p_prev (formed on the fly at the neighbours),
-// q = A p, returns p.q.  Each warp handles two slices per step and issues
-// every load of both before any arithmetic, so two slices' streams and
-// gathers are in flight per warp (the loop is latency-bound otherwise).
-template <bool kFirst, bool kCol16>
-__device__ __forceinline__ CSum cg_phase_a(const MArgs &a, const MPart &P, float beta,
-                                             const float *__restrict__ z,
-                                             const float *__restrict__ pp,
-                                             float *__restrict__ pcur, float *__restrict__ q,
-                                             float2 *__restrict__ e) {
+// The search direction is carried as an unevaluated FP32 pair (hi, lo):
+// rounding p = z + beta p_prev to one FP32 number each iteration perturbs
+// the direction by eps32 relative and, on the Jacobi-scaled Neumann
+// systems (lowest eigenvalues near eps32), sometimes stalls the last decade
+// of convergence for hundreds of iterations; the pair removes that.  The
+// operator is applied to p_hi (the FP32 value of p); the correction
+// e += alpha p takes both parts.
+struct Dir {
+  const float *ph, *pl;  // p_prev (hi, lo)
+  float *ch, *cl;        // p (hi, lo), written by phase A
+};
+
+// p = z + (bh + bl)(ph + pl) as an FP32 pair: the product's rounding error
+// comes from an FMA, the sum uses TwoSum, then a Fast2Sum renormalisation.
+__device__ __forceinline__ float2 p_update(float z, float bh, float bl, float ph, float pl) {
+  const float th = __fmul_rn(bh, ph);
+  const float terr = fmaf(bh, ph, -th);
+  const float tl = fmaf(bh, pl, fmaf(bl, ph, terr));
+  const float s = __fadd_rn(th, z);
+  const float bp = __fsub_rn(s, th);
+  const float err = __fadd_rn(__fsub_rn(th, __fsub_rn(s, bp)), __fsub_rn(z, bp));
+  const float lo = __fadd_rn(tl, err);
+  const float hi = __fadd_rn(s, lo);
+  return make_float2(hi, __fsub_rn(lo, __fsub_rn(hi, s)));
+}
+
+// CG phase A with plain loads: p = z + beta p_prev (formed at each gathered
+// neighbour), q = A p_hi, returns p_hi.q.  One slice per warp step.
+template <bool kFirst>
+__device__ __forceinline__ CSum cg_phase_a(const MArgs &a, const MPart &P, float bh, float bl,
+                                           const Dir &d) {
   CSum cpq;
-  const int n = P.n;
-  const int64_t *__restrict__ sptr = a.A.sptr;
-  const int *__restrict__ col = a.A.col;
-  const float *__restrict__ w32 = a.w32;
-  const float *__restrict__ e32 = a.e32;
-  for (int s0 = P.sb + P.warp; s0 < P.se; s0 += 2 * P.nwarps) {
-    int row[2], wd[2];
-    bool ok[2], hase[2];
-    int64_t base[2];
-#pragma unroll
-    for (int u = 0; u < 2; ++u) {
-      const int sl = s0 + u * P.nwarps;
-      row[u] = sl * 32 + P.lane;
-      ok[u] = (sl < P.se) && (row[u] < n);
-      base[u] = 0;
-      wd[u] = 0;
-      hase[u] = false;
-      if (sl < P.se) {
-        base[u] = sptr[sl];
-        wd[u] = (int)((sptr[sl + 1] - base[u]) >> 5);
-        hase[u] = a.sflag[sl] != 0;
-      }
-    }
-    if (wd[0] > 4 || wd[1] > 4) {  // wide slices: one row at a time
-#pragma unroll
-      for (int u = 0; u < 2; ++u) {
-        if (!ok[u]) continue;
-        auto pf = [&](int k) { return kFirst ? z[k] : fmaf(beta, pp[k], z[k]); };
-        const float pi = pf(row[u]);
-        const float t = arow32(a, s0 + u * P.nwarps, P.lane, row[u], pf);
-        pcur[row[u]] = pi;
-        q[row[u]] = t;
-        if (kFirst) e[row[u]] = make_float2(0.0f, 0.0f);
-        cpq.add(pi * t);
-      }
-      continue;
-    }
-    int c[2][4];
-    float w[2][4], ex[2], zo[2], po[2];
-#pragma unroll
-    for (int u = 0; u < 2; ++u) {
-#pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        const bool use = ok[u] && k < wd[u];
-        if (kCol16)
-          c[u][k] = use ? row[u] + (int)ld_stream16(a.col16 + base[u] + 32 * k + P.lane)
-                        : (ok[u] ? row[u] : 0);
-        else
-          c[u][k] = use ? ld_stream(col + base[u] + 32 * k + P.lane) : (ok[u] ? row[u] : 0);
-        w[u][k] = use ? ld_stream(w32 + base[u] + 32 * k + P.lane) : 0.0f;
-      }
-      ex[u] = (ok[u] && hase[u]) ? ld_stream(e32 + row[u]) : 0.0f;
-      zo[u] = ok[u] ? z[row[u]] : 0.0f;
-      po[u] = (!kFirst && ok[u]) ? pp[row[u]] : 0.0f;
-    }
-    float nb[2][4];
-#pragma unroll
-    for (int u = 0; u < 2; ++u)
-#pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        const int ck = c[u][k];
-        nb[u][k] = kFirst ? z[ck] : fmaf(beta, pp[ck], z[ck]);
-      }
-#pragma unroll
-    for (int u = 0; u < 2; ++u) {
-      if (!ok[u]) continue;
-      const float pi = kFirst ? zo[u] : fmaf(beta, po[u], zo[u]);
-      float t = ex[u] * pi;
-#pragma unroll
-      for (int k = 0; k < 4; ++k) t = fmaf(w[u][k], pi - nb[u][k], t);
-      pcur[row[u]] = pi;
-      q[row[u]] = t;
-      if (kFirst) e[row[u]] = make_float2(0.0f, 0.0f);
-      cpq.add(pi * t);
-    }
+  const float *__restrict__ z = a.z;
+  auto pf = [&](int k) -> float2 {
+    return kFirst ? make_float2(z[k], 0.0f) : p_update(z[k], bh, bl, d.ph[k], d.pl[k]);
+  };
+  for (int s = P.sb + P.warp; s < P.se; s += P.nwarps) {
+    const int row = s * kSlice + P.lane;
+    if (row >= P.n) continue;
+    const float2 pi = pf(row);
+    const float t = arow32(a, s, P.lane, row, [&](int k) { return pf(k).x; });
+    d.ch[row] = pi.x;
+    d.cl[row] = pi.y;
+    a.q[row] = t;
+    if (kFirst) a.e[row] = make_float2(0.0f, 0.0f);
+    cpq.add(pi.x * t);
   }
   return cpq;
 }
 
-// CG phase B: e += alpha p (FP32 pair), rs -= alpha q, z = rs/m; sums
-// rs.z and rs.rs (over the rows the FP32 iteration moves).  kUB slices
-// per warp step, loads first.  With kPair the residual is carried as an
-// FP32 pair (rs + rsl): rounding the residual recurrence to one FP32
-// number delays the last decades of convergence (the lowest eigenvalues of
-// the Jacobi-scaled matrix approach the FP32 rounding level), so the pair
-// is switched on below kPairFrom relative residual; earlier iterations
-// stream the high part only (the two parts live in separate arrays).
-// Measured (and emulated in numpy): promoting the residual only late does
-// not help -- the lost orthogonality dates from the first iterations -- so
-// the pair runs from the start unless the caller opts out.
-constexpr int kUB = 2;
-constexpr double kPairFrom = 1.0e300;  // always
-// With kUpdE the correction takes the two pending steps at once,
-// e += a1 p_prev + a2 p_cur (both p buffers are intact in phase B), so the
-// correction is read and written every second iteration only.
+// (hi, lo) += (ah + al)(ph + pl) for the correction (FP32 pairs).
+__device__ __forceinline__ float2 df_axpy2(float2 e, float ah, float al, float ph, float pl) {
+  const float th = __fmul_rn(ah, ph);
+  const float terr = fmaf(ah, ph, -th);
+  const float tl = fmaf(ah, pl, fmaf(al, ph, terr));
+  const float s = __fadd_rn(e.x, th);
+  const float bp = __fsub_rn(s, e.x);
+  const float err = __fadd_rn(__fsub_rn(e.x, __fsub_rn(s, bp)), __fsub_rn(th, bp));
+  const float lo = __fadd_rn(__fadd_rn(e.y, tl), err);
+  const float hi = __fadd_rn(s, lo);
+  return make_float2(hi, __fsub_rn(lo, __fsub_rn(hi, s)));
+}
+
+// One row of CG phase B: e += a1 p_prev + alpha p (kUpdE), r -= alpha q
+// (an FP32 pair with kPair), z = r/m; accumulates r.z and r.r (moving rows).
 template <bool kPair, bool kUpdE>
-__device__ __forceinline__ void cg_phase_b(const MPart &P, float a1, float a1_lo,
-                                           const float *__restrict__ pprev, float alpha,
-                                           float alpha_lo, const float *__restrict__ pcur,
-                                           const float *__restrict__ q, float *__restrict__ rs,
-                                           float *__restrict__ rsl, float *__restrict__ z,
-                                           float2 *__restrict__ e,
-                                           const float *__restrict__ minv, CSum &crz,
+__device__ __forceinline__ void cg_row_b(float a1, float a1_lo, float alpha, float alpha_lo,
+                                         float qv, float rv, float rl, float mv, float2 ev,
+                                         float p1h, float p1l, float pvh, float pvl, float2 &eo,
+                                         float &ro, float &rlo, float &zo, CSum &crz, CSum &crr) {
+  if (kUpdE) eo = df_axpy2(df_axpy2(ev, a1, a1_lo, p1h, p1l), alpha, alpha_lo, pvh, pvl);
+  float r;
+  if (kPair) {
+    const float2 rp = df_axpy(make_float2(rv, rl), -alpha, -alpha_lo, qv);
+    r = rp.x;
+    rlo = rp.y;
+  } else {
+    r = fmaf(-alpha, qv, rv);
+  }
+  const float zz = r * mv;
+  ro = r;
+  zo = zz;
+  crz.add(r * zz);
+  if (mv != 0.0f) crr.add(r * r);
+}
+
+// CG phase B with plain loads.
+template <bool kPair, bool kUpdE>
+__device__ __forceinline__ void cg_phase_b(const MArgs &a, const MPart &P, float a1, float a1_lo,
+                                           float alpha, float alpha_lo, const Dir &d, CSum &crz,
                                            CSum &crr) {
-  const int n = P.n;
-  for (int s0 = P.sb + P.warp; s0 < P.se; s0 += kUB * P.nwarps) {
-    int row[kUB];
-    bool ok[kUB];
-    float2 ev[kUB];
-    float p1[kUB], pv[kUB], qv[kUB], rv[kUB], rl[kUB], mv[kUB];
-#pragma unroll
-    for (int u = 0; u < kUB; ++u) {
-      const int sl = s0 + u * P.nwarps;
-      row[u] = sl * 32 + P.lane;
-      ok[u] = (sl < P.se) && (row[u] < n);
-      if (ok[u]) {
-        if (kUpdE) {
-          ev[u] = e[row[u]];
-          p1[u] = pprev[row[u]];
-          pv[u] = pcur[row[u]];
-        }
-        qv[u] = q[row[u]];
-        rv[u] = rs[row[u]];
-        rl[u] = kPair ? rsl[row[u]] : 0.0f;
-        mv[u] = minv[row[u]];
-      }
-    }
-#pragma unroll
-    for (int u = 0; u < kUB; ++u) {
-      if (!ok[u]) continue;
-      if (kUpdE) e[row[u]] = df_axpy(df_axpy(ev[u], a1, a1_lo, p1[u]), alpha, alpha_lo, pv[u]);
-      float r;
-      if (kPair) {
-        const float2 rp = df_axpy(make_float2(rv[u], rl[u]), -alpha, -alpha_lo, qv[u]);
-        r = rp.x;
-        rsl[row[u]] = rp.y;
-      } else {
-        r = fmaf(-alpha, qv[u], rv[u]);
-      }
-      const float zz = r * mv[u];
-      rs[row[u]] = r;
-      z[row[u]] = zz;
-      crz.add(r * zz);
-      if (mv[u] != 0.0f) crr.add(r * r);
-    }
+  MFOR_ROWS(P) {
+    float2 eo;
+    float ro, rlo = 0.0f, zo;
+    cg_row_b<kPair, kUpdE>(a1, a1_lo, alpha, alpha_lo, a.q[row], a.rs[row],
+                           kPair ? a.rsl[row] : 0.0f, a.minv[row],
+                           kUpdE ? a.e[row] : make_float2(0.0f, 0.0f), kUpdE ? d.ph[row] : 0.0f,
+                           kUpdE ? d.pl[row] : 0.0f, kUpdE ? d.ch[row] : 0.0f,
+                           kUpdE ? d.cl[row] : 0.0f, eo, ro, rlo, zo, crz, crr);
+    if (kUpdE) a.e[row] = eo;
+    a.rs[row] = ro;
+    if (kPair) a.rsl[row] = rlo;
+    a.z[row] = zo;
   }
 }
 
@@ -510,58 +460,66 @@ __device__ __forceinline__ void cg_phase_b(const MPart &P, float a1, float a1_lo
 // Staged phases.  Each block walks its slice range in chunks of 32 slices
 // (1024 rows: one slice per warp in phase A, one row per thread in phase
 // B).  Warp 0 keeps bulk copies (TMA) running ahead into shared memory,
-// so the streams arrive without occupying registers or warps:
-//  * phase A keeps a window of z and p_prev around the chunk it works on
-//    -- chunks i-3 .. i+3 of the block's rows, reaching into the
-//    neighbouring blocks' rows -- in a ring of kWinSlots chunk slots, so
-//    the neighbour gathers of q = A p read shared memory (under the RCM
-//    numbering of a 2-D mesh with up to ~3000 rows per level, every
-//    neighbour lies in the window; one outside it is read from global
-//    memory), and stages each chunk's weights and column offsets in
-//    kAStages buffers;
-//  * phase B stages all of its row vectors in kBStages buffers.
+// so the streams arrive without occupying registers or warps.
+//  * Phase A: z and p_prev (both parts) of each chunk of the window land
+//    kLandAhead chunks ahead; one pass per row then forms the p pair once,
+//    writes p_hi into a ring of kPRingRows rows of shared memory (indexed
+//    by (row - first row of the block) mod kPRingRows) and the own rows'
+//    pair to global memory.  The ring holds chunks i-3 .. i+4 while chunk i
+//    is computed, so q = A p gathers every neighbour within +-3072 rows
+//    from shared memory (under the RCM numbering of a 2-D mesh with up to
+//    ~3000 rows per level, all of them); one further away is formed from
+//    global memory.  The chunk's weights and column offsets come through
+//    kAStages stages.  The window reaches into the neighbouring blocks'
+//    rows; the first window chunks (i-3 .. i+3 of chunk 0) are formed with
+//    plain loads.
+//  * Phase B stages all of its row vectors in kBStages stages.
 // The two phases reuse the same shared memory (a grid barrier separates
 // them).  A chunk with more than kStSlotCap slots (mean row width above 5)
 // reads its weights and offsets from global memory instead.
 constexpr int kStChunkSlices = 32;
 constexpr int kStRows = kStChunkSlices * kSlice;  // = threads per block
 constexpr int kStSlotCap = kStRows * 5;
-constexpr int kWinHalo = 3;                      // window: chunks i-3 .. i+3
-constexpr int kWinSlots = 10;                    // window + 3 chunks in flight
+constexpr int kWinHalo = 3;                      // gathers from chunks i-3 .. i+3
 constexpr int kWinSpan = (2 * kWinHalo + 1) * kStRows;
+constexpr int kPRingRows = 8 * kStRows;          // chunks i-3 .. i+4
+constexpr int kLandSlots = 4;
+constexpr int kLandAhead = 3;                    // landing copies in flight
 constexpr int kAStages = 4;
-constexpr int kBStages = 6;
-// window slot: z[1024] | pp[1024]
-constexpr uint32_t kWinSlotBytes = 2 * kStRows * 4;
-// phase-A stage (after the window): w32[kStSlotCap] | col16[kStSlotCap]
-constexpr uint32_t kA_Base = kWinSlots * kWinSlotBytes;
+constexpr int kBStages = 5;
+// phase A: p ring | landing slots (z | pp_hi | pp_lo) | stages (w32 | col16)
+constexpr uint32_t kLandBytes = 3 * kStRows * 4;
+constexpr uint32_t kL_Base = kPRingRows * 4;
+constexpr uint32_t kA_Base = kL_Base + kLandSlots * kLandBytes;
 constexpr uint32_t kA_C = kStSlotCap * 4;
 constexpr uint32_t kA_Bytes = kA_C + kStSlotCap * 2;
-// phase-B stage: q | rs | rsl | minv | pprev | pcur (1024 floats each) | e[1024] float2
-constexpr uint32_t kB_Q = 0, kB_RS = kStRows * 4, kB_RSL = 2 * kStRows * 4,
-                   kB_MINV = 3 * kStRows * 4, kB_PPREV = 4 * kStRows * 4,
-                   kB_PCUR = 5 * kStRows * 4, kB_E = 6 * kStRows * 4;
+// phase B stage: q | rs | rsl | minv | p1h | p1l | pvh | pvl (1024 floats each) | e[1024] float2
+constexpr uint32_t kB_Q = 0, kB_RS = 1 * kStRows * 4, kB_RSL = 2 * kStRows * 4,
+                   kB_MINV = 3 * kStRows * 4, kB_P1H = 4 * kStRows * 4,
+                   kB_P1L = 5 * kStRows * 4, kB_PVH = 6 * kStRows * 4,
+                   kB_PVL = 7 * kStRows * 4, kB_E = 8 * kStRows * 4;
 constexpr uint32_t kB_Bytes = kB_E + kStRows * 8;
 constexpr uint32_t kRegionA = kA_Base + kAStages * kA_Bytes;
 constexpr uint32_t kRegionB = kBStages * kB_Bytes;
 constexpr uint32_t kStHeader = 256;
 constexpr size_t kStSmem = kStHeader + (kRegionA > kRegionB ? kRegionA : kRegionB);
 static_assert(kA_Bytes % 128 == 0 && kB_Bytes % 128 == 0 && kA_Base % 128 == 0, "alignment");
-static_assert(kStSmem + 2048 <= 227 * 1024, "shared memory per block");
+static_assert(kStSmem + 3072 <= 227 * 1024, "shared memory per block");
+static_assert(kLandAhead + 1 == kLandSlots, "landing ring");
 
 struct StHdr {
-  uint64_t win[kWinSlots];  // window chunk landed
-  uint64_t sa[kAStages];    // phase-A stage landed
-  uint64_t sb[kBStages];    // phase-B stage landed
-  int64_t base[kAStages];   // first slot of the chunk in each phase-A stage
-  int ok[kAStages];         // 1: its weights and offsets are staged
+  uint64_t land[kLandSlots];  // landing slot filled
+  uint64_t sa[kAStages];      // phase-A stage filled
+  uint64_t sb[kBStages];      // phase-B stage filled
+  int64_t base[kAStages];     // first slot of the chunk in each phase-A stage
+  int ok[kAStages];           // 1: its weights and offsets are staged
 };
 static_assert(sizeof(StHdr) <= kStHeader, "stage header");
 
 // Running counts of the copies issued into each ring (the same in every
 // thread): ring slot = count % size, mbarrier parity = (count / size) & 1.
 struct StCount {
-  uint32_t win = 0, sa = 0, sb = 0;
+  uint32_t land = 0, sa = 0, sb = 0;
 };
 
 __device__ __forceinline__ unsigned char *st_region(unsigned char *smem) {
@@ -587,25 +545,28 @@ __device__ __forceinline__ int st_chunks(const MPart &P) {
   return (P.se > P.sb) ? (P.se - P.sb + kStChunkSlices - 1) / kStChunkSlices : 0;
 }
 
-// Lane 0 of warp 0: window chunk j (rows R0 + 1024 j .., clipped to the
-// padded row range [0, nrows)) of z and p_prev into its ring slot.
+// Lane 0 of warp 0: z and p_prev (hi, lo) of window chunk j (rows R0 +
+// 1024 j .., j >= 1, clipped to the padded row range) into landing slot seq.
 template <bool kFirst>
-__device__ __forceinline__ void issue_win(const MPart &P, unsigned char *smem, uint32_t seq,
-                                          int j, int nrows, const float *z, const float *pp) {
+__device__ __forceinline__ void issue_land(const MArgs &a, const MPart &P, unsigned char *smem,
+                                           uint32_t seq, int j, int nrows, const Dir &d) {
   StHdr *H = reinterpret_cast<StHdr *>(smem);
-  const uint32_t slot = seq % kWinSlots;
+  const uint32_t slot = seq % kLandSlots;
   const int c0 = P.sb * kSlice + j * kStRows;
-  const int lo = max(c0, 0), hi = min(c0 + kStRows, nrows);
-  uint64_t *bar = &H->win[slot];
-  if (hi <= lo) {
+  const int hi = min(c0 + kStRows, nrows);
+  uint64_t *bar = &H->land[slot];
+  if (hi <= c0) {
     mbar_arrive_expect_tx(bar, 0);
     return;
   }
-  const uint32_t bytes = (uint32_t)(hi - lo) * 4u;
-  unsigned char *dst = st_region(smem) + slot * kWinSlotBytes + (uint32_t)(lo - c0) * 4u;
-  mbar_arrive_expect_tx(bar, kFirst ? bytes : 2u * bytes);
-  bulk_g2s(dst, z + lo, bytes, bar);
-  if (!kFirst) bulk_g2s(dst + kStRows * 4, pp + lo, bytes, bar);
+  const uint32_t bytes = (uint32_t)(hi - c0) * 4u;
+  unsigned char *dst = st_region(smem) + kL_Base + slot * kLandBytes;
+  mbar_arrive_expect_tx(bar, kFirst ? bytes : 3u * bytes);
+  bulk_g2s(dst, a.z + c0, bytes, bar);
+  if (!kFirst) {
+    bulk_g2s(dst + kStRows * 4, d.ph + c0, bytes, bar);
+    bulk_g2s(dst + 2 * kStRows * 4, d.pl + c0, bytes, bar);
+  }
 }
 
 // Warp 0: weights and column offsets of chunk j into phase-A stage seq.
@@ -629,22 +590,32 @@ __device__ __forceinline__ void issue_slots(const MArgs &a, const MPart &P, unsi
   }
 }
 
-// Staged phase A: p = z + beta p_prev, q = A p, returns p.q.  Same
+// Forms the p pair of row r (from z and p_prev given), puts p_hi in the
+// ring and stores the pair when the row is the block's own.
+template <bool kFirst>
+__device__ __forceinline__ void p_form(float *ring, int r, int R0, int Rend, int n, float zr,
+                                       float bh, float bl, float phr, float plr, const Dir &d) {
+  const float2 p = kFirst ? make_float2(zr, 0.0f) : p_update(zr, bh, bl, phr, plr);
+  ring[(r - R0) & (kPRingRows - 1)] = p.x;
+  if (r >= R0 && r < Rend && r < n) {
+    d.ch[r] = p.x;
+    d.cl[r] = p.y;
+  }
+}
+
+// Staged phase A: p = z + beta p_prev, q = A p_hi, returns p_hi.q.  Same
 // arithmetic, in the same order, as cg_phase_a.
 template <bool kFirst>
-__device__ __forceinline__ CSum cg_phase_a_st(const MArgs &a, const MPart &P, float beta,
-                                             const float *__restrict__ z,
-                                             const float *__restrict__ pp,
-                                             float *__restrict__ pcur, float *__restrict__ q,
-                                             float2 *__restrict__ e, unsigned char *smem,
-                                             StCount &cnt) {
+__device__ __forceinline__ CSum cg_phase_a_st(const MArgs &a, const MPart &P, float bh, float bl,
+                                              const Dir &d, unsigned char *smem, StCount &cnt) {
   StHdr *H = reinterpret_cast<StHdr *>(smem);
   CSum cpq;
   const int nch = st_chunks(P);
   if (nch == 0) return cpq;
   const int nrows = a.A.nslices * kSlice;
+  const int R0 = P.sb * kSlice, Rend = P.se * kSlice;
   const int jlast = nch - 1 + kWinHalo;  // last window chunk any row needs
-  const uint32_t w0 = cnt.win + kWinHalo;  // sequence number of window chunk 0
+  float *ring = reinterpret_cast<float *>(st_region(smem));
   Bounds B;
   B.jb = -64;
   B.v = 0;
@@ -652,10 +623,28 @@ __device__ __forceinline__ CSum cg_phase_a_st(const MArgs &a, const MPart &P, fl
     if (P.lane == 0) {
       fence_proxy_async_global();
       fence_proxy_async_smem();
-      for (int j = -kWinHalo; j <= jlast && j < kWinSlots - kWinHalo - 1; ++j)
-        issue_win<kFirst>(P, smem, w0 + j, j, nrows, z, pp);
+      for (int j = kWinHalo + 1; j <= jlast && j <= kWinHalo + kLandAhead; ++j)
+        issue_land<kFirst>(a, P, smem, cnt.land + (j - kWinHalo - 1), j, nrows, d);
     }
     for (int j = 0; j < kAStages - 1 && j < nch; ++j) issue_slots(a, P, smem, B, cnt.sa + j, j);
+  }
+  // window chunks -3 .. 3 with plain loads (one row of each per thread)
+  {
+    float zr[2 * kWinHalo + 1], phr[2 * kWinHalo + 1], plr[2 * kWinHalo + 1];
+#pragma unroll
+    for (int jj = 0; jj < 2 * kWinHalo + 1; ++jj) {
+      const int j = jj - kWinHalo, r = R0 + j * kStRows + (int)threadIdx.x;
+      const bool in = j <= jlast && r >= 0 && r < nrows;
+      zr[jj] = in ? a.z[r] : 0.0f;
+      phr[jj] = (in && !kFirst) ? d.ph[r] : 0.0f;
+      plr[jj] = (in && !kFirst) ? d.pl[r] : 0.0f;
+    }
+#pragma unroll
+    for (int jj = 0; jj < 2 * kWinHalo + 1; ++jj) {
+      const int j = jj - kWinHalo, r = R0 + j * kStRows + (int)threadIdx.x;
+      if (j <= jlast && r >= 0 && r < nrows)
+        p_form<kFirst>(ring, r, R0, Rend, P.n, zr[jj], bh, bl, phr[jj], plr[jj], d);
+    }
   }
   // this warp's slice bounds and its rows' excess e_i, one chunk ahead
   int64_t my0 = 0, my1 = 0;
@@ -668,11 +657,12 @@ __device__ __forceinline__ CSum cg_phase_a_st(const MArgs &a, const MPart &P, fl
       if (a.sflag[s] && s * kSlice + P.lane < P.n) myex = ld_stream(a.e32 + s * kSlice + P.lane);
     }
   }
-  const float *ring = reinterpret_cast<const float *>(st_region(smem));
+  __syncthreads();
   for (int i = 0; i < nch; ++i) {
     if (P.warp == 0) {
-      const int jw = i + kWinSlots - kWinHalo - 1;
-      if (P.lane == 0 && jw <= jlast) issue_win<kFirst>(P, smem, w0 + jw, jw, nrows, z, pp);
+      const int jl = i + kWinHalo + 1 + kLandAhead;
+      if (P.lane == 0 && jl <= jlast)
+        issue_land<kFirst>(a, P, smem, cnt.land + (jl - kWinHalo - 1), jl, nrows, d);
       if (i + kAStages - 1 < nch)
         issue_slots(a, P, smem, B, cnt.sa + i + kAStages - 1, i + kAStages - 1);
     }
@@ -686,17 +676,26 @@ __device__ __forceinline__ CSum cg_phase_a_st(const MArgs &a, const MPart &P, fl
       n1 = a.A.sptr[sn + 1];
       if (a.sflag[sn] && rn < P.n) nex = ld_stream(a.e32 + rn);
     }
-    // window chunks i-3 .. i+3 (all of them before the first chunk)
-    for (int j = (i == 0 ? -kWinHalo : i + kWinHalo); j <= i + kWinHalo && j <= jlast; ++j) {
-      const uint32_t sq = w0 + j;
-      mbar_wait(&H->win[sq % kWinSlots], (sq / kWinSlots) & 1u, a.gs.err);
+    // form p for window chunk i+4 (used from the next chunk on)
+    const int jf = i + kWinHalo + 1;
+    if (jf <= jlast) {
+      const uint32_t sq = cnt.land + (uint32_t)i;
+      const uint32_t slot = sq % kLandSlots;
+      mbar_wait(&H->land[slot], (sq / kLandSlots) & 1u, a.gs.err);
+      const int r = R0 + jf * kStRows + (int)threadIdx.x;
+      if (r < nrows) {
+        const float *L = reinterpret_cast<const float *>(st_region(smem) + kL_Base +
+                                                         slot * kLandBytes);
+        const int t = threadIdx.x;
+        p_form<kFirst>(ring, r, R0, Rend, P.n, L[t], bh, bl, kFirst ? 0.0f : L[kStRows + t],
+                       kFirst ? 0.0f : L[2 * kStRows + t], d);
+      }
     }
     const uint32_t ga = cnt.sa + i, stg = ga % kAStages;
     mbar_wait(&H->sa[stg], (ga / kAStages) & 1u, a.gs.err);
     if (s < P.se) {
       const int row = s * kSlice + P.lane;
-      const int wlo = P.sb * kSlice + (i - kWinHalo) * kStRows;  // first window row
-      const uint32_t slot0 = (w0 + i - kWinHalo) % kWinSlots;   // its ring slot
+      const int wlo = R0 + (i - kWinHalo) * kStRows;  // first row of the window
       const int wd = (int)((my1 - my0) >> 5);
       const float *ws;
       const int16_t *cs;
@@ -709,19 +708,14 @@ __device__ __forceinline__ CSum cg_phase_a_st(const MArgs &a, const MPart &P, fl
         ws = a.w32 + my0 + P.lane;
         cs = a.col16 + my0 + P.lane;
       }
-      // p at row k: from the window when it holds k, else global memory
+      // p_hi at row k: from the ring when the window holds k, else formed
+      // from global memory
       auto pat = [&](int k) -> float {
-        const int rel = k - wlo;
-        if ((unsigned)rel < (unsigned)kWinSpan) {
-          uint32_t sl = slot0 + (uint32_t)(rel >> 10);
-          if (sl >= kWinSlots) sl -= kWinSlots;
-          const float *w = ring + sl * (kWinSlotBytes / 4) + (rel & (kStRows - 1));
-          return kFirst ? w[0] : fmaf(beta, w[kStRows], w[0]);
-        }
-        return kFirst ? z[k] : fmaf(beta, pp[k], z[k]);
+        if ((unsigned)(k - wlo) < (unsigned)kWinSpan) return ring[(k - R0) & (kPRingRows - 1)];
+        return kFirst ? a.z[k] : p_update(a.z[k], bh, bl, d.ph[k], d.pl[k]).x;
       };
       if (row < P.n) {
-        const float pi = pat(row);
+        const float pi = ring[(row - R0) & (kPRingRows - 1)];
         float t = myex * pi;
         if (wd <= 4) {
           int c[4];
@@ -738,9 +732,8 @@ __device__ __forceinline__ CSum cg_phase_a_st(const MArgs &a, const MPart &P, fl
         } else {
           for (int k = 0; k < wd; ++k) t = fmaf(ws[32 * k], pi - pat(row + (int)cs[32 * k]), t);
         }
-        pcur[row] = pi;
-        q[row] = t;
-        if (kFirst) e[row] = make_float2(0.0f, 0.0f);
+        a.q[row] = t;
+        if (kFirst) a.e[row] = make_float2(0.0f, 0.0f);
         cpq.add(pi * t);
       }
     }
@@ -749,7 +742,7 @@ __device__ __forceinline__ CSum cg_phase_a_st(const MArgs &a, const MPart &P, fl
     myex = nex;
     __syncthreads();
   }
-  cnt.win = w0 + (uint32_t)(jlast + 1);
+  if (jlast > kWinHalo) cnt.land += (uint32_t)(jlast - kWinHalo);
   cnt.sa += (uint32_t)nch;
   return cpq;
 }
@@ -757,8 +750,7 @@ __device__ __forceinline__ CSum cg_phase_a_st(const MArgs &a, const MPart &P, fl
 // Lane 0 of warp 0: bulk copies of phase-B chunk j into stage seq.
 template <bool kPair, bool kUpdE>
 __device__ __forceinline__ void issue_b(const MArgs &a, const MPart &P, unsigned char *smem,
-                                        uint32_t seq, int j, const float *pprev,
-                                        const float *pcur) {
+                                        uint32_t seq, int j, const Dir &d) {
   StHdr *H = reinterpret_cast<StHdr *>(smem);
   const uint32_t stg = seq % kBStages;
   const int c0 = P.sb + kStChunkSlices * j;
@@ -766,7 +758,7 @@ __device__ __forceinline__ void issue_b(const MArgs &a, const MPart &P, unsigned
   const uint32_t rows = (uint32_t)(c1 - c0) * kSlice;
   const size_t r0 = (size_t)c0 * kSlice;
   unsigned char *b = st_region(smem) + stg * kB_Bytes;
-  const uint32_t bytes = rows * 4u * (kPair ? 4u : 3u) + (kUpdE ? rows * 16u : 0u);
+  const uint32_t bytes = rows * 4u * (kPair ? 4u : 3u) + (kUpdE ? rows * 24u : 0u);
   uint64_t *bar = &H->sb[stg];
   mbar_arrive_expect_tx(bar, bytes);
   bulk_g2s(b + kB_Q, a.q + r0, rows * 4u, bar);
@@ -774,8 +766,10 @@ __device__ __forceinline__ void issue_b(const MArgs &a, const MPart &P, unsigned
   if (kPair) bulk_g2s(b + kB_RSL, a.rsl + r0, rows * 4u, bar);
   bulk_g2s(b + kB_MINV, a.minv + r0, rows * 4u, bar);
   if (kUpdE) {
-    bulk_g2s(b + kB_PPREV, pprev + r0, rows * 4u, bar);
-    bulk_g2s(b + kB_PCUR, pcur + r0, rows * 4u, bar);
+    bulk_g2s(b + kB_P1H, d.ph + r0, rows * 4u, bar);
+    bulk_g2s(b + kB_P1L, d.pl + r0, rows * 4u, bar);
+    bulk_g2s(b + kB_PVH, d.ch + r0, rows * 4u, bar);
+    bulk_g2s(b + kB_PVL, d.cl + r0, rows * 4u, bar);
     bulk_g2s(b + kB_E, a.e + r0, rows * 8u, bar);
   }
 }
@@ -783,56 +777,40 @@ __device__ __forceinline__ void issue_b(const MArgs &a, const MPart &P, unsigned
 // Staged phase B: the arithmetic of cg_phase_b, one row per thread.
 template <bool kPair, bool kUpdE>
 __device__ __forceinline__ void cg_phase_b_st(const MArgs &a, const MPart &P, float a1,
-                                           float a1_lo, const float *__restrict__ pprev,
-                                           float alpha, float alpha_lo,
-                                           const float *__restrict__ pcur, CSum &crz,
-                                           CSum &crr, unsigned char *smem, StCount &cnt) {
+                                              float a1_lo, float alpha, float alpha_lo,
+                                              const Dir &d, CSum &crz, CSum &crr,
+                                              unsigned char *smem, StCount &cnt) {
   StHdr *H = reinterpret_cast<StHdr *>(smem);
   const int nch = st_chunks(P);
   if (P.warp == 0 && P.lane == 0) {
     fence_proxy_async_global();
     fence_proxy_async_smem();
     for (int j = 0; j < kBStages - 1 && j < nch; ++j)
-      issue_b<kPair, kUpdE>(a, P, smem, cnt.sb + j, j, pprev, pcur);
+      issue_b<kPair, kUpdE>(a, P, smem, cnt.sb + j, j, d);
   }
-  float *__restrict__ rs = a.rs;
-  float *__restrict__ rsl = a.rsl;
-  float *__restrict__ z = a.z;
-  float2 *__restrict__ e = a.e;
   for (int i = 0; i < nch; ++i) {
     if (P.warp == 0 && P.lane == 0 && i + kBStages - 1 < nch)
-      issue_b<kPair, kUpdE>(a, P, smem, cnt.sb + i + kBStages - 1, i + kBStages - 1, pprev,
-                            pcur);
+      issue_b<kPair, kUpdE>(a, P, smem, cnt.sb + i + kBStages - 1, i + kBStages - 1, d);
     const uint32_t gi = cnt.sb + i, stg = gi % kBStages;
     mbar_wait(&H->sb[stg], (gi / kBStages) & 1u, a.gs.err);
     const int s = P.sb + kStChunkSlices * i + P.warp;
     const int row = s * kSlice + P.lane;
     if (s < P.se && row < P.n) {
-      const unsigned char *b = st_region(smem) + stg * kB_Bytes;
+      const float *b = reinterpret_cast<const float *>(st_region(smem) + stg * kB_Bytes);
       const int t = threadIdx.x;
-      const float qv = reinterpret_cast<const float *>(b + kB_Q)[t];
-      const float rv = reinterpret_cast<const float *>(b + kB_RS)[t];
-      const float mv = reinterpret_cast<const float *>(b + kB_MINV)[t];
-      if (kUpdE) {
-        const float2 ev = reinterpret_cast<const float2 *>(b + kB_E)[t];
-        const float p1 = reinterpret_cast<const float *>(b + kB_PPREV)[t];
-        const float pv = reinterpret_cast<const float *>(b + kB_PCUR)[t];
-        e[row] = df_axpy(df_axpy(ev, a1, a1_lo, p1), alpha, alpha_lo, pv);
-      }
-      float r;
-      if (kPair) {
-        const float rl = reinterpret_cast<const float *>(b + kB_RSL)[t];
-        const float2 rp = df_axpy(make_float2(rv, rl), -alpha, -alpha_lo, qv);
-        r = rp.x;
-        rsl[row] = rp.y;
-      } else {
-        r = fmaf(-alpha, qv, rv);
-      }
-      const float zz = r * mv;
-      rs[row] = r;
-      z[row] = zz;
-      crz.add(r * zz);
-      if (mv != 0.0f) crr.add(r * r);
+      float2 eo;
+      float ro, rlo = 0.0f, zo;
+      cg_row_b<kPair, kUpdE>(
+          a1, a1_lo, alpha, alpha_lo, b[kB_Q / 4 + t], b[kB_RS / 4 + t],
+          kPair ? b[kB_RSL / 4 + t] : 0.0f, b[kB_MINV / 4 + t],
+          kUpdE ? reinterpret_cast<const float2 *>(b + kB_E / 4)[t] : make_float2(0.0f, 0.0f),
+          kUpdE ? b[kB_P1H / 4 + t] : 0.0f, kUpdE ? b[kB_P1L / 4 + t] : 0.0f,
+          kUpdE ? b[kB_PVH / 4 + t] : 0.0f, kUpdE ? b[kB_PVL / 4 + t] : 0.0f, eo, ro, rlo, zo,
+          crz, crr);
+      if (kUpdE) a.e[row] = eo;
+      a.rs[row] = ro;
+      if (kPair) a.rsl[row] = rlo;
+      a.z[row] = zo;
     }
     __syncthreads();
   }
@@ -848,7 +826,7 @@ __device__ __forceinline__ void mixed_cg_body(const MArgs &a) {
   if (kStaged) {
     if (threadIdx.x == 0) {
       StHdr *H = reinterpret_cast<StHdr *>(st_smem);
-      for (int i = 0; i < kWinSlots; ++i) mbar_init(&H->win[i], 1);
+      for (int i = 0; i < kLandSlots; ++i) mbar_init(&H->land[i], 1);
       for (int i = 0; i < kAStages; ++i) mbar_init(&H->sa[i], 1);
       for (int i = 0; i < kBStages; ++i) mbar_init(&H->sb[i], 1);
       mbar_init_fence();
@@ -861,8 +839,8 @@ __device__ __forceinline__ void mixed_cg_body(const MArgs &a) {
   __shared__ struct {
     double rz, rr_upd, relres, pend_alpha, alpha, rz_new;
     double bnorm2, scale, delta2, target2, res0;
-    float alpha_f, alpha_lo, a1, a1_lo, beta;
-    int action, status, updates, pair;
+    float alpha_f, alpha_lo, a1, a1_lo, beta, beta_lo;
+    int action, status, updates;
   } sh;
   __shared__ float2 red2[kMaxNV * 32];
   enum { kContinue = 0, kUpdate = 1, kStop = 2 };
@@ -882,33 +860,31 @@ __device__ __forceinline__ void mixed_cg_body(const MArgs &a) {
     sh.rr_upd = res[3];  // ||r||^2 (moving rows) at the last reliable update
     sh.pend_alpha = 0.0;
     sh.beta = 0.0f;
+    sh.beta_lo = 0.0f;
     sh.updates = 0;
-    sh.pair = sh.relres <= kPairFrom;
     sh.status = !(sh.relres == sh.relres) ? FVC_ERR_NAN
                 : (sh.relres <= a.target) ? FVC_OK
                                           : FVC_ERR_NOCONV;
   }
   __syncthreads();
   int status = sh.status;
-  bool pair = sh.pair != 0;
-  float beta = 0.0f;
-  float *pprev = a.pb, *pcur = a.pa;
-  bool pending = false;  // an alpha*p not yet added to e
+  float bh = 0.0f, bl = 0.0f;  // beta as an FP32 pair
+  bool flip = false;           // which buffers hold p_prev / p this iteration
+  bool pending = false;        // an alpha*p not yet added to e
   while (status == FVC_ERR_NOCONV && it < a.maxit) {
     ++it;
-    // p = z + beta p_prev (formed on the fly at the neighbours); q = A p; p.q
+    Dir d;
+    d.ph = flip ? a.pa : a.pb;
+    d.pl = flip ? a.pal : a.pbl;
+    d.ch = flip ? a.pb : a.pa;
+    d.cl = flip ? a.pbl : a.pal;
+    // p = z + beta p_prev (an FP32 pair); q = A p_hi; p_hi.q
     CSum pq[1];
-    if (kStaged) {
-      pq[0] = (it == 1)
-                  ? cg_phase_a_st<true>(a, P, beta, a.z, pprev, pcur, a.q, a.e, st_smem, gch)
-                  : cg_phase_a_st<false>(a, P, beta, a.z, pprev, pcur, a.q, a.e, st_smem, gch);
-    } else if (a.col16) {
-      pq[0] = (it == 1) ? cg_phase_a<true, true>(a, P, beta, a.z, pprev, pcur, a.q, a.e)
-                        : cg_phase_a<false, true>(a, P, beta, a.z, pprev, pcur, a.q, a.e);
-    } else {
-      pq[0] = (it == 1) ? cg_phase_a<true, false>(a, P, beta, a.z, pprev, pcur, a.q, a.e)
-                        : cg_phase_a<false, false>(a, P, beta, a.z, pprev, pcur, a.q, a.e);
-    }
+    if (kStaged)
+      pq[0] = (it == 1) ? cg_phase_a_st<true>(a, P, bh, bl, d, st_smem, gch)
+                        : cg_phase_a_st<false>(a, P, bh, bl, d, st_smem, gch);
+    else
+      pq[0] = (it == 1) ? cg_phase_a<true>(a, P, bh, bl, d) : cg_phase_a<false>(a, P, bh, bl, d);
     if (!grid_allreduce_ff<1>(a.gs, ep, pq, red2, [&](const double *t) {
           const double alpha_d = sh.rz / t[0];
           sh.alpha = alpha_d;
@@ -924,35 +900,16 @@ __device__ __forceinline__ void mixed_cg_body(const MArgs &a) {
     // e += a_prev p_prev + alpha p (FP32 pair)
     CSum acc[2];
     if (kStaged) {
-      if (pending) {
-        if (pair)
-          cg_phase_b_st<true, true>(a, P, a1, a1_lo, pprev, alpha, alpha_lo, pcur, acc[0],
-                                    acc[1], st_smem, gch);
-        else
-          cg_phase_b_st<false, true>(a, P, a1, a1_lo, pprev, alpha, alpha_lo, pcur, acc[0],
-                                     acc[1], st_smem, gch);
-      } else {
-        if (pair)
-          cg_phase_b_st<true, false>(a, P, a1, a1_lo, pprev, alpha, alpha_lo, pcur, acc[0],
-                                     acc[1], st_smem, gch);
-        else
-          cg_phase_b_st<false, false>(a, P, a1, a1_lo, pprev, alpha, alpha_lo, pcur, acc[0],
-                                      acc[1], st_smem, gch);
-      }
+      if (pending)
+        cg_phase_b_st<true, true>(a, P, a1, a1_lo, alpha, alpha_lo, d, acc[0], acc[1], st_smem,
+                                  gch);
+      else
+        cg_phase_b_st<true, false>(a, P, a1, a1_lo, alpha, alpha_lo, d, acc[0], acc[1], st_smem,
+                                   gch);
     } else if (pending) {
-      if (pair)
-        cg_phase_b<true, true>(P, a1, a1_lo, pprev, alpha, alpha_lo, pcur, a.q, a.rs, a.rsl,
-                               a.z, a.e, a.minv, acc[0], acc[1]);
-      else
-        cg_phase_b<false, true>(P, a1, a1_lo, pprev, alpha, alpha_lo, pcur, a.q, a.rs, a.rsl,
-                                a.z, a.e, a.minv, acc[0], acc[1]);
+      cg_phase_b<true, true>(a, P, a1, a1_lo, alpha, alpha_lo, d, acc[0], acc[1]);
     } else {
-      if (pair)
-        cg_phase_b<true, false>(P, a1, a1_lo, pprev, alpha, alpha_lo, pcur, a.q, a.rs, a.rsl,
-                                a.z, a.e, a.minv, acc[0], acc[1]);
-      else
-        cg_phase_b<false, false>(P, a1, a1_lo, pprev, alpha, alpha_lo, pcur, a.q, a.rs, a.rsl,
-                                 a.z, a.e, a.minv, acc[0], acc[1]);
+      cg_phase_b<true, false>(a, P, a1, a1_lo, alpha, alpha_lo, d, acc[0], acc[1]);
     }
     const bool was_pending = pending;
     pending = !pending;
@@ -968,7 +925,9 @@ __device__ __forceinline__ void mixed_cg_body(const MArgs &a) {
           } else if (t[1] <= sh.delta2 * sh.rr_upd || t[1] <= sh.target2 || it >= a.maxit) {
             sh.action = kUpdate;
           } else {
-            sh.beta = (float)(rz_new / sh.rz);
+            const double beta = rz_new / sh.rz;
+            sh.beta = (float)beta;
+            sh.beta_lo = (float)(beta - (double)sh.beta);
             sh.rz = rz_new;
             sh.action = kContinue;
           }
@@ -978,7 +937,7 @@ __device__ __forceinline__ void mixed_cg_body(const MArgs &a) {
     if (action == kUpdate) {
       // reliable update: fold e (and a deferred alpha p) into x, recompute
       // the true residual in FP64
-      fold_correction(a, pending ? pcur : nullptr, sh.pend_alpha);
+      fold_correction(a, pending ? d.ch : nullptr, pending ? d.cl : nullptr, sh.pend_alpha);
       pending = false;
       if (!grid_barrier(a.gs, ep)) return;
       if (!residual_sweep(a, ep, false, res, red)) return;
@@ -999,27 +958,26 @@ __device__ __forceinline__ void mixed_cg_body(const MArgs &a) {
           sh.status = FVC_OK;
           sh.action = kStop;
         } else {
-          if (relres <= kPairFrom) sh.pair = 1;  // the sweep wrote both parts
           sh.rr_upd = res[3];
           // beta from the replaced (true) residual, or with update_beta from
           // the recursive one; the next alpha uses the true r.z
-          sh.beta = (float)((a.update_beta ? sh.rz_new : res[2]) / sh.rz);
+          const double beta = (a.update_beta ? sh.rz_new : res[2]) / sh.rz;
+          sh.beta = (float)beta;
+          sh.beta_lo = (float)(beta - (double)sh.beta);
           sh.rz = res[2];
         }
         sh.pend_alpha = 0.0;
       }
       __syncthreads();
       action = sh.action;
-      pair = sh.pair != 0;
     }
     if (action == kStop) {
       status = sh.status;
       break;
     }
-    beta = sh.beta;
-    float *tmp = pprev;
-    pprev = pcur;
-    pcur = tmp;
+    bh = sh.beta;
+    bl = sh.beta_lo;
+    flip = !flip;
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     a.iresult[0] = sh.updates;
@@ -1256,6 +1214,8 @@ int32_t run_mixed(const DeviceMatrix &A0, Scratch &S, int code, const double *b,
   a.v = S.f[7];
   a.z = S.f[8];
   a.rsl = (code == 1) ? S.f[9] : nullptr;
+  a.pal = S.f[5];  // CG only (BiCGSTAB uses these buffers as r0 and t)
+  a.pbl = S.f[6];
   a.gs = make_sync(S, blocks);
   a.target = (o.refine_tol > 0) ? o.refine_tol : tol;
   a.inner_tol = (o.inner_tol > 0) ? o.inner_tol : (code == 1 ? 0.1 : 1e-4);
