@@ -164,6 +164,94 @@ __device__ __forceinline__ bool grid_allreduce(const GridSync &gs, unsigned int 
   return true;
 }
 
+// Grid-wide deterministic sum of NV FP64 values per thread, for the FP64
+// solvers.  GB300 issues FP64 at ~2 lanes per clock per SM, so the block
+// sum avoids a butterfly in every warp (5 x 32 lanes x 32 warps adds):
+// the values go to shared memory (buf: NV x blockDim doubles), four warps
+// (one per SM sub-partition) add 8 values per lane each, warp 0 adds those
+// and finishes with a shuffle tree -- a fixed order, about 2.5x fewer FP64
+// instructions (blockDim.x must be a multiple of 128).  The block's
+// partial is published with a release add on the grid counter; every block waits for all arrivals and sums all
+// partials in block order itself.  Lane 0 of warp 0 then calls f(totals)
+// -- the place for the iteration's scalar FP64 work (one thread instead of
+// 1024) -- and one __syncthreads hands its results (through shared memory)
+// to the block.  Returns false when a wait exceeded its bound (gs.err set).
+template <int NV, typename F>
+__device__ __forceinline__ bool grid_allreduce_d(const GridSync &gs, unsigned int &episode,
+                                                 const double (&v)[NV], double *buf, F &&f) {
+  __shared__ int s_ok;
+  __shared__ double s_part[NV][128];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int bd = blockDim.x, per = bd >> 7;  // values per lane of the first level
+#pragma unroll
+  for (int q = 0; q < NV; ++q) buf[q * bd + threadIdx.x] = v[q];
+  if (threadIdx.x == 0) s_ok = 1;
+  __syncthreads();
+  if (warp < 4) {
+#pragma unroll
+    for (int q = 0; q < NV; ++q) {
+      const double *b = buf + q * bd + warp * (bd >> 2) + lane;
+      double u = b[0];
+      for (int k = 1; k < per; ++k) u = __dadd_rn(u, b[32 * k]);
+      s_part[q][warp * 32 + lane] = u;
+    }
+  }
+  __syncthreads();
+  const unsigned int ep = ++episode;
+  if (warp == 0) {
+    const unsigned int nb = gs.nblocks;
+    double *part = gs.partials + (size_t)(ep & 3u) * kMaxNV * nb;
+    double bsum[NV];
+#pragma unroll
+    for (int q = 0; q < NV; ++q) {
+      double u = s_part[q][lane];
+#pragma unroll
+      for (int k = 1; k < 4; ++k) u = __dadd_rn(u, s_part[q][32 * k + lane]);
+      bsum[q] = warp_sum(u);
+    }
+    bool ok = true;
+    if (lane == 0) {
+#pragma unroll
+      for (int q = 0; q < NV; ++q) part[(size_t)q * nb + blockIdx.x] = bsum[q];
+      red_add_release(gs.count, 1u);
+      const unsigned int target = ep * nb;
+      const uint64_t t0 = global_ns();
+      unsigned int spins = 0;
+      while (ld_acquire(gs.count) < target) {
+        if (*(volatile int *)gs.err != 0) {
+          ok = false;
+          break;
+        }
+        if ((++spins & 255u) == 0 && global_ns() - t0 > kBarrierTimeoutNs) {
+          atomicExch(gs.err, 7 /* FVC_ERR_TIMEOUT */);
+          ok = false;
+          break;
+        }
+        __nanosleep(20);
+      }
+    }
+    ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+    double t[NV];
+#pragma unroll
+    for (int q = 0; q < NV; ++q) {
+      double u = 0.0;
+      if (ok) {
+        const double *pp = part + (size_t)q * nb;
+        for (unsigned int b = lane; b < nb; b += 32) u = __dadd_rn(u, __ldcg(pp + b));
+      }
+      t[q] = warp_sum(u);
+    }
+    if (lane == 0) {
+      if (ok)
+        f(t);
+      else
+        s_ok = 0;
+    }
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
 __device__ __forceinline__ bool grid_barrier(const GridSync &gs, unsigned int &episode) {
   double none[1];
   return grid_allreduce<0>(gs, episode, none, nullptr);

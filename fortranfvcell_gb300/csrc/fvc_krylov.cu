@@ -113,15 +113,21 @@ __device__ __forceinline__ bool epilogue(const KArgs &a, unsigned int &ep, doubl
 // ---------------------------------------------------------------------
 __global__ void __launch_bounds__(1024, 1) pcg_f64(KArgs a) {
   __shared__ double red[kMaxNV * 32];
+  __shared__ double buf[2 * 1024];
+  // scalars of the recurrence, updated by lane 0 of warp 0 inside the
+  // all-reduces and read by every thread after them
+  __shared__ struct {
+    double d, alpha, beta, conv, crit;
+    int stop;  // 0 go on, 1 converged, 2 NaN/Inf
+  } sh;
   const Part P(a.A.nslices, a.A.n);
   double *r = a.v0, *z = a.v1, *q = a.v4, *x = a.x;
   const double *minv = a.minv, *b = a.b;
+  const bool rule0 = a.stop_rule == 0;
   unsigned int ep = 0;
-  double acc[2];
 
   // r = b - A x ; z = r/m ; p = z ; d = r.z  (x = 0 when init)
-  acc[0] = 0.0;
-  acc[1] = 0.0;
+  double acc[2] = {0.0, 0.0};
   FOR_ROWS(P) {
     double ax;
     if (a.init) {
@@ -137,13 +143,17 @@ __global__ void __launch_bounds__(1024, 1) pcg_f64(KArgs a) {
     acc[0] = fma(ri, zi, acc[0]);
     acc[1] = fma(b[row], b[row], acc[1]);
   }
-  if (!reduce<2>(a, ep, acc, red)) return;
-  double d = acc[0];
-  const double bnorm2 = acc[1];
-  const double conv = (a.stop_rule == 0) ? a.tol * sqrt(fabs(d)) : a.tol * sqrt(bnorm2);
+  if (!grid_allreduce_d<2>(a.gs, ep, acc, buf, [&](const double *t) {
+        sh.d = t[0];
+        sh.conv = rule0 ? a.tol * sqrt(fabs(t[0])) : a.tol * sqrt(t[1]);
+        sh.beta = 0.0;
+        sh.crit = 0.0;
+        sh.stop = 0;
+      }))
+    return;
 
-  double beta = 0.0, crit = 0.0;
   double *pprev = a.v2, *pcur = a.v2;
+  double beta = 0.0;
   int j, status = FVC_OK;
   for (j = 1; j <= a.maxit; ++j) {
     // q = A p  (p = z + beta*p formed on the fly for j >= 2); p.q
@@ -166,29 +176,41 @@ __global__ void __launch_bounds__(1024, 1) pcg_f64(KArgs a) {
         pq[0] = fma(pi, qi, pq[0]);
       }
     }
-    if (!reduce<1>(a, ep, pq, red)) return;
-    const double alpha = d / pq[0];
+    if (!grid_allreduce_d<1>(a.gs, ep, pq, buf,
+                             [&](const double *t) { sh.alpha = sh.d / t[0]; }))
+      return;
+    const double alpha = sh.alpha;
     // x += alpha p ; r -= alpha q ; z = r/m ; r.z (and r.r for stop_rule 1)
-    acc[0] = 0.0;
-    acc[1] = 0.0;
+    double rz[1] = {0.0}, rr2[2] = {0.0, 0.0};
     FOR_ROWS(P) {
       x[row] = fma(alpha, pcur[row], x[row]);
       const double ri = fma(-alpha, q[row], r[row]);
       const double zi = ri * minv[row];
       r[row] = ri;
       z[row] = zi;
-      acc[0] = fma(ri, zi, acc[0]);
-      acc[1] = fma(ri, ri, acc[1]);
+      if (rule0) {
+        rz[0] = fma(ri, zi, rz[0]);
+      } else {
+        rr2[0] = fma(ri, zi, rr2[0]);
+        rr2[1] = fma(ri, ri, rr2[1]);
+      }
     }
-    if (!reduce<2>(a, ep, acc, red)) return;
-    beta = acc[0] / d;
-    d = beta * d;
-    crit = (a.stop_rule == 0) ? sqrt(fabs(d)) : sqrt(acc[1]);
-    if (!(crit == crit) || isinf(d)) {
+    // beta = r.z / d ; d = beta d ; the reference's stopping test
+    auto step = [&](const double *t) {
+      sh.beta = t[0] / sh.d;
+      sh.d = sh.beta * sh.d;
+      sh.crit = rule0 ? sqrt(fabs(sh.d)) : sqrt(t[1]);
+      sh.stop = (!(sh.crit == sh.crit) || isinf(sh.d)) ? 2 : (sh.crit < sh.conv ? 1 : 0);
+    };
+    const bool ok = rule0 ? grid_allreduce_d<1>(a.gs, ep, rz, buf, step)
+                          : grid_allreduce_d<2>(a.gs, ep, rr2, buf, step);
+    if (!ok) return;
+    if (sh.stop == 2) {
       status = FVC_ERR_NAN;
       break;
     }
-    if (crit < conv) break;
+    if (sh.stop == 1) break;
+    beta = sh.beta;
     pprev = pcur;
     pcur = (pcur == a.v2) ? a.v3 : a.v2;
   }
@@ -196,7 +218,7 @@ __global__ void __launch_bounds__(1024, 1) pcg_f64(KArgs a) {
     j = a.maxit;
     status = FVC_ERR_NOCONV;
   }
-  finish(a, j, status, conv, crit, 0);
+  finish(a, j, status, sh.conv, sh.crit, 0);
   epilogue(a, ep, red, false);
 }
 
@@ -510,7 +532,8 @@ int sm_count() {
 template <typename K>
 Launch persistent_launch(K kernel, const DeviceMatrix &A, const fvc_opts &o) {
   Launch L;
-  L.threads = (o.block_threads > 0) ? o.block_threads : 1024;
+  // 128..1024 threads in multiples of 128 (the block reductions assume it)
+  L.threads = (o.block_threads > 0) ? std::min(1024, std::max(128, o.block_threads & ~127)) : 1024;
   int occ = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, L.threads, 0);
   if (occ <= 0) occ = 1;
