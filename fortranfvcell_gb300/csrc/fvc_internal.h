@@ -32,6 +32,7 @@ struct DeviceMatrix {
   int16_t *col16 = nullptr; // column - row per slot (when every one fits)
   uint8_t *sflag = nullptr; // per slice: 1 if some row has e_i != 0
   bool col16_ok = false;
+  int ell_w = 0;             // FP32 copy padded to this uniform slice width (0: SELL)
   bool have32 = false;
   // host-side description of the source layout, for value updates
   int matriz = 0, unsym = 0, nad = 0;

@@ -478,8 +478,12 @@ __global__ void __launch_bounds__(256) spmv_f64(SellView<double> A, const double
 }
 
 // FP32 difference form: y_i = e_i x_i + sum_k w_ik (x_i - x_k)
+// y = A x in the FP32 difference form.  ell_w > 0: the weights and 16-bit
+// column offsets are laid out ell_w slots per slice (padding slots add 0);
+// otherwise SELL-32 with the FP64 matrix's columns.
 __global__ void __launch_bounds__(256) spmv_f32(int n, int nslices, const int64_t *__restrict__ sptr,
                                                 const int *__restrict__ col,
+                                                const int16_t *__restrict__ col16, int ell_w,
                                                 const float *__restrict__ w32,
                                                 const float *__restrict__ e32,
                                                 const float *__restrict__ x, float *__restrict__ y) {
@@ -488,13 +492,20 @@ __global__ void __launch_bounds__(256) spmv_f32(int n, int nslices, const int64_
   for (int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < nslices; s += nw) {
     const int row = s * 32 + lane;
     if (row >= n) continue;
-    const int64_t base = sptr[s];
-    const int w = (int)((sptr[s + 1] - base) >> 5);
     const float xi = __ldg(x + row);
     float t = ld_stream(e32 + row) * xi;
-    for (int kk = 0; kk < w; ++kk)
-      t = fmaf(ld_stream(w32 + base + 32 * kk + lane),
-               xi - __ldg(x + ld_stream(col + base + 32 * kk + lane)), t);
+    if (ell_w > 0) {
+      const int64_t base = (int64_t)s * 32 * ell_w + lane;
+      for (int kk = 0; kk < ell_w; ++kk)
+        t = fmaf(ld_stream(w32 + base + 32 * kk),
+                 xi - __ldg(x + row + (int)ld_stream16(col16 + base + 32 * kk)), t);
+    } else {
+      const int64_t base = sptr[s];
+      const int w = (int)((sptr[s + 1] - base) >> 5);
+      for (int kk = 0; kk < w; ++kk)
+        t = fmaf(ld_stream(w32 + base + 32 * kk + lane),
+                 xi - __ldg(x + ld_stream(col + base + 32 * kk + lane)), t);
+    }
     y[row] = t;
   }
 }
@@ -673,7 +684,8 @@ int32_t launch_spmv_f32(const DeviceMatrix &A, const float *x, float *y, cudaStr
   const int threads = 256;
   int blocks = (A.nslices + 7) / 8;
   blocks = std::max(1, std::min(blocks, sm_count() * 8));
-  spmv_f32<<<blocks, threads, 0, stream>>>(A.n, A.nslices, A.sptr, A.col, A.val32, A.diag32, x, y);
+  spmv_f32<<<blocks, threads, 0, stream>>>(A.n, A.nslices, A.sptr, A.col, A.col16, A.ell_w,
+                                           A.val32, A.diag32, x, y);
   count_launch();
   return cudaPeekAtLastError() == cudaSuccess ? FVC_OK : FVC_ERR_CUDA;
 }

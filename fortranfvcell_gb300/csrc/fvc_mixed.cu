@@ -182,31 +182,59 @@ __device__ __forceinline__ float2 df_axpy(float2 e, float ah, float al, float p)
   return make_float2(hi, __fsub_rn(lo, __fsub_rn(hi, s)));
 }
 
-// e_i (FP64 sum, rounded once), Jacobi 1/m, the FP32 weights, the 16-bit
-// column offsets (col - row) and the per-slice "has excess" flags.
-__global__ void build_f32_operator(int n, int nslices, const int64_t *__restrict__ sptr,
-                                   const int *__restrict__ col, const double *__restrict__ val,
-                                   const double *__restrict__ jac, float *__restrict__ w32,
-                                   float *__restrict__ e32, float *__restrict__ minv32,
-                                   int16_t *__restrict__ col16, uint8_t *__restrict__ sflag,
-                                   int *__restrict__ col16_overflow) {
+// Layout scan: flags[0] = 1 if some column offset (col - row) needs more
+// than 16 bits, flags[1] / flags[2] = smallest / largest slice width.
+__global__ void scan_slices(int n, int nslices, const int64_t *__restrict__ sptr,
+                            const int *__restrict__ col, int *__restrict__ flags) {
   const int lane = threadIdx.x & 31;
   const int nw = (gridDim.x * blockDim.x) >> 5;
   for (int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < nslices; s += nw) {
     const int row = s * 32 + lane;
     const int64_t base = sptr[s];
     const int wd = (int)((sptr[s + 1] - base) >> 5);
-    double off = 0.0;  // sum of a_ik over true off-diagonal slots
     bool wide = false;
+    for (int k = 0; k < wd; ++k) {
+      const int d = (row < n) ? col[base + 32 * k + lane] - row : 0;
+      if (d < -32768 || d > 32767) wide = true;
+    }
+    if (__any_sync(0xffffffffu, wide) && lane == 0) atomicExch(flags, 1);
+    if (lane == 0) {
+      atomicMin(flags + 1, wd);
+      atomicMax(flags + 2, wd);
+    }
+  }
+}
+
+// e_i (FP64 sum, rounded once), Jacobi 1/m, the FP32 weights, the 16-bit
+// column offsets (col - row) and the per-slice "has excess" flags.  With
+// ell_w > 0 the weights and offsets are laid out with every slice ell_w
+// slots wide (slice s at slot 32 ell_w s); the slots a narrower slice lacks
+// get weight 0 and offset 0, which add exactly 0 to every row sum.
+__global__ void build_f32_operator(int n, int nslices, const int64_t *__restrict__ sptr,
+                                   const int *__restrict__ col, const double *__restrict__ val,
+                                   const double *__restrict__ jac, float *__restrict__ w32,
+                                   float *__restrict__ e32, float *__restrict__ minv32,
+                                   int16_t *__restrict__ col16, uint8_t *__restrict__ sflag,
+                                   int ell_w) {
+  const int lane = threadIdx.x & 31;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  for (int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < nslices; s += nw) {
+    const int row = s * 32 + lane;
+    const int64_t base = sptr[s];
+    const int wd = (int)((sptr[s + 1] - base) >> 5);
+    const int64_t dbase = (ell_w > 0) ? (int64_t)s * 32 * ell_w : base;
+    double off = 0.0;  // sum of a_ik over true off-diagonal slots
     for (int k = 0; k < wd; ++k) {
       const int64_t q = base + 32 * k + lane;
       const bool diag_slot = (row < n) && (col[q] == row);
       const double a = (row < n && !diag_slot) ? val[q] : 0.0;
       off += a;
-      w32[q] = (float)(-a);
-      const int d = (row < n) ? col[q] - row : 0;
-      if (d < -32768 || d > 32767) wide = true;
-      col16[q] = (int16_t)d;
+      w32[dbase + 32 * k + lane] = (float)(-a);
+      col16[dbase + 32 * k + lane] = (int16_t)((row < n) ? col[q] - row : 0);
+    }
+    for (int k = wd; k < ell_w; ++k) {
+      w32[dbase + 32 * k + lane] = 0.0f;
+      col16[dbase + 32 * k + lane] = 0;
     }
     float ev = 0.0f;
     if (row < n) {
@@ -219,7 +247,6 @@ __global__ void build_f32_operator(int n, int nslices, const int64_t *__restrict
     }
     const bool any_e = __any_sync(0xffffffffu, ev != 0.0f);
     if (lane == 0) sflag[s] = any_e ? 1 : 0;
-    if (__any_sync(0xffffffffu, wide) && lane == 0) atomicExch(col16_overflow, 1);
   }
 }
 
@@ -229,6 +256,7 @@ struct MArgs {
   const float *e32;     // row excess
   const float *minv;    // Jacobi 1/m (0 on rows whose m is beyond FP32)
   const int16_t *col16; // column offsets (col - row), when col16_ok
+  int ell_w;            // > 0: w32/col16 hold every slice ell_w slots wide
   const uint8_t *sflag; // per slice: some row has e_i != 0
   const double *jac;    // m in FP64
   const double *b;
@@ -253,6 +281,15 @@ struct MArgs {
 // (A y)_row in FP32 difference form, y supplied by a functor.
 template <typename YF>
 __device__ __forceinline__ float arow32(const MArgs &a, int s, int lane, int row, YF yf) {
+  if (a.ell_w > 0) {  // uniform layout: 16-bit offsets, padding slots add 0
+    const int64_t base = (int64_t)s * 32 * a.ell_w + lane;
+    const float yi = yf(row);
+    float t = ld_stream(a.e32 + row) * yi;
+    for (int k = 0; k < a.ell_w; ++k)
+      t = fmaf(ld_stream(a.w32 + base + 32 * k),
+               yi - yf(row + (int)ld_stream16(a.col16 + base + 32 * k)), t);
+    return t;
+  }
   const int64_t base = a.A.sptr[s];
   const int w = (int)((a.A.sptr[s + 1] - base) >> 5);
   const int *cp = a.A.col + base + lane;
@@ -590,6 +627,24 @@ __device__ __forceinline__ void issue_slots(const MArgs &a, const MPart &P, unsi
   }
 }
 
+// Lane 0 of warp 0: chunk j of a uniform-width-kW layout (slice s starts
+// at slot 32 kW s) into phase-A stage seq.
+template <int kW>
+__device__ __forceinline__ void issue_slots_u(const MArgs &a, const MPart &P, unsigned char *smem,
+                                              uint32_t seq, int j) {
+  StHdr *H = reinterpret_cast<StHdr *>(smem);
+  const uint32_t stg = seq % kAStages;
+  const int c0 = P.sb + kStChunkSlices * j;
+  const int c1 = min(P.se, c0 + kStChunkSlices);
+  const int64_t s0 = (int64_t)c0 * kSlice * kW;
+  const uint32_t nsl = (uint32_t)(c1 - c0) * kSlice * kW;
+  uint64_t *bar = &H->sa[stg];
+  unsigned char *b = st_region(smem) + kA_Base + stg * kA_Bytes;
+  mbar_arrive_expect_tx(bar, nsl * 6u);
+  bulk_g2s(b, a.w32 + s0, nsl * 4u, bar);
+  bulk_g2s(b + kA_C, a.col16 + s0, nsl * 2u, bar);
+}
+
 // Forms the p pair of row r (from z and p_prev given), puts p_hi in the
 // ring and stores the pair when the row is the block's own.
 template <bool kFirst>
@@ -604,8 +659,10 @@ __device__ __forceinline__ void p_form(float *ring, int r, int R0, int Rend, int
 }
 
 // Staged phase A: p = z + beta p_prev, q = A p_hi, returns p_hi.q.  Same
-// arithmetic, in the same order, as cg_phase_a.
-template <bool kFirst>
+// arithmetic, in the same order, as cg_phase_a.  kW > 0: every slice has
+// width kW (slot offsets follow from the slice index; no slice-pointer
+// loads, no capacity check, fixed unrolled row loop); kW == 0: general.
+template <bool kFirst, int kW>
 __device__ __forceinline__ CSum cg_phase_a_st(const MArgs &a, const MPart &P, float bh, float bl,
                                               const Dir &d, unsigned char *smem, StCount &cnt) {
   StHdr *H = reinterpret_cast<StHdr *>(smem);
@@ -626,7 +683,13 @@ __device__ __forceinline__ CSum cg_phase_a_st(const MArgs &a, const MPart &P, fl
       for (int j = kWinHalo + 1; j <= jlast && j <= kWinHalo + kLandAhead; ++j)
         issue_land<kFirst>(a, P, smem, cnt.land + (j - kWinHalo - 1), j, nrows, d);
     }
-    for (int j = 0; j < kAStages - 1 && j < nch; ++j) issue_slots(a, P, smem, B, cnt.sa + j, j);
+    for (int j = 0; j < kAStages - 1 && j < nch; ++j) {
+      if (kW > 0) {
+        if (P.lane == 0) issue_slots_u<kW>(a, P, smem, cnt.sa + j, j);
+      } else {
+        issue_slots(a, P, smem, B, cnt.sa + j, j);
+      }
+    }
   }
   // window chunks -3 .. 3 with plain loads (one row of each per thread)
   {
@@ -652,8 +715,10 @@ __device__ __forceinline__ CSum cg_phase_a_st(const MArgs &a, const MPart &P, fl
   {
     const int s = P.sb + P.warp;
     if (s < P.se) {
-      my0 = a.A.sptr[s];
-      my1 = a.A.sptr[s + 1];
+      if (kW == 0) {
+        my0 = a.A.sptr[s];
+        my1 = a.A.sptr[s + 1];
+      }
       if (a.sflag[s] && s * kSlice + P.lane < P.n) myex = ld_stream(a.e32 + s * kSlice + P.lane);
     }
   }
@@ -663,8 +728,13 @@ __device__ __forceinline__ CSum cg_phase_a_st(const MArgs &a, const MPart &P, fl
       const int jl = i + kWinHalo + 1 + kLandAhead;
       if (P.lane == 0 && jl <= jlast)
         issue_land<kFirst>(a, P, smem, cnt.land + (jl - kWinHalo - 1), jl, nrows, d);
-      if (i + kAStages - 1 < nch)
-        issue_slots(a, P, smem, B, cnt.sa + i + kAStages - 1, i + kAStages - 1);
+      if (i + kAStages - 1 < nch) {
+        if (kW > 0) {
+          if (P.lane == 0) issue_slots_u<kW>(a, P, smem, cnt.sa + i + kAStages - 1, i + kAStages - 1);
+        } else {
+          issue_slots(a, P, smem, B, cnt.sa + i + kAStages - 1, i + kAStages - 1);
+        }
+      }
     }
     const int s = P.sb + kStChunkSlices * i + P.warp;
     // next chunk's slice bounds, loaded while this chunk is processed
@@ -672,8 +742,10 @@ __device__ __forceinline__ CSum cg_phase_a_st(const MArgs &a, const MPart &P, fl
     float nex = 0.0f;
     if (s + kStChunkSlices < P.se) {
       const int sn = s + kStChunkSlices, rn = sn * kSlice + P.lane;
-      n0 = a.A.sptr[sn];
-      n1 = a.A.sptr[sn + 1];
+      if (kW == 0) {
+        n0 = a.A.sptr[sn];
+        n1 = a.A.sptr[sn + 1];
+      }
       if (a.sflag[sn] && rn < P.n) nex = ld_stream(a.e32 + rn);
     }
     // form p for window chunk i+4 (used from the next chunk on)
@@ -696,11 +768,15 @@ __device__ __forceinline__ CSum cg_phase_a_st(const MArgs &a, const MPart &P, fl
     if (s < P.se) {
       const int row = s * kSlice + P.lane;
       const int wlo = R0 + (i - kWinHalo) * kStRows;  // first row of the window
-      const int wd = (int)((my1 - my0) >> 5);
+      const int wd = (kW > 0) ? kW : (int)((my1 - my0) >> 5);
       const float *ws;
       const int16_t *cs;
-      if (H->ok[stg]) {
-        const unsigned char *b = st_region(smem) + kA_Base + stg * kA_Bytes;
+      const unsigned char *b = st_region(smem) + kA_Base + stg * kA_Bytes;
+      if (kW > 0) {
+        const int off = P.warp * kSlice * kW + P.lane;
+        ws = reinterpret_cast<const float *>(b) + off;
+        cs = reinterpret_cast<const int16_t *>(b + kA_C) + off;
+      } else if (H->ok[stg]) {
         const int64_t off = my0 - H->base[stg];
         ws = reinterpret_cast<const float *>(b) + off + P.lane;
         cs = reinterpret_cast<const int16_t *>(b + kA_C) + off + P.lane;
@@ -717,7 +793,18 @@ __device__ __forceinline__ CSum cg_phase_a_st(const MArgs &a, const MPart &P, fl
       if (row < P.n) {
         const float pi = ring[(row - R0) & (kPRingRows - 1)];
         float t = myex * pi;
-        if (wd <= 4) {
+        if (kW > 0) {
+          constexpr int W = kW > 0 ? kW : 1;
+          int c[W];
+          float w[W];
+#pragma unroll
+          for (int k = 0; k < kW; ++k) {
+            c[k] = row + (int)cs[32 * k];
+            w[k] = ws[32 * k];
+          }
+#pragma unroll
+          for (int k = 0; k < kW; ++k) t = fmaf(w[k], pi - pat(c[k]), t);
+        } else if (wd <= 4) {
           int c[4];
           float w[4], nb[4];
 #pragma unroll
@@ -817,7 +904,7 @@ __device__ __forceinline__ void cg_phase_b_st(const MArgs &a, const MPart &P, fl
   cnt.sb += (uint32_t)nch;
 }
 
-template <bool kStaged>
+template <bool kStaged, int kW>
 __device__ __forceinline__ void mixed_cg_body(const MArgs &a) {
   __shared__ double red[kMaxNV * 32];
   extern __shared__ __align__(128) unsigned char st_smem[];
@@ -881,8 +968,8 @@ __device__ __forceinline__ void mixed_cg_body(const MArgs &a) {
     // p = z + beta p_prev (an FP32 pair); q = A p_hi; p_hi.q
     CSum pq[1];
     if (kStaged)
-      pq[0] = (it == 1) ? cg_phase_a_st<true>(a, P, bh, bl, d, st_smem, gch)
-                        : cg_phase_a_st<false>(a, P, bh, bl, d, st_smem, gch);
+      pq[0] = (it == 1) ? cg_phase_a_st<true, kW>(a, P, bh, bl, d, st_smem, gch)
+                        : cg_phase_a_st<false, kW>(a, P, bh, bl, d, st_smem, gch);
     else
       pq[0] = (it == 1) ? cg_phase_a<true>(a, P, bh, bl, d) : cg_phase_a<false>(a, P, bh, bl, d);
     if (!grid_allreduce_ff<1>(a.gs, ep, pq, red2, [&](const double *t) {
@@ -989,11 +1076,19 @@ __device__ __forceinline__ void mixed_cg_body(const MArgs &a) {
   }
 }
 
-__global__ void __launch_bounds__(1024, 1) mixed_cg(MArgs a) { mixed_cg_body<false>(a); }
+__global__ void __launch_bounds__(1024, 1) mixed_cg(MArgs a) { mixed_cg_body<false, 0>(a); }
 
-// Staged form: 1024 threads, kStSmem bytes of dynamic shared memory, and
-// the 16-bit column offsets (col16) present.
-__global__ void __launch_bounds__(1024, 1) mixed_cg_staged(MArgs a) { mixed_cg_body<true>(a); }
+// Staged forms: 1024 threads, kStSmem bytes of dynamic shared memory, and
+// the 16-bit column offsets (col16) present; _w3/_w4 when every slice has
+// width 3 / 4 in the padded uniform layout (ell_w; cells of triangle /
+// quadrilateral meshes).
+__global__ void __launch_bounds__(1024, 1) mixed_cg_staged(MArgs a) { mixed_cg_body<true, 0>(a); }
+__global__ void __launch_bounds__(1024, 1) mixed_cg_staged_w3(MArgs a) {
+  mixed_cg_body<true, 3>(a);
+}
+__global__ void __launch_bounds__(1024, 1) mixed_cg_staged_w4(MArgs a) {
+  mixed_cg_body<true, 4>(a);
+}
 
 // The reference's Jacobi BiCGSTAB (Iterativos.f:140-234) in FP32 on the
 // correction equation A e = r, inside FP64 defect correction.
@@ -1121,7 +1216,24 @@ int sm_count_m() {
 
 int32_t build_f32_copy(DeviceMatrix &A, cudaStream_t stream) {
   if (A.have32) return FVC_OK;
-  const size_t sl = (size_t)std::max<int64_t>(A.slots, 1);
+  int *flags = nullptr;  // [0] a column offset overflows 16 bits, [1] min, [2] max slice width
+  if (cudaMalloc(&flags, 3 * sizeof(int)) != cudaSuccess) return FVC_ERR_CUDA;
+  const int init[3] = {0, 1 << 30, 0};
+  cudaMemcpyAsync(flags, init, sizeof(init), cudaMemcpyHostToDevice, stream);
+  int blocks = std::max(1, std::min((A.nslices + 7) / 8, sm_count_m() * 8));
+  scan_slices<<<blocks, 256, 0, stream>>>(A.n, A.nslices, A.sptr, A.col, flags);
+  count_launch();
+  int hf[3] = {1, 0, 0};
+  cudaMemcpyAsync(hf, flags, sizeof(hf), cudaMemcpyDeviceToHost, stream);
+  cudaError_t ce = cudaStreamSynchronize(stream);
+  cudaFree(flags);
+  if (ce != cudaSuccess) return FVC_ERR_CUDA;
+  A.col16_ok = (hf[0] == 0);
+  // slices at most 4 wide (the cells of triangle / quadrilateral meshes):
+  // pad them all to the widest, so the staged kernel needs no slice pointers
+  A.ell_w = (A.col16_ok && A.nslices > 0 && hf[2] >= 3 && hf[2] <= 4) ? hf[2] : 0;
+  const size_t sl = std::max<size_t>(
+      1, A.ell_w > 0 ? (size_t)A.nslices * kSlice * A.ell_w : (size_t)A.slots);
   if (!A.val32 && cudaMalloc(&A.val32, sizeof(float) * sl) != cudaSuccess) return FVC_ERR_CUDA;
   // row arrays cover whole slices (the staged loops copy 32-row units)
   const size_t nrow = (size_t)A.nslices * kSlice + 64;
@@ -1131,20 +1243,12 @@ int32_t build_f32_copy(DeviceMatrix &A, cudaStream_t stream) {
     return FVC_ERR_CUDA;
   if (!A.col16 && cudaMalloc(&A.col16, sizeof(int16_t) * sl) != cudaSuccess) return FVC_ERR_CUDA;
   if (!A.sflag && cudaMalloc(&A.sflag, (size_t)A.nslices + 1) != cudaSuccess) return FVC_ERR_CUDA;
-  int *ovf = nullptr;
-  if (cudaMalloc(&ovf, sizeof(int)) != cudaSuccess) return FVC_ERR_CUDA;
-  cudaMemsetAsync(ovf, 0, sizeof(int), stream);
-  int blocks = std::max(1, std::min((A.nslices + 7) / 8, sm_count_m() * 8));
   build_f32_operator<<<blocks, 256, 0, stream>>>(A.n, A.nslices, A.sptr, A.col, A.val, A.jac,
                                                  A.val32, A.diag32, A.minv32, A.col16, A.sflag,
-                                                 ovf);
+                                                 A.ell_w);
   count_launch();
-  int hovf = 1;
-  cudaMemcpyAsync(&hovf, ovf, sizeof(int), cudaMemcpyDeviceToHost, stream);
-  const cudaError_t ce = cudaStreamSynchronize(stream);
-  cudaFree(ovf);
+  ce = cudaStreamSynchronize(stream);
   if (ce != cudaSuccess) return FVC_ERR_CUDA;
-  A.col16_ok = (hovf == 0);
   A.have32 = true;
   return FVC_OK;
 }
@@ -1170,7 +1274,11 @@ int32_t run_mixed(const DeviceMatrix &A0, Scratch &S, int code, const double *b,
   const int threads = (o.block_threads > 0) ? o.block_threads : 1024;
   // CG streams through shared-memory stages when its layout allows
   const bool staged = code == 1 && threads == kStRows && A.col16_ok && o.staging == 0;
-  auto kern = (code == 1) ? (staged ? mixed_cg_staged : mixed_cg) : mixed_bicgstab;
+  auto kern = (code != 1) ? mixed_bicgstab
+              : !staged        ? mixed_cg
+              : A.ell_w == 4   ? mixed_cg_staged_w4
+              : A.ell_w == 3   ? mixed_cg_staged_w3
+                               : mixed_cg_staged;
   const size_t dsmem = staged ? kStSmem : 0;
   if (staged) {
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsmem) !=
@@ -1200,6 +1308,7 @@ int32_t run_mixed(const DeviceMatrix &A0, Scratch &S, int code, const double *b,
   a.e32 = A.diag32;
   a.minv = A.minv32;
   a.col16 = A.col16_ok ? A.col16 : nullptr;
+  a.ell_w = A.ell_w;
   a.sflag = A.sflag;
   a.jac = A.jac;
   a.b = b;

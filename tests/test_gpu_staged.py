@@ -69,9 +69,24 @@ def test_staged_matches_plain_on_mesh():
     assert _relres(s, x1, b) <= 1e-8
 
 
+def test_staged_matches_plain_triangles():
+    # triangle-only mesh: every slice has width 3 (the uniform-width-3 kernel)
+    from fortranfvcell_gb300 import mesh
+    m = mesh.square_mesh(300, kind="tri", jitter=0.2, seed=5)
+    ps = mesh.pressure_system(m, 1, True, pin_cell=1)
+    s = dict(n=ps.neq, ia=ps.ia, ja=ps.ja, au=ps.au, ad=ps.ad, nad=ps.nad)
+    b = np.random.default_rng(8).uniform(-1, 1, s["n"])
+    (st1, x1), (st0, x0) = _solve_both(s, b)
+    assert st1.status == 0 and st0.status == 0
+    assert st1.iterations == st0.iterations
+    assert np.array_equal(x1, x0)
+    assert _relres(s, x1, b) <= 1e-8
+
+
 def test_staged_matches_plain_beyond_window():
     # couplings 4000 rows apart: beyond the staged kernel's shared-memory
-    # window (+-3072 rows), so those neighbours come from global memory
+    # window (+-3072 rows), so those neighbours come from global memory;
+    # slices of width 3 and 4 mixed (the general staged kernel)
     s = laplace_csrd(4000, 12)
     b = np.random.default_rng(3).uniform(-1, 1, s["n"])
     (st1, x1), (st0, x0) = _solve_both(s, b)
