@@ -145,4 +145,34 @@ void oref_getres(double *u, double *x, const int32_t *num, int32_t neq,
 #ifdef __cplusplus
 }
 #endif
+
+/* SIMPLE outer-loop cells (fvc_oracle_simple.c).  Arrays follow the
+ * reference's Fortran layouts: coor(2,nnode), ix(ld,numel) with the
+ * material in row ld, nelcon(nshared,numel), pedge(nshared+1,numel),
+ * sedge(3,nshared+1,numel), e(10,nmat), 2-vectors (2,numel), iM(4,numel). */
+int32_t oref_gform(const double *coor, const int32_t *ix, int32_t ld, int32_t numel,
+                   int32_t nshared, const int32_t *nelcon, const int32_t *pedge,
+                   const double *sedge, int32_t kind, int32_t comp, const double *u,
+                   double *grad);
+int32_t oref_pform_momentum(const double *coor, const int32_t *ix, int32_t ld, int32_t numel,
+                            int32_t nshared, const int32_t *nelcon, const int32_t *num,
+                            const int32_t *pedge, const double *sedge, const double *e,
+                            int32_t comp, int32_t iws, const double *u, const double *u0,
+                            const double *w, const double *g_own, const double *g_oth,
+                            const double *gradp, double dt, int32_t bs, double under_u,
+                            int32_t simple_c, int32_t matriz, int32_t unsym, const int32_t *ia,
+                            const int32_t *ja, double *ad, double *au, double *b, double *im,
+                            double *d, double *rescell);
+int32_t oref_pform_pc(const double *coor, const int32_t *ix, int32_t ld, int32_t numel,
+                      int32_t nshared, const int32_t *nelcon, const int32_t *num,
+                      const int32_t *pedge, const double *sedge, const double *e,
+                      const double *w, const double *d, const double *p,
+                      const double *gradp, int32_t intvel, int32_t matriz, int32_t unsym,
+                      const int32_t *ia, const int32_t *ja, double *ad, double *au, double *b,
+                      double *rescell);
+void oref_simple_update(double *w, double *pre, const double *u1, const double *u2,
+                        const double *prec, const double *gradpc, const double *d,
+                        int32_t numel, double under_pc);
+void oref_divergente(double *div, const double *gu1, const double *gu2, int32_t numel);
+
 #endif

@@ -46,8 +46,9 @@ _lib = None
 def lib():
     global _lib
     if _lib is None:
-        if not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(
-            os.path.join(HERE, "fvc_oracle.c")
+        srcs = ("fvc_oracle.c", "fvc_oracle_simple.c", "fvc_oracle.h")
+        if not os.path.exists(LIB_PATH) or any(
+            os.path.getmtime(LIB_PATH) < os.path.getmtime(os.path.join(HERE, f)) for f in srcs
         ):
             build()
         L = C.CDLL(LIB_PATH)
@@ -75,9 +76,17 @@ def lib():
             "oref_pcg_omp_sample": [vp] * 7 + [I, I, D, I, I, I, I, C.POINTER(Stats)],
             "oref_smachn": [],
             "oref_getres": [vp, vp, vp, I, I, I],
+            "oref_gform": [vp, vp, I, I, I, vp, vp, vp, I, I, vp, vp],
+            "oref_pform_momentum": [vp, vp, I, I, I, vp, vp, vp, vp, vp, I, I, vp, vp, vp, vp,
+                                    vp, vp, D, I, D, I, I, I, vp, vp, vp, vp, vp, vp, vp, vp],
+            "oref_pform_pc": [vp, vp, I, I, I, vp, vp, vp, vp, vp, vp, vp, vp, vp, I, I, I, vp,
+                              vp, vp, vp, vp, vp],
+            "oref_simple_update": [vp, vp, vp, vp, vp, vp, vp, I, D],
+            "oref_divergente": [vp, vp, vp, I],
         }
         res = {"oref_dot": D, "oref_smachn": D, "oref_banda_csr": I, "oref_datastruc": I,
-               "oref_solver": I, "oref_pcg_omp_sample": I}
+               "oref_solver": I, "oref_pcg_omp_sample": I, "oref_gform": I,
+               "oref_pform_momentum": I, "oref_pform_pc": I}
         for name, argt in sig.items():
             f = getattr(L, name)
             f.argtypes = argt
@@ -225,3 +234,80 @@ def pcg_omp_sample(ad, au, x, b, iax, ja, neq, nad, tol, maxit, matriz, nthreads
                                        _p(ja), neq, nad, tol, maxit, matriz, nthreads,
                                        int(init), C.byref(st))
     return status, st
+
+
+# ----------------------------------------------------------------------
+# SIMPLE outer-loop cells (fvc_oracle_simple.c).  A "cavity" bundle is a
+# dict with coor (nnode,2), ix (numel,ld), nelcon (numel,nshared),
+# pedge (numel,nshared+1), sedge (numel,nshared+1,3), e (nmat,10), num,
+# and nshared; cell fields are cell-ordered numpy arrays, 2-vectors
+# shaped (numel, 2), iM (numel, 4).
+
+def _c(a, t):
+    return np.ascontiguousarray(a, t)
+
+
+def gform(m, kind, comp, u, grad):
+    """Green-Gauss gradient of u (Pform.f gform): kind 1 = momentum ghost
+    rules for component comp, kind 2 = pressure ghost rules.  grad (numel,2)
+    is read (the pressure rules extrapolate with it) and overwritten."""
+    u = _c(u, np.float64)
+    assert grad.flags.c_contiguous and grad.dtype == np.float64
+    rc = lib().oref_gform(_p(_c(m["coor"], np.float64)), _p(_c(m["ix"], np.int32)),
+                          m["ix"].shape[1], m["ix"].shape[0], m["nshared"],
+                          _p(_c(m["nelcon"], np.int32)), _p(_c(m["pedge"], np.int32)),
+                          _p(_c(m["sedge"], np.float64)), kind, comp, _p(u), _p(grad))
+    if rc != 0:
+        raise ValueError("boundary code without a defined ghost value")
+    return grad
+
+
+def pform_momentum(m, comp, iws, u, u0, w, g_own, g_oth, gradp, dt, ia, ja, matriz,
+                   b, im, d, rescell, ad=None, au=None, bs=False, under_u=0.7,
+                   simple_c=False, unsym=True):
+    """Momentum system of component comp (cell_si_eb_i_ggl): iws 1 assembles
+    (ad, au), adds to b and writes iM, d, the cell residual; iws 3 adds the
+    time term rho cc A/dt u to b only."""
+    numel = m["ix"].shape[0]
+    ad = np.zeros(1) if ad is None else ad
+    au = np.zeros(1) if au is None else au
+    rc = lib().oref_pform_momentum(
+        _p(_c(m["coor"], np.float64)), _p(_c(m["ix"], np.int32)), m["ix"].shape[1], numel,
+        m["nshared"], _p(_c(m["nelcon"], np.int32)), _p(_c(m["num"], np.int32)),
+        _p(_c(m["pedge"], np.int32)), _p(_c(m["sedge"], np.float64)), _p(_c(m["e"], np.float64)),
+        comp, iws, _p(_c(u, np.float64)), _p(_c(u0, np.float64)), _p(_c(w, np.float64)),
+        _p(_c(g_own, np.float64)), _p(_c(g_oth, np.float64)), _p(_c(gradp, np.float64)),
+        dt, int(bs), under_u, int(simple_c), matriz, int(unsym), _p(_c(ia, np.int32)),
+        _p(_c(ja, np.int32)), _p(ad), _p(au), _p(b), _p(im), _p(d), _p(rescell))
+    if rc != 0:
+        raise ValueError("oref_pform_momentum failed")
+    return ad, au
+
+
+def pform_pc(m, w, d, p, gradp, ia, ja, matriz, ad, au, b, rescell, int_vel=5, unsym=True):
+    """Pressure-correction system with its right-hand side (cell_si_p_i_ggl
+    iws 1 with cellVel)."""
+    numel = m["ix"].shape[0]
+    rc = lib().oref_pform_pc(
+        _p(_c(m["coor"], np.float64)), _p(_c(m["ix"], np.int32)), m["ix"].shape[1], numel,
+        m["nshared"], _p(_c(m["nelcon"], np.int32)), _p(_c(m["num"], np.int32)),
+        _p(_c(m["pedge"], np.int32)), _p(_c(m["sedge"], np.float64)), _p(_c(m["e"], np.float64)),
+        _p(_c(w, np.float64)), _p(_c(d, np.float64)), _p(_c(p, np.float64)),
+        _p(_c(gradp, np.float64)), int_vel, matriz, int(unsym), _p(_c(ia, np.int32)),
+        _p(_c(ja, np.int32)), _p(ad), _p(au), _p(b), _p(rescell))
+    if rc != 0:
+        raise ValueError("oref_pform_pc: unsupported intVel")
+    return ad, au
+
+
+def simple_update(w, p, u1, u2, pc, gradpc, d, under_pc):
+    lib().oref_simple_update(_p(w), _p(p), _p(_c(u1, np.float64)), _p(_c(u2, np.float64)),
+                             _p(_c(pc, np.float64)), _p(_c(gradpc, np.float64)),
+                             _p(_c(d, np.float64)), w.shape[0], under_pc)
+
+
+def divergente(gu1, gu2):
+    div = np.zeros(gu1.shape[0])
+    lib().oref_divergente(_p(div), _p(_c(gu1, np.float64)), _p(_c(gu2, np.float64)),
+                          gu1.shape[0])
+    return div
