@@ -65,6 +65,23 @@ class FvcStats(C.Structure):
         return {f: getattr(self, f) for f, _ in self._fields_}
 
 
+class FvcCellMesh(C.Structure):
+    """fvc_cell_mesh: device pointers to a mesh in the reference's layouts."""
+    _fields_ = [
+        ("numel", I32),
+        ("nshared", I32),
+        ("nnode", I32),
+        ("nmat", I32),
+        ("coor", C.c_void_p),
+        ("ix", C.c_void_p),
+        ("nelcon", C.c_void_p),
+        ("num", C.c_void_p),
+        ("pedge", C.c_void_p),
+        ("sedge", C.c_void_p),
+        ("e", C.c_void_p),
+    ]
+
+
 # name -> (argtypes, restype); mirrors include/fvcgpu.h
 SIGNATURES = {
     "fvc_solver": ([P] * 5 + [PI32, PI32, PI32, PI32, PI32, PF64, PI32, PI32, PI32, PI32], None),
@@ -93,6 +110,14 @@ SIGNATURES = {
     "fvc_mesh_datastruc": ([P, I32, I32, I32, I32, P, P, PI32, C.POINTER(I64)], I32),
     "fvc_assemble_pressure": ([P, I32, P, I32, I32, I32, P, P, P, P, I32, I32, I32, I32, P, P,
                                P, P], I32),
+    "fvc_cells_gradient": ([C.POINTER(FvcCellMesh), I32, I32, P, P, P], I32),
+    "fvc_cells_momentum": ([C.POINTER(FvcCellMesh), I32, I32, P, P, P, P, P, P, F64, I32, F64,
+                            I32, I32, P, P, P, P, P, P, P, P, P], I32),
+    "fvc_cells_pressure_correction": ([C.POINTER(FvcCellMesh), P, P, P, P, I32, I32, P, P, P, P,
+                                       P, P, P], I32),
+    "fvc_cells_simple_update": ([I32, P, P, P, P, P, P, P, F64, P], I32),
+    "fvc_cells_divergence": ([I32, P, P, P, P], I32),
+    "fvc_getres": ([I32, P, P, P, I32, P], I32),
 }
 
 _lib = None

@@ -20,7 +20,9 @@ LIBDIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIBDIR, "libfvcgpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["fvc_krylov.cu", "fvc_mixed.cu", "fvc_gather.cu", "fvc_assembly.cu",
-           "fvc_noalloc.cu", "fvc_api.cpp", "fvc_mesh.cpp"]
+           "fvc_noalloc.cu", "fvc_simple.cu", "fvc_api.cpp", "fvc_mesh.cpp"]
+# files whose kernels reproduce the reference's rounding: no FMA contraction
+NO_FMAD = {"fvc_simple.cu"}
 
 
 def nvcc() -> str:
@@ -37,6 +39,8 @@ def _compile(src: str, verbose_ptxas: bool) -> str:
            "-Xcompiler", "-fPIC,-O3,-Wall", *ARCH]
     if src.endswith(".cu"):
         cmd += ["--expt-relaxed-constexpr"]
+        if src in NO_FMAD:
+            cmd += ["--fmad=false"]
         if verbose_ptxas:
             cmd += ["-Xptxas", "-v"]
     else:

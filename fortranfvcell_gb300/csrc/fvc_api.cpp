@@ -193,11 +193,12 @@ int32_t upload_raw(fvc_context *c, const double *ad, const double *au, const dou
   const double *h2 = pick(c->raw2_which, ad, au, al);
   if (!h1 || (c->raw2_which && !h2) || !ad) return FVC_ERR_ARG;
   cudaStream_t s = c->stream;
-  if (cudaMemcpyAsync(c->d_raw1, h1, sizeof(double) * c->raw1_n, cudaMemcpyHostToDevice, s) !=
+  // host or device arrays (unified addressing)
+  if (cudaMemcpyAsync(c->d_raw1, h1, sizeof(double) * c->raw1_n, cudaMemcpyDefault, s) !=
       cudaSuccess)
     return FVC_ERR_CUDA;
   if (c->raw2_which &&
-      cudaMemcpyAsync(c->d_raw2, h2, sizeof(double) * c->raw2_n, cudaMemcpyHostToDevice, s) !=
+      cudaMemcpyAsync(c->d_raw2, h2, sizeof(double) * c->raw2_n, cudaMemcpyDefault, s) !=
           cudaSuccess)
     return FVC_ERR_CUDA;
   int32_t rc = fvc::launch_gather_values(c->A.slots, c->d_src, c->d_raw1, c->d_raw2, c->A.val, s);

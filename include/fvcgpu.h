@@ -253,6 +253,83 @@ int32_t fvc_assemble_pressure(const double *coor, int32_t nnode,
                               const int32_t *ia, const int32_t *ja, double *ad,
                               double *au);
 
+/* ---- SIMPLE outer-iteration cells (GPU, one thread per cell) ------------
+ * The isothermal incompressible cell routines of the SIMPLE loop
+ * (src/Simple.f:299-660), each reproducing the reference's arithmetic bit
+ * for bit.  All pointers are DEVICE pointers; arrays keep the reference's
+ * Fortran layouts; `stream` is a cudaStream_t (NULL: the default stream).
+ * Cell fields are cell-ordered (1..numel), systems equation-ordered (num).
+ * Boundary codes per face (pedge): 0 wall, 1 moving wall, 2 prescribed
+ * velocity, 3 prescribed pressure, 4 locally parabolic; pedge(nshared+1,c)
+ * = -1 pins the cell's p', -2 fixes its velocity (1e60 diagonals). */
+typedef struct {
+  int32_t numel, nshared, nnode, nmat;
+  const double *coor;     /* (2, nnode)                                      */
+  const int32_t *ix;      /* (nshared+1, numel): 1-based nodes, 0 unused;
+                             row nshared+1 the material                      */
+  const int32_t *nelcon;  /* (nshared, numel): face neighbours, -1 boundary  */
+  const int32_t *num;     /* (numel): equation of each cell                  */
+  const int32_t *pedge;   /* (nshared+1, numel): boundary codes              */
+  const double *sedge;    /* (3, nshared+1, numel): boundary values u, v, p  */
+  const double *e;        /* (10, nmat): e(1) viscosity, e(2) density,
+                             e(6) time coefficient, e(7) TVD limiter 1..7    */
+} fvc_cell_mesh;
+
+/* Green-Gauss cell gradient over the polygon of neighbour / ghost-cell
+ * centroids (gform, src/Pform.f:466-646).  kind 1: velocity component comp
+ * (1 or 2) with the ghost rules of src/CellibSimple.f:655-669; kind 2:
+ * pressure-like field with those of src/CellibPressure.f:449-462, which
+ * extrapolate with the cell's previous gradient: grad(2,numel) is read and
+ * overwritten.  FVC_ERR_UNSUPPORTED for a velocity boundary code outside
+ * 0..4 (the reference leaves that ghost value undefined). */
+int32_t fvc_cells_gradient(const fvc_cell_mesh *m, int32_t kind, int32_t comp,
+                           const double *u, double *grad, void *stream);
+
+/* Momentum equation of velocity component comp (cell_si_eb_i_ggl,
+ * src/CellibSimple.f:591-940), one call of the reference's pform.
+ * iws 1: assembles row num(c) of (ad, au) for matriz 1 (CSRD) or 4
+ * (ELLPACK), b(num(c)) = the cell's right-hand side, iM(comp|comp+2,c),
+ * d(comp,c) and rescell(c).  u: this component, u0: the pressure, w(2,*):
+ * velocity, g_own / g_oth: the gradients of this / the other component,
+ * gradp: the pressure gradient.  iws 3: only b(num(c)) = rho cc A/dt u
+ * (second order in time with bs: 2 rho cc A/dt u - rho cc A/(2dt) u0). */
+int32_t fvc_cells_momentum(const fvc_cell_mesh *m, int32_t comp, int32_t iws,
+                           const double *u, const double *u0, const double *w,
+                           const double *g_own, const double *g_oth,
+                           const double *gradp, double dt, int32_t bs,
+                           double under_u, int32_t simple_c, int32_t matriz,
+                           const int32_t *ia, const int32_t *ja, double *ad,
+                           double *au, double *b, double *im, double *d,
+                           double *rescell, void *stream);
+
+/* Pressure-correction equation with its right-hand side (cell_si_p_i_ggl
+ * iws = 1, src/CellibPressure.f:477-572): coefficients, minus the face mass
+ * fluxes of cellVel (src/CellibSimple.f:1947-2073; int_vel 1 linear, 2
+ * Rhie-Chow, 5 Ferziger-Peric) into b(num(c)), the mass residual into
+ * rescell(c).  w: the predicted velocity, d(2,*): momentum D, p: pressure,
+ * gradp: its gradient. */
+int32_t fvc_cells_pressure_correction(const fvc_cell_mesh *m, const double *w,
+                                      const double *d, const double *p,
+                                      const double *gradp, int32_t int_vel,
+                                      int32_t matriz, const int32_t *ia,
+                                      const int32_t *ja, double *ad, double *au,
+                                      double *b, double *rescell, void *stream);
+
+/* simpleUpdate (src/Simple.f:871-910): w = u - d grad p', p += under_pc p'. */
+int32_t fvc_cells_simple_update(int32_t numel, double *w, double *p,
+                                const double *u1, const double *u2,
+                                const double *pc, const double *gradpc,
+                                const double *d, double under_pc, void *stream);
+
+/* divergente (src/Simple.f:1070-1078): div = du1/dx + du2/dy. */
+int32_t fvc_cells_divergence(int32_t numel, double *div, const double *gu1,
+                             const double *gu2, void *stream);
+
+/* getRes (src/Solver.f:368-391): to_equations != 0: x(num(c)) = u(c);
+ * else u(c) = x(num(c)). */
+int32_t fvc_getres(int32_t numel, const int32_t *num, double *u, double *x,
+                   int32_t to_equations, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
