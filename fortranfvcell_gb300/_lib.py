@@ -82,6 +82,25 @@ class FvcCellMesh(C.Structure):
     ]
 
 
+class FvcSimpleOpts(C.Structure):
+    _fields_ = [
+        ("dt", F64),
+        ("under_u", F64),
+        ("under_pc", F64),
+        ("simple_c", I32),
+        ("bs", I32),
+        ("int_vel", I32),
+        ("matriz_u", I32),
+        ("code_u", I32),
+        ("tol_u", F64),
+        ("matriz_pc", I32),
+        ("code_pc", I32),
+        ("tol_pc", F64),
+        ("maxit", I32),
+        ("precision", I32),
+    ]
+
+
 # name -> (argtypes, restype); mirrors include/fvcgpu.h
 SIGNATURES = {
     "fvc_solver": ([P] * 5 + [PI32, PI32, PI32, PI32, PI32, PF64, PI32, PI32, PI32, PI32], None),
@@ -118,6 +137,14 @@ SIGNATURES = {
     "fvc_cells_simple_update": ([I32, P, P, P, P, P, P, P, F64, P], I32),
     "fvc_cells_divergence": ([I32, P, P, P, P], I32),
     "fvc_getres": ([I32, P, P, P, I32, P], I32),
+    "fvc_simple_opts_default": ([C.POINTER(FvcSimpleOpts)], None),
+    "fvc_simple_create": ([C.POINTER(P), I32, I32, I32, I32, I32, P, P, P, P, P, P, P,
+                           C.POINTER(FvcSimpleOpts)], I32),
+    "fvc_simple_iterate": ([P, I32, P, P], I32),
+    "fvc_simple_time_step": ([P], I32),
+    "fvc_simple_fields": ([P, P, P], I32),
+    "fvc_simple_set_fields": ([P, P, P], I32),
+    "fvc_simple_destroy": ([P], I32),
 }
 
 _lib = None

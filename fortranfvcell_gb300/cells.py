@@ -87,3 +87,74 @@ def divergence(div, gu1, gu2) -> None:
 def getres(num, u, x, to_equations: bool) -> None:
     _lib.check(_lib.load().fvc_getres(u.shape[0], _addr(num), _addr(u), _addr(x),
                                       int(to_equations), _stream()), "fvc_getres")
+
+
+def simple_opts(**kw):
+    """fvc_simple_opts with the library defaults, overridden by keyword."""
+    o = _lib.FvcSimpleOpts()
+    _lib.load().fvc_simple_opts_default(C.byref(o))
+    for k, v in kw.items():
+        if k == "precision":
+            v = {"fp64": _lib.FVC_PREC_FP64, "mixed": _lib.FVC_PREC_MIXED}.get(v, v)
+        setattr(o, k, v)
+    return o
+
+
+class SimpleLoop:
+    """The isothermal SIMPLE outer iteration resident on the GPU
+    (fvc_simple_* of include/fvcgpu.h).  Mesh arrays are host numpy arrays
+    in the reference layouts (see CellMesh); ``opts`` from simple_opts()."""
+
+    def __init__(self, coor, ix, nelcon, num, pedge, sedge, e, opts=None, device: int = 0):
+        self._L = _lib.load()
+        ix = np.ascontiguousarray(ix, np.int32)
+        self.numel, ld = ix.shape
+        self._keep = [np.ascontiguousarray(coor, np.float64), ix,
+                      np.ascontiguousarray(nelcon, np.int32), np.ascontiguousarray(num, np.int32),
+                      np.ascontiguousarray(pedge, np.int32), np.ascontiguousarray(sedge, np.float64),
+                      np.ascontiguousarray(e, np.float64)]
+        coor_, ix_, nel_, num_, pe_, se_, e_ = self._keep
+        h = C.c_void_p()
+        o = simple_opts() if opts is None else opts
+        _lib.check(self._L.fvc_simple_create(
+            C.byref(h), device, self.numel, coor_.shape[0], ld - 1, e_.reshape(-1, 10).shape[0],
+            *[a.ctypes.data_as(C.c_void_p) for a in self._keep], C.byref(o)), "fvc_simple_create")
+        self._h = h
+
+    def iterate(self, nit: int):
+        """Runs nit outer iterations; returns (residuals (nit,3), solver
+        iterations (nit,3)) -- the cell-residual norms of u1, u2 and p'."""
+        res = np.zeros((nit, 3))
+        its = np.zeros((nit, 3), np.int32)
+        _lib.check(self._L.fvc_simple_iterate(self._h, nit, res.ctypes.data_as(C.c_void_p),
+                                              its.ctypes.data_as(C.c_void_p)),
+                   "fvc_simple_iterate")
+        return res, its
+
+    def time_step(self) -> None:
+        _lib.check(self._L.fvc_simple_time_step(self._h), "fvc_simple_time_step")
+
+    def fields(self):
+        w = np.zeros((self.numel, 2))
+        p = np.zeros(self.numel)
+        _lib.check(self._L.fvc_simple_fields(self._h, w.ctypes.data_as(C.c_void_p),
+                                             p.ctypes.data_as(C.c_void_p)), "fvc_simple_fields")
+        return w, p
+
+    def set_fields(self, w=None, p=None) -> None:
+        w = None if w is None else np.ascontiguousarray(w, np.float64)
+        p = None if p is None else np.ascontiguousarray(p, np.float64)
+        _lib.check(self._L.fvc_simple_set_fields(
+            self._h, None if w is None else w.ctypes.data_as(C.c_void_p),
+            None if p is None else p.ctypes.data_as(C.c_void_p)), "fvc_simple_set_fields")
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._L.fvc_simple_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -330,6 +330,67 @@ int32_t fvc_cells_divergence(int32_t numel, double *div, const double *gu1,
 int32_t fvc_getres(int32_t numel, const int32_t *num, double *u, double *x,
                    int32_t to_equations, void *stream);
 
+/* ---- SIMPLE outer iteration on the GPU ------------------------------------
+ * The isothermal incompressible SIMPLE/SIMPLEC iteration of src/Simple.f:
+ * 299-660 with every field, matrix and right-hand side resident on the
+ * device: per outer iteration the velocity and pressure gradients, both
+ * momentum systems, their solves, the p' system, its solve, the p' gradient
+ * and the update, in the reference's order and with its control flow (a
+ * momentum equation whose b.b < 1e-32 is not solved; no p' solve and no
+ * update when the mass residual is below 1e-32).  The linear systems go
+ * through the solver of this library (fvc_solve) with the reference's
+ * warm-start rules.  Only the residual norms come back to the host. */
+typedef struct fvc_simple fvc_simple;
+
+typedef struct {
+  double dt;          /* time step of the time term rho cc A/dt            */
+  double under_u;     /* momentum under-relaxation (underU)                 */
+  double under_pc;    /* pressure under-relaxation (underPc)                */
+  int32_t simple_c;   /* 1: SIMPLEC's d = A/(aP - sum aNb)                  */
+  int32_t bs;         /* 1: second-order backward time term                 */
+  int32_t int_vel;    /* face velocity interpolation (1, 2, 5)             */
+  int32_t matriz_u;   /* momentum storage: 4 ELLPACK (reference) or 1 CSRD  */
+  int32_t code_u;     /* momentum solver: 2 BiCGSTAB (reference), 3 GMRES   */
+  double tol_u;
+  int32_t matriz_pc;  /* p' storage: 1 CSRD (reference) or 4 ELLPACK        */
+  int32_t code_pc;    /* p' solver: 1 PCG (reference), 2, 3                 */
+  double tol_pc;
+  int32_t maxit;      /* per linear solve                                   */
+  int32_t precision;  /* FVC_PREC_FP64 or FVC_PREC_MIXED for the solves     */
+} fvc_simple_opts;
+
+/* Defaults: dt 1e10 (steady), underU 0.7, underPc 0.3, SIMPLE, intVel 5,
+ * momentum ELLPACK + BiCGSTAB, p' CSRD + PCG, tolerances 1e-8, maxit 50000,
+ * FP64 solves. */
+void fvc_simple_opts_default(fvc_simple_opts *o);
+
+/* Uploads a mesh (HOST arrays in the layouts of fvc_cell_mesh; num is the
+ * equation numbering, e.g. fvc_mesh_rcm) and builds the momentum and p'
+ * structures.  Fields start at rest (w = 0, p = 0) and the time term is
+ * formed from them (call fvc_simple_time_step to start a new time step). */
+int32_t fvc_simple_create(fvc_simple **s, int32_t device, int32_t numel,
+                          int32_t nnode, int32_t nshared, int32_t nmat,
+                          const double *coor, const int32_t *ix,
+                          const int32_t *nelcon, const int32_t *num,
+                          const int32_t *pedge, const double *sedge,
+                          const double *e, const fvc_simple_opts *opts);
+
+/* Runs nit outer iterations.  res (host, 3*nit, may be NULL) receives the
+ * reference's cell-residual norms (u1, u2, p') of each iteration; its
+ * (host, 3*nit, may be NULL) the linear-solver iterations (0: not solved). */
+int32_t fvc_simple_iterate(fvc_simple *s, int32_t nit, double *res, int32_t *its);
+
+/* Starts a new time step: w0 = w and the time term from the current fields
+ * (src/Simple.f:229-266). */
+int32_t fvc_simple_time_step(fvc_simple *s);
+
+/* Host copies of the velocity w(2,numel) and pressure p(numel); either may
+ * be NULL.  fvc_simple_set_fields uploads them (e.g. to restart). */
+int32_t fvc_simple_fields(const fvc_simple *s, double *w, double *p);
+int32_t fvc_simple_set_fields(fvc_simple *s, const double *w, const double *p);
+
+int32_t fvc_simple_destroy(fvc_simple *s);
+
 #ifdef __cplusplus
 }
 #endif

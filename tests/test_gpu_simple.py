@@ -1,0 +1,85 @@
+"""The GPU-resident SIMPLE outer iteration (fvc_simple_*) against the
+reference's iteration restated on the CPU (tests/_simple_ref.py): the
+same residual history and fields, to the accuracy of the linear solves
+(which differ between the two only in rounding)."""
+import numpy as np
+import pytest
+
+from _simple_ref import SimpleRef, cavity
+
+pytestmark = pytest.mark.gpu
+
+
+def gpu_loop(case, **kw):
+    from fortranfvcell_gb300.cells import SimpleLoop, simple_opts
+    return SimpleLoop(case["coor"], case["ix"], case["nelcon"], case["num"], case["pedge"],
+                      case["sedge"], case["e"], opts=simple_opts(**kw))
+
+
+@pytest.mark.parametrize("kind,nx,matriz_u", [("quad", 20, 4), ("tri", 12, 1),
+                                              ("mixed", 14, 1)])
+def test_simple_loop_matches_reference(orc, kind, nx, matriz_u):
+    case = cavity(orc, nx, kind=kind, jitter=0.15 if kind != "quad" else 0.0)
+    ref = SimpleRef(orc, case, tol_pcg=1e-13, tol_bcg=1e-13, matriz_u=matriz_u)
+    loop = gpu_loop(case, tol_u=1e-13, tol_pc=1e-13, matriz_u=matriz_u)
+    nit = 25
+    hist = np.array([ref.step() for _ in range(nit)])
+    res, its = loop.iterate(nit)
+    w, p = loop.fields()
+    loop.close()
+    np.testing.assert_allclose(res, hist, rtol=1e-7, atol=1e-15)
+    np.testing.assert_allclose(w, ref.w, rtol=0, atol=1e-9 * np.abs(ref.w).max())
+    np.testing.assert_allclose(p, ref.p, rtol=0, atol=1e-9 * np.abs(ref.p).max())
+    if kind == "quad":  # iteration 1 on the uniform mesh: v's right-hand side is zero
+        assert its[0, 1] == 0 and its[0, 0] > 0
+
+
+def test_simple_loop_reaches_steady_cavity(orc):
+    # Re = 100 cavity, 200 outer iterations at the reference's default
+    # solver tolerances; the GPU and CPU states agree to 1e-6
+    case = cavity(orc, 32)
+    ref = SimpleRef(orc, case)
+    loop = gpu_loop(case)
+    hist = np.array([ref.step() for _ in range(200)])
+    res, _ = loop.iterate(200)
+    w, p = loop.fields()
+    assert res[-1].max() < 1e-3 * res[1].max()
+    np.testing.assert_allclose(w, ref.w, rtol=0, atol=1e-6)
+    np.testing.assert_allclose(res[-1], hist[-1], rtol=1e-3)
+
+
+def test_simple_loop_mixed_precision_solves(orc):
+    case = cavity(orc, 24)
+    fp64 = gpu_loop(case)
+    mixed = gpu_loop(case, precision="mixed")
+    r64, _ = fp64.iterate(60)
+    rmx, _ = mixed.iterate(60)
+    w64, _ = fp64.fields()
+    wmx, _ = mixed.fields()
+    np.testing.assert_allclose(rmx[-1], r64[-1], rtol=1e-3)
+    np.testing.assert_allclose(wmx, w64, rtol=0, atol=1e-6)
+
+
+def test_time_steps_and_restart(orc):
+    # transient run: two time steps of 10 outer iterations (second-order
+    # backward time term), then a restart from downloaded fields
+    case = cavity(orc, 12)
+    a = gpu_loop(case, dt=0.05, bs=1)
+    a.iterate(10)
+    a.time_step()
+    ra, _ = a.iterate(10)
+    w, p = a.fields()
+    b = gpu_loop(case, dt=0.05, bs=1)
+    b.set_fields(w, p)
+    wb, pb = b.fields()
+    assert np.array_equal(wb, w) and np.array_equal(pb, p)
+    assert np.isfinite(ra).all()
+
+
+def test_bad_inputs_rejected(orc):
+    from fortranfvcell_gb300 import FvcError
+    case = cavity(orc, 6)
+    with pytest.raises(FvcError):
+        gpu_loop(case, int_vel=3)
+    with pytest.raises(FvcError):
+        gpu_loop(case, matriz_u=2)
