@@ -359,7 +359,53 @@ def run_ours(args):
         "clocks": clocks,
         "cpu_baseline": cpu,
     }
+    if rank == 0 and not args.no_simple:
+        line["simple_c1"] = run_simple_c1(args)
     return line
+
+
+def run_simple_c1(args):
+    """The C1 configuration: the Re = 100 lid-driven cavity on 64 x 64 quads,
+    200 SIMPLE outer iterations (u, v BiCGSTAB on ELLPACK, p' PCG on CSRD,
+    tolerances 1e-8, underU 0.7, underPc 0.3, steady).  GPU: the
+    device-resident loop (cells.SimpleLoop), wall time.  CPU: the same
+    iteration restated over the oracle (sequential solvers, one core)."""
+    from fortranfvcell_gb300.cases import lid_driven_cavity
+    from fortranfvcell_gb300.cells import SimpleLoop
+    case = lid_driven_cavity(args.simple_nx)
+    nit = args.simple_its
+    loop = SimpleLoop(case["coor"], case["ix"], case["nelcon"], case["num"], case["pedge"],
+                      case["sedge"], case["e"])
+    loop.iterate(2)                       # warm-up: kernels and solver scratch
+    loop.set_fields(np.zeros((case["numel"], 2)), np.zeros(case["numel"]))
+    loop.close()
+    loop = SimpleLoop(case["coor"], case["ix"], case["nelcon"], case["num"], case["pedge"],
+                      case["sedge"], case["e"])
+    t0 = time.perf_counter()
+    res, its = loop.iterate(nit)
+    gpu_s = time.perf_counter() - t0
+    w, _ = loop.fields()
+    loop.close()
+    out = {"workload": f"lid-driven cavity Re={1.0 / case['e'][0, 0]:g}, {args.simple_nx}x"
+                       f"{args.simple_nx} quads, {nit} SIMPLE outer iterations",
+           "gpu_s": round(gpu_s, 4), "outer_its_per_s": round(nit / gpu_s, 2),
+           "solver_iterations": [int(v) for v in its.sum(axis=0)],
+           "final_residuals": [float(f"{v:.3e}") for v in res[-1]],
+           "u_min_centreline": float(np.round(np.min(0.5 * (
+               w[:, 0].reshape(args.simple_nx, -1)[:, args.simple_nx // 2 - 1]
+               + w[:, 0].reshape(args.simple_nx, -1)[:, args.simple_nx // 2])), 4))}
+    if not args.no_cpu:
+        from oracle import oracle
+        from oracle.simple_ref import SimpleRef
+        ref = SimpleRef(oracle, case)
+        t0 = time.perf_counter()
+        for _ in range(nit):
+            ref.step()
+        cpu_s = time.perf_counter() - t0
+        out["cpu_port_s"] = round(cpu_s, 4)
+        out["cpu_kind"] = "port (restated reference, sequential solvers, 1 core)"
+        out["max_abs_w_difference"] = float(f"{np.abs(w - ref.w).max():.2e}")
+    return out
 
 
 def run_profile_case(args):
@@ -473,6 +519,9 @@ def main():
     ap.add_argument("--nx", type=int, default=NX_DEFAULT)
     ap.add_argument("--inner-tol", type=float, default=0.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-simple", action="store_true", help="skip the C1 SIMPLE leg")
+    ap.add_argument("--simple-nx", type=int, default=64)
+    ap.add_argument("--simple-its", type=int, default=200)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--ref-sample-its", type=int, default=300)
     ap.add_argument("--profile-its", type=int, default=0,

@@ -1,10 +1,9 @@
-"""Lid-driven cavity set-up and the SIMPLE outer iteration of the reference
-(src/Simple.f:299-660, isothermal branch) driven through the oracle's
-restated cell routines and solvers.  Test infrastructure: the GPU SIMPLE
-driver is checked against this."""
+"""Lid-driven cavity set-up on the oracle's graph chain, and the reference's
+SIMPLE iteration (oracle/simple_ref.py) the GPU loop is checked against."""
 import numpy as np
 
 from _systems import graph
+from oracle.simple_ref import SimpleRef  # noqa: F401
 
 
 def cavity(orc, nx, kind="quad", nu=0.01, rho=1.0, lid=1.0, pin_cell=1, limiter=7, cc=1.0,
@@ -33,107 +32,3 @@ def cavity(orc, nx, kind="quad", nu=0.01, rho=1.0, lid=1.0, pin_cell=1, limiter=
     e[0, 0], e[0, 1], e[0, 5], e[0, 6] = nu, rho, cc, limiter
     return dict(coor=m.coor, ix=ix, nelcon=nelcon, num=num, ident=ident, pedge=pedge,
                 sedge=sedge, e=e, nshared=nsh, numel=numel, mesh=m)
-
-
-class SimpleRef:
-    """One reference SIMPLE state advanced by the oracle.  Defaults follow
-    the C1 configuration: u, v BiCGSTAB on ELLPACK, p' PCG on CSRD, steady
-    (large dt), no second-order time term, SIMPLE (not SIMPLEC)."""
-
-    def __init__(self, orc, case, dt=1.0e10, under_u=0.7, under_pc=0.3, simple_c=False,
-                 tol_pcg=1e-8, tol_bcg=1e-8, maxit=50000, matriz_u=4, matriz_pc=1,
-                 int_vel=5):
-        self.orc, self.m = orc, case
-        self.dt, self.under_u, self.under_pc, self.simple_c = dt, under_u, under_pc, simple_c
-        self.tol_pcg, self.tol_bcg, self.maxit = tol_pcg, tol_bcg, maxit
-        self.mu, self.mpc, self.int_vel = matriz_u, matriz_pc, int_vel
-        n = case["numel"]
-        self.n = n
-        self.iau, self.jau, self.nadu = orc.datastruc(case["ident"], matriz_u, True)
-        self.iapc, self.japc, self.nadpc = orc.datastruc(case["ident"], matriz_pc, True)
-        z2 = lambda: np.zeros((n, 2))
-        self.w, self.gu1, self.gu2, self.gp, self.gpc, self.d = z2(), z2(), z2(), z2(), z2(), z2()
-        self.im = np.zeros((n, 4))
-        self.p, self.pc = np.zeros(n), np.zeros(n)
-        self.u1, self.u2 = np.zeros(n), np.zeros(n)
-        self.it = 0
-        self.r0 = {}
-        self.history = []
-        # time term F = rho cc A/dt u (before the loop, Simple.f:247-266)
-        self.b10, self.b20 = np.zeros(n), np.zeros(n)
-        for comp, b0 in ((1, self.b10), (2, self.b20)):
-            u = self.w[:, comp - 1].copy()
-            orc.pform_momentum(case, comp, 3, u, u, self.w, self.gu1, self.gu2, self.gp, dt,
-                               self.iau, self.jau, matriz_u, b0, self.im, self.d,
-                               np.zeros(n), bs=False, under_u=under_u, simple_c=simple_c)
-
-    def _nnz(self, matriz, ja):
-        return ja.size
-
-    def _momentum(self, comp):
-        orc, m, n = self.orc, self.m, self.n
-        u = self.u1 if comp == 1 else self.u2
-        g_own, g_oth = (self.gu1, self.gu2) if comp == 1 else (self.gu2, self.gu1)
-        ad = np.zeros(n)
-        au = np.zeros(self.jau.size)
-        b = np.zeros(n)
-        rc = np.zeros(n)
-        orc.pform_momentum(m, comp, 1, u, self.p, self.w, g_own, g_oth, self.gp, self.dt,
-                           self.iau, self.jau, self.mu, b, self.im, self.d, rc, ad=ad, au=au,
-                           bs=False, under_u=self.under_u, simple_c=self.simple_c)
-        b0 = self.b10 if comp == 1 else self.b20
-        b = b + b0                                      # asumb
-        sx = np.zeros(n)
-        orc.lib().oref_getres(orc._p(sx), orc._p(b0), orc._p(m["num"]), n, n, 0)
-        rc = rc + sx
-        return ad, au, b, rc
-
-    def _solve(self, ad, au, b, x_cells, code, matriz, ia, ja, nad, tol):
-        orc, m, n = self.orc, self.m, self.n
-        sx = np.zeros(n)
-        orc.lib().oref_getres(orc._p(np.ascontiguousarray(x_cells)), orc._p(sx),
-                              orc._p(m["num"]), n, n, 1)
-        st = orc.solver(ad, au, au, sx, b, ia, ja, n, nad, True, tol, self.maxit, code, matriz)
-        out = np.zeros(n)
-        orc.lib().oref_getres(orc._p(out), orc._p(sx), orc._p(m["num"]), n, n, 0)
-        return out, st
-
-    def step(self):
-        """One outer iteration; returns (rU1, rU2, rPc) as Simple.f computes
-        them (cell-residual 2-norms)."""
-        orc, m, n = self.orc, self.m, self.n
-        self.it += 1
-        self.u1, self.u2 = self.w[:, 0].copy(), self.w[:, 1].copy()          # guess
-        orc.gform(m, 1, 1, self.u1, self.gu1)
-        orc.gform(m, 1, 2, self.u2, self.gu2)
-        self.div = orc.divergente(self.gu1, self.gu2)
-        orc.gform(m, 2, 3, self.p, self.gp)
-        ad1, au1, b1, rc1 = self._momentum(1)
-        ad2, au2, b2, rc2 = self._momentum(2)
-        # a momentum equation whose right-hand side vanishes is not solved
-        # (Simple.f:437-441, 462-466: b.b < 1e-32)
-        self.solved = (float(b1 @ b1) >= 1.0e-32, float(b2 @ b2) >= 1.0e-32)
-        if self.solved[0]:
-            self.u1, self.st_u1 = self._solve(ad1, au1, b1, self.u1, 2, self.mu, self.iau,
-                                              self.jau, self.nadu, self.tol_bcg)
-        if self.solved[1]:
-            self.u2, self.st_u2 = self._solve(ad2, au2, b2, self.u2, 2, self.mu, self.iau,
-                                              self.jau, self.nadu, self.tol_bcg)
-        wp = np.stack([self.u1, self.u2], axis=1)                            # updateVel
-        adp, aup, bp, rcp = np.zeros(n), np.zeros(self.japc.size), np.zeros(n), np.zeros(n)
-        orc.pform_pc(m, wp, self.d, self.p, self.gp, self.iapc, self.japc, self.mpc, adp, aup,
-                     bp, rcp, int_vel=self.int_vel)
-        self.systems = dict(u1=(ad1, au1, b1), u2=(ad2, au2, b2), pc=(adp, aup, bp))
-        r_pc = float(np.sqrt(rcp @ rcp))
-        r_u1 = float(np.sqrt(rc1 @ rc1))
-        r_u2 = float(np.sqrt(rc2 @ rc2))
-        if self.it == 1:
-            self.r0 = dict(pc=r_pc, u1=r_u1, u2=r_u2)
-        if r_pc >= 1.0e-32:
-            self.pc, self.st_pc = self._solve(adp, aup, bp, self.pc, 1, self.mpc, self.iapc,
-                                              self.japc, self.nadpc, self.tol_pcg)
-            orc.gform(m, 2, 2, self.pc, self.gpc)
-            orc.simple_update(self.w, self.p, self.u1, self.u2, self.pc, self.gpc, self.d,
-                              self.under_pc)
-        self.history.append((r_u1, r_u2, r_pc))
-        return r_u1, r_u2, r_pc

@@ -49,3 +49,13 @@ def test_pc_coefficients_match_pressure_restatement(orc):
     # the right-hand side is minus the face mass fluxes: it sums to zero
     # over the cells (every interior flux appears twice, walls carry none)
     assert abs(b.sum()) < 1e-12 * np.abs(b).sum()
+
+
+def test_product_cavity_builder_matches_oracle_chain(orc):
+    from _simple_ref import cavity
+    from fortranfvcell_gb300.cases import lid_driven_cavity
+    for kind, nx, jit in (("quad", 16, 0.0), ("tri", 9, 0.1), ("mixed", 10, 0.2)):
+        a = cavity(orc, nx, kind=kind, jitter=jit)
+        b = lid_driven_cavity(nx, kind=kind, jitter=jit)
+        for k in ("coor", "ix", "nelcon", "num", "ident", "pedge", "sedge", "e"):
+            assert np.array_equal(a[k], b[k]), (kind, k)
