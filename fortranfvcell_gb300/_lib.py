@@ -44,7 +44,7 @@ class FvcOpts(C.Structure):
         ("want_residual", I32),
         ("update_beta", I32),
         ("staging", I32),
-        ("reserved", I32),
+        ("max_blocks", I32),
     ]
 
 

@@ -118,6 +118,19 @@ __device__ __forceinline__ bool grid_allreduce(const GridSync &gs, unsigned int 
   } else {
     __syncthreads();
   }
+  if (gs.nblocks == 1) {  // one block: its sum is the total (same value)
+    ++episode;
+    if (NV > 0) {
+      if (threadIdx.x == 0)
+#pragma unroll
+        for (int q = 0; q < NV; ++q) red[q] = v[q];
+      __syncthreads();
+#pragma unroll
+      for (int q = 0; q < NV; ++q) v[q] = red[q];
+      __syncthreads();
+    }
+    return true;
+  }
   const unsigned int ep = ++episode;
   const unsigned int nb = gs.nblocks;
   double *part = gs.partials + (size_t)(ep & 3u) * kMaxNV * nb;
@@ -210,36 +223,41 @@ __device__ __forceinline__ bool grid_allreduce_d(const GridSync &gs, unsigned in
       bsum[q] = warp_sum(u);
     }
     bool ok = true;
-    if (lane == 0) {
-#pragma unroll
-      for (int q = 0; q < NV; ++q) part[(size_t)q * nb + blockIdx.x] = bsum[q];
-      red_add_release(gs.count, 1u);
-      const unsigned int target = ep * nb;
-      const uint64_t t0 = global_ns();
-      unsigned int spins = 0;
-      while (ld_acquire(gs.count) < target) {
-        if (*(volatile int *)gs.err != 0) {
-          ok = false;
-          break;
-        }
-        if ((++spins & 255u) == 0 && global_ns() - t0 > kBarrierTimeoutNs) {
-          atomicExch(gs.err, 7 /* FVC_ERR_TIMEOUT */);
-          ok = false;
-          break;
-        }
-        __nanosleep(20);
-      }
-    }
-    ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
     double t[NV];
+    if (nb == 1) {  // one block: its sum is the total (same value)
 #pragma unroll
-    for (int q = 0; q < NV; ++q) {
-      double u = 0.0;
-      if (ok) {
-        const double *pp = part + (size_t)q * nb;
-        for (unsigned int b = lane; b < nb; b += 32) u = __dadd_rn(u, __ldcg(pp + b));
+      for (int q = 0; q < NV; ++q) t[q] = bsum[q];
+    } else {
+      if (lane == 0) {
+#pragma unroll
+        for (int q = 0; q < NV; ++q) part[(size_t)q * nb + blockIdx.x] = bsum[q];
+        red_add_release(gs.count, 1u);
+        const unsigned int target = ep * nb;
+        const uint64_t t0 = global_ns();
+        unsigned int spins = 0;
+        while (ld_acquire(gs.count) < target) {
+          if (*(volatile int *)gs.err != 0) {
+            ok = false;
+            break;
+          }
+          if ((++spins & 255u) == 0 && global_ns() - t0 > kBarrierTimeoutNs) {
+            atomicExch(gs.err, 7 /* FVC_ERR_TIMEOUT */);
+            ok = false;
+            break;
+          }
+          __nanosleep(20);
+        }
       }
-      t[q] = warp_sum(u);
+      ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+#pragma unroll
+      for (int q = 0; q < NV; ++q) {
+        double u = 0.0;
+        if (ok) {
+          const double *pp = part + (size_t)q * nb;
+          for (unsigned int b = lane; b < nb; b += 32) u = __dadd_rn(u, __ldcg(pp + b));
+        }
+        t[q] = warp_sum(u);
+      }
     }
     if (lane == 0) {
       if (ok)

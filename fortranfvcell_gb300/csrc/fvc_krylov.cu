@@ -552,6 +552,7 @@ Launch persistent_launch(K kernel, const DeviceMatrix &A, const fvc_opts &o) {
   const int warps = L.threads / 32;
   const int need = (A.nslices + warps - 1) / warps;
   L.blocks = std::max(1, std::min(occ * sm_count(), need));
+  if (o.max_blocks > 0) L.blocks = std::min(L.blocks, o.max_blocks);
   return L;
 }
 

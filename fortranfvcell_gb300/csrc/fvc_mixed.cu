@@ -121,40 +121,45 @@ __device__ __forceinline__ bool grid_allreduce_ff(const GridSync &gs, unsigned i
       }
       bsum[q] = (double)s + (double)c;
     }
-    // publish the block's partials, then wait until every block has
     bool ok = true;
-    if (lane == 0) {
-#pragma unroll
-      for (int q = 0; q < NV; ++q) part[(size_t)q * nb + blockIdx.x] = bsum[q];
-      red_add_release(gs.count, 1u);
-      const unsigned int target = ep * nb;
-      const uint64_t t0 = global_ns();
-      unsigned int spins = 0;
-      while (ld_acquire(gs.count) < target) {
-        if (*(volatile int *)gs.err != 0) {
-          ok = false;
-          break;
-        }
-        if ((++spins & 255u) == 0 && global_ns() - t0 > kBarrierTimeoutNs) {
-          atomicExch(gs.err, 7 /* FVC_ERR_TIMEOUT */);
-          ok = false;
-          break;
-        }
-        __nanosleep(20);
-      }
-    }
-    ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
-    // every block sums the partials itself, in block order (identical
-    // totals everywhere; no second round trip through a release flag)
     double t[NV];
+    if (nb == 1) {  // one block: its sum is the total (same value)
 #pragma unroll
-    for (int q = 0; q < NV; ++q) {
-      double u = 0.0;
-      if (ok) {
-        const double *pp = part + (size_t)q * nb;
-        for (unsigned int b = lane; b < nb; b += 32) u = __dadd_rn(u, __ldcg(pp + b));
+      for (int q = 0; q < NV; ++q) t[q] = bsum[q];
+    } else {
+      // publish the block's partials, then wait until every block has
+      if (lane == 0) {
+#pragma unroll
+        for (int q = 0; q < NV; ++q) part[(size_t)q * nb + blockIdx.x] = bsum[q];
+        red_add_release(gs.count, 1u);
+        const unsigned int target = ep * nb;
+        const uint64_t t0 = global_ns();
+        unsigned int spins = 0;
+        while (ld_acquire(gs.count) < target) {
+          if (*(volatile int *)gs.err != 0) {
+            ok = false;
+            break;
+          }
+          if ((++spins & 255u) == 0 && global_ns() - t0 > kBarrierTimeoutNs) {
+            atomicExch(gs.err, 7 /* FVC_ERR_TIMEOUT */);
+            ok = false;
+            break;
+          }
+          __nanosleep(20);
+        }
       }
-      t[q] = warp_sum(u);
+      ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+      // every block sums the partials itself, in block order (identical
+      // totals everywhere; no second round trip through a release flag)
+#pragma unroll
+      for (int q = 0; q < NV; ++q) {
+        double u = 0.0;
+        if (ok) {
+          const double *pp = part + (size_t)q * nb;
+          for (unsigned int b = lane; b < nb; b += 32) u = __dadd_rn(u, __ldcg(pp + b));
+        }
+        t[q] = warp_sum(u);
+      }
     }
     if (lane == 0) {
       if (ok)
@@ -1294,6 +1299,7 @@ int32_t run_mixed(const DeviceMatrix &A0, Scratch &S, int code, const double *b,
   if (o.blocks_per_sm > 0 && o.blocks_per_sm < occ) occ = o.blocks_per_sm;
   const int warps = threads / 32;
   int blocks = std::max(1, std::min(occ * sm_count_m(), (A.nslices + warps - 1) / warps));
+  if (o.max_blocks > 0) blocks = std::min(blocks, o.max_blocks);
   if (ensure_sync(S, (size_t)blocks) != FVC_OK) return FVC_ERR_CUDA;
   reset_sync(S, stream);
   MArgs a{};

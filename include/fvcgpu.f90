@@ -29,7 +29,7 @@ module fvcgpu
      integer(c_int32_t) :: want_residual
      integer(c_int32_t) :: update_beta
      integer(c_int32_t) :: staging
-     integer(c_int32_t) :: reserved
+     integer(c_int32_t) :: max_blocks
   end type fvc_opts
 
   type, bind(C) :: fvc_stats

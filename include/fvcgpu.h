@@ -92,7 +92,7 @@ typedef struct {
                           shared memory with bulk asynchronous copies when
                           the layout allows (1024 threads, 16-bit column
                           offsets); 1: plain loads                        */
-  int32_t reserved;
+  int32_t max_blocks;  /* cap on the persistent grid (0 -> automatic)      */
 } fvc_opts;
 
 typedef struct {
