@@ -1,6 +1,7 @@
 // fvc_internal.h -- host-side declarations shared by the translation units
 // of libfvcgpu (not part of the public C ABI).
 #pragma once
+#include <algorithm>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -85,5 +86,19 @@ int32_t launch_reciprocal(const DeviceMatrix &A, cudaStream_t stream);
 int32_t launch_spmv_f32(const DeviceMatrix &A, const float *x, float *y,
                         cudaStream_t stream);
 int32_t build_f32_copy(DeviceMatrix &A, cudaStream_t stream);
+
+// Threads per block of a persistent solver launch when the caller sets
+// none (or a multiple of 128 it asked for, clamped to 128..1024).  The
+// automatic choice is one block per SM with the fewest warps that still
+// cover every slice: a system too small to fill the GPU with 1024-thread
+// blocks spreads its rows over more SMs, because at a few thousand rows per
+// SM the FP64 pipe (about two lanes per clock per SM on this GPU) and not
+// the memory system sets the iteration time.  Systems of 152 x 1024 rows
+// and more get 1024 threads.
+inline int block_threads_for(int requested, int nslices, int sms) {
+  if (requested > 0) return std::min(1024, std::max(128, requested & ~127));
+  const int warps = (nslices + std::max(sms, 1) - 1) / std::max(sms, 1);
+  return std::min(1024, std::max(128, (warps * 32 + 127) / 128 * 128));
+}
 
 }  // namespace fvc

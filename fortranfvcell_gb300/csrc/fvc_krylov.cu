@@ -37,7 +37,7 @@ struct KArgs {
   const double *minv;
   const double *b;
   double *x;
-  double *v0, *v1, *v2, *v3, *v4, *v5, *v6;
+  double *v0, *v1, *v2, *v3, *v4, *v5, *v6, *v7;
   double *g;  // GMRES basis
   GridSync gs;
   double tol;
@@ -223,20 +223,35 @@ __global__ void __launch_bounds__(1024, 1) pcg_f64(KArgs a) {
 }
 
 // ---------------------------------------------------------------------
-// BiCGSTAB (Iterativos.f:140-234).  v0 = r (shadow r0), v1 = s (the
-// reference's b), v2 = p, v3 = z, v4 = v, v5 = t.
+// BiCGSTAB (Iterativos.f:140-234) in three grid synchronisations per
+// iteration instead of five: the preconditioned vectors the two SpMVs
+// gather (z = p/m and z = s/m) are formed on the fly from vectors the
+// previous all-reduce finalised, as each neighbour is read, so no barrier
+// publishes them.  Forming them needs the previous p, v and s while the
+// new ones are written, so p, v and s are double-buffered.  The per-row
+// arithmetic and its order are those of the reference recurrence:
+//   phase 1  p = s + beta (p - w v) ; v = A (p/m) ; s.r ; v.r   -> alpha
+//   phase 2  s' = s - alpha v ; t = A (s'/m) ; t.s' ; t.t       -> w
+//   phase 3  x += alpha p/m ; x += w s'/m ; s'' = s' - w t ;
+//            s''.(s'/m) ; r.s'' ; s''.s''                       -> beta, stop
+// v0 = r (shadow r0), v1/v2 = s, v3/v4 = p, v5/v6 = v, v7 = t.
 // ---------------------------------------------------------------------
 __global__ void __launch_bounds__(1024, 1) bicgstab_f64(KArgs a) {
   __shared__ double red[kMaxNV * 32];
+  __shared__ double buf[3 * 1024];
+  __shared__ struct {
+    double d, conv, rr0, alpha, w, beta, crit;
+    int stop;  // 0 go on, 1 converged, 2 NaN/Inf
+  } sh;
   const Part P(a.A.nslices, a.A.n);
-  double *r = a.v0, *sv = a.v1, *p = a.v2, *z = a.v3, *v = a.v4, *t = a.v5;
-  double *x = a.x;
+  double *r = a.v0, *t = a.v7, *x = a.x;
+  double *scur = a.v1, *snxt = a.v2, *pold = a.v3, *pnew = a.v4, *vold = a.v5, *vnew = a.v6;
   const double *minv = a.minv, *b = a.b;
+  const bool rule0 = a.stop_rule == 0;
   unsigned int ep = 0;
-  double acc[2];
 
-  acc[0] = 0.0;
-  acc[1] = 0.0;
+  // r = b - A x ; p = s = r ; d = r.(r/m)   (x = 0 when init)
+  double acc[2] = {0.0, 0.0}, acc3[3];
   FOR_ROWS(P) {
     double ax;
     if (a.init) {
@@ -247,85 +262,114 @@ __global__ void __launch_bounds__(1024, 1) bicgstab_f64(KArgs a) {
     }
     const double ri = b[row] - ax;
     r[row] = ri;
-    p[row] = ri;
-    sv[row] = ri;
-    const double zi = ri * minv[row];
-    z[row] = zi;
-    acc[0] = fma(ri, zi, acc[0]);
+    pnew[row] = ri;
+    scur[row] = ri;
+    acc[0] = fma(ri, ri * minv[row], acc[0]);
     acc[1] = fma(b[row], b[row], acc[1]);
   }
-  if (!reduce<2>(a, ep, acc, red)) return;
-  const double d = acc[0];
-  const double bnorm2 = acc[1];
-  const double conv = (a.stop_rule == 0) ? a.tol * sqrt(fabs(d)) : a.tol * sqrt(bnorm2);
-  double crit = 0.0;
+  if (!grid_allreduce_d<2>(a.gs, ep, acc, buf, [&](const double *q) {
+        sh.d = q[0];
+        sh.conv = rule0 ? a.tol * sqrt(fabs(q[0])) : a.tol * sqrt(q[1]);
+        sh.crit = 0.0;
+        sh.stop = 0;
+      }))
+    return;
   int j, status = FVC_OK;
+  double alpha = 0.0, w = 0.0, beta = 0.0;
   for (j = 1; j <= a.maxit; ++j) {
-    // v = A z ; rr0 = s.r ; v.r
+    // phase 1: v = A z with z = p/m, p formed from the previous p, v, s
+    acc[0] = 0.0;
+    acc[1] = 0.0;
+    if (j == 1) {
+      FOR_ROWS(P) {
+        const double *pc = pnew;
+        const double vi =
+            sell_row_fma(a.A, s_, P.lane, row, [&](int k) { return pc[k] * minv[k]; });
+        vnew[row] = vi;
+        const double ri = r[row];
+        acc[0] = fma(scur[row], ri, acc[0]);
+        acc[1] = fma(vi, ri, acc[1]);
+      }
+    } else {
+      FOR_ROWS(P) {
+        const double *po = pold, *vo = vold, *sc = scur;
+        auto pf = [&](int k) { return fma(beta, fma(-w, vo[k], po[k]), sc[k]); };
+        pnew[row] = pf(row);
+        const double vi =
+            sell_row_fma(a.A, s_, P.lane, row, [&](int k) { return pf(k) * minv[k]; });
+        vnew[row] = vi;
+        const double ri = r[row];
+        acc[0] = fma(sc[row], ri, acc[0]);
+        acc[1] = fma(vi, ri, acc[1]);
+      }
+    }
+    if (!grid_allreduce_d<2>(a.gs, ep, acc, buf, [&](const double *q) {
+          sh.rr0 = q[0];
+          sh.alpha = q[0] / q[1];
+        }))
+      return;
+    alpha = sh.alpha;
+    // phase 2: s' = s - alpha v ; t = A z with z = s'/m
     acc[0] = 0.0;
     acc[1] = 0.0;
     FOR_ROWS(P) {
-      const double vi = sell_row_fma(a.A, s_, P.lane, row, [&](int k) { return z[k]; });
-      v[row] = vi;
-      const double ri = r[row];
-      acc[0] = fma(sv[row], ri, acc[0]);
-      acc[1] = fma(vi, ri, acc[1]);
-    }
-    if (!reduce<2>(a, ep, acc, red)) return;
-    const double rr0 = acc[0];
-    const double alpha = rr0 / acc[1];
-    // x += alpha z ; s -= alpha v ; z = s/m
-    FOR_ROWS(P) {
-      x[row] = fma(alpha, z[row], x[row]);
-      const double si = fma(-alpha, v[row], sv[row]);
-      sv[row] = si;
-      z[row] = si * minv[row];
-    }
-    if (!grid_barrier(a.gs, ep)) return;
-    // t = A z ; t.s ; t.t
-    acc[0] = 0.0;
-    acc[1] = 0.0;
-    FOR_ROWS(P) {
-      const double ti = sell_row_fma(a.A, s_, P.lane, row, [&](int k) { return z[k]; });
+      const double *sc = scur, *vn = vnew;
+      auto sf = [&](int k) { return fma(-alpha, vn[k], sc[k]); };
+      snxt[row] = sf(row);
+      const double ti =
+          sell_row_fma(a.A, s_, P.lane, row, [&](int k) { return sf(k) * minv[k]; });
       t[row] = ti;
-      acc[0] = fma(ti, sv[row], acc[0]);
+      acc[0] = fma(ti, snxt[row], acc[0]);
       acc[1] = fma(ti, ti, acc[1]);
     }
-    if (!reduce<2>(a, ep, acc, red)) return;
-    const double w = acc[0] / acc[1];
-    // x += w z ; s -= w t ; s.z ; r.s (and s.s for stop_rule 1)
-    double acc3[3] = {0.0, 0.0, 0.0};
+    if (!grid_allreduce_d<2>(a.gs, ep, acc, buf,
+                             [&](const double *q) { sh.w = q[0] / q[1]; }))
+      return;
+    w = sh.w;
+    // phase 3: x += alpha z ; x += w z' ; s'' = s' - w t ; s''.z' ; r.s'' ; s''.s''
+    acc3[0] = 0.0;
+    acc3[1] = 0.0;
+    acc3[2] = 0.0;
     FOR_ROWS(P) {
-      const double zi = z[row];
-      x[row] = fma(w, zi, x[row]);
-      const double si = fma(-w, t[row], sv[row]);
-      sv[row] = si;
-      acc3[0] = fma(si, zi, acc3[0]);
+      const double mi = minv[row];
+      const double s1 = snxt[row];
+      const double z1 = s1 * mi;
+      double xi = fma(alpha, pnew[row] * mi, x[row]);
+      x[row] = fma(w, z1, xi);
+      const double si = fma(-w, t[row], s1);
+      snxt[row] = si;
+      acc3[0] = fma(si, z1, acc3[0]);
       acc3[1] = fma(r[row], si, acc3[1]);
       acc3[2] = fma(si, si, acc3[2]);
     }
-    if (!reduce<3>(a, ep, acc3, red)) return;
-    double beta = acc3[0] / d;
-    crit = (a.stop_rule == 0) ? sqrt(fabs(beta)) : sqrt(acc3[2]);
-    if (!(crit == crit) || !(w == w)) {
+    if (!grid_allreduce_d<3>(a.gs, ep, acc3, buf, [&](const double *q) {
+          const double b0 = q[0] / sh.d;
+          sh.crit = rule0 ? sqrt(fabs(b0)) : sqrt(q[2]);
+          sh.stop = (!(sh.crit == sh.crit) || !(sh.w == sh.w)) ? 2 : (sh.crit < sh.conv ? 1 : 0);
+          sh.beta = (q[1] / sh.rr0) * (sh.alpha / sh.w);
+        }))
+      return;
+    if (sh.stop == 2) {
       status = FVC_ERR_NAN;
       break;
     }
-    if (crit < conv) break;
-    beta = (acc3[1] / rr0) * (alpha / w);
-    // p = s + beta (p - w v) ; z = p/m
-    FOR_ROWS(P) {
-      const double pi = fma(beta, fma(-w, v[row], p[row]), sv[row]);
-      p[row] = pi;
-      z[row] = pi * minv[row];
-    }
-    if (!grid_barrier(a.gs, ep)) return;
+    if (sh.stop == 1) break;
+    beta = sh.beta;
+    double *tmp = scur;
+    scur = snxt;
+    snxt = tmp;
+    tmp = pold;
+    pold = pnew;
+    pnew = tmp;
+    tmp = vold;
+    vold = vnew;
+    vnew = tmp;
   }
   if (j > a.maxit) {
     j = a.maxit;
     status = FVC_ERR_NOCONV;
   }
-  finish(a, j, status, conv, crit, 0);
+  finish(a, j, status, sh.conv, sh.crit, 0);
   epilogue(a, ep, red, false);
 }
 
@@ -544,7 +588,7 @@ template <typename K>
 Launch persistent_launch(K kernel, const DeviceMatrix &A, const fvc_opts &o) {
   Launch L;
   // 128..1024 threads in multiples of 128 (the block reductions assume it)
-  L.threads = (o.block_threads > 0) ? std::min(1024, std::max(128, o.block_threads & ~127)) : 1024;
+  L.threads = block_threads_for(o.block_threads, A.nslices, sm_count());
   int occ = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, L.threads, 0);
   if (occ <= 0) occ = 1;
@@ -597,6 +641,7 @@ int32_t run_persistent(K kernel, const DeviceMatrix &A, Scratch &S, const double
   a.v4 = S.v[4];
   a.v5 = S.v[5];
   a.v6 = S.v[6];
+  a.v7 = S.v[7];
   a.g = S.g;
   a.gs = make_sync(S, L.blocks);
   a.tol = tol;
@@ -658,7 +703,7 @@ int32_t run_pcg(const DeviceMatrix &A, Scratch &S, const double *b, double *x, d
 
 int32_t run_bicgstab(const DeviceMatrix &A, Scratch &S, const double *b, double *x, double tol,
                      int maxit, int init, const fvc_opts &o, cudaStream_t stream, fvc_stats *st) {
-  return run_persistent(bicgstab_f64, A, S, b, x, tol, maxit, init, o, stream, st, 6, false);
+  return run_persistent(bicgstab_f64, A, S, b, x, tol, maxit, init, o, stream, st, 8, false);
 }
 
 int32_t run_gmres(const DeviceMatrix &A, Scratch &S, const double *b, double *x, double tol,

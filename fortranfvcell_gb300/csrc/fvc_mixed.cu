@@ -1276,7 +1276,7 @@ int32_t run_mixed(const DeviceMatrix &A0, Scratch &S, int code, const double *b,
   for (int i = 0; i < 10; ++i)  // f[4] holds the float2 correction
     if (!S.f[i] && cudaMalloc(&S.f[i], sizeof(float) * (i == 4 ? 2 : 1) * (n + 64)) != cudaSuccess)
       return FVC_ERR_CUDA;
-  const int threads = (o.block_threads > 0) ? o.block_threads : 1024;
+  const int threads = block_threads_for(o.block_threads, A.nslices, sm_count_m());
   // CG streams through shared-memory stages when its layout allows
   const bool staged = code == 1 && threads == kStRows && A.col16_ok && o.staging == 0;
   auto kern = (code != 1) ? mixed_bicgstab
