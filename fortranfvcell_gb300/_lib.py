@@ -137,6 +137,9 @@ SIGNATURES = {
     "fvc_cells_simple_update": ([I32, P, P, P, P, P, P, P, F64, P], I32),
     "fvc_cells_divergence": ([I32, P, P, P, P], I32),
     "fvc_getres": ([I32, P, P, P, I32, P], I32),
+    "fvc_cells_energy": ([C.POINTER(FvcCellMesh), I32, I32, P, P, P, P, P, P, P, F64, I32, I32,
+                          P, P, P, P, P, P, P], I32),
+    "fvc_cells_energy_gradient": ([C.POINTER(FvcCellMesh), I32, P, P, P, P, P], I32),
     "fvc_simple_opts_default": ([C.POINTER(FvcSimpleOpts)], None),
     "fvc_simple_create": ([C.POINTER(P), I32, I32, I32, I32, I32, P, P, P, P, P, P, P,
                            C.POINTER(FvcSimpleOpts)], I32),

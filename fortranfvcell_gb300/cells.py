@@ -73,6 +73,23 @@ def pressure_correction(m: CellMesh, w, d, p, gradp, ia, ja, matriz, ad, au, b, 
         "fvc_cells_pressure_correction")
 
 
+def energy(m: CellMesh, lib: int, iws: int, pedge, sedge, u, u0, ro, w, grad, dt, ia, ja,
+           matriz, ad, au, b, rescell, bs=False) -> None:
+    """Energy / transported-scalar system (lib 3: ideal-gas enthalpy cell,
+    lib 4: transport cell); pedge, sedge: the scalar's (numel, nshared+1)
+    device boundary arrays, ro (numel, 3) the densities."""
+    _lib.check(_lib.load().fvc_cells_energy(
+        C.byref(m.s), lib, iws, _addr(pedge), _addr(sedge), _addr(u), _addr(u0), _addr(ro),
+        _addr(w), _addr(grad), dt, int(bs), matriz, _addr(ia), _addr(ja), _addr(ad), _addr(au),
+        _addr(b), _addr(rescell), _stream()), "fvc_cells_energy")
+
+
+def energy_gradient(m: CellMesh, lib: int, pedge, sedge, u, grad) -> None:
+    _lib.check(_lib.load().fvc_cells_energy_gradient(
+        C.byref(m.s), lib, _addr(pedge), _addr(sedge), _addr(u), _addr(grad), _stream()),
+        "fvc_cells_energy_gradient")
+
+
 def simple_update(w, p, u1, u2, pc, gradpc, d, under_pc) -> None:
     _lib.check(_lib.load().fvc_cells_simple_update(
         w.shape[0], _addr(w), _addr(p), _addr(u1), _addr(u2), _addr(pc), _addr(gradpc),

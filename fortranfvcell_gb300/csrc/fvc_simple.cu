@@ -11,6 +11,9 @@
 //              cellVel face fluxes (CellibSimple.f:1947-2073, intVel 1/2/5)
 //   scatter    assbly for CSRD and ELLPACK (Assbly.f:32-54, Csr.f:142-176,
 //              EllPack.f:68-93): each cell writes its own row only
+//   energy     cell_e_eb_idg_ggl (CellibTrans.f:39-349, ideal-gas enthalpy)
+//              and cell_t_eb_ggl (CellibTrans.f:390-655, scalar transport):
+//              iws 1 system, 2 gradient, 4 time term and volume source
 //   sweeps     simpleUpdate, divergente (Simple.f:871-910, 1070-1078),
 //              getRes (Solver.f:368-391)
 // The arithmetic follows the reference statement by statement and this
@@ -609,6 +612,226 @@ __global__ void getres_kernel(int numel, const int32_t *num, double *u, double *
     u[i] = x[num[i] - 1];
 }
 
+// ---- energy / scalar transport cells (src/CellibTrans.f) -----------------
+// lib 3: cell_e_eb_idg_ggl (ideal-gas enthalpy, CellibTrans.f:39-349);
+// lib 4: cell_t_eb_ggl (scalar transport, CellibTrans.f:390-655).  The
+// scalar's own boundary arrays pe(nshared+1,*), se(nshared+1,*) (one value
+// per face; face nshared+1 a volume source).  ro(3,*): densities at n-1, n
+// and the current iterate.  The reference declares the boundary enthalpy
+// of lib 3 and the inflow density of lib 4 integer: both are truncated
+// toward zero here as there.
+struct EnArgs {
+  int lib, iws, bs, matriz;
+  double dt;
+  const int32_t *pe;
+  const double *se;
+  const double *u, *u0, *ro, *w, *grad;
+  const int32_t *ia, *ja;
+  double *ad, *au, *b, *rescell;
+};
+
+__device__ __forceinline__ int epedge(const int32_t *pe, int nsh, int i, int c) {
+  return pe[(i - 1) + (size_t)(c - 1) * (nsh + 1)];
+}
+__device__ __forceinline__ double esedge(const double *se, int nsh, int i, int c) {
+  return se[(i - 1) + (size_t)(c - 1) * (nsh + 1)];
+}
+__device__ __forceinline__ double ro3(const double *ro, int k, int c) {  // ro(k, c), (3, *)
+  return ro[(k - 1) + 3 * (size_t)(c - 1)];
+}
+
+__global__ void energy_gradient_kernel(Mesh m, int lib, const int32_t *__restrict__ pe,
+                                       const double *__restrict__ se,
+                                       const double *__restrict__ u, double *__restrict__ grad) {
+  const int nel = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  if (nel > m.numel) return;
+  Stencil S;
+  Geom G;
+  gather(S, m, nel);
+  geom(G, S);
+  const double uP = u[nel - 1];
+  const double go1 = v2(grad, 1, nel), go2 = v2(grad, 2, nel);
+  const double cesp = prop(m, nel, 4), tref = prop(m, nel, 5);
+  double ug[MS];
+  for (int i = 1; i <= S.ns; ++i) {
+    const int v = S.viz[i - 1];
+    if (v > 0) {
+      ug[i - 1] = u[v - 1];
+      continue;
+    }
+    const int pcode = epedge(pe, m.nshared, i, nel);
+    const double sface = esedge(se, m.nshared, i, nel);
+    if (lib == 3) {  // CellibTrans.f:131-144
+      if (pcode == 2) {
+        const int enthalpia = (int)(cesp * (sface - tref));
+        ug[i - 1] = (double)enthalpia;
+      } else {
+        const double gama = 2.0 * G.ca[i - 1];
+        ug[i - 1] = uP + gama * (go1 * G.n[0][i - 1] + go2 * G.n[1][i - 1]);
+      }
+    } else {  // CellibTrans.f:460-464
+      ug[i - 1] = (pcode == 2) ? 2.0 * sface - uP : uP;
+    }
+  }
+  double g1, g2;
+  green_gauss(G, S.ns, ug, g1, g2);
+  grad[2 * (size_t)(nel - 1)] = g1;
+  grad[2 * (size_t)(nel - 1) + 1] = g2;
+}
+
+__global__ void energy_kernel(Mesh m, EnArgs a) {
+  const int nel = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  if (nel > m.numel) return;
+  const double ZERO = 1.0e-14, eps = 1.0e-14;
+  Stencil S;
+  Geom G;
+  gather(S, m, nel);
+  geom(G, S);
+  const int ns = S.ns, nsh = m.nshared, lib = a.lib;
+  const double kc = prop(m, nel, 3);
+  const double cesp = prop(m, nel, 4);
+  const double tref = prop(m, nel, 5);
+  const double cc = prop(m, nel, 6);
+  const int icod = (int)prop(m, nel, 7);
+  const int spec_mass = (int)prop(m, nel, 2);  // lib 4: an integer in the reference
+  const double *u = a.u, *ro = a.ro, *w = a.w, *grad = a.grad;
+  const double uP = u[nel - 1];
+  int ldl[MS + 1];
+  for (int i = 0; i <= MS; ++i) ldl[i] = 0;
+  for (int j = 1; j <= ns; ++j) ldl[j - 1] = (S.viz[j - 1] > 0) ? m.num[S.viz[j - 1] - 1] : 0;
+  ldl[nsh] = m.num[nel - 1];
+  double la[MS + 1];
+  for (int i = 0; i <= MS; ++i) la[i] = 0.0;
+  if (a.iws == 4) {  // label 400: time term and volume source
+    double mm = ro3(ro, 2, nel) * cc * G.area / a.dt;
+    double p = mm * uP;
+    if (a.bs) {
+      mm = ro3(ro, 1, nel) * cc * G.area / a.dt;
+      p = 2 * p - 0.5 * mm * a.u0[nel - 1];
+    }
+    if (epedge(a.pe, nsh, nsh + 1, nel) != 0) p = p + esedge(a.se, nsh, nsh + 1, nel) * G.area;
+    assbly(a.ad, a.au, a.b, a.ia, a.ja, la, p, ldl, nsh, a.matriz, true, false);
+    return;
+  }
+  const double roc = ro3(ro, 3, nel);
+  double rof = roc;  // lib 4 carries it from face to face
+  double p = 0.0, sp = 0.0, cd = 0.0, cvc = 0.0;
+  double aa[MS];
+  for (int i = 1; i <= ns; ++i) {
+    const int v = S.viz[i - 1];
+    const double n1 = G.n[0][i - 1], n2 = G.n[1][i - 1];
+    const double meta = G.meta[i - 1];
+    if (v < 0) {
+      const int pcode = epedge(a.pe, nsh, i, nel);
+      const double sface = esedge(a.se, nsh, i, nel);
+      aa[i - 1] = 0.0;
+      const double wfn = v2(w, 1, nel) * n1 + v2(w, 2, nel) * n2;
+      double cv = (lib == 3 ? roc : rof) * wfn * meta;
+      if (pcode == 0) {
+        p = p + sface * meta;
+      } else if (pcode == 1) {
+        if (lib == 3) {
+          const double ap = (kc / cesp) * meta / G.ca[i - 1];
+          sp = sp + ap;
+          const int enthalpia = (int)(cesp * (sface - tref));
+          p = p + ap * enthalpia;
+        } else {
+          const double ap = kc * meta / G.ca[i - 1];
+          sp = sp + ap;
+          p = p + ap * sface;
+        }
+      } else if (pcode == 2) {
+        if (lib == 3) {
+          if (fabs(wfn) > ZERO) {
+            if (cv < 0.0) {
+              cv = prop(m, nel, 2) * wfn * meta;
+              const int enthalpia = (int)(cesp * (sface - tref));
+              p = p - cv * enthalpia;
+            } else {
+              sp = sp + cv;
+            }
+          }
+        } else {
+          if (cv < 0.0) {
+            cv = spec_mass * wfn * meta;
+            p = p - cv * sface;
+          } else {
+            sp = sp + cv;
+          }
+        }
+      } else if (pcode == 4) {
+        sp = sp + cv;
+      }
+    } else {
+      double alpha = G.mksif[i - 1] / G.mksi[i - 1];
+      double kf;
+      if (lib == 3)
+        kf = alpha / (kc / cesp) + (1.0 - alpha) / (prop(m, v, 3) / prop(m, v, 4));
+      else
+        kf = alpha / kc + (1.0 - alpha) / prop(m, v, 3);
+      kf = 1.0 / kf;
+      const double wf1 = (1.0 - alpha) * v2(w, 1, nel) + alpha * v2(w, 1, v);
+      const double wf2 = (1.0 - alpha) * v2(w, 2, nel) + alpha * v2(w, 2, v);
+      double gf1 = (1.0 - alpha) * v2(grad, 1, nel) + alpha * v2(grad, 1, v);
+      double gf2 = (1.0 - alpha) * v2(grad, 2, nel) + alpha * v2(grad, 2, v);
+      const double k1 = G.ksi[0][i - 1], k2 = G.ksi[1][i - 1], mk = G.mksi[i - 1];
+      const double nk = n1 * k1 + n2 * k2;
+      const double wfn = wf1 * n1 + wf2 * n2;
+      const double uv = u[v - 1];
+      double gfk = gf1 * k1 + gf2 * k2;
+      gf1 = gf1 + ((uv - uP) / mk - gfk) * k1;
+      gf2 = gf2 + ((uv - uP) / mk - gfk) * k2;
+      const double gfn = gf1 * n1 + gf2 * n2;
+      gfk = gf1 * k1 + gf2 * k2;
+      const double dfd = (kf * meta) / (nk * mk);
+      cd = kf * meta * (gfn - gfk / nk);
+      aa[i - 1] = dfd;
+      p = p + cd;
+      if (lib == 3) {
+        rof = (1.0 - alpha) * ro3(ro, 3, nel) + alpha * ro3(ro, 3, v);
+      } else {
+        if (wfn > 0.0)
+          rof = ro3(ro, 3, nel);
+        else if (wfn < 0.0)
+          rof = ro3(ro, 3, v);
+        else
+          rof = (1.0 - alpha) * ro3(ro, 3, nel) + alpha * ro3(ro, 3, v);
+      }
+      const double cv = rof * wfn * meta;
+      if (cv < 0.0) {
+        const double du = uP - uv + eps;
+        const double gpk = v2(grad, 1, v) * (G.xc[0][MS] - G.xc[0][i - 1]) +
+                           v2(grad, 2, v) * (G.xc[1][MS] - G.xc[1][i - 1]);
+        alpha = G.mksif[i - 1] / G.mksi[i - 1];
+        const double r = 2.0 * gpk / du - 1.0;
+        cvc = (1.0 - alpha) * limit(r, icod) * du;
+      } else {
+        const double du = uv - uP + eps;
+        const double gpk = (v2(grad, 1, nel) * k1 + v2(grad, 2, nel) * k2) * mk;
+        alpha = G.mksif[i - 1] / G.mksi[i - 1];
+        const double r = 2.0 * gpk / du - 1.0;
+        cvc = alpha * limit(r, icod) * du;
+      }
+      cvc = cvc + gf1 * G.km[0][i - 1] + gf2 * G.km[1][i - 1];
+      aa[i - 1] = aa[i - 1] + fmax(-cv, 0.0);
+      sp = sp + cv;
+      p = p - cv * cvc;
+    }
+  }
+  double aP = sp;
+  for (int i = 1; i <= ns; ++i) aP = aP + aa[i - 1];
+  double mm = ro3(ro, 3, nel) * cc * G.area / a.dt;
+  if (a.bs) mm = 1.5 * mm;
+  aP = aP + mm;
+  double rm = p - aP * uP;
+  for (int i = 1; i <= ns; ++i)
+    rm = rm + aa[i - 1] * ((S.viz[i - 1] > 0) ? u[S.viz[i - 1] - 1] : 0.0);
+  a.rescell[nel - 1] = rm;
+  for (int i = 1; i <= ns; ++i) la[i - 1] = aa[i - 1];
+  la[nsh] = aP;
+  assbly(a.ad, a.au, a.b, a.ia, a.ja, la, p, ldl, nsh, a.matriz, true, true);
+}
+
 Mesh view(const fvc_cell_mesh *m) {
   Mesh v;
   v.numel = m->numel;
@@ -627,6 +850,12 @@ Mesh view(const fvc_cell_mesh *m) {
 bool mesh_ok(const fvc_cell_mesh *m) {
   return m && m->numel > 0 && (m->nshared == 3 || m->nshared == 4) && m->coor && m->ix &&
          m->nelcon && m->num && m->pedge && m->sedge && m->e;
+}
+
+// the energy cells take their own boundary arrays: geometry and materials only
+bool mesh_geom_ok(const fvc_cell_mesh *m) {
+  return m && m->numel > 0 && (m->nshared == 3 || m->nshared == 4) && m->coor && m->ix &&
+         m->nelcon && m->num && m->e;
 }
 
 constexpr int kThreads = 128;
@@ -749,6 +978,54 @@ int32_t fvc_cells_divergence(int32_t numel, double *div, const double *gu1, cons
   if (numel <= 0 || !div || !gu1 || !gu2) return FVC_ERR_ARG;
   cudaStream_t s = (cudaStream_t)stream;
   fvc::cells::divergence_kernel<<<grid(numel), kThreads, 0, s>>>(numel, div, gu1, gu2);
+  fvc::count_launch();
+  return cudaPeekAtLastError() == cudaSuccess ? FVC_OK : FVC_ERR_CUDA;
+}
+
+int32_t fvc_cells_energy_gradient(const fvc_cell_mesh *m, int32_t lib, const int32_t *pedge,
+                                  const double *sedge, const double *u, double *grad,
+                                  void *stream) {
+  if (!fvc::cells::mesh_geom_ok(m) || (lib != 3 && lib != 4) || !pedge || !sedge || !u || !grad)
+    return FVC_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  fvc::cells::energy_gradient_kernel<<<grid(m->numel), kThreads, 0, s>>>(
+      fvc::cells::view(m), lib, pedge, sedge, u, grad);
+  fvc::count_launch();
+  return cudaPeekAtLastError() == cudaSuccess ? FVC_OK : FVC_ERR_CUDA;
+}
+
+int32_t fvc_cells_energy(const fvc_cell_mesh *m, int32_t lib, int32_t iws, const int32_t *pedge,
+                         const double *sedge, const double *u, const double *u0,
+                         const double *ro, const double *w, const double *grad, double dt,
+                         int32_t bs, int32_t matriz, const int32_t *ia, const int32_t *ja,
+                         double *ad, double *au, double *b, double *rescell, void *stream) {
+  if (!fvc::cells::mesh_geom_ok(m) || (lib != 3 && lib != 4) || (iws != 1 && iws != 4) ||
+      (matriz != 1 && matriz != 4) || !pedge || !sedge || !u || !ro || !b || dt == 0.0)
+    return FVC_ERR_ARG;
+  if (iws == 1 && (!w || !grad || !ad || !au || !rescell || (matriz == 1 && (!ia || !ja))))
+    return FVC_ERR_ARG;
+  if (iws == 4 && bs && !u0) return FVC_ERR_ARG;
+  fvc::cells::EnArgs a;
+  a.lib = lib;
+  a.iws = iws;
+  a.bs = bs;
+  a.matriz = matriz;
+  a.dt = dt;
+  a.pe = pedge;
+  a.se = sedge;
+  a.u = u;
+  a.u0 = u0;
+  a.ro = ro;
+  a.w = w;
+  a.grad = grad;
+  a.ia = ia;
+  a.ja = ja;
+  a.ad = ad;
+  a.au = au;
+  a.b = b;
+  a.rescell = rescell;
+  cudaStream_t s = (cudaStream_t)stream;
+  fvc::cells::energy_kernel<<<grid(m->numel), kThreads, 0, s>>>(fvc::cells::view(m), a);
   fvc::count_launch();
   return cudaPeekAtLastError() == cudaSuccess ? FVC_OK : FVC_ERR_CUDA;
 }

@@ -325,6 +325,38 @@ int32_t fvc_cells_simple_update(int32_t numel, double *w, double *p,
 int32_t fvc_cells_divergence(int32_t numel, double *div, const double *gu1,
                              const double *gu2, void *stream);
 
+/* Energy / transported-scalar cells of src/CellibTrans.f, one call of the
+ * reference's pform (iws 1, 4) for the scalar u.  lib 3: the ideal-gas
+ * enthalpy cell cell_e_eb_idg_ggl (:39-349; material k(3) conductivity,
+ * k(4) specific heat, k(5) reference temperature); lib 4: the transport
+ * cell cell_t_eb_ggl (:390-655).  pedge(nshared+1,numel) and
+ * sedge(nshared+1,numel) are the scalar's boundary codes and values (0 flux,
+ * 1 prescribed value, 2 inflow/outflow, 4 outflow; face nshared+1 a volume
+ * source when its code is nonzero); m->pedge and m->sedge are not used.
+ * ro(3,numel): density at levels n-1, n and the current iterate; w(2,*):
+ * velocity; grad(2,*): the scalar's gradient.  iws 1: row num(c) of
+ * (ad, au) for matriz 1 (CSRD) or 4 (ELLPACK), b(num(c)) and rescell(c);
+ * iws 4: b(num(c)) = the time term ro cc A/dt u (second order with bs:
+ * 2 ro(2) cc A/dt u - ro(1) cc A/(2dt) u0) plus the volume source.  As in
+ * the reference, lib 3 truncates the boundary enthalpy cEsp (T - tRef) and
+ * lib 4 the inflow density k(2) to integers. */
+int32_t fvc_cells_energy(const fvc_cell_mesh *m, int32_t lib, int32_t iws,
+                         const int32_t *pedge, const double *sedge,
+                         const double *u, const double *u0, const double *ro,
+                         const double *w, const double *grad, double dt,
+                         int32_t bs, int32_t matriz, const int32_t *ia,
+                         const int32_t *ja, double *ad, double *au, double *b,
+                         double *rescell, void *stream);
+
+/* Green-Gauss gradient of the scalar (gform with lib 3 or 4, src/Pform.f:
+ * 466-646): ghost values from the rules of src/CellibTrans.f:131-144 (lib
+ * 3: the inflow enthalpy, else extrapolation with the cell's previous
+ * gradient, so grad(2,numel) is read and overwritten) and :460-464 (lib 4:
+ * 2 sedge - u at inflow faces, else u). */
+int32_t fvc_cells_energy_gradient(const fvc_cell_mesh *m, int32_t lib,
+                                  const int32_t *pedge, const double *sedge,
+                                  const double *u, double *grad, void *stream);
+
 /* getRes (src/Solver.f:368-391): to_equations != 0: x(num(c)) = u(c);
  * else u(c) = x(num(c)). */
 int32_t fvc_getres(int32_t numel, const int32_t *num, double *u, double *x,

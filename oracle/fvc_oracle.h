@@ -175,4 +175,19 @@ void oref_simple_update(double *w, double *pre, const double *u1, const double *
                         int32_t numel, double under_pc);
 void oref_divergente(double *div, const double *gu1, const double *gu2, int32_t numel);
 
+/* Energy / scalar transport cells (src/CellibTrans.f): lib 3 the ideal-gas
+ * enthalpy cell, lib 4 the transport cell.  pedge and sedge here are the
+ * scalar's (nshared+1, numel) arrays; ro(3, numel) the densities. */
+int32_t oref_gform_energy(const double *coor, const int32_t *ix, int32_t ld, int32_t numel,
+                          int32_t nshared, const int32_t *nelcon, const int32_t *pedge,
+                          const double *sedge, const double *e, int32_t lib, const double *u,
+                          double *grad);
+int32_t oref_pform_energy(const double *coor, const int32_t *ix, int32_t ld, int32_t numel,
+                          int32_t nshared, const int32_t *nelcon, const int32_t *num,
+                          const int32_t *pedge, const double *sedge, const double *e,
+                          int32_t lib, int32_t iws, const double *u, const double *u0,
+                          const double *ro, const double *w, const double *grad, double dt,
+                          int32_t bs, int32_t matriz, int32_t unsym, const int32_t *ia,
+                          const int32_t *ja, double *ad, double *au, double *b, double *rescell);
+
 #endif

@@ -16,6 +16,8 @@
  *   cellVel (intVel 1, 2, 5)     src/CellibSimple.f:1947-2073
  *   cell_si_p_i_ggl iws=1,2      src/CellibPressure.f:390-620
  *   simpleUpdate, divergente     src/Simple.f:871-910, :1070-1078
+ *   cell_e_eb_idg_ggl iws 1,2,4  src/CellibTrans.f:39-349 (ideal-gas enthalpy)
+ *   cell_t_eb_ggl iws 1,2,4      src/CellibTrans.f:390-655 (scalar transport)
  * Meshes may mix triangles and quadrilaterals: a cell's loops run over its
  * own sides (for single-type meshes this is the reference's nshared).
  * Parity: restatement only (no Fortran compiler exists to run the
@@ -574,4 +576,232 @@ void oref_simple_update(double *w, double *pre, const double *u1, const double *
 /* divergente (Simple.f:1070-1078). */
 void oref_divergente(double *div, const double *gu1, const double *gu2, int32_t numel) {
   for (int32_t i = 1; i <= numel; ++i) F1(div, i) = F2(gu1, 2, 1, i) + F2(gu2, 2, 2, i);
+}
+
+/* ---- energy / scalar transport cells (src/CellibTrans.f) ---------------
+ * lib 3: cell_e_eb_idg_ggl, the ideal-gas enthalpy equation
+ *        (CellibTrans.f:39-349); lib 4: cell_t_eb_ggl, the scalar
+ *        transport equation (CellibTrans.f:390-655).  pedge(nshared+1,*)
+ *        and sedge(nshared+1,*) hold the scalar's boundary codes and values
+ *        (one value per face, nst = 1); face nshared+1 carries a volume
+ *        source when its code is nonzero.  ro(3,*) is the density at the
+ *        time levels n-1, n and the current iterate.
+ * Two of the reference's variables are declared integer, and the
+ * restatement keeps that: the boundary enthalpy cEsp (T - tRef) of lib 3
+ * (`enthalpia`) and the inflow density k(2) of lib 4 (`specificMassA`) are
+ * truncated toward zero. */
+
+/* Ghost value of boundary face i for the gradient (iws 2). */
+static double energy_ghost(int32_t lib, int32_t pe, double sface, double uP, const Geom *G,
+                           int32_t i, double go1, double go2, double cesp, double tref) {
+  if (lib == 3) { /* CellibTrans.f:131-144 */
+    if (pe == 2) {
+      const int32_t enthalpia = (int32_t)(cesp * (sface - tref));
+      return (double)enthalpia;
+    }
+    const double gama = 2.0 * G->ca[i - 1];
+    return uP + gama * (go1 * G->n[0][i - 1] + go2 * G->n[1][i - 1]);
+  }
+  /* lib 4: CellibTrans.f:460-464 */
+  if (pe == 2) return 2.0 * sface - uP;
+  return uP;
+}
+
+/* gform for the scalar (Pform.f:466-646 with lib 3 or 4, iws 2): grad(2,*)
+ * holds the previous gradient on entry (lib 3 extrapolates with it). */
+int32_t oref_gform_energy(const double *coor, const int32_t *ix, int32_t ld, int32_t numel,
+                          int32_t nshared, const int32_t *nelcon, const int32_t *pedge,
+                          const double *sedge, const double *e, int32_t lib, const double *u,
+                          double *grad) {
+  const int32_t ldp = nshared + 1;
+  if (lib != 3 && lib != 4) return -1;
+  for (int32_t nel = 1; nel <= numel; ++nel) {
+    Stencil S;
+    Geom G;
+    gather(&S, coor, ix, ld, nshared, nelcon, nel);
+    geom(&G, &S);
+    const double uP = F1(u, nel);
+    const double go1 = F2(grad, 2, 1, nel), go2 = F2(grad, 2, 2, nel);
+    const double cesp = PROP(e, ix, ld, nel, 4), tref = PROP(e, ix, ld, nel, 5);
+    double ug[MS];
+    for (int32_t i = 1; i <= S.ns; ++i) {
+      const int32_t v = S.viz[i - 1];
+      if (v > 0)
+        ug[i - 1] = F1(u, v);
+      else
+        ug[i - 1] = energy_ghost(lib, F2(pedge, ldp, i, nel), F2(sedge, ldp, i, nel), uP, &G, i,
+                                 go1, go2, cesp, tref);
+    }
+    double g1, g2;
+    green_gauss(&G, S.ns, ug, &g1, &g2);
+    F2(grad, 2, 1, nel) = g1;
+    F2(grad, 2, 2, nel) = g2;
+  }
+  return 0;
+}
+
+/* pform for the scalar (Pform.f:65-436 with lib 3 or 4).  iws 1: the
+ * system (label 100: coefficients, b(num(c)) = p, rescell(c) = the cell
+ * residual); iws 4: b(num(c)) = the time term of u and u0 plus the volume
+ * source (label 400).  u0 is the level n-1 field (bs only). */
+int32_t oref_pform_energy(const double *coor, const int32_t *ix, int32_t ld, int32_t numel,
+                          int32_t nshared, const int32_t *nelcon, const int32_t *num,
+                          const int32_t *pedge, const double *sedge, const double *e,
+                          int32_t lib, int32_t iws, const double *u, const double *u0,
+                          const double *ro, const double *w, const double *grad, double dt,
+                          int32_t bs, int32_t matriz, int32_t unsym, const int32_t *ia,
+                          const int32_t *ja, double *ad, double *au, double *b, double *rescell) {
+  const int32_t ldp = nshared + 1;
+  const double ZERO = 1.0e-14, eps = 1.0e-14;
+  if ((lib != 3 && lib != 4) || (iws != 1 && iws != 4)) return -1;
+  for (int32_t nel = 1; nel <= numel; ++nel) {
+    Stencil S;
+    Geom G;
+    gather(&S, coor, ix, ld, nshared, nelcon, nel);
+    geom(&G, &S);
+    const int32_t ns = S.ns;
+    const double kc = PROP(e, ix, ld, nel, 3);
+    const double cesp = PROP(e, ix, ld, nel, 4);
+    const double tref = PROP(e, ix, ld, nel, 5);
+    const double cc = PROP(e, ix, ld, nel, 6);
+    const int32_t icod = (int32_t)PROP(e, ix, ld, nel, 7);
+    const int32_t spec_mass = (int32_t)PROP(e, ix, ld, nel, 2); /* lib 4: integer */
+    const double uP = F1(u, nel);
+    int32_t ldl[MS + 1];
+    for (int32_t i = 0; i <= MS; ++i) ldl[i] = 0;
+    for (int32_t j = 1; j <= ns; ++j) ldl[j - 1] = (S.viz[j - 1] > 0) ? F1(num, S.viz[j - 1]) : 0;
+    ldl[nshared] = F1(num, nel);
+    double la[MS + 1];
+    for (int32_t i = 0; i <= MS; ++i) la[i] = 0.0;
+    if (iws == 4) { /* label 400 */
+      double m = F2(ro, 3, 2, nel) * cc * G.area / dt;
+      double p = m * uP;
+      if (bs) {
+        m = F2(ro, 3, 1, nel) * cc * G.area / dt;
+        p = 2 * p - 0.5 * m * F1(u0, nel);
+      }
+      if (F2(pedge, ldp, ldp, nel) != 0) p = p + F2(sedge, ldp, ldp, nel) * G.area;
+      oref_assbly(ad, au, au, b, ia, ja, la, p, ldl, nshared, matriz, unsym, 1, 0);
+      continue;
+    }
+    const double roc = F2(ro, 3, 3, nel);
+    double rof = roc; /* lib 4 keeps it as a running value across faces */
+    double p = 0.0, sp = 0.0, cd = 0.0, cvc = 0.0;
+    double a[MS + 1];
+    for (int32_t i = 1; i <= ns; ++i) {
+      const int32_t v = S.viz[i - 1];
+      const double n1 = G.n[0][i - 1], n2 = G.n[1][i - 1];
+      const double meta = G.meta[i - 1];
+      if (v < 0) {
+        const int32_t pe = F2(pedge, ldp, i, nel);
+        const double sface = F2(sedge, ldp, i, nel);
+        a[i - 1] = 0.0;
+        const double wfn = F2(w, 2, 1, nel) * n1 + F2(w, 2, 2, nel) * n2;
+        double cv = (lib == 3 ? roc : rof) * wfn * meta;
+        if (pe == 0) {
+          p = p + sface * meta;
+        } else if (pe == 1) {
+          if (lib == 3) {
+            const double ap = (kc / cesp) * meta / G.ca[i - 1];
+            sp = sp + ap;
+            const int32_t enthalpia = (int32_t)(cesp * (sface - tref));
+            p = p + ap * enthalpia;
+          } else {
+            const double ap = kc * meta / G.ca[i - 1];
+            sp = sp + ap;
+            p = p + ap * sface;
+          }
+        } else if (pe == 2) {
+          if (lib == 3) {
+            if (fabs(wfn) > ZERO) {
+              if (cv < 0.0) {
+                cv = PROP(e, ix, ld, nel, 2) * wfn * meta;
+                const int32_t enthalpia = (int32_t)(cesp * (sface - tref));
+                p = p - cv * enthalpia;
+              } else {
+                sp = sp + cv;
+              }
+            }
+          } else {
+            if (cv < 0.0) {
+              cv = spec_mass * wfn * meta;
+              p = p - cv * sface;
+            } else {
+              sp = sp + cv;
+            }
+          }
+        } else if (pe == 4) {
+          sp = sp + cv;
+        }
+      } else {
+        double alpha = G.mksif[i - 1] / G.mksi[i - 1];
+        double kf;
+        if (lib == 3)
+          kf = alpha / (kc / cesp) + (1.0 - alpha) / (PROP(e, ix, ld, v, 3) / PROP(e, ix, ld, v, 4));
+        else
+          kf = alpha / kc + (1.0 - alpha) / PROP(e, ix, ld, v, 3);
+        kf = 1.0 / kf;
+        const double wf1 = (1.0 - alpha) * F2(w, 2, 1, nel) + alpha * F2(w, 2, 1, v);
+        const double wf2 = (1.0 - alpha) * F2(w, 2, 2, nel) + alpha * F2(w, 2, 2, v);
+        double gf1 = (1.0 - alpha) * F2(grad, 2, 1, nel) + alpha * F2(grad, 2, 1, v);
+        double gf2 = (1.0 - alpha) * F2(grad, 2, 2, nel) + alpha * F2(grad, 2, 2, v);
+        const double k1 = G.ksi[0][i - 1], k2 = G.ksi[1][i - 1], mk = G.mksi[i - 1];
+        const double nk = n1 * k1 + n2 * k2;
+        const double wfn = wf1 * n1 + wf2 * n2;
+        double gfk = gf1 * k1 + gf2 * k2;
+        gf1 = gf1 + ((F1(u, v) - uP) / mk - gfk) * k1;
+        gf2 = gf2 + ((F1(u, v) - uP) / mk - gfk) * k2;
+        const double gfn = gf1 * n1 + gf2 * n2;
+        gfk = gf1 * k1 + gf2 * k2;
+        const double dfd = (kf * meta) / (nk * mk);
+        cd = kf * meta * (gfn - gfk / nk);
+        a[i - 1] = dfd;
+        p = p + cd;
+        if (lib == 3) {
+          rof = (1.0 - alpha) * F2(ro, 3, 3, nel) + alpha * F2(ro, 3, 3, v);
+        } else {
+          if (wfn > 0.0)
+            rof = F2(ro, 3, 3, nel);
+          else if (wfn < 0.0)
+            rof = F2(ro, 3, 3, v);
+          else
+            rof = (1.0 - alpha) * F2(ro, 3, 3, nel) + alpha * F2(ro, 3, 3, v);
+        }
+        const double cv = rof * wfn * meta;
+        if (cv < 0.0) {
+          const double du = uP - F1(u, v) + eps;
+          const double gpk = F2(grad, 2, 1, v) * (G.xc[0][MS] - G.xc[0][i - 1]) +
+                             F2(grad, 2, 2, v) * (G.xc[1][MS] - G.xc[1][i - 1]);
+          alpha = G.mksif[i - 1] / G.mksi[i - 1];
+          const double r = 2.0 * gpk / du - 1.0;
+          cvc = (1.0 - alpha) * limit(r, icod) * du;
+        } else {
+          const double du = F1(u, v) - uP + eps;
+          const double gpk = (F2(grad, 2, 1, nel) * k1 + F2(grad, 2, 2, nel) * k2) * mk;
+          alpha = G.mksif[i - 1] / G.mksi[i - 1];
+          const double r = 2.0 * gpk / du - 1.0;
+          cvc = alpha * limit(r, icod) * du;
+        }
+        cvc = cvc + gf1 * G.km[0][i - 1] + gf2 * G.km[1][i - 1];
+        a[i - 1] = a[i - 1] + fmax(-cv, 0.0);
+        sp = sp + cv;
+        p = p - cv * cvc;
+      }
+    }
+    double aP = sp;
+    for (int32_t i = 1; i <= ns; ++i) aP = aP + a[i - 1];
+    double m = F2(ro, 3, 3, nel) * cc * G.area / dt;
+    if (bs) m = 1.5 * m;
+    aP = aP + m;
+    /* rm = F - K u; a boundary face's coefficient is zero and its
+       neighbour value counts as 0 */
+    double rm = p - aP * uP;
+    for (int32_t i = 1; i <= ns; ++i)
+      rm = rm + a[i - 1] * ((S.viz[i - 1] > 0) ? F1(u, S.viz[i - 1]) : 0.0);
+    F1(rescell, nel) = rm;
+    for (int32_t i = 1; i <= ns; ++i) la[i - 1] = a[i - 1];
+    la[nshared] = aP;
+    oref_assbly(ad, au, au, b, ia, ja, la, p, ldl, nshared, matriz, unsym, 1, 1);
+  }
+  return 0;
 }

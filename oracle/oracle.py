@@ -83,10 +83,14 @@ def lib():
                               vp, vp, vp, vp, vp],
             "oref_simple_update": [vp, vp, vp, vp, vp, vp, vp, I, D],
             "oref_divergente": [vp, vp, vp, I],
+            "oref_gform_energy": [vp, vp, I, I, I, vp, vp, vp, vp, I, vp, vp],
+            "oref_pform_energy": [vp, vp, I, I, I, vp, vp, vp, vp, vp, I, I, vp, vp, vp, vp,
+                                  vp, D, I, I, I, vp, vp, vp, vp, vp, vp],
         }
         res = {"oref_dot": D, "oref_smachn": D, "oref_banda_csr": I, "oref_datastruc": I,
                "oref_solver": I, "oref_pcg_omp_sample": I, "oref_gform": I,
-               "oref_pform_momentum": I, "oref_pform_pc": I}
+               "oref_pform_momentum": I, "oref_pform_pc": I, "oref_gform_energy": I,
+               "oref_pform_energy": I}
         for name, argt in sig.items():
             f = getattr(L, name)
             f.argtypes = argt
@@ -311,3 +315,40 @@ def divergente(gu1, gu2):
     lib().oref_divergente(_p(div), _p(_c(gu1, np.float64)), _p(_c(gu2, np.float64)),
                           gu1.shape[0])
     return div
+
+
+def gform_energy(m, lib_, pedge, sedge, u, grad):
+    """Green-Gauss gradient of the energy / transported scalar u (gform with
+    lib 3: ideal-gas enthalpy ghost rules, lib 4: transport ghost rules).
+    pedge, sedge: the scalar's (numel, nshared+1) boundary arrays.  grad
+    (numel,2) is read (lib 3 extrapolates with it) and overwritten."""
+    assert grad.flags.c_contiguous and grad.dtype == np.float64
+    rc = lib().oref_gform_energy(
+        _p(_c(m["coor"], np.float64)), _p(_c(m["ix"], np.int32)), m["ix"].shape[1],
+        m["ix"].shape[0], m["nshared"], _p(_c(m["nelcon"], np.int32)), _p(_c(pedge, np.int32)),
+        _p(_c(sedge, np.float64)), _p(_c(m["e"], np.float64)), lib_, _p(_c(u, np.float64)),
+        _p(grad))
+    if rc != 0:
+        raise ValueError("oref_gform_energy: lib must be 3 or 4")
+    return grad
+
+
+def pform_energy(m, lib_, iws, pedge, sedge, u, u0, ro, w, grad, dt, ia, ja, matriz, b,
+                 rescell, ad=None, au=None, bs=False, unsym=True):
+    """Energy / scalar system (cell_e_eb_idg_ggl for lib 3, cell_t_eb_ggl
+    for lib 4): iws 1 assembles (ad, au), b and the cell residual; iws 4
+    writes the time term plus the volume source into b only.  ro (numel,3):
+    densities at levels n-1, n and the current iterate."""
+    numel = m["ix"].shape[0]
+    ad = np.zeros(1) if ad is None else ad
+    au = np.zeros(1) if au is None else au
+    rc = lib().oref_pform_energy(
+        _p(_c(m["coor"], np.float64)), _p(_c(m["ix"], np.int32)), m["ix"].shape[1], numel,
+        m["nshared"], _p(_c(m["nelcon"], np.int32)), _p(_c(m["num"], np.int32)),
+        _p(_c(pedge, np.int32)), _p(_c(sedge, np.float64)), _p(_c(m["e"], np.float64)),
+        lib_, iws, _p(_c(u, np.float64)), _p(_c(u0, np.float64)), _p(_c(ro, np.float64)),
+        _p(_c(w, np.float64)), _p(_c(grad, np.float64)), dt, int(bs), matriz, int(unsym),
+        _p(_c(ia, np.int32)), _p(_c(ja, np.int32)), _p(ad), _p(au), _p(b), _p(rescell))
+    if rc != 0:
+        raise ValueError("oref_pform_energy: lib must be 3 or 4 and iws 1 or 4")
+    return ad, au
