@@ -132,6 +132,9 @@ SIGNATURES = {
     "fvc_cells_gradient": ([C.POINTER(FvcCellMesh), I32, I32, P, P, P], I32),
     "fvc_cells_momentum": ([C.POINTER(FvcCellMesh), I32, I32, P, P, P, P, P, P, F64, I32, F64,
                             I32, I32, P, P, P, P, P, P, P, P, P], I32),
+    "fvc_cells_momentum_ideal_gas": ([C.POINTER(FvcCellMesh), I32, I32, P, P, P, P, P, P, P, P,
+                                      F64, F64, F64, I32, F64, I32, I32, P, P, P, P, P, P, P, P,
+                                      P], I32),
     "fvc_cells_pressure_correction": ([C.POINTER(FvcCellMesh), P, P, P, P, I32, I32, P, P, P, P,
                                        P, P, P], I32),
     "fvc_cells_simple_update": ([I32, P, P, P, P, P, P, P, F64, P], I32),

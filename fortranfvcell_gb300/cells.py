@@ -65,6 +65,18 @@ def momentum(m: CellMesh, comp, iws, u, u0, w, g_own, g_oth, gradp, dt, ia, ja, 
         "fvc_cells_momentum")
 
 
+def momentum_ideal_gas(m: CellMesh, comp, iws, u, u0, w, g_own, g_oth, gradp, ro, div, grav,
+                       dt, ia, ja, matriz, ad, au, b, im, d, rescell, bs=False, under_u=0.7,
+                       simple_c=False) -> None:
+    """Ideal-gas momentum cells (buoyancy): ro (numel, 3) densities, div
+    (numel) divergence, grav = (gx, gy)."""
+    _lib.check(_lib.load().fvc_cells_momentum_ideal_gas(
+        C.byref(m.s), comp, iws, _addr(u), _addr(u0), _addr(w), _addr(g_own), _addr(g_oth),
+        _addr(gradp), _addr(ro), _addr(div), float(grav[0]), float(grav[1]), dt, int(bs),
+        under_u, int(simple_c), matriz, _addr(ia), _addr(ja), _addr(ad), _addr(au), _addr(b),
+        _addr(im), _addr(d), _addr(rescell), _stream()), "fvc_cells_momentum_ideal_gas")
+
+
 def pressure_correction(m: CellMesh, w, d, p, gradp, ia, ja, matriz, ad, au, b, rescell,
                         int_vel=5) -> None:
     _lib.check(_lib.load().fvc_cells_pressure_correction(

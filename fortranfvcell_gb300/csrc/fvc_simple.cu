@@ -3,7 +3,8 @@
 //   gradient   Green-Gauss over ghost / neighbour centroids (src/Pform.f:
 //              466-646 gform; CellibSimple.f:895-926; CellibPressure.f:
 //              577-612), momentum and pressure ghost rules
-//   momentum   cell_si_eb_i_ggl iws1 = 1 (CellibSimple.f:686-894): TVD
+//   momentum   cell_si_eb_i_ggl iws1 = 1 (CellibSimple.f:686-894) and the
+//              ideal-gas cell_si_eb_idg_ggl (CellibSimple.f:54-377): TVD
 //              deferred correction, non-orthogonal correction, transposed
 //              stress, second-order face pressure, under-relaxation, D, iM
 //              and the cell residual; iws1 = 3 (:928-935) the time term
@@ -55,6 +56,10 @@ __device__ __forceinline__ double prop(const Mesh &m, int c, int i) {  // e(i, m
 }
 __device__ __forceinline__ double v2(const double *a, int k, int c) {  // a(k, c), (2, *)
   return a[(k - 1) + 2 * (size_t)(c - 1)];
+}
+
+__device__ __forceinline__ double ro3(const double *ro, int k, int c) {  // ro(k, c), (3, *)
+  return ro[(k - 1) + 3 * (size_t)(c - 1)];
 }
 
 struct Stencil {
@@ -321,10 +326,13 @@ __global__ void gradient_kernel(Mesh m, int kind, int comp, const double *__rest
   grad[2 * (size_t)(nel - 1) + 1] = g2;
 }
 
+// idg = 1 selects the ideal-gas cell cell_si_eb_idg_ggl (CellibSimple.f:
+// 54-377): densities ro(3,*) instead of e(2), the -2/3 mu div(w) terms,
+// buoyancy (ro - e(2)) g A, no fixed-velocity pin
 struct MomArgs {
-  int comp, iws, bs, simple_c, matriz;
-  double dt, under_u;
-  const double *u, *u0, *w, *g_own, *g_oth, *gradp;
+  int comp, iws, bs, simple_c, matriz, idg;
+  double dt, under_u, grav[2];
+  const double *u, *u0, *w, *g_own, *g_oth, *gradp, *ro, *div;
   const int32_t *ia, *ja;
   double *ad, *au, *b, *im, *d, *rescell;
 };
@@ -351,14 +359,17 @@ __global__ void momentum_kernel(Mesh m, MomArgs a) {
   ldl[nsh] = m.num[nel - 1];
   double la[MS + 1];
   for (int i = 0; i <= MS; ++i) la[i] = 0.0;
+  const bool idg = a.idg != 0;
+  const double *ro = a.ro;
   if (a.iws == 3) {
-    double mm = prop(m, nel, 2) * cc * G.area / a.dt;
+    double mm = (idg ? ro3(ro, 2, nel) : prop(m, nel, 2)) * cc * G.area / a.dt;
     double p = mm * uP;
-    mm = prop(m, nel, 2) * cc * G.area / a.dt;
+    mm = (idg ? ro3(ro, 1, nel) : prop(m, nel, 2)) * cc * G.area / a.dt;
     if (a.bs) p = 2 * p - 0.5 * mm * u0[nel - 1];
     assbly(a.ad, a.au, a.b, a.ia, a.ja, la, p, ldl, nsh, a.matriz, true, false);
     return;
   }
+  const double rhoP = idg ? ro3(ro, 3, nel) : rhoA;  // the cell's current density
   double p = 0.0, pf = 0.0, sp = 0.0, cd = 0.0, cvc = 0.0;
   double aa[MS + 1];
   for (int i = 1; i <= ns; ++i) {
@@ -373,6 +384,7 @@ __global__ void momentum_kernel(Mesh m, MomArgs a) {
         p = p + ap * (v2(g_own, comp, nel) * n1 + v2(g_oth, comp, nel) * n2);
       else
         p = p + ap * (v2(g_own, comp, nel) * n2 + v2(g_oth, comp, nel) * n1);
+      if (idg) p = p - (2.0 / 3.0) * ap * a.div[nel - 1] * G.n[comp - 1][i - 1];
       double pface;
       if (pe == 3) {
         pface = sedge(m, 3, i, nel);
@@ -396,7 +408,7 @@ __global__ void momentum_kernel(Mesh m, MomArgs a) {
         const double wfn = v2(w, 1, nel) * n1 + v2(w, 2, nel) * n2;
         if (fabs(wfn) > ZERO) {
           if (wfn > 0.0) {
-            const double cv = rhoA * wfn * meta;
+            const double cv = rhoP * wfn * meta;
             sp = sp + cv;
           } else if (wfn < 0.0) {
             const double cv = rhoA * wfn * meta;
@@ -405,7 +417,7 @@ __global__ void momentum_kernel(Mesh m, MomArgs a) {
         }
       } else if (pe == 4) {
         const double wfn = v2(w, 1, nel) * n1 + v2(w, 2, nel) * n2;
-        const double cv = rhoA * wfn * meta;
+        const double cv = rhoP * wfn * meta;
         sp = sp + cv;
       }
     } else {
@@ -428,7 +440,7 @@ __global__ void momentum_kernel(Mesh m, MomArgs a) {
       cd = kf * meta * (gfn - gfk / nk);
       aa[i - 1] = dfd;
       p = p + cd;
-      const double rof = rhoA;
+      const double rof = idg ? (1.0 - alpha) * ro3(ro, 3, nel) + alpha * ro3(ro, 3, v) : rhoA;
       const double cv = rof * wfn * meta;
       if (cv < 0.0) {
         const double du = uP - u[v - 1] + eps;
@@ -462,16 +474,22 @@ __global__ void momentum_kernel(Mesh m, MomArgs a) {
         p = p + kf * meta * (gf1 * n1 + gf2 * n2);
       else
         p = p + kf * meta * (gf1 * n2 + gf2 * n1);
+      if (idg) {  // -2/3 mu div(w) on the face
+        const double gdiv = (1.0 - alpha) * a.div[nel - 1] + alpha * a.div[v - 1];
+        p = p - (2.0 / 3.0) * kf * gdiv * meta * G.n[comp - 1][i - 1];
+      }
     }
   }
-  if (pedge(m, nsh + 1, nel) == -2) sp = sp + cnst;
+  if (!idg && pedge(m, nsh + 1, nel) == -2) sp = sp + cnst;
   double aP = sp;
   for (int i = 1; i <= ns; ++i) aP = aP + aa[i - 1];
-  double mm = prop(m, nel, 2) * cc * G.area / a.dt;
+  double mm = rhoP * cc * G.area / a.dt;
   if (a.bs) mm = 1.5 * mm;
   aP = aP + mm;
   aP = aP / a.under_u;
   p = p + (1 - a.under_u) * aP * uP;
+  if (idg)  // buoyancy (rho - rho_ref) g A with rho_ref = e(2)
+    p = p + (ro3(ro, 3, nel) - rhoA) * a.grav[comp - 1] * G.area;
   double rm = 0.0, anb = 0.0;
   for (int i = 1; i <= ns; ++i) {
     rm = rm + aa[i - 1] * ((S.viz[i - 1] > 0) ? u[S.viz[i - 1] - 1] : 0.0);
@@ -635,9 +653,6 @@ __device__ __forceinline__ int epedge(const int32_t *pe, int nsh, int i, int c) 
 }
 __device__ __forceinline__ double esedge(const double *se, int nsh, int i, int c) {
   return se[(i - 1) + (size_t)(c - 1) * (nsh + 1)];
-}
-__device__ __forceinline__ double ro3(const double *ro, int k, int c) {  // ro(k, c), (3, *)
-  return ro[(k - 1) + 3 * (size_t)(c - 1)];
 }
 
 __global__ void energy_gradient_kernel(Mesh m, int lib, const int32_t *__restrict__ pe,
@@ -919,6 +934,58 @@ int32_t fvc_cells_momentum(const fvc_cell_mesh *m, int32_t comp, int32_t iws, co
   a.g_own = g_own;
   a.g_oth = g_oth;
   a.gradp = gradp;
+  a.ia = ia;
+  a.ja = ja;
+  a.ad = ad;
+  a.au = au;
+  a.b = b;
+  a.im = im;
+  a.d = d;
+  a.rescell = rescell;
+  a.idg = 0;
+  a.ro = nullptr;
+  a.div = nullptr;
+  a.grav[0] = a.grav[1] = 0.0;
+  cudaStream_t s = (cudaStream_t)stream;
+  fvc::cells::momentum_kernel<<<grid(m->numel), kThreads, 0, s>>>(fvc::cells::view(m), a);
+  fvc::count_launch();
+  return cudaPeekAtLastError() == cudaSuccess ? FVC_OK : FVC_ERR_CUDA;
+}
+
+int32_t fvc_cells_momentum_ideal_gas(const fvc_cell_mesh *m, int32_t comp, int32_t iws,
+                                     const double *u, const double *u0, const double *w,
+                                     const double *g_own, const double *g_oth,
+                                     const double *gradp, const double *ro, const double *div,
+                                     double gx, double gy, double dt, int32_t bs, double under_u,
+                                     int32_t simple_c, int32_t matriz, const int32_t *ia,
+                                     const int32_t *ja, double *ad, double *au, double *b,
+                                     double *im, double *d, double *rescell, void *stream) {
+  if (!fvc::cells::mesh_ok(m) || (comp != 1 && comp != 2) || (iws != 1 && iws != 3) ||
+      (matriz != 1 && matriz != 4) || !u || !b || !ro || dt == 0.0)
+    return FVC_ERR_ARG;
+  if (iws == 1 && (!w || !g_own || !g_oth || !gradp || !div || !ad || !au || !im || !d ||
+                   !rescell || !u0 || (matriz == 1 && (!ia || !ja))))
+    return FVC_ERR_ARG;
+  if (iws == 3 && bs && !u0) return FVC_ERR_ARG;
+  fvc::cells::MomArgs a;
+  a.comp = comp;
+  a.iws = iws;
+  a.bs = bs;
+  a.simple_c = simple_c;
+  a.matriz = matriz;
+  a.idg = 1;
+  a.dt = dt;
+  a.under_u = under_u;
+  a.grav[0] = gx;
+  a.grav[1] = gy;
+  a.u = u;
+  a.u0 = u0;
+  a.w = w;
+  a.g_own = g_own;
+  a.g_oth = g_oth;
+  a.gradp = gradp;
+  a.ro = ro;
+  a.div = div;
   a.ia = ia;
   a.ja = ja;
   a.ad = ad;

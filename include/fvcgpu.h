@@ -302,6 +302,26 @@ int32_t fvc_cells_momentum(const fvc_cell_mesh *m, int32_t comp, int32_t iws,
                            double *au, double *b, double *im, double *d,
                            double *rescell, void *stream);
 
+/* Momentum equation of the ideal-gas cell cell_si_eb_idg_ggl (src/
+ * CellibSimple.f:54-377): the arguments of fvc_cells_momentum plus ro(3,
+ * numel), the densities at levels n-1, n and the current iterate (used
+ * where the incompressible cell takes the material's e(2)), div(numel), the
+ * velocity divergence of the -2/3 mu div(w) terms, and gravity (gx, gy) for
+ * the buoyancy source (ro - e(2)) g A.  There is no fixed-velocity pin
+ * (pedge -2 is ignored); iws 3 takes the time levels from ro rows 1-2. */
+int32_t fvc_cells_momentum_ideal_gas(const fvc_cell_mesh *m, int32_t comp,
+                                     int32_t iws, const double *u,
+                                     const double *u0, const double *w,
+                                     const double *g_own, const double *g_oth,
+                                     const double *gradp, const double *ro,
+                                     const double *div, double gx, double gy,
+                                     double dt, int32_t bs, double under_u,
+                                     int32_t simple_c, int32_t matriz,
+                                     const int32_t *ia, const int32_t *ja,
+                                     double *ad, double *au, double *b,
+                                     double *im, double *d, double *rescell,
+                                     void *stream);
+
 /* Pressure-correction equation with its right-hand side (cell_si_p_i_ggl
  * iws = 1, src/CellibPressure.f:477-572): coefficients, minus the face mass
  * fluxes of cellVel (src/CellibSimple.f:1947-2073; int_vel 1 linear, 2

@@ -175,6 +175,20 @@ void oref_simple_update(double *w, double *pre, const double *u1, const double *
                         int32_t numel, double under_pc);
 void oref_divergente(double *div, const double *gu1, const double *gu2, int32_t numel);
 
+/* Ideal-gas momentum cell cell_si_eb_idg_ggl (src/CellibSimple.f:54-377):
+ * the arguments of oref_pform_momentum plus ro(3,numel) densities, div(numel)
+ * the velocity divergence and grav[2] the gravity vector. */
+int32_t oref_pform_momentum_idg(const double *coor, const int32_t *ix, int32_t ld,
+                                int32_t numel, int32_t nshared, const int32_t *nelcon,
+                                const int32_t *num, const int32_t *pedge, const double *sedge,
+                                const double *e, int32_t comp, int32_t iws, const double *u,
+                                const double *u0, const double *w, const double *g_own,
+                                const double *g_oth, const double *gradp, const double *ro,
+                                const double *div, const double *grav, double dt, int32_t bs,
+                                double under_u, int32_t simple_c, int32_t matriz, int32_t unsym,
+                                const int32_t *ia, const int32_t *ja, double *ad, double *au,
+                                double *b, double *im, double *d, double *rescell);
+
 /* Energy / scalar transport cells (src/CellibTrans.f): lib 3 the ideal-gas
  * enthalpy cell, lib 4 the transport cell.  pedge and sedge here are the
  * scalar's (nshared+1, numel) arrays; ro(3, numel) the densities. */

@@ -13,6 +13,7 @@
  *   areacell (tri / quad)        src/Celllib.f:282-358, :509-522
  *   limit                        src/Celllib.f:370-456
  *   cell_si_eb_i_ggl iws1=1,2,3  src/CellibSimple.f:591-940
+ *   cell_si_eb_idg_ggl iws1=1,3  src/CellibSimple.f:54-377 (ideal gas, buoyancy)
  *   cellVel (intVel 1, 2, 5)     src/CellibSimple.f:1947-2073
  *   cell_si_p_i_ggl iws=1,2      src/CellibPressure.f:390-620
  *   simpleUpdate, divergente     src/Simple.f:871-910, :1070-1078
@@ -286,15 +287,23 @@ int32_t oref_gform(const double *coor, const int32_t *ix, int32_t ld, int32_t nu
 /* Material property k(i) of cell c: e(i, ix(ld, c)). */
 #define PROP(e, ix, ld, c, i) F2(e, 10, i, F2(ix, ld, ld, c))
 
-int32_t oref_pform_momentum(const double *coor, const int32_t *ix, int32_t ld, int32_t numel,
-                            int32_t nshared, const int32_t *nelcon, const int32_t *num,
-                            const int32_t *pedge, const double *sedge, const double *e,
-                            int32_t comp, int32_t iws, const double *u, const double *u0,
-                            const double *w, const double *g_own, const double *g_oth,
-                            const double *gradp, double dt, int32_t bs, double under_u,
-                            int32_t simple_c, int32_t matriz, int32_t unsym, const int32_t *ia,
-                            const int32_t *ja, double *ad, double *au, double *b, double *im,
-                            double *d, double *rescell) {
+/* The momentum cells: cell_si_eb_i_ggl (incompressible, idg = 0) and
+ * cell_si_eb_idg_ggl (ideal gas, idg = 1; CellibSimple.f:54-536).  The
+ * ideal-gas cell takes the density from ro(3,*) (row 3 the current iterate,
+ * rows 1-2 the time levels) wherever the incompressible one uses the
+ * material's e(2), adds the -2/3 mu div(w) terms, the buoyancy source
+ * (ro - e(2)) g A and has no fixed-velocity pin (pedge -2). */
+static int32_t pform_momentum_cells(const double *coor, const int32_t *ix, int32_t ld,
+                                    int32_t numel, int32_t nshared, const int32_t *nelcon,
+                                    const int32_t *num, const int32_t *pedge, const double *sedge,
+                                    const double *e, int32_t comp, int32_t iws, const double *u,
+                                    const double *u0, const double *w, const double *g_own,
+                                    const double *g_oth, const double *gradp, double dt,
+                                    int32_t bs, double under_u, int32_t simple_c, int32_t matriz,
+                                    int32_t unsym, const int32_t *ia, const int32_t *ja,
+                                    double *ad, double *au, double *b, double *im, double *d,
+                                    double *rescell, int32_t idg, const double *ro,
+                                    const double *div, const double *grav) {
   const int32_t ldp = nshared + 1;
   const double ZERO = 1.0e-7, eps = 1.0e-14, cnst = 1.0e60;
   for (int32_t nel = 1; nel <= numel; ++nel) {
@@ -315,13 +324,15 @@ int32_t oref_pform_momentum(const double *coor, const int32_t *ix, int32_t ld, i
     double la[MS + 1];
     for (int32_t i = 0; i <= MS; ++i) la[i] = 0.0;
     if (iws == 3) { /* F = rho cc A/dt u (label 300) */
-      double m = PROP(e, ix, ld, nel, 2) * cc * G.area / dt;
+      double m = (idg ? F2(ro, 3, 2, nel) : PROP(e, ix, ld, nel, 2)) * cc * G.area / dt;
       double p = m * uP;
-      m = PROP(e, ix, ld, nel, 2) * cc * G.area / dt;
+      m = (idg ? F2(ro, 3, 1, nel) : PROP(e, ix, ld, nel, 2)) * cc * G.area / dt;
       if (bs) p = 2 * p - 0.5 * m * F1(u0, nel);
       oref_assbly(ad, au, au, b, ia, ja, la, p, ldl, nshared, matriz, unsym, 1, 0);
       continue;
     }
+    /* ideal gas: the cell's current density (specificMass) */
+    const double rhoP = idg ? F2(ro, 3, 3, nel) : rhoA;
     double p = 0.0, pf = 0.0, sp = 0.0, cd = 0.0, cvc = 0.0;
     double a[MS + 1];
     for (int32_t i = 1; i <= ns; ++i) {
@@ -336,6 +347,7 @@ int32_t oref_pform_momentum(const double *coor, const int32_t *ix, int32_t ld, i
           p = p + ap * (F2(g_own, 2, comp, nel) * n1 + F2(g_oth, 2, comp, nel) * n2);
         else
           p = p + ap * (F2(g_own, 2, comp, nel) * n2 + F2(g_oth, 2, comp, nel) * n1);
+        if (idg) p = p - (2.0 / 3.0) * ap * F1(div, nel) * G.n[comp - 1][i - 1];
         double pface;
         if (pe == 3) {
           pface = F3(sedge, 3, ldp, 3, i, nel);
@@ -360,7 +372,7 @@ int32_t oref_pform_momentum(const double *coor, const int32_t *ix, int32_t ld, i
           const double wfn = F2(w, 2, 1, nel) * n1 + F2(w, 2, 2, nel) * n2;
           if (fabs(wfn) > ZERO) {
             if (wfn > 0.0) {
-              const double cv = rhoA * wfn * meta;
+              const double cv = rhoP * wfn * meta;
               sp = sp + cv;
             } else if (wfn < 0.0) {
               const double cv = rhoA * wfn * meta;
@@ -369,7 +381,7 @@ int32_t oref_pform_momentum(const double *coor, const int32_t *ix, int32_t ld, i
           }
         } else if (pe == 4) {
           const double wfn = F2(w, 2, 1, nel) * n1 + F2(w, 2, 2, nel) * n2;
-          const double cv = rhoA * wfn * meta;
+          const double cv = rhoP * wfn * meta;
           sp = sp + cv;
         }
       } else {
@@ -392,7 +404,8 @@ int32_t oref_pform_momentum(const double *coor, const int32_t *ix, int32_t ld, i
         cd = kf * meta * (gfn - gfk / nk);
         a[i - 1] = dfd;
         p = p + cd;
-        const double rof = rhoA;
+        const double rof =
+            idg ? (1.0 - alpha) * F2(ro, 3, 3, nel) + alpha * F2(ro, 3, 3, v) : rhoA;
         const double cv = rof * wfn * meta;
         if (cv < 0.0) {
           const double du = uP - F1(u, v) + eps;
@@ -428,16 +441,22 @@ int32_t oref_pform_momentum(const double *coor, const int32_t *ix, int32_t ld, i
           p = p + kf * meta * (gf1 * n1 + gf2 * n2);
         else
           p = p + kf * meta * (gf1 * n2 + gf2 * n1);
+        if (idg) { /* -2/3 mu div(w) on the face */
+          const double gdiv = (1.0 - alpha) * F1(div, nel) + alpha * F1(div, v);
+          p = p - (2.0 / 3.0) * kf * gdiv * meta * G.n[comp - 1][i - 1];
+        }
       }
     }
-    if (F2(pedge, ldp, ldp, nel) == -2) sp = sp + cnst;
+    if (!idg && F2(pedge, ldp, ldp, nel) == -2) sp = sp + cnst;
     double aP = sp;
     for (int32_t i = 1; i <= ns; ++i) aP = aP + a[i - 1];
-    double m = PROP(e, ix, ld, nel, 2) * cc * G.area / dt;
+    double m = rhoP * cc * G.area / dt;
     if (bs) m = 1.5 * m;
     aP = aP + m;
     aP = aP / under_u;
     p = p + (1 - under_u) * aP * uP;
+    if (idg) /* buoyancy: (rho - rho_ref) g A, rho_ref = e(2) */
+      p = p + (F2(ro, 3, 3, nel) - rhoA) * grav[comp - 1] * G.area;
     double rm = 0.0, anb = 0.0;
     for (int32_t i = 1; i <= ns; ++i) {
       rm = rm + a[i - 1] * ((S.viz[i - 1] > 0) ? F1(u, S.viz[i - 1]) : 0.0);
@@ -457,6 +476,36 @@ int32_t oref_pform_momentum(const double *coor, const int32_t *ix, int32_t ld, i
     oref_assbly(ad, au, au, b, ia, ja, la, p, ldl, nshared, matriz, unsym, 1, 1);
   }
   return 0;
+}
+
+int32_t oref_pform_momentum(const double *coor, const int32_t *ix, int32_t ld, int32_t numel,
+                            int32_t nshared, const int32_t *nelcon, const int32_t *num,
+                            const int32_t *pedge, const double *sedge, const double *e,
+                            int32_t comp, int32_t iws, const double *u, const double *u0,
+                            const double *w, const double *g_own, const double *g_oth,
+                            const double *gradp, double dt, int32_t bs, double under_u,
+                            int32_t simple_c, int32_t matriz, int32_t unsym, const int32_t *ia,
+                            const int32_t *ja, double *ad, double *au, double *b, double *im,
+                            double *d, double *rescell) {
+  return pform_momentum_cells(coor, ix, ld, numel, nshared, nelcon, num, pedge, sedge, e, comp,
+                              iws, u, u0, w, g_own, g_oth, gradp, dt, bs, under_u, simple_c,
+                              matriz, unsym, ia, ja, ad, au, b, im, d, rescell, 0, NULL, NULL,
+                              NULL);
+}
+
+int32_t oref_pform_momentum_idg(const double *coor, const int32_t *ix, int32_t ld,
+                                int32_t numel, int32_t nshared, const int32_t *nelcon,
+                                const int32_t *num, const int32_t *pedge, const double *sedge,
+                                const double *e, int32_t comp, int32_t iws, const double *u,
+                                const double *u0, const double *w, const double *g_own,
+                                const double *g_oth, const double *gradp, const double *ro,
+                                const double *div, const double *grav, double dt, int32_t bs,
+                                double under_u, int32_t simple_c, int32_t matriz, int32_t unsym,
+                                const int32_t *ia, const int32_t *ja, double *ad, double *au,
+                                double *b, double *im, double *d, double *rescell) {
+  return pform_momentum_cells(coor, ix, ld, numel, nshared, nelcon, num, pedge, sedge, e, comp,
+                              iws, u, u0, w, g_own, g_oth, gradp, dt, bs, under_u, simple_c,
+                              matriz, unsym, ia, ja, ad, au, b, im, d, rescell, 1, ro, div, grav);
 }
 
 /* cellVel (CellibSimple.f:1947-2073): face flux w_f.n |f| for intVel 1, 2, 5.

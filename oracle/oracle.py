@@ -84,13 +84,16 @@ def lib():
             "oref_simple_update": [vp, vp, vp, vp, vp, vp, vp, I, D],
             "oref_divergente": [vp, vp, vp, I],
             "oref_gform_energy": [vp, vp, I, I, I, vp, vp, vp, vp, I, vp, vp],
+            "oref_pform_momentum_idg": [vp, vp, I, I, I, vp, vp, vp, vp, vp, I, I, vp, vp, vp,
+                                        vp, vp, vp, vp, vp, vp, D, I, D, I, I, I, vp, vp, vp,
+                                        vp, vp, vp, vp, vp],
             "oref_pform_energy": [vp, vp, I, I, I, vp, vp, vp, vp, vp, I, I, vp, vp, vp, vp,
                                   vp, D, I, I, I, vp, vp, vp, vp, vp, vp],
         }
         res = {"oref_dot": D, "oref_smachn": D, "oref_banda_csr": I, "oref_datastruc": I,
                "oref_solver": I, "oref_pcg_omp_sample": I, "oref_gform": I,
                "oref_pform_momentum": I, "oref_pform_pc": I, "oref_gform_energy": I,
-               "oref_pform_energy": I}
+               "oref_pform_energy": I, "oref_pform_momentum_idg": I}
         for name, argt in sig.items():
             f = getattr(L, name)
             f.argtypes = argt
@@ -285,6 +288,28 @@ def pform_momentum(m, comp, iws, u, u0, w, g_own, g_oth, gradp, dt, ia, ja, matr
         _p(_c(ja, np.int32)), _p(ad), _p(au), _p(b), _p(im), _p(d), _p(rescell))
     if rc != 0:
         raise ValueError("oref_pform_momentum failed")
+    return ad, au
+
+
+def pform_momentum_idg(m, comp, iws, u, u0, w, g_own, g_oth, gradp, ro, div, grav, dt, ia, ja,
+                       matriz, b, im, d, rescell, ad=None, au=None, bs=False, under_u=0.7,
+                       simple_c=False, unsym=True):
+    """Ideal-gas momentum system (cell_si_eb_idg_ggl): as pform_momentum with
+    the densities ro (numel,3), the divergence div (numel) and gravity (2,)."""
+    numel = m["ix"].shape[0]
+    ad = np.zeros(1) if ad is None else ad
+    au = np.zeros(1) if au is None else au
+    rc = lib().oref_pform_momentum_idg(
+        _p(_c(m["coor"], np.float64)), _p(_c(m["ix"], np.int32)), m["ix"].shape[1], numel,
+        m["nshared"], _p(_c(m["nelcon"], np.int32)), _p(_c(m["num"], np.int32)),
+        _p(_c(m["pedge"], np.int32)), _p(_c(m["sedge"], np.float64)), _p(_c(m["e"], np.float64)),
+        comp, iws, _p(_c(u, np.float64)), _p(_c(u0, np.float64)), _p(_c(w, np.float64)),
+        _p(_c(g_own, np.float64)), _p(_c(g_oth, np.float64)), _p(_c(gradp, np.float64)),
+        _p(_c(ro, np.float64)), _p(_c(div, np.float64)), _p(_c(grav, np.float64)), dt, int(bs),
+        under_u, int(simple_c), matriz, int(unsym), _p(_c(ia, np.int32)), _p(_c(ja, np.int32)),
+        _p(ad), _p(au), _p(b), _p(im), _p(d), _p(rescell))
+    if rc != 0:
+        raise ValueError("oref_pform_momentum_idg failed")
     return ad, au
 
 

@@ -103,6 +103,49 @@ def test_momentum_bit_exact(orc, kind, nx, seed, matriz):
             assert np.array_equal(host(tb), b), (comp, bs)
 
 
+@pytest.mark.parametrize("kind,nx,seed,matriz", [("quad", 9, 14, 4), ("tri", 7, 15, 1),
+                                                 ("mixed", 8, 16, 1), ("mixed", 8, 17, 4)])
+def test_momentum_ideal_gas_bit_exact(orc, kind, nx, seed, matriz):
+    from fortranfvcell_gb300 import cells
+    case, rng = random_case(orc, kind, nx, seed)
+    n = case["numel"]
+    f = fields(rng, n)
+    ro = rng.uniform(0.8, 1.4, (n, 3))
+    div = rng.uniform(-0.5, 0.5, n)
+    grav = np.array([0.3, -9.81])
+    ia, ja, _ = orc.datastruc(case["ident"], matriz, True)
+    m = mesh_on_gpu(case)
+    ia_d, ja_d = dev(ia, np.int32), dev(ja.ravel(), np.int32)
+    for comp in (1, 2):
+        u = f["u1"] if comp == 1 else f["u2"]
+        g_own, g_oth = (f["g1"], f["g2"]) if comp == 1 else (f["g2"], f["g1"])
+        for simple_c, bs in ((False, False), (True, True)):
+            ad, au = np.zeros(n), np.zeros(ja.size)
+            b, im, d, rc = np.zeros(n), np.zeros((n, 4)), f["d"].copy(), np.zeros(n)
+            orc.pform_momentum_idg(case, comp, 1, u, f["p"], f["w"], g_own, g_oth, f["gp"], ro,
+                                   div, grav, 0.37, ia, ja, matriz, b, im, d, rc, ad=ad, au=au,
+                                   under_u=0.7, simple_c=simple_c, bs=bs)
+            t = {k: dev(v) for k, v in dict(ad=np.zeros(n), au=np.zeros(ja.size), b=np.zeros(n),
+                                              im=np.zeros((n, 4)), d=f["d"].copy(),
+                                              rc=np.zeros(n)).items()}
+            cells.momentum_ideal_gas(m, comp, 1, dev(u), dev(f["p"]), dev(f["w"]), dev(g_own),
+                                     dev(g_oth), dev(f["gp"]), dev(ro), dev(div), grav, 0.37,
+                                     ia_d, ja_d, matriz, t["ad"], t["au"], t["b"], t["im"],
+                                     t["d"], t["rc"], under_u=0.7, simple_c=simple_c, bs=bs)
+            for k, ref in (("ad", ad), ("au", au), ("b", b), ("im", im), ("d", d), ("rc", rc)):
+                assert np.array_equal(host(t[k]), ref), (comp, simple_c, k)
+        for bs in (False, True):    # time term from the densities of levels n-1, n
+            b = np.zeros(n)
+            orc.pform_momentum_idg(case, comp, 3, u, f["u2"], f["w"], g_own, g_oth, f["gp"], ro,
+                                   div, grav, 0.37, ia, ja, matriz, b, np.zeros((n, 4)),
+                                   np.zeros((n, 2)), np.zeros(n), bs=bs)
+            tb = dev(np.zeros(n))
+            cells.momentum_ideal_gas(m, comp, 3, dev(u), dev(f["u2"]), None, None, None, None,
+                                     dev(ro), None, grav, 0.37, ia_d, ja_d, matriz, None, None,
+                                     tb, None, None, None, bs=bs)
+            assert np.array_equal(host(tb), b), (comp, bs)
+
+
 @pytest.mark.parametrize("kind,nx,seed,matriz", [("quad", 9, 8, 1), ("quad", 9, 9, 4),
                                                  ("tri", 7, 10, 1), ("mixed", 8, 11, 1)])
 def test_pressure_correction_bit_exact(orc, kind, nx, seed, matriz):

@@ -59,3 +59,55 @@ def test_product_cavity_builder_matches_oracle_chain(orc):
         b = lid_driven_cavity(nx, kind=kind, jitter=jit)
         for k in ("coor", "ix", "nelcon", "num", "ident", "pedge", "sedge", "e"):
             assert np.array_equal(a[k], b[k]), (kind, k)
+
+
+def test_ideal_gas_momentum_hydrostatic_rest(orc):
+    # at rest with a uniform density rho != rho_ref and the hydrostatic
+    # pressure p = (rho - rho_ref) g . x, buoyancy balances the pressure
+    # force in every cell (second-order face pressure is exact for a linear p)
+    case = cavity(orc, 10)
+    case["sedge"][:] = 0.0                  # fixed walls all round (no lid)
+    n = case["numel"]
+    m = case["mesh"]
+    xc = m.coor[m.ix - 1].mean(axis=1)
+    rho_ref = case["e"][0, 1]
+    rho = 1.3 * rho_ref
+    grav = np.array([0.0, -9.81])
+    p = (rho - rho_ref) * (xc @ grav)
+    gp = np.tile((rho - rho_ref) * grav, (n, 1))
+    ro = np.full((n, 3), rho)
+    ia, ja, _ = orc.datastruc(case["ident"], 1, True)
+    z2 = np.zeros((n, 2))
+    for comp in (1, 2):
+        b, rc = np.zeros(n), np.zeros(n)
+        orc.pform_momentum_idg(case, comp, 1, np.zeros(n), p, z2, z2, z2, gp, ro, np.zeros(n),
+                               grav, 1e10, ia, ja, 1, b, np.zeros((n, 4)), z2.copy(), rc,
+                               ad=np.zeros(n), au=np.zeros(ja.size))
+        scale = abs(rho - rho_ref) * 9.81 / n
+        assert np.abs(b).max() < 1e-12 * scale * n and np.abs(rc).max() < 1e-12 * scale * n
+
+
+def test_ideal_gas_momentum_reduces_to_incompressible(orc):
+    # constant density equal to e(2), no divergence, no gravity: the ideal-gas
+    # cell gives the incompressible cell's system (up to the rounding of the
+    # interpolated face density)
+    case = cavity(orc, 9, kind="mixed", jitter=0.2)
+    n = case["numel"]
+    rng = np.random.default_rng(11)
+    w, gu, gv, gp = (rng.uniform(-1, 1, (n, 2)) for _ in range(4))
+    u, p = rng.uniform(-1, 1, n), rng.uniform(-1, 1, n)
+    ro = np.full((n, 3), case["e"][0, 1])
+    ia, ja, _ = orc.datastruc(case["ident"], 1, True)
+    out = []
+    for idg in (False, True):
+        ad, au, b = np.zeros(n), np.zeros(ja.size), np.zeros(n)
+        im, d, rc = np.zeros((n, 4)), np.zeros((n, 2)), np.zeros(n)
+        if idg:
+            orc.pform_momentum_idg(case, 1, 1, u, p, w, gu, gv, gp, ro, np.zeros(n),
+                                   np.zeros(2), 0.2, ia, ja, 1, b, im, d, rc, ad=ad, au=au)
+        else:
+            orc.pform_momentum(case, 1, 1, u, p, w, gu, gv, gp, 0.2, ia, ja, 1, b, im, d, rc,
+                               ad=ad, au=au)
+        out.append((ad, au, b, im, d, rc))
+    for x, y in zip(*out):
+        np.testing.assert_allclose(y, x, rtol=1e-12, atol=1e-14 * np.abs(x).max())
