@@ -37,6 +37,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 TOL = 1e-8
+C4_TOL = 1e-8
 NX_DEFAULT = 1672
 L2_BYTES = 129 * 1024 * 1024
 
@@ -361,6 +362,8 @@ def run_ours(args):
     }
     if rank == 0 and not args.no_simple:
         line["simple_c1"] = run_simple_c1(args)
+    if rank == 0 and args.c4_cases > 0:
+        line["batched_c4"] = run_batched_c4(args)
     return line
 
 
@@ -405,6 +408,114 @@ def run_simple_c1(args):
         out["cpu_port_s"] = round(cpu_s, 4)
         out["cpu_kind"] = "port (restated reference, sequential solvers, 1 core)"
         out["max_abs_w_difference"] = float(f"{np.abs(w - ref.w).max():.2e}")
+    return out
+
+
+def c4_sides(ncases, seed=7):
+    """Mesh sides of the batched workload: N = round(exp U[ln 32, ln 256])."""
+    rng = np.random.default_rng(seed)
+    return np.rint(np.exp(rng.uniform(np.log(32.0), np.log(256.0), ncases))).astype(int)
+
+
+def run_batched_c4(args):
+    """The C4 configuration, pressure-correction field: ncases independent
+    p' systems of lid-driven cavities on N x N quads (N log-uniform in
+    [32, 256], seed 7; cell 1 pinned; b ~ U[-1,1], seed 1000+k), Jacobi-PCG
+    with the reference's stopping test at tol 1e-8 from x = 0.
+    GPU batched: one persistent launch for all systems (fvc_solve_batched),
+    CUDA-event time.  GPU sequential: the same systems one fvc_solve at a
+    time (matrices already on the device).  CPU: the restated OpenMP PCG
+    (pcg_omp) on whole systems of a seeded sample, extrapolated by
+    rows x iterations."""
+    import torch
+    from fortranfvcell_gb300 import Context, make_opts, mesh, pack_block_diagonal
+    sides = c4_sides(args.c4_cases)
+    t0 = time.time()
+    systems = []
+    for k, nside in enumerate(sides):
+        s = mesh.pressure_system(mesh.square_mesh(int(nside), kind="quad"), matriz=1,
+                                 unsym=True, pin_cell=1)
+        systems.append(dict(ad=s.ad, au=s.au, ia=s.ia, ja=s.ja, n=s.neq, nad=s.nad,
+                            b=np.random.default_rng(1000 + k).uniform(-1.0, 1.0, s.neq)))
+    pk = pack_block_diagonal(systems)
+    rows = int(sum(s["n"] for s in systems))
+    log(f"C4 setup: {len(systems)} systems, {rows} rows, {time.time() - t0:.1f} s")
+    opts = make_opts("fp64", init=1, block_threads=getattr(args, "c4_threads", 0))
+    stream = torch.cuda.Stream()
+    ctx = Context(device=0, stream=stream)
+    ctx.set_matrix(1, True, pk["neq"], pk["nad"], pk["ad"], pk["au"], pk["au"], pk["ia"],
+                   pk["ja"])
+    b = np.zeros(pk["neq"])
+    for s, r in zip(systems, pk["rows"]):
+        b[r] = s["b"]
+    bd = torch.from_numpy(b).cuda()
+    xd = torch.zeros(pk["neq"], dtype=torch.float64, device="cuda")
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            ctx.solve_batched(pk["row_start"], bd, xd, C4_TOL, 50000, opts)
+        runs = [ctx.solve_batched(pk["row_start"], bd, xd, C4_TOL, 50000, opts)[1]
+                for _ in range(max(1, min(args.steps, 3)))]
+    batch_ms = min(st[0].solve_ms for st in runs)
+    its = np.array([t.iterations for t in runs[-1]])
+    worst_rel = max(t.rel_residual for t in runs[-1])
+    ctx.close()
+    if getattr(args, "c4_batched_only", False):
+        return {"batched_ms": round(batch_ms, 3), "iterations_max": int(its.max())}
+    # the same systems one solve at a time
+    opts = make_opts("fp64", init=1)
+    ctxs = []
+    for s in systems:
+        c = Context(device=0, stream=stream)
+        c.set_matrix(1, True, s["n"], s["nad"], s["ad"], s["au"], s["au"], s["ia"], s["ja"])
+        ctxs.append((c, torch.from_numpy(s["b"]).cuda(),
+                     torch.zeros(s["n"], dtype=torch.float64, device="cuda")))
+    with torch.cuda.stream(stream):
+        for c, sb, sx in ctxs[:8]:
+            c.solve(1, sb, sx, C4_TOL, 50000, opts)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        seq_kernel_ms = sum(c.solve(1, sb, sx, C4_TOL, 50000, opts).solve_ms
+                            for c, sb, sx in ctxs)
+        torch.cuda.synchronize()
+        seq_wall_ms = (time.perf_counter() - t1) * 1e3
+    for c, _, _ in ctxs:
+        c.close()
+    out = {"workload": f"{len(systems)} p' systems of N x N quad cavities, N = round(exp "
+                       f"U[ln 32, ln 256]) seed 7 ({int(sides.min())}..{int(sides.max())}), "
+                       f"{rows} rows in all, Jacobi-PCG, reference stopping test, tol {C4_TOL:g}",
+           "batched_ms": round(batch_ms, 3),
+           "systems_per_s": round(len(systems) / (batch_ms * 1e-3), 2),
+           "sequential_gpu_kernel_ms": round(seq_kernel_ms, 3),
+           "sequential_gpu_wall_ms": round(seq_wall_ms, 3),
+           "batched_over_sequential": round(seq_kernel_ms / batch_ms, 2),
+           "iterations": {"min": int(its.min()), "median": int(np.median(its)),
+                          "max": int(its.max())},
+           "worst_rel_residual_fp64": float(f"{worst_rel:.3e}")}
+    if not args.no_cpu:
+        from oracle import oracle
+        threads = os.cpu_count() or 1
+        order = np.random.default_rng(3).permutation(len(systems))
+        done, el = 0.0, 0.0
+        for k in order:
+            s = systems[k]
+            x = np.zeros(s["n"])
+            t1 = time.perf_counter()
+            oracle.pcg_omp_sample(s["ad"], s["au"], x, s["b"].copy(), s["ia"], s["ja"], s["n"],
+                                  s["nad"], C4_TOL, 50000, 1, threads)
+            el += time.perf_counter() - t1
+            done += s["n"] * its[k]
+            if el > args.cpu_seconds:
+                break
+        total = float((its * np.array([s["n"] for s in systems])).sum())
+        cpu_s = total / (done / el)
+        out["cpu_port_s"] = round(cpu_s, 3)
+        if done >= total:
+            out["cpu_kind"] = (f"port: pcg_omp on {threads} host threads, every system of the "
+                               f"batch solved in turn ({el:.1f} s)")
+        else:
+            out["cpu_kind"] = (f"port: pcg_omp on {threads} host threads, whole systems of a "
+                               f"seeded sample ({el:.1f} s), extrapolated by rows x iterations")
+        out["batched_over_cpu"] = round(cpu_s / (batch_ms * 1e-3), 1)
     return out
 
 
@@ -522,6 +633,8 @@ def main():
     ap.add_argument("--no-simple", action="store_true", help="skip the C1 SIMPLE leg")
     ap.add_argument("--simple-nx", type=int, default=64)
     ap.add_argument("--simple-its", type=int, default=200)
+    ap.add_argument("--c4-cases", type=int, default=256,
+                    help="batched C4 leg: number of systems (0 skips it)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--ref-sample-its", type=int, default=300)
     ap.add_argument("--profile-its", type=int, default=0,

@@ -114,6 +114,7 @@ SIGNATURES = {
     "fvc_matrix_set": ([P, I32, I32, I32, I32, P, P, P, P, P], I32),
     "fvc_matrix_update_values": ([P, P, P, P], I32),
     "fvc_solve": ([P, I32, P, P, F64, I32, C.POINTER(FvcOpts), C.POINTER(FvcStats)], I32),
+    "fvc_solve_batched": ([P, I32, P, P, P, F64, I32, C.POINTER(FvcOpts), P], I32),
     "fvc_spmv": ([P, P, P], I32),
     "fvc_spmv_fast": ([P, P, P], I32),
     "fvc_spmv_f32": ([P, P, P], I32),

@@ -476,6 +476,23 @@ int32_t fvc_solve(fvc_context *c, int32_t code, const double *d_b, double *d_x, 
   return rc;
 }
 
+int32_t fvc_solve_batched(fvc_context *c, int32_t nsys, const int32_t *row_start,
+                          const double *d_b, double *d_x, double tol, int32_t maxit,
+                          const fvc_opts *opts, fvc_stats *st) {
+  if (!c || !c->has_matrix || !d_b || !d_x || maxit < 1 || nsys < 1 || !row_start)
+    return FVC_ERR_ARG;
+  fvc_opts o;
+  if (opts)
+    o = *opts;
+  else
+    fvc_opts_default(&o);
+  if (o.precision != FVC_PREC_FP64) return FVC_ERR_UNSUPPORTED;
+  cudaSetDevice(c->device);
+  const int init = (o.init < 0) ? default_init(1, c->matriz) : (o.init ? 1 : 0);
+  return fvc::run_pcg_batched(c->A, c->S, nsys, row_start, d_b, d_x, tol, maxit, init, o,
+                              c->stream, st);
+}
+
 }  // extern "C"
 
 namespace {

@@ -43,7 +43,8 @@ struct GridSync {
   int *err;                // sticky error (FVC_ERR_TIMEOUT on a stuck wait)
   double *partials;        // 4 slots x kMaxNV x nblocks
   double *totals;          // 4 slots x kMaxNV
-  unsigned int nblocks;
+  unsigned int nblocks;    // blocks that synchronise through this state
+  unsigned int base;       // blockIdx.x of the first of them (0 for a whole grid)
 };
 
 constexpr int kMaxNV = 4;
@@ -137,7 +138,7 @@ __device__ __forceinline__ bool grid_allreduce(const GridSync &gs, unsigned int 
   double *tot = gs.totals + (ep & 3u) * kMaxNV;
   if (threadIdx.x == 0) {
 #pragma unroll
-    for (int q = 0; q < NV; ++q) part[(size_t)q * nb + blockIdx.x] = v[q];
+    for (int q = 0; q < NV; ++q) part[(size_t)q * nb + (blockIdx.x - gs.base)] = v[q];
     const unsigned int old = atom_add_acq_rel(gs.count, 1u);
     s_last = (old == ep * nb - 1u);
     s_ok = 1;
@@ -230,7 +231,7 @@ __device__ __forceinline__ bool grid_allreduce_d(const GridSync &gs, unsigned in
     } else {
       if (lane == 0) {
 #pragma unroll
-        for (int q = 0; q < NV; ++q) part[(size_t)q * nb + blockIdx.x] = bsum[q];
+        for (int q = 0; q < NV; ++q) part[(size_t)q * nb + (blockIdx.x - gs.base)] = bsum[q];
         red_add_release(gs.count, 1u);
         const unsigned int target = ep * nb;
         const uint64_t t0 = global_ns();
@@ -414,6 +415,7 @@ inline GridSync make_sync(const Scratch &S, int nblocks) {
   g.partials = S.partials;
   g.totals = S.partials + 4 * kMaxNV * (size_t)nblocks;
   g.nblocks = (unsigned int)nblocks;
+  g.base = 0;
   return g;
 }
 

@@ -77,6 +77,10 @@ int32_t run_bicgstab(const DeviceMatrix &A, Scratch &S, const double *b,
 int32_t run_gmres(const DeviceMatrix &A, Scratch &S, const double *b, double *x,
                   double tol, int maxit, const fvc_opts &o, cudaStream_t stream,
                   fvc_stats *st);
+int32_t run_pcg_batched(const DeviceMatrix &A, Scratch &S, int nsys,
+                        const int32_t *row_start, const double *b, double *x,
+                        double tol, int maxit, int init, const fvc_opts &o,
+                        cudaStream_t stream, fvc_stats *st);
 int32_t run_mixed(const DeviceMatrix &A, Scratch &S, int code, const double *b,
                   double *x, double tol, int maxit, int init, const fvc_opts &o,
                   cudaStream_t stream, fvc_stats *st);

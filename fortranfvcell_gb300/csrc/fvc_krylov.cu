@@ -20,8 +20,10 @@
 // roughly halve the FP64 instructions per row; they move results only at
 // rounding level, like the dot products, which are tree sums in a fixed
 // (deterministic) order instead of the reference's sequential sums.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstring>
 #include <vector>
 
 #include "fvc_device.cuh"
@@ -60,6 +62,17 @@ struct Part {
     se = min(nslices, sb + spb);
     n = nrows;
   }
+  // slices [s0, s1) of one system of a batch, shared by nb blocks; this
+  // block is the rank-th of them
+  __device__ Part(int s0, int s1, int nrows, int rank, int nb) {
+    lane = threadIdx.x & 31;
+    warp = threadIdx.x >> 5;
+    nwarps = blockDim.x >> 5;
+    const int spb = (s1 - s0 + nb - 1) / nb;
+    sb = s0 + rank * spb;
+    se = min(s1, sb + spb);
+    n = nrows;
+  }
 };
 
 #define FOR_ROWS(P)                                          \
@@ -72,22 +85,28 @@ __device__ __forceinline__ bool reduce(const KArgs &a, unsigned int &ep, double 
   return grid_allreduce<NV>(a.gs, ep, v, red);
 }
 
-__device__ __forceinline__ void finish(const KArgs &a, int iters, int status,
-                                       double conv, double crit, int inner) {
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    a.iresult[0] = iters;
-    a.iresult[1] = status;
-    a.iresult[2] = inner;
-    a.result[1] = conv;
-    a.result[2] = crit;
+__device__ __forceinline__ void finish_to(double *result, int *iresult, bool lead, int iters,
+                                          int status, double conv, double crit, int inner) {
+  if (lead && threadIdx.x == 0) {
+    iresult[0] = iters;
+    iresult[1] = status;
+    iresult[2] = inner;
+    result[1] = conv;
+    result[2] = crit;
   }
 }
 
+__device__ __forceinline__ void finish(const KArgs &a, int iters, int status,
+                                       double conv, double crit, int inner) {
+  finish_to(a.result, a.iresult, blockIdx.x == 0, iters, status, conv, crit, inner);
+}
+
 // Energy norm x.Ax and the FP64 residual ||b-Ax||^2, ||b||^2 in one pass
-// (x must be complete at every row: called right after a grid barrier).
-__device__ __forceinline__ bool epilogue(const KArgs &a, unsigned int &ep, double *red,
-                                         bool energy_xb) {
-  const Part P(a.A.nslices, a.A.n);
+// over the rows of P (x must be complete at every row: called right after
+// a synchronisation of gs); the lead block writes result[0, 3, 4].
+__device__ __forceinline__ bool epilogue_to(const KArgs &a, const Part &P, const GridSync &gs,
+                                            double *result, bool lead, unsigned int &ep,
+                                            double *red, bool energy_xb) {
   double acc[3] = {0.0, 0.0, 0.0};
   const double *x = a.x;
   FOR_ROWS(P) {
@@ -98,20 +117,30 @@ __device__ __forceinline__ bool epilogue(const KArgs &a, unsigned int &ep, doubl
     acc[1] = fma(rr, rr, acc[1]);
     acc[2] = fma(bi, bi, acc[2]);
   }
-  if (!reduce<3>(a, ep, acc, red)) return false;
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    a.result[0] = acc[0];
-    a.result[3] = acc[1];
-    a.result[4] = acc[2];
+  if (!grid_allreduce<3>(gs, ep, acc, red)) return false;
+  if (lead && threadIdx.x == 0) {
+    result[0] = acc[0];
+    result[3] = acc[1];
+    result[4] = acc[2];
   }
   return true;
+}
+
+__device__ __forceinline__ bool epilogue(const KArgs &a, unsigned int &ep, double *red,
+                                         bool energy_xb) {
+  return epilogue_to(a, Part(a.A.nslices, a.A.n), a.gs, a.result, blockIdx.x == 0, ep, red,
+                     energy_xb);
 }
 
 // ---------------------------------------------------------------------
 // PCG (Iterativos.f:29-106).  v0 = r, v1 = z, v2/v3 = p (double buffer),
 // v4 = q (the reference's z = A p).
 // ---------------------------------------------------------------------
-__global__ void __launch_bounds__(1024, 1) pcg_f64(KArgs a) {
+// The iteration over the rows of P, synchronising through gs; the lead
+// block writes result / iresult.  pcg_f64 runs it over the whole matrix,
+// pcg_batched over one system of a batch per group of blocks.
+__device__ __forceinline__ void pcg_run(const KArgs &a, const Part &P, const GridSync &gs,
+                                        double *result, int *iresult, bool lead) {
   __shared__ double red[kMaxNV * 32];
   __shared__ double buf[2 * 1024];
   // scalars of the recurrence, updated by lane 0 of warp 0 inside the
@@ -120,7 +149,6 @@ __global__ void __launch_bounds__(1024, 1) pcg_f64(KArgs a) {
     double d, alpha, beta, conv, crit;
     int stop;  // 0 go on, 1 converged, 2 NaN/Inf
   } sh;
-  const Part P(a.A.nslices, a.A.n);
   double *r = a.v0, *z = a.v1, *q = a.v4, *x = a.x;
   const double *minv = a.minv, *b = a.b;
   const bool rule0 = a.stop_rule == 0;
@@ -143,7 +171,7 @@ __global__ void __launch_bounds__(1024, 1) pcg_f64(KArgs a) {
     acc[0] = fma(ri, zi, acc[0]);
     acc[1] = fma(b[row], b[row], acc[1]);
   }
-  if (!grid_allreduce_d<2>(a.gs, ep, acc, buf, [&](const double *t) {
+  if (!grid_allreduce_d<2>(gs, ep, acc, buf, [&](const double *t) {
         sh.d = t[0];
         sh.conv = rule0 ? a.tol * sqrt(fabs(t[0])) : a.tol * sqrt(t[1]);
         sh.beta = 0.0;
@@ -176,7 +204,7 @@ __global__ void __launch_bounds__(1024, 1) pcg_f64(KArgs a) {
         pq[0] = fma(pi, qi, pq[0]);
       }
     }
-    if (!grid_allreduce_d<1>(a.gs, ep, pq, buf,
+    if (!grid_allreduce_d<1>(gs, ep, pq, buf,
                              [&](const double *t) { sh.alpha = sh.d / t[0]; }))
       return;
     const double alpha = sh.alpha;
@@ -202,8 +230,8 @@ __global__ void __launch_bounds__(1024, 1) pcg_f64(KArgs a) {
       sh.crit = rule0 ? sqrt(fabs(sh.d)) : sqrt(t[1]);
       sh.stop = (!(sh.crit == sh.crit) || isinf(sh.d)) ? 2 : (sh.crit < sh.conv ? 1 : 0);
     };
-    const bool ok = rule0 ? grid_allreduce_d<1>(a.gs, ep, rz, buf, step)
-                          : grid_allreduce_d<2>(a.gs, ep, rr2, buf, step);
+    const bool ok = rule0 ? grid_allreduce_d<1>(gs, ep, rz, buf, step)
+                          : grid_allreduce_d<2>(gs, ep, rr2, buf, step);
     if (!ok) return;
     if (sh.stop == 2) {
       status = FVC_ERR_NAN;
@@ -218,9 +246,37 @@ __global__ void __launch_bounds__(1024, 1) pcg_f64(KArgs a) {
     j = a.maxit;
     status = FVC_ERR_NOCONV;
   }
-  finish(a, j, status, sh.conv, sh.crit, 0);
-  epilogue(a, ep, red, false);
+  finish_to(result, iresult, lead, j, status, sh.conv, sh.crit, 0);
+  epilogue_to(a, P, gs, result, lead, ep, red, false);
 }
+
+__global__ void __launch_bounds__(1024, 1) pcg_f64(KArgs a) {
+  pcg_run(a, Part(a.A.nslices, a.A.n), a.gs, a.result, a.iresult, blockIdx.x == 0);
+}
+
+// One system of a batch: its slices, its synchronisation state (counter,
+// partials, nblocks and first block) and its result slots.
+struct BatchSys {
+  int s0, s1;
+  GridSync gs;
+  double *result;
+  int *iresult;
+};
+
+// Batched PCG: the matrix is block diagonal, each system starting at a
+// slice boundary; every block belongs to one system (sys_of_block) and
+// synchronises only with that system's blocks, so each system iterates and
+// stops on its own inside one cooperative launch.
+__global__ void __launch_bounds__(1024, 1) pcg_batched(KArgs a, const BatchSys *__restrict__ sys,
+                                                        const int *__restrict__ sys_of_block) {
+  const BatchSys d = sys[sys_of_block[blockIdx.x]];
+  const int rank = (int)(blockIdx.x - d.gs.base);
+  pcg_run(a, Part(d.s0, d.s1, a.A.n, rank, (int)d.gs.nblocks), d.gs, d.result, d.iresult,
+          rank == 0);
+}
+
+// ---------------------------------------------------------------------
+
 
 // ---------------------------------------------------------------------
 // BiCGSTAB (Iterativos.f:140-234) in three grid synchronisations per
@@ -709,6 +765,200 @@ int32_t run_bicgstab(const DeviceMatrix &A, Scratch &S, const double *b, double 
 int32_t run_gmres(const DeviceMatrix &A, Scratch &S, const double *b, double *x, double tol,
                   int maxit, const fvc_opts &o, cudaStream_t stream, fvc_stats *st) {
   return run_persistent(gmres_f64, A, S, b, x, tol, maxit, 1, o, stream, st, 0, true);
+}
+
+int32_t run_pcg_batched(const DeviceMatrix &A, Scratch &S, int nsys, const int32_t *row_start,
+                        const double *b, double *x, double tol, int maxit, int init,
+                        const fvc_opts &o, cudaStream_t stream, fvc_stats *st) {
+  if (nsys < 1 || !row_start || row_start[0] != 0 || row_start[nsys] != A.n) return FVC_ERR_ARG;
+  for (int s = 0; s < nsys; ++s)
+    if (row_start[s] % 32 != 0 || row_start[s + 1] <= row_start[s]) return FVC_ERR_ARG;
+  // 128-thread blocks by default: twice the co-resident blocks of 256, so the
+  // one-block minimum of the small systems takes a smaller share (C4 batch of
+  // 256 cavities: 184 ms at 128 threads, 215 at 256, 386 at 512)
+  const int threads = (o.block_threads > 0) ? block_threads_for(o.block_threads, 0, 1) : 128;
+  int occ = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, pcg_batched, threads, 0);
+  if (occ <= 0) occ = 1;
+  if (o.blocks_per_sm > 0 && o.blocks_per_sm < occ) occ = o.blocks_per_sm;
+  int cap = occ * sm_count();
+  if (o.max_blocks > 0) cap = std::min(cap, o.max_blocks);
+  if (nsys > cap) {
+    fprintf(stderr, "fvcgpu: %d systems exceed the %d co-resident blocks of one launch\n", nsys,
+            cap);
+    return FVC_ERR_ARG;
+  }
+  // blocks per system in proportion to slices x sqrt(rows) (work per
+  // iteration x the growth of the iteration count with the mesh size),
+  // at most one slice per warp.  Water-filling: a system whose share is
+  // below one block gets one, the others share the rest, and blocks left
+  // over by rounding go to the largest remainders.
+  const int warps = threads / 32;
+  std::vector<int> nb(nsys, 0), slices(nsys), most(nsys);
+  std::vector<double> wt(nsys), frac(nsys, 0.0);
+  std::vector<char> fixed(nsys, 0);
+  double wleft = 0.0;
+  for (int s = 0; s < nsys; ++s) {
+    const int rows = row_start[s + 1] - row_start[s];
+    slices[s] = (rows + 31) / 32;
+    most[s] = (slices[s] + warps - 1) / warps;
+    wt[s] = slices[s] * std::sqrt((double)rows);
+    wleft += wt[s];
+  }
+  long capleft = cap;
+  for (bool changed = true; changed;) {
+    changed = false;
+    for (int s = 0; s < nsys; ++s) {
+      if (fixed[s]) continue;
+      const double share = capleft * wt[s] / wleft;
+      if (share < 1.0 || share >= most[s]) {
+        nb[s] = share < 1.0 ? 1 : most[s];
+        fixed[s] = 1;
+        capleft -= nb[s];
+        wleft -= wt[s];
+        changed = true;
+      }
+    }
+    if (wleft <= 0.0) break;
+  }
+  long total = 0;
+  for (int s = 0; s < nsys; ++s) {
+    if (!fixed[s]) {
+      const double share = capleft * wt[s] / wleft;
+      nb[s] = std::max(1, (int)std::floor(share));
+      frac[s] = share - nb[s];
+    }
+    total += nb[s];
+  }
+  while (total < cap) {  // rounding leftovers: largest remainder first
+    int k = -1;
+    for (int s = 0; s < nsys; ++s)
+      if (!fixed[s] && nb[s] < most[s] && (k < 0 || frac[s] > frac[k])) k = s;
+    if (k < 0 || frac[k] <= 0.0) break;
+    ++nb[k];
+    frac[k] = 0.0;
+    ++total;
+  }
+  while (total > cap) {  // trim the largest shares (nsys <= cap keeps one each)
+    int k = 0;
+    for (int s = 1; s < nsys; ++s)
+      if (nb[s] > nb[k]) k = s;
+    --nb[k];
+    --total;
+  }
+  // one device buffer: per system a 64-byte counter sector, partials and
+  // totals, results; then the error word, descriptors and block map
+  size_t part_doubles = 0;
+  for (int s = 0; s < nsys; ++s) part_doubles += (size_t)4 * kMaxNV * (nb[s] + 1);
+  const size_t ctr_bytes = (size_t)nsys * 64 + 64;
+  const size_t res_bytes = (size_t)nsys * 16 * sizeof(double);
+  const size_t ires_bytes = (size_t)nsys * 16 * sizeof(int);
+  const size_t sys_bytes = (size_t)nsys * sizeof(BatchSys);
+  const size_t sob_bytes = (size_t)total * sizeof(int);
+  const size_t bytes =
+      ctr_bytes + part_doubles * sizeof(double) + res_bytes + ires_bytes + sys_bytes + sob_bytes;
+  char *buf = nullptr;
+  if (cudaMallocAsync((void **)&buf, bytes, stream) != cudaSuccess) return FVC_ERR_CUDA;
+  unsigned int *ctr = reinterpret_cast<unsigned int *>(buf);
+  int *err = reinterpret_cast<int *>(buf + (size_t)nsys * 64);
+  double *part = reinterpret_cast<double *>(buf + ctr_bytes);
+  double *res = part + part_doubles;
+  int *ires = reinterpret_cast<int *>(res + (size_t)nsys * 16);
+  BatchSys *dsys = reinterpret_cast<BatchSys *>(reinterpret_cast<char *>(ires) + ires_bytes);
+  int *dsob = reinterpret_cast<int *>(reinterpret_cast<char *>(dsys) + sys_bytes);
+  std::vector<BatchSys> hsys(nsys);
+  std::vector<int> hsob((size_t)total);
+  size_t poff = 0;
+  int b0 = 0;
+  for (int s = 0; s < nsys; ++s) {
+    BatchSys &d = hsys[s];
+    d.s0 = row_start[s] / 32;
+    d.s1 = d.s0 + slices[s];
+    d.gs.count = ctr + (size_t)s * 16;
+    d.gs.flag = ctr + (size_t)s * 16 + 8;
+    d.gs.err = err;
+    d.gs.partials = part + poff;
+    d.gs.totals = part + poff + (size_t)4 * kMaxNV * nb[s];
+    d.gs.nblocks = (unsigned int)nb[s];
+    d.gs.base = (unsigned int)b0;
+    d.result = res + (size_t)s * 16;
+    d.iresult = ires + (size_t)s * 16;
+    poff += (size_t)4 * kMaxNV * (nb[s] + 1);
+    for (int k = 0; k < nb[s]; ++k) hsob[(size_t)b0 + k] = s;
+    b0 += nb[s];
+  }
+  int32_t rc = ensure_vectors(S, (size_t)A.n, 5, 1, false);
+  if (rc != FVC_OK) {
+    cudaFreeAsync(buf, stream);
+    return rc;
+  }
+  cudaMemsetAsync(buf, 0, ctr_bytes, stream);
+  cudaMemsetAsync(res, 0, res_bytes + ires_bytes, stream);
+  cudaMemcpyAsync(dsys, hsys.data(), sys_bytes, cudaMemcpyHostToDevice, stream);
+  cudaMemcpyAsync(dsob, hsob.data(), sob_bytes, cudaMemcpyHostToDevice, stream);
+  KArgs a{};
+  a.A = view64(A);
+  a.m = A.jac;
+  a.minv = A.jinv;
+  a.b = b;
+  a.x = x;
+  a.v0 = S.v[0];
+  a.v1 = S.v[1];
+  a.v2 = S.v[2];
+  a.v3 = S.v[3];
+  a.v4 = S.v[4];
+  a.tol = tol;
+  a.maxit = maxit;
+  a.init = init;
+  a.stop_rule = o.stop_rule;
+  const BatchSys *psys = dsys;
+  const int *psob = dsob;
+  void *args[] = {&a, &psys, &psob};
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventRecord(e0, stream);
+  cudaError_t ce = cudaLaunchCooperativeKernel((const void *)pcg_batched, dim3((unsigned)total),
+                                               dim3(threads), args, 0, stream);
+  count_launch();
+  cudaEventRecord(e1, stream);
+  std::vector<double> hres((size_t)nsys * 16);
+  std::vector<int> hires((size_t)nsys * 16);
+  int herr = 0;
+  if (ce == cudaSuccess) {
+    cudaMemcpyAsync(hres.data(), res, res_bytes, cudaMemcpyDeviceToHost, stream);
+    cudaMemcpyAsync(hires.data(), ires, ires_bytes, cudaMemcpyDeviceToHost, stream);
+    cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, stream);
+  } else {
+    fprintf(stderr, "fvcgpu: batched launch failed: %s\n", cudaGetErrorString(ce));
+  }
+  cudaFreeAsync(buf, stream);
+  cudaError_t ce2 = cudaStreamSynchronize(stream);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (ce != cudaSuccess || ce2 != cudaSuccess) return FVC_ERR_CUDA;
+  if (herr != 0) return FVC_ERR_TIMEOUT;
+  int32_t worst = FVC_OK;
+  for (int s = 0; s < nsys; ++s) {
+    const double *r = &hres[(size_t)s * 16];
+    const int *ir = &hires[(size_t)s * 16];
+    if (ir[1] == FVC_ERR_NAN) worst = FVC_ERR_NAN;
+    else if (ir[1] != FVC_OK && worst == FVC_OK) worst = ir[1];
+    if (st) {
+      fvc_stats &t = st[s];
+      memset(&t, 0, sizeof(t));
+      t.status = ir[1];
+      t.iterations = ir[0];
+      t.energy = r[0];
+      t.conv = r[1];
+      t.final_crit = r[2];
+      t.rel_residual = (r[4] > 0) ? std::sqrt(r[3] / r[4]) : std::sqrt(r[3]);
+      t.solve_ms = ms;
+    }
+  }
+  return worst;
 }
 
 int32_t launch_spmv(const DeviceMatrix &A, const double *x, double *y, cudaStream_t stream,

@@ -130,7 +130,7 @@ __device__ __forceinline__ bool grid_allreduce_ff(const GridSync &gs, unsigned i
       // publish the block's partials, then wait until every block has
       if (lane == 0) {
 #pragma unroll
-        for (int q = 0; q < NV; ++q) part[(size_t)q * nb + blockIdx.x] = bsum[q];
+        for (int q = 0; q < NV; ++q) part[(size_t)q * nb + (blockIdx.x - gs.base)] = bsum[q];
         red_add_release(gs.count, 1u);
         const unsigned int target = ep * nb;
         const uint64_t t0 = global_ns();

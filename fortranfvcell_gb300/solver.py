@@ -136,6 +136,24 @@ class Context:
         st.status = rc
         return st
 
+    def solve_batched(self, row_start, b_dev, x_dev, tol: float, maxit: int,
+                      opts: FvcOpts | None = None, raise_on_error: bool = True):
+        """Batched PCG of the block-diagonal matrix on this context (see
+        pack_block_diagonal): one persistent launch, each system on its own
+        blocks with its own stopping test.  Returns (status, [FvcStats] per
+        system)."""
+        rs = np.ascontiguousarray(row_start, np.int32)
+        nsys = rs.size - 1
+        st = (FvcStats * nsys)()
+        o = opts if opts is not None else make_opts()
+        rc = self._L.fvc_solve_batched(self._h, nsys, rs.ctypes.data_as(C.c_void_p),
+                                       C.c_void_p(_addr(b_dev)), C.c_void_p(_addr(x_dev)),
+                                       float(tol), int(maxit), C.byref(o),
+                                       C.cast(st, C.c_void_p))
+        if raise_on_error and rc != _lib.FVC_OK:
+            raise FvcError(rc, f"batched PCG ended with status {_lib.STATUS_NAMES.get(rc, rc)}")
+        return rc, list(st)
+
     def trace(self, max_records: int = 256):
         """(iterations, rel. residuals) at the residual replacements of the
         last mixed-precision CG solve."""
@@ -179,3 +197,35 @@ def _addr(t) -> int:
 
 def kernel_launches() -> int:
     return int(_lib.load().fvc_kernel_launches())
+
+
+def pack_block_diagonal(systems):
+    """Packs CSRD systems (each a dict with ad, au, ia, ja: 1-based, negated
+    off-diagonals, as src/Datastruct.f builds them for matriz 1) into one
+    block-diagonal CSRD matrix whose systems start at multiples of 32 rows,
+    as fvc_solve_batched requires; the rows in between are identity rows.
+    Returns dict(ad, au, ia, ja, neq, nad, row_start, rows): rows[s] is the
+    index array of system s's rows in the packed vectors."""
+    starts, rows, n = [], [], 0
+    for s in systems:
+        k = int(s["ad"].size)
+        starts.append(n)
+        rows.append(np.arange(n, n + k))
+        n += (k + 31) // 32 * 32
+    row_start = np.array(starts + [n], np.int32)
+    ad = np.ones(n)
+    nnz = [np.diff(np.asarray(s["ia"])) for s in systems]
+    counts = np.zeros(n, np.int64)
+    for r, c in zip(rows, nnz):
+        counts[r] = c
+    ia = np.ones(n + 1, np.int64)
+    ia[1:] = 1 + np.cumsum(counts)
+    ja = np.empty(int(counts.sum()), np.int32)
+    au = np.empty(ja.size)
+    for s, r, st in zip(systems, rows, starts):
+        ad[r] = s["ad"]
+        lo, hi = ia[r[0]] - 1, ia[r[-1] + 1] - 1
+        ja[lo:hi] = np.asarray(s["ja"][: hi - lo]) + st
+        au[lo:hi] = s["au"][: hi - lo]
+    return dict(ad=ad, au=au, ia=ia.astype(np.int32), ja=ja, neq=n, nad=int(ja.size),
+                row_start=row_start, rows=rows)

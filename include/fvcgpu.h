@@ -147,6 +147,25 @@ int32_t fvc_solve(fvc_context *ctx, int32_t code, const double *d_b, double *d_x
                   double tol, int32_t maxit, const fvc_opts *opts,
                   fvc_stats *stats);
 
+/* Batched Jacobi-PCG (src/Iterativos.f:29-106) of nsys independent systems
+ * in one persistent launch: the context's matrix holds them block-
+ * diagonally, system s on rows row_start[s] .. row_start[s+1]-1 (host
+ * array of nsys+1 entries, row_start[0] = 0, row_start[nsys] = neq, every
+ * start a multiple of 32).  Rows that pad a system to the next start must
+ * be identity rows with b = 0 and x = 0.  Each system runs on its own group
+ * of blocks with its own reductions and stopping test (tol, maxit and the
+ * warm-start rule as in fvc_solve with code 1), so the iteration counts of
+ * the systems are independent.  nsys is limited to the co-resident blocks of
+ * one launch (FVC_ERR_ARG beyond).  st (host, nsys entries, may be NULL)
+ * receives each system's statistics; solve_ms is the launch's time.
+ * Returns FVC_OK when every system converged, else FVC_ERR_NAN if one broke
+ * down or the first other failure.  FP64 only (FVC_ERR_UNSUPPORTED for
+ * FVC_PREC_MIXED).  No counterpart in the reference, which solves one
+ * system per call (src/Solver.f:28-346). */
+int32_t fvc_solve_batched(fvc_context *ctx, int32_t nsys, const int32_t *row_start,
+                          const double *d_b, double *d_x, double tol,
+                          int32_t maxit, const fvc_opts *opts, fvc_stats *st);
+
 /* y = A x with DEVICE vectors, the reference's summation order, FP64
  * (bit-identical to src/Matvec.f for the loaded format).  Asynchronous on
  * the context's stream. */

@@ -1,0 +1,92 @@
+"""Batched PCG (fvc_solve_batched): many independent pressure-correction
+systems of different sizes and cell shapes in one persistent launch, each
+checked against the restated reference PCG (src/Iterativos.f:29-106) run
+on that system alone."""
+import numpy as np
+import pytest
+
+from _systems import pressure
+
+pytestmark = pytest.mark.gpu
+
+REL_TOL = 1e-10
+ITS_TOL = 2
+
+
+def batch(orc):
+    from fortranfvcell_gb300 import mesh
+    shapes = [("quad", 1), ("tri", 3), ("quad", 17), ("mixed", 9), ("tri", 14), ("quad", 5),
+              ("mixed", 23), ("quad", 31), ("tri", 2), ("mixed", 12)]
+    systems = []
+    for k, (kind, nx) in enumerate(shapes):
+        m = mesh.square_mesh(nx, kind=kind, jitter=0.2 if kind != "quad" else 0.0, seed=k)
+        s = pressure(orc, m, 1, True)
+        s["b"] = np.random.default_rng(100 + k).uniform(-1, 1, s["n"])
+        systems.append(s)
+    return systems
+
+
+def solve_batch(systems, tol, maxit, raise_on_error=True):
+    import torch
+    from fortranfvcell_gb300 import Context, make_opts, pack_block_diagonal
+    pk = pack_block_diagonal(systems)
+    ctx = Context(device=0)
+    ctx.set_matrix(1, True, pk["neq"], pk["nad"], pk["ad"], pk["au"], pk["au"], pk["ia"],
+                   pk["ja"])
+    b = np.zeros(pk["neq"])
+    for s, r in zip(systems, pk["rows"]):
+        b[r] = s["b"]
+    bd = torch.from_numpy(b).cuda()
+    xd = torch.zeros(pk["neq"], dtype=torch.float64, device="cuda")
+    rc, st = ctx.solve_batched(pk["row_start"], bd, xd, tol, maxit, make_opts("fp64", init=1),
+                               raise_on_error=raise_on_error)
+    x = xd.cpu().numpy()
+    ctx.close()
+    return rc, st, [x[r] for r in pk["rows"]]
+
+
+def test_batched_pcg_matches_reference_per_system(orc):
+    systems = batch(orc)
+    rc, st, xs = solve_batch(systems, 1e-10, 20000)
+    assert rc == 0
+    for s, t, x in zip(systems, st, xs):
+        x_ref = np.zeros(s["n"])
+        status, so = orc.solver(s["ad"].copy(), s["au"].copy(), s["au"].copy(), x_ref,
+                                s["b"].copy(), s["ia"], s["ja"], s["n"], s["nad"], True, 1e-10,
+                                20000, 1, 1)
+        assert status == 0 and t.status == 0
+        err = np.linalg.norm(x - x_ref) / np.linalg.norm(x_ref)
+        assert err <= REL_TOL, (s["n"], err)
+        assert abs(t.iterations - so.iterations) <= ITS_TOL, (s["n"], t.iterations, so.iterations)
+        assert abs(t.energy - so.energy) <= 1e-9 * abs(so.energy)
+
+
+def test_batched_systems_stop_independently(orc):
+    # a small iteration limit: the one-cell and the 2x2 systems converge,
+    # the large ones report non-convergence, each on its own
+    from fortranfvcell_gb300 import _lib
+    systems = batch(orc)
+    rc, st, _ = solve_batch(systems, 1e-10, 12, raise_on_error=False)
+    assert rc == _lib.FVC_ERR_NOCONV
+    for s, t in zip(systems, st):
+        if s["n"] <= 8:
+            assert t.status == 0 and t.iterations <= 12, s["n"]
+        if s["n"] >= 200:
+            assert t.status == _lib.FVC_ERR_NOCONV and t.iterations == 12, s["n"]
+
+
+def test_batched_rejects_unaligned_layout(orc):
+    import torch
+    from fortranfvcell_gb300 import Context, FvcError, pack_block_diagonal
+    systems = batch(orc)[:3]
+    pk = pack_block_diagonal(systems)
+    ctx = Context(device=0)
+    ctx.set_matrix(1, True, pk["neq"], pk["nad"], pk["ad"], pk["au"], pk["au"], pk["ia"],
+                   pk["ja"])
+    bd = torch.zeros(pk["neq"], dtype=torch.float64, device="cuda")
+    xd = torch.zeros_like(bd)
+    bad = pk["row_start"].copy()
+    bad[1] += 1                              # not a multiple of 32
+    with pytest.raises(FvcError):
+        ctx.solve_batched(bad, bd, xd, 1e-8, 100)
+    ctx.close()
