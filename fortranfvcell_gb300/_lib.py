@@ -139,6 +139,10 @@ SIGNATURES = {
     "fvc_cells_pressure_correction": ([C.POINTER(FvcCellMesh), P, P, P, P, I32, I32, P, P, P, P,
                                        P, P, P], I32),
     "fvc_cells_simple_update": ([I32, P, P, P, P, P, P, P, F64, P], I32),
+    "fvc_cells_pressure_correction_ideal_gas": ([C.POINTER(FvcCellMesh), P, P, P, P, P, I32,
+                                                 F64, I32, I32, P, P, P, P, P, P, P], I32),
+    "fvc_cells_enthalpy_temperature": ([I32, P, P, F64, F64, I32, P], I32),
+    "fvc_cells_ideal_gas_density": ([I32, P, P, I32, I32, F64, F64, P], I32),
     "fvc_cells_divergence": ([I32, P, P, P, P], I32),
     "fvc_getres": ([I32, P, P, P, I32, P], I32),
     "fvc_cells_energy": ([C.POINTER(FvcCellMesh), I32, I32, P, P, P, P, P, P, P, F64, I32, I32,

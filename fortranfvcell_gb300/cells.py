@@ -102,6 +102,26 @@ def energy_gradient(m: CellMesh, lib: int, pedge, sedge, u, grad) -> None:
         "fvc_cells_energy_gradient")
 
 
+def pressure_correction_ideal_gas(m: CellMesh, w, d, p, gradp, ro, dt, ia, ja, matriz, ad, au,
+                                  b, rescell, int_vel=5, bs=False) -> None:
+    _lib.check(_lib.load().fvc_cells_pressure_correction_ideal_gas(
+        C.byref(m.s), _addr(w), _addr(d), _addr(p), _addr(gradp), _addr(ro), int_vel, dt,
+        int(bs), matriz, _addr(ia), _addr(ja), _addr(ad), _addr(au), _addr(b), _addr(rescell),
+        _stream()), "fvc_cells_pressure_correction_ideal_gas")
+
+
+def enthalpy_temperature(h, t, cp, tref, to_temperature: bool) -> None:
+    _lib.check(_lib.load().fvc_cells_enthalpy_temperature(
+        h.shape[0], _addr(h), _addr(t), cp, tref, int(to_temperature), _stream()),
+        "fvc_cells_enthalpy_temperature")
+
+
+def ideal_gas_density(ro, temp, row, celsius=True, pressure_ratio=1.0, under_ro=1.0) -> None:
+    _lib.check(_lib.load().fvc_cells_ideal_gas_density(
+        ro.shape[0], _addr(ro), _addr(temp), int(celsius), row, pressure_ratio, under_ro,
+        _stream()), "fvc_cells_ideal_gas_density")
+
+
 def simple_update(w, p, u1, u2, pc, gradpc, d, under_pc) -> None:
     _lib.check(_lib.load().fvc_cells_simple_update(
         w.shape[0], _addr(w), _addr(p), _addr(u1), _addr(u2), _addr(pc), _addr(gradpc),

@@ -12,6 +12,8 @@
 //              cellVel face fluxes (CellibSimple.f:1947-2073, intVel 1/2/5)
 //   scatter    assbly for CSRD and ELLPACK (Assbly.f:32-54, Csr.f:142-176,
 //              EllPack.f:68-93): each cell writes its own row only
+//   p' (gas)   cell_si_p_idg_ggl iws = 1 (CellibPressure.f:43-246), the
+//              EnthalpyForTemp and idealGas sweeps (IdealGas.f)
 //   energy     cell_e_eb_idg_ggl (CellibTrans.f:39-349, ideal-gas enthalpy)
 //              and cell_t_eb_ggl (CellibTrans.f:390-655, scalar transport):
 //              iws 1 system, 2 gradient, 4 time term and volume source
@@ -308,6 +310,13 @@ __global__ void gradient_kernel(Mesh m, int kind, int comp, const double *__rest
       else {
         atomicExch(err, 1);
         ug[i - 1] = 0.0;
+      }
+    } else if (kind == 3) {  // ideal-gas pressure: comp 2 = p', 3 = p
+      if (pe == 3) {
+        ug[i - 1] = (comp == 2) ? 0.0 : sedge(m, 3, i, nel);
+      } else {
+        const double gama = 2.0 * G.ca[i - 1];
+        ug[i - 1] = uP + gama * (go1 * G.n[0][i - 1] + go2 * G.n[1][i - 1]);
       }
     } else {
       if (pe == 3) {
@@ -630,6 +639,126 @@ __global__ void getres_kernel(int numel, const int32_t *num, double *u, double *
     u[i] = x[num[i] - 1];
 }
 
+// ---- ideal gas: p' cell (CellibPressure.f:43-246), property sweeps --------
+struct PcIdgArgs {
+  int intvel, matriz, bs;
+  double dt;
+  const double *w, *d, *p, *gradp, *ro;
+  const int32_t *ia, *ja;
+  double *ad, *au, *b, *rescell;
+};
+
+__global__ void pc_idg_kernel(Mesh m, PcIdgArgs a) {
+  const int nel = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  if (nel > m.numel) return;
+  const double cnst = 1.0e60, ZERO = 1.0e-7;
+  Stencil S;
+  Geom G;
+  gather(S, m, nel);
+  geom(G, S);
+  const int ns = S.ns, nsh = m.nshared;
+  const double *w = a.w, *d = a.d, *ro = a.ro;
+  const double rhoP = ro3(ro, 3, nel), rhoA = prop(m, nel, 2);
+  int ldl[MS + 1];
+  for (int i = 0; i <= MS; ++i) ldl[i] = 0;
+  for (int j = 1; j <= ns; ++j) ldl[j - 1] = (S.viz[j - 1] > 0) ? m.num[S.viz[j - 1] - 1] : 0;
+  ldl[nsh] = m.num[nel - 1];
+  double la[MS + 1];
+  for (int i = 0; i <= MS; ++i) la[i] = 0.0;
+  double pp = 0.0, sp = 0.0, kf = 0.0;
+  for (int i = 1; i <= ns; ++i) {
+    const int v = S.viz[i - 1];
+    const double n1 = G.n[0][i - 1], n2 = G.n[1][i - 1];
+    if (v < 0) {
+      const int pe = pedge(m, i, nel);
+      la[i - 1] = 0.0;
+      if (pe == 2) {
+        const double wfn = sedge(m, 1, i, nel) * n1 + sedge(m, 2, i, nel) * n2;
+        const double cv = rhoA * wfn * G.meta[i - 1];
+        pp = pp - cv;
+      } else if (pe == 3) {
+        const double ddf1 = v2(d, 1, nel), ddf2 = v2(d, 2, nel);
+        if (a.intvel == 2) {
+          const double dd1 = ddf1 * n1, dd2 = ddf2 * n2;
+          const double ndd = dd1 * n1 + dd2 * n2;
+          const double dfd = (rhoP * ndd * G.meta[i - 1]) / G.ca[i - 1];
+          sp = sp + dfd;
+        } else if (a.intvel == 5) {
+          const double ndd = 0.5 * (ddf1 + ddf2);
+          const double dfd = (rhoP * G.meta[i - 1] * ndd) / G.ca[i - 1];
+          sp = sp + dfd;
+        }
+        const double wfn = v2(w, 1, nel) * n1 + v2(w, 2, nel) * n2;
+        double cv = 0.0;
+        if (fabs(wfn) > ZERO) {
+          if (wfn > 0.0)
+            cv = rhoP * wfn * G.meta[i - 1];
+          else if (wfn < 0.0)
+            cv = rhoA * wfn * G.meta[i - 1];
+        }
+        pp = pp - cv;
+      }
+    } else {
+      const double alpha = G.mksif[i - 1] / G.mksi[i - 1];
+      kf = (1.0 - alpha) * ro3(ro, 3, nel) + alpha * ro3(ro, 3, v);
+      double ddf[2];
+      ddf[0] = (1.0 - alpha) * v2(d, 1, nel) + alpha * v2(d, 1, v);
+      ddf[1] = (1.0 - alpha) * v2(d, 2, nel) + alpha * v2(d, 2, v);
+      double ndd;
+      if (a.intvel == 5) {
+        ndd = 0.5 * (ddf[0] + ddf[1]);
+      } else {
+        const double dd1 = ddf[0] * n1, dd2 = ddf[1] * n2;
+        ndd = dd1 * n1 + dd2 * n2;
+      }
+      const double nk = n1 * G.ksi[0][i - 1] + n2 * G.ksi[1][i - 1];
+      la[i - 1] = (kf * G.meta[i - 1] * ndd) / (nk * G.mksi[i - 1]);
+      const double wfn = cell_vel(a.intvel, w, a.gradp, ddf, G, a.p, nel, v, i, alpha);
+      pp = pp - kf * wfn;
+    }
+  }
+  if (pedge(m, nsh + 1, nel) == -1) sp = sp + cnst;
+  la[nsh] = sp;
+  for (int i = 1; i <= ns; ++i) la[nsh] = la[nsh] + la[i - 1];
+  double cvc;
+  if (a.bs)
+    cvc = (1.5 * ro3(ro, 3, nel) - 2.0 * ro3(ro, 2, nel) + 0.5 * ro3(ro, 1, nel));
+  else
+    cvc = (ro3(ro, 3, nel) - ro3(ro, 2, nel));
+  pp = pp - G.area * cvc / a.dt;
+  a.rescell[nel - 1] = fabs(pp);
+  assbly(a.ad, a.au, a.b, a.ia, a.ja, la, pp, ldl, nsh, a.matriz, true, true);
+}
+
+// EnthalpyForTemp (IdealGas.f:20-50): to_temp: t = tRef + h/cP, else
+// h = cP (t - tRef)
+__global__ void enthalpy_temp_kernel(int numel, double *h, double *t, double cp, double tref,
+                                     int to_temp) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= numel) return;
+  if (to_temp)
+    t[i] = tref + h[i] / cp;
+  else
+    h[i] = cp * (t[i] - tref);
+}
+
+// idealGas with fIdealGas (IdealGas.f:66-91,148-155): air of the reference's
+// idealGas.fi (O2/N2/Ar molar masses and fractions, R, Pa, 273.15)
+__global__ void ideal_gas_kernel(int numel, double *ro, const double *temp, int celsius, int row,
+                                 double pressure_ratio, double under_ro) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= numel) return;
+  const double Pa = 1.01325e5, R = 8.31431, mO2 = 32.0e-3, mN2 = 28.0e-3, mAr = 39.95e-3;
+  const double dO2 = 0.21, dN2 = 0.78, dAr = 0.01, tConv = 273.15;
+  const double t = celsius ? tConv : 0.0;
+  const double mm = dO2 * mO2 + dN2 * mN2 + dAr * mAr;
+  const double P = pressure_ratio * Pa;
+  const double tk = t + temp[i];
+  const double av = (P * mm) / (R * tk);
+  double &r = ro[(row - 1) + 3 * (size_t)i];
+  r = (1.0 - under_ro) * r + under_ro * av;
+}
+
 // ---- energy / scalar transport cells (src/CellibTrans.f) -----------------
 // lib 3: cell_e_eb_idg_ggl (ideal-gas enthalpy, CellibTrans.f:39-349);
 // lib 4: cell_t_eb_ggl (scalar transport, CellibTrans.f:390-655).  The
@@ -880,7 +1009,8 @@ inline int grid(int n) { return (n + kThreads - 1) / kThreads; }
 
 int32_t gradient(const fvc_cell_mesh *m, int kind, int comp, const double *u, double *grad,
                  cudaStream_t s) {
-  if (!mesh_ok(m) || !u || !grad || (kind != 1 && kind != 2) || comp < 1 || comp > 3)
+  if (!mesh_ok(m) || !u || !grad || kind < 1 || kind > 3 || comp < 1 || comp > 3 ||
+      (kind == 3 && comp == 1))
     return FVC_ERR_ARG;
   int *err = nullptr;
   if (cudaMallocAsync(&err, sizeof(int), s) != cudaSuccess) return FVC_ERR_CUDA;
@@ -1025,6 +1155,60 @@ int32_t fvc_cells_pressure_correction(const fvc_cell_mesh *m, const double *w, c
   a.rescell = rescell;
   cudaStream_t s = (cudaStream_t)stream;
   fvc::cells::pc_kernel<<<grid(m->numel), kThreads, 0, s>>>(fvc::cells::view(m), a);
+  fvc::count_launch();
+  return cudaPeekAtLastError() == cudaSuccess ? FVC_OK : FVC_ERR_CUDA;
+}
+
+int32_t fvc_cells_pressure_correction_ideal_gas(const fvc_cell_mesh *m, const double *w,
+                                                const double *d, const double *p,
+                                                const double *gradp, const double *ro,
+                                                int32_t int_vel, double dt, int32_t bs,
+                                                int32_t matriz, const int32_t *ia,
+                                                const int32_t *ja, double *ad, double *au,
+                                                double *b, double *rescell, void *stream) {
+  if (!fvc::cells::mesh_ok(m) || !w || !d || !p || !gradp || !ro || !ad || !au || !b ||
+      !rescell || (matriz != 1 && matriz != 4) || (matriz == 1 && (!ia || !ja)) || dt == 0.0)
+    return FVC_ERR_ARG;
+  if (int_vel != 1 && int_vel != 2 && int_vel != 5) return FVC_ERR_UNSUPPORTED;
+  fvc::cells::PcIdgArgs a;
+  a.intvel = int_vel;
+  a.matriz = matriz;
+  a.bs = bs;
+  a.dt = dt;
+  a.w = w;
+  a.d = d;
+  a.p = p;
+  a.gradp = gradp;
+  a.ro = ro;
+  a.ia = ia;
+  a.ja = ja;
+  a.ad = ad;
+  a.au = au;
+  a.b = b;
+  a.rescell = rescell;
+  cudaStream_t s = (cudaStream_t)stream;
+  fvc::cells::pc_idg_kernel<<<grid(m->numel), kThreads, 0, s>>>(fvc::cells::view(m), a);
+  fvc::count_launch();
+  return cudaPeekAtLastError() == cudaSuccess ? FVC_OK : FVC_ERR_CUDA;
+}
+
+int32_t fvc_cells_enthalpy_temperature(int32_t numel, double *h, double *t, double cp,
+                                       double tref, int32_t to_temperature, void *stream) {
+  if (numel <= 0 || !h || !t || cp == 0.0) return FVC_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  fvc::cells::enthalpy_temp_kernel<<<grid(numel), kThreads, 0, s>>>(numel, h, t, cp, tref,
+                                                                    to_temperature ? 1 : 0);
+  fvc::count_launch();
+  return cudaPeekAtLastError() == cudaSuccess ? FVC_OK : FVC_ERR_CUDA;
+}
+
+int32_t fvc_cells_ideal_gas_density(int32_t numel, double *ro, const double *temp,
+                                    int32_t celsius, int32_t row, double pressure_ratio,
+                                    double under_ro, void *stream) {
+  if (numel <= 0 || !ro || !temp || row < 1 || row > 3) return FVC_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  fvc::cells::ideal_gas_kernel<<<grid(numel), kThreads, 0, s>>>(
+      numel, ro, temp, celsius ? 1 : 0, row, pressure_ratio, under_ro);
   fvc::count_launch();
   return cudaPeekAtLastError() == cudaSuccess ? FVC_OK : FVC_ERR_CUDA;
 }

@@ -299,7 +299,9 @@ typedef struct {
  * (1 or 2) with the ghost rules of src/CellibSimple.f:655-669; kind 2:
  * pressure-like field with those of src/CellibPressure.f:449-462, which
  * extrapolate with the cell's previous gradient: grad(2,numel) is read and
- * overwritten.  FVC_ERR_UNSUPPORTED for a velocity boundary code outside
+ * overwritten; kind 3: the ideal-gas pressure rules of src/CellibPressure.f:
+ * 115-129 (comp 2: p', a prescribed-pressure face's ghost is 0; comp 3: p,
+ * the ghost is sedge(3)).  FVC_ERR_UNSUPPORTED for a velocity boundary code outside
  * 0..4 (the reference leaves that ghost value undefined). */
 int32_t fvc_cells_gradient(const fvc_cell_mesh *m, int32_t kind, int32_t comp,
                            const double *u, double *grad, void *stream);
@@ -353,6 +355,38 @@ int32_t fvc_cells_pressure_correction(const fvc_cell_mesh *m, const double *w,
                                       int32_t matriz, const int32_t *ia,
                                       const int32_t *ja, double *ad, double *au,
                                       double *b, double *rescell, void *stream);
+
+/* Pressure correction of the ideal-gas cell cell_si_p_idg_ggl iws = 1
+ * (src/CellibPressure.f:43-246): as fvc_cells_pressure_correction with face
+ * densities interpolated from ro(3,numel) (row 3, the current iterate),
+ * prescribed-pressure faces (code 3) weighted by D and by the outflow /
+ * backflow mass flux, no flux term for code 4, the mass storage term
+ * -A (ro3 - ro2)/dt (with bs: -A (1.5 ro3 - 2 ro2 + 0.5 ro1)/dt), and
+ * rescell(c) = |b(num(c))|. */
+int32_t fvc_cells_pressure_correction_ideal_gas(const fvc_cell_mesh *m,
+                                                const double *w, const double *d,
+                                                const double *p, const double *gradp,
+                                                const double *ro, int32_t int_vel,
+                                                double dt, int32_t bs, int32_t matriz,
+                                                const int32_t *ia, const int32_t *ja,
+                                                double *ad, double *au, double *b,
+                                                double *rescell, void *stream);
+
+/* EnthalpyForTemp (src/IdealGas.f:20-50): to_temperature != 0: t = tref +
+ * h/cp; else h = cp (t - tref).  The reference takes cp = e(4,1) and tref =
+ * e(5,1) of material 1. */
+int32_t fvc_cells_enthalpy_temperature(int32_t numel, double *h, double *t,
+                                       double cp, double tref,
+                                       int32_t to_temperature, void *stream);
+
+/* idealGas (src/IdealGas.f:66-91): row `row` (1..3) of ro(3,numel) relaxed
+ * toward the density of air P M/(R T): ro = (1 - under_ro) ro + under_ro
+ * P M/(R T), P = 101325 Pa x pressure_ratio (cPc0/cPc of a closed domain;
+ * 1 otherwise), T = temp + 273.15 when celsius. */
+int32_t fvc_cells_ideal_gas_density(int32_t numel, double *ro,
+                                    const double *temp, int32_t celsius,
+                                    int32_t row, double pressure_ratio,
+                                    double under_ro, void *stream);
 
 /* simpleUpdate (src/Simple.f:871-910): w = u - d grad p', p += under_pc p'. */
 int32_t fvc_cells_simple_update(int32_t numel, double *w, double *p,

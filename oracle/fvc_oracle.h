@@ -189,6 +189,20 @@ int32_t oref_pform_momentum_idg(const double *coor, const int32_t *ix, int32_t l
                                 const int32_t *ia, const int32_t *ja, double *ad, double *au,
                                 double *b, double *im, double *d, double *rescell);
 
+/* Ideal-gas pressure correction (cell_si_p_idg_ggl iws 1) and the property
+ * sweeps EnthalpyForTemp / idealGas (src/IdealGas.f). */
+int32_t oref_pform_pc_idg(const double *coor, const int32_t *ix, int32_t ld, int32_t numel,
+                          int32_t nshared, const int32_t *nelcon, const int32_t *num,
+                          const int32_t *pedge, const double *sedge, const double *e,
+                          const double *w, const double *d, const double *p,
+                          const double *gradp, const double *ro, int32_t intvel, double dt,
+                          int32_t bs, int32_t matriz, int32_t unsym, const int32_t *ia,
+                          const int32_t *ja, double *ad, double *au, double *b,
+                          double *rescell);
+void oref_enthalpy_temp(double *h, double *t, const double *e, int32_t numel, int32_t to_temp);
+void oref_ideal_gas(double *ro, const double *temp, int32_t numel, int32_t celsius, int32_t row,
+                    double pressure_ratio, double under_ro);
+
 /* Energy / scalar transport cells (src/CellibTrans.f): lib 3 the ideal-gas
  * enthalpy cell, lib 4 the transport cell.  pedge and sedge here are the
  * scalar's (nshared+1, numel) arrays; ro(3, numel) the densities. */

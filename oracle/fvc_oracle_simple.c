@@ -19,6 +19,8 @@
  *   simpleUpdate, divergente     src/Simple.f:871-910, :1070-1078
  *   cell_e_eb_idg_ggl iws 1,2,4  src/CellibTrans.f:39-349 (ideal-gas enthalpy)
  *   cell_t_eb_ggl iws 1,2,4      src/CellibTrans.f:390-655 (scalar transport)
+ *   cell_si_p_idg_ggl iws 1,2    src/CellibPressure.f:43-246 (ideal-gas p')
+ *   EnthalpyForTemp, idealGas    src/IdealGas.f:20-91,148-155
  * Meshes may mix triangles and quadrilaterals: a cell's loops run over its
  * own sides (for single-type meshes this is the reference's nshared).
  * Parity: restatement only (no Fortran compiler exists to run the
@@ -265,6 +267,14 @@ int32_t oref_gform(const double *coor, const int32_t *ix, int32_t ld, int32_t nu
           ug[i - 1] = uP;
         else
           return -1; /* the reference leaves the ghost value undefined */
+      } else if (kind == 3) { /* ideal-gas pressure (CellibPressure.f:115-129):
+                                comp 2 = p' (gform iws1 2), comp 3 = p (iws1 3) */
+        if (pe == 3) {
+          ug[i - 1] = (comp == 2) ? 0.0 : F3(sedge, 3, ldp, 3, i, nel);
+        } else {
+          const double gama = 2.0 * G.ca[i - 1];
+          ug[i - 1] = uP + gama * (go1 * G.n[0][i - 1] + go2 * G.n[1][i - 1]);
+        }
       } else {       /* pressure, gform's iws = 2 (CellibPressure.f:449-462) */
         if (pe == 3) {
           ug[i - 1] = 0.0;
@@ -853,4 +863,134 @@ int32_t oref_pform_energy(const double *coor, const int32_t *ix, int32_t ld, int
     oref_assbly(ad, au, au, b, ia, ja, la, p, ldl, nshared, matriz, unsym, 1, 1);
   }
   return 0;
+}
+
+
+/* ---- ideal gas (src/CellibPressure.f:43-389, src/IdealGas.f) ----------- */
+
+/* Pressure correction of the ideal-gas cell cell_si_p_idg_ggl, iws = 1
+ * (CellibPressure.f:122-246): face densities interpolated from ro(3,*),
+ * prescribed-pressure faces (pe 3) with the D-weighted coefficient and the
+ * outflow / backflow mass flux, the mass storage term -A (rho - rho_n)/dt
+ * (second order with bs), rescell = |b|. */
+int32_t oref_pform_pc_idg(const double *coor, const int32_t *ix, int32_t ld, int32_t numel,
+                          int32_t nshared, const int32_t *nelcon, const int32_t *num,
+                          const int32_t *pedge, const double *sedge, const double *e,
+                          const double *w, const double *d, const double *p,
+                          const double *gradp, const double *ro, int32_t intvel, double dt,
+                          int32_t bs, int32_t matriz, int32_t unsym, const int32_t *ia,
+                          const int32_t *ja, double *ad, double *au, double *b,
+                          double *rescell) {
+  const int32_t ldp = nshared + 1;
+  const double cnst = 1.0e60, ZERO = 1.0e-7;
+  if (intvel != 1 && intvel != 2 && intvel != 5) return -1;
+  for (int32_t nel = 1; nel <= numel; ++nel) {
+    Stencil S;
+    Geom G;
+    gather(&S, coor, ix, ld, nshared, nelcon, nel);
+    geom(&G, &S);
+    const int32_t ns = S.ns;
+    const double rhoP = F2(ro, 3, 3, nel);
+    const double rhoA = PROP(e, ix, ld, nel, 2);
+    int32_t ldl[MS + 1];
+    for (int32_t i = 0; i <= MS; ++i) ldl[i] = 0;
+    for (int32_t j = 1; j <= ns; ++j) ldl[j - 1] = (S.viz[j - 1] > 0) ? F1(num, S.viz[j - 1]) : 0;
+    ldl[nshared] = F1(num, nel);
+    double la[MS + 1];
+    for (int32_t i = 0; i <= MS; ++i) la[i] = 0.0;
+    double pp = 0.0, sp = 0.0, kf = 0.0;
+    for (int32_t i = 1; i <= ns; ++i) {
+      const int32_t v = S.viz[i - 1];
+      const double n1 = G.n[0][i - 1], n2 = G.n[1][i - 1];
+      if (v < 0) {
+        const int32_t pe = F2(pedge, ldp, i, nel);
+        la[i - 1] = 0.0;
+        if (pe == 2) {
+          const double wfn = F3(sedge, 3, ldp, 1, i, nel) * n1 + F3(sedge, 3, ldp, 2, i, nel) * n2;
+          const double cv = rhoA * wfn * G.meta[i - 1];
+          pp = pp - cv;
+        } else if (pe == 3) {
+          const double ddf1 = F2(d, 2, 1, nel), ddf2 = F2(d, 2, 2, nel);
+          if (intvel == 2) {
+            const double dd1 = ddf1 * n1, dd2 = ddf2 * n2;
+            const double ndd = dd1 * n1 + dd2 * n2;
+            const double dfd = (rhoP * ndd * G.meta[i - 1]) / G.ca[i - 1];
+            sp = sp + dfd;
+          } else if (intvel == 5) {
+            const double ndd = 0.5 * (ddf1 + ddf2);
+            const double dfd = (rhoP * G.meta[i - 1] * ndd) / G.ca[i - 1];
+            sp = sp + dfd;
+          }
+          const double wfn = F2(w, 2, 1, nel) * n1 + F2(w, 2, 2, nel) * n2;
+          double cv = 0.0;
+          if (fabs(wfn) > ZERO) {
+            if (wfn > 0.0)
+              cv = rhoP * wfn * G.meta[i - 1];
+            else if (wfn < 0.0)
+              cv = rhoA * wfn * G.meta[i - 1];
+          }
+          pp = pp - cv;
+        }
+      } else {
+        const double alpha = G.mksif[i - 1] / G.mksi[i - 1];
+        kf = (1.0 - alpha) * F2(ro, 3, 3, nel) + alpha * F2(ro, 3, 3, v);
+        double ddf[2];
+        ddf[0] = (1.0 - alpha) * F2(d, 2, 1, nel) + alpha * F2(d, 2, 1, v);
+        ddf[1] = (1.0 - alpha) * F2(d, 2, 2, nel) + alpha * F2(d, 2, 2, v);
+        double ndd;
+        if (intvel == 5) {
+          ndd = 0.5 * (ddf[0] + ddf[1]);
+        } else {
+          const double dd1 = ddf[0] * n1, dd2 = ddf[1] * n2;
+          ndd = dd1 * n1 + dd2 * n2;
+        }
+        const double nk = n1 * G.ksi[0][i - 1] + n2 * G.ksi[1][i - 1];
+        la[i - 1] = (kf * G.meta[i - 1] * ndd) / (nk * G.mksi[i - 1]);
+        const double wfn = cell_vel(intvel, w, gradp, ddf, &G, p, nel, v, i, alpha);
+        pp = pp - kf * wfn;
+      }
+    }
+    if (F2(pedge, ldp, ldp, nel) == -1) sp = sp + cnst;
+    la[nshared] = sp;
+    for (int32_t i = 1; i <= ns; ++i) la[nshared] = la[nshared] + la[i - 1];
+    double cvc;
+    if (bs)
+      cvc = (1.5 * F2(ro, 3, 3, nel) - 2.0 * F2(ro, 3, 2, nel) + 0.5 * F2(ro, 3, 1, nel));
+    else
+      cvc = (F2(ro, 3, 3, nel) - F2(ro, 3, 2, nel));
+    pp = pp - G.area * cvc / dt;
+    F1(rescell, nel) = fabs(pp);
+    oref_assbly(ad, au, au, b, ia, ja, la, pp, ldl, nshared, matriz, unsym, 1, 1);
+  }
+  return 0;
+}
+
+/* EnthalpyForTemp (IdealGas.f:20-50): to_temp != 0: t = tRef + h/cP,
+ * else h = cP (t - tRef); cP = e(4,1), tRef = e(5,1) (material 1). */
+void oref_enthalpy_temp(double *h, double *t, const double *e, int32_t numel, int32_t to_temp) {
+  const double cp = e[3], tref = e[4];
+  for (int32_t i = 1; i <= numel; ++i) {
+    if (to_temp)
+      F1(t, i) = tref + F1(h, i) / cp;
+    else
+      F1(h, i) = cp * (F1(t, i) - tref);
+  }
+}
+
+/* idealGas (IdealGas.f:66-91) with fIdealGas (:148-155): row `row` of
+ * ro(3,*) relaxed toward P M / (R T) for air (O2/N2/Ar molar masses and
+ * fractions, R, Pa and 273.15 of the reference's idealGas.fi); P = Pa
+ * pressure_ratio (cPc0/cPc), celsius adds 273.15 to temp. */
+void oref_ideal_gas(double *ro, const double *temp, int32_t numel, int32_t celsius, int32_t row,
+                    double pressure_ratio, double under_ro) {
+  const double Pa = 1.01325e5, R = 8.31431, mO2 = 32.0e-3, mN2 = 28.0e-3, mAr = 39.95e-3;
+  const double dO2 = 0.21, dN2 = 0.78, dAr = 0.01, tConv = 273.15;
+  const double t = celsius ? tConv : 0.0;
+  const double m = dO2 * mO2 + dN2 * mN2 + dAr * mAr;
+  const double P = pressure_ratio * Pa;
+  for (int32_t i = 1; i <= numel; ++i) {
+    const double tk = t + F1(temp, i);
+    const double a = (P * m) / (R * tk);
+    F2(ro, 3, row, i) = (1.0 - under_ro) * F2(ro, 3, row, i) + under_ro * a;
+  }
 }

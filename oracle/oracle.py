@@ -84,6 +84,10 @@ def lib():
             "oref_simple_update": [vp, vp, vp, vp, vp, vp, vp, I, D],
             "oref_divergente": [vp, vp, vp, I],
             "oref_gform_energy": [vp, vp, I, I, I, vp, vp, vp, vp, I, vp, vp],
+            "oref_pform_pc_idg": [vp, vp, I, I, I, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, I,
+                                  D, I, I, I, vp, vp, vp, vp, vp, vp],
+            "oref_enthalpy_temp": [vp, vp, vp, I, I],
+            "oref_ideal_gas": [vp, vp, I, I, I, D, D],
             "oref_pform_momentum_idg": [vp, vp, I, I, I, vp, vp, vp, vp, vp, I, I, vp, vp, vp,
                                         vp, vp, vp, vp, vp, vp, D, I, D, I, I, I, vp, vp, vp,
                                         vp, vp, vp, vp, vp],
@@ -93,7 +97,7 @@ def lib():
         res = {"oref_dot": D, "oref_smachn": D, "oref_banda_csr": I, "oref_datastruc": I,
                "oref_solver": I, "oref_pcg_omp_sample": I, "oref_gform": I,
                "oref_pform_momentum": I, "oref_pform_pc": I, "oref_gform_energy": I,
-               "oref_pform_energy": I, "oref_pform_momentum_idg": I}
+               "oref_pform_energy": I, "oref_pform_momentum_idg": I, "oref_pform_pc_idg": I}
         for name, argt in sig.items():
             f = getattr(L, name)
             f.argtypes = argt
@@ -377,3 +381,32 @@ def pform_energy(m, lib_, iws, pedge, sedge, u, u0, ro, w, grad, dt, ia, ja, mat
     if rc != 0:
         raise ValueError("oref_pform_energy: lib must be 3 or 4 and iws 1 or 4")
     return ad, au
+
+
+def pform_pc_idg(m, w, d, p, gradp, ro, dt, ia, ja, matriz, ad, au, b, rescell, int_vel=5,
+                 bs=False, unsym=True):
+    """Ideal-gas pressure-correction system (cell_si_p_idg_ggl iws 1)."""
+    numel = m["ix"].shape[0]
+    rc = lib().oref_pform_pc_idg(
+        _p(_c(m["coor"], np.float64)), _p(_c(m["ix"], np.int32)), m["ix"].shape[1], numel,
+        m["nshared"], _p(_c(m["nelcon"], np.int32)), _p(_c(m["num"], np.int32)),
+        _p(_c(m["pedge"], np.int32)), _p(_c(m["sedge"], np.float64)), _p(_c(m["e"], np.float64)),
+        _p(_c(w, np.float64)), _p(_c(d, np.float64)), _p(_c(p, np.float64)),
+        _p(_c(gradp, np.float64)), _p(_c(ro, np.float64)), int_vel, dt, int(bs), matriz,
+        int(unsym), _p(_c(ia, np.int32)), _p(_c(ja, np.int32)), _p(ad), _p(au), _p(b),
+        _p(rescell))
+    if rc != 0:
+        raise ValueError("oref_pform_pc_idg: unsupported intVel")
+    return ad, au
+
+
+def enthalpy_temp(h, t, e, to_temp):
+    """EnthalpyForTemp in place: to_temp -> t from h, else h from t."""
+    lib().oref_enthalpy_temp(_p(h), _p(t), _p(_c(e, np.float64)), h.shape[0], int(to_temp))
+
+
+def ideal_gas(ro, temp, row, celsius=True, pressure_ratio=1.0, under_ro=1.0):
+    """idealGas: ro[:, row-1] relaxed toward the air density at temp."""
+    assert ro.flags.c_contiguous and ro.shape[1] == 3
+    lib().oref_ideal_gas(_p(ro), _p(_c(temp, np.float64)), ro.shape[0], int(celsius), row,
+                         pressure_ratio, under_ro)

@@ -191,3 +191,56 @@ def test_update_sweeps_bit_exact(orc):
     u = dev(np.zeros(n))
     cells.getres(dev(num), u, x, False)
     assert np.array_equal(host(u), f["u1"])
+
+
+@pytest.mark.parametrize("kind,nx,seed,matriz,int_vel", [("quad", 9, 21, 1, 5), ("tri", 7, 22, 4, 2),
+                                                         ("mixed", 8, 23, 1, 5),
+                                                         ("mixed", 8, 24, 1, 1)])
+def test_pressure_correction_ideal_gas_bit_exact(orc, kind, nx, seed, matriz, int_vel):
+    from fortranfvcell_gb300 import cells
+    case, rng = random_case(orc, kind, nx, seed)
+    n = case["numel"]
+    f = fields(rng, n)
+    ro = rng.uniform(0.9, 1.3, (n, 3))
+    ia, ja, _ = orc.datastruc(case["ident"], matriz, True)
+    m = mesh_on_gpu(case)
+    for bs in (False, True):
+        ad, au, b, rc = np.zeros(n), np.zeros(ja.size), np.zeros(n), np.zeros(n)
+        orc.pform_pc_idg(case, f["w"], f["d"], f["p"], f["gp"], ro, 0.05, ia, ja, matriz, ad, au,
+                         b, rc, int_vel=int_vel, bs=bs)
+        t = {k: dev(np.zeros(s)) for k, s in (("ad", n), ("au", ja.size), ("b", n), ("rc", n))}
+        cells.pressure_correction_ideal_gas(m, dev(f["w"]), dev(f["d"]), dev(f["p"]), dev(f["gp"]),
+                                            dev(ro), 0.05, dev(ia, np.int32),
+                                            dev(ja.ravel(), np.int32), matriz, t["ad"], t["au"],
+                                            t["b"], t["rc"], int_vel=int_vel, bs=bs)
+        for k, ref in (("ad", ad), ("au", au), ("b", b), ("rc", rc)):
+            assert np.array_equal(host(t[k]), ref), (bs, k)
+    for comp in (2, 3):                 # ideal-gas pressure gradient rules (p', p)
+        g_ref = f["gp"].copy()
+        orc.gform(case, 3, comp, f["p"], g_ref)
+        g = dev(f["gp"])
+        cells.gradient(m, 3, comp, dev(f["p"]), g)
+        assert np.array_equal(host(g), g_ref), comp
+
+
+def test_ideal_gas_sweeps_bit_exact(orc):
+    from fortranfvcell_gb300 import cells
+    rng = np.random.default_rng(31)
+    n = 1000
+    temp = rng.uniform(-20, 80, n)
+    ro_ref = rng.uniform(1.0, 1.3, (n, 3))
+    ro = dev(ro_ref)
+    for row, under in ((3, 1.0), (2, 0.7)):
+        orc.ideal_gas(ro_ref, temp, row, pressure_ratio=1.1, under_ro=under)
+        cells.ideal_gas_density(ro, dev(temp), row, pressure_ratio=1.1, under_ro=under)
+        assert np.array_equal(host(ro), ro_ref), row
+    e = np.zeros((1, 10))
+    e[0, 3], e[0, 4] = 1012.0, 20.0
+    h_ref, t_ref = rng.uniform(-5e3, 5e4, n), np.zeros(n)
+    h, t = dev(h_ref), dev(t_ref)
+    orc.enthalpy_temp(h_ref, t_ref, e, True)
+    cells.enthalpy_temperature(h, t, 1012.0, 20.0, True)
+    assert np.array_equal(host(t), t_ref)
+    orc.enthalpy_temp(h_ref, t_ref, e, False)
+    cells.enthalpy_temperature(h, t, 1012.0, 20.0, False)
+    assert np.array_equal(host(h), h_ref)

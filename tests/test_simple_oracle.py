@@ -111,3 +111,57 @@ def test_ideal_gas_momentum_reduces_to_incompressible(orc):
         out.append((ad, au, b, im, d, rc))
     for x, y in zip(*out):
         np.testing.assert_allclose(y, x, rtol=1e-12, atol=1e-14 * np.abs(x).max())
+
+
+def test_ideal_gas_pc_reduces_to_incompressible_and_stores_mass(orc):
+    case = cavity(orc, 9, kind="mixed", jitter=0.2)
+    n = case["numel"]
+    nsh = case["nshared"]
+    case["pedge"][:, :nsh] = np.where(case["nelcon"] < 0,
+                                      np.random.default_rng(1).integers(0, 3, (n, nsh)), 0)
+    rng = np.random.default_rng(4)
+    w, d, gp = rng.uniform(-1, 1, (n, 2)), rng.uniform(0.5, 1.5, (n, 2)), rng.uniform(-1, 1, (n, 2))
+    p = rng.uniform(-1, 1, n)
+    ia, ja, _ = orc.datastruc(case["ident"], 1, True)
+    ro = np.full((n, 3), case["e"][0, 1])
+    outs = []
+    for idg in (False, True):
+        ad, au, b, rc = np.zeros(n), np.zeros(ja.size), np.zeros(n), np.zeros(n)
+        if idg:
+            orc.pform_pc_idg(case, w, d, p, gp, ro, 0.1, ia, ja, 1, ad, au, b, rc)
+        else:
+            orc.pform_pc(case, w, d, p, gp, ia, ja, 1, ad, au, b, rc)
+        outs.append((ad, au, b, rc))
+    (ad0, au0, b0, rc0), (ad1, au1, b1, rc1) = outs
+    assert np.array_equal(ad1, ad0) and np.array_equal(au1, au0) and np.array_equal(b1, b0)
+    assert np.array_equal(rc1, np.abs(rc0))
+    # at rest the right-hand side is the mass storage -A (rho - rho_n)/dt
+    ro = rng.uniform(1.0, 1.3, (n, 3))
+    b = np.zeros(n)
+    orc.pform_pc_idg(case, np.zeros((n, 2)), d, np.zeros(n), np.zeros((n, 2)), ro, 0.1, ia, ja,
+                     1, np.zeros(n), np.zeros(ja.size), b, np.zeros(n))
+    m = case["mesh"]
+    area = np.zeros(n)
+    for c in range(n):
+        xy = m.coor[m.ix[c, :m.nsides[c]] - 1]
+        area[c] = 0.5 * abs(np.dot(xy[:, 0], np.roll(xy[:, 1], -1))
+                            - np.dot(xy[:, 1], np.roll(xy[:, 0], -1)))
+    np.testing.assert_allclose(b[case["num"] - 1], -area * (ro[:, 2] - ro[:, 1]) / 0.1,
+                               rtol=1e-12)
+
+
+def test_ideal_gas_density_and_enthalpy(orc):
+    t = np.array([20.0, -10.0, 300.0])
+    ro = np.zeros((3, 3))
+    orc.ideal_gas(ro, t, 3)
+    M = 0.21 * 0.032 + 0.78 * 0.028 + 0.01 * 0.03995
+    np.testing.assert_allclose(ro[:, 2], 101325.0 * M / (8.31431 * (t + 273.15)), rtol=1e-15)
+    assert abs(ro[0, 2] - 1.204) < 1e-3                     # air at 20 C
+    e = np.zeros((1, 10))
+    e[0, 3], e[0, 4] = 1012.0, 20.0
+    h, tt = np.zeros(3), t.copy()
+    orc.enthalpy_temp(h, tt, e, False)
+    np.testing.assert_allclose(h, 1012.0 * (t - 20.0))
+    t2 = np.zeros(3)
+    orc.enthalpy_temp(h, t2, e, True)
+    np.testing.assert_allclose(t2, t, rtol=1e-15)
