@@ -152,6 +152,9 @@ SIGNATURES = {
     "fvc_simple_create": ([C.POINTER(P), I32, I32, I32, I32, I32, P, P, P, P, P, P, P,
                            C.POINTER(FvcSimpleOpts)], I32),
     "fvc_simple_iterate": ([P, I32, P, P], I32),
+    "fvc_simple_iterate_energy": ([P, I32, P, P], I32),
+    "fvc_simple_energy": ([P, P, P, F64, F64, F64], I32),
+    "fvc_simple_energy_fields": ([P, P, P, P], I32),
     "fvc_simple_time_step": ([P], I32),
     "fvc_simple_fields": ([P, P, P], I32),
     "fvc_simple_set_fields": ([P, P, P], I32),

@@ -39,3 +39,51 @@ def lid_driven_cavity(nx: int, kind: str = "quad", nu: float = 0.01, rho: float 
     e[0, 0], e[0, 1], e[0, 5], e[0, 6] = nu, rho, cc, limiter
     return dict(coor=m.coor, ix=ix, nelcon=nelcon, num=num, ident=ident, pedge=pedge,
                 sedge=sedge, e=e, nshared=nsh, numel=numel, mesh=m)
+
+
+# air at 20 C, the material of the reference's natural-convection deck
+# (viscosity, reference density, conductivity, specific heat, reference
+# temperature): mu, rho, k, cp, tRef
+AIR = (1.72e-5, 1.204, 2.42e-2, 1.012e3, 20.0)
+
+
+def natural_convection_cavity(nx: int, ra: float = 1.0e6, dt_wall: float = 1.0,
+                              t0: float = 20.0, kind: str = "quad", limiter: int = 7,
+                              jitter: float = 0.0, seed: int = 1234) -> dict:
+    """Differentially heated square cavity for the ideal-gas SIMPLE loop
+    (material type 55): walls no-slip (pedge 0), the left wall at
+    t0 + dt_wall/2 and the right one at t0 - dt_wall/2 (energy pedge 1),
+    top and bottom adiabatic (energy pedge 0, zero flux), gravity (0, -9.81),
+    cell 1's pressure correction pinned.  The side L is set so that
+    Ra = g beta dt_wall L^3 / (nu alpha) with beta = 1/(t0 + 273.15) K and
+    nu, alpha of air; the returned dict adds pedgeE, sedgeE, gravity, t0 and
+    side to the keys of lid_driven_cavity."""
+    mu, rho, k, cp, tref = AIR
+    nu, alpha, g = mu / rho, k / (rho * cp), 9.81
+    beta = 1.0 / (t0 + 273.15)
+    side = (ra * nu * alpha / (g * beta * dt_wall)) ** (1.0 / 3.0)
+    c = lid_driven_cavity(nx, kind=kind, lid=0.0, limiter=limiter, jitter=jitter, seed=seed)
+    c["coor"] = c["coor"] * side
+    c["mesh"].coor = c["coor"]
+    c["pedge"][:, :c["nshared"]] = 0          # no moving lid
+    c["sedge"][:] = 0.0
+    c["e"] = np.zeros((1, 10))
+    c["e"][0, :7] = [mu, rho, k, cp, tref, 1.0, limiter]
+    nsh, n = c["nshared"], c["numel"]
+    m = c["mesh"]
+    a = c["coor"][m.ix - 1]
+    nxt = np.take_along_axis(m.ix, (np.arange(nsh)[None, :] + 1) % m.nsides[:, None], axis=1)
+    b = c["coor"][nxt - 1]
+    used = np.arange(nsh)[None, :] < m.nsides[:, None]
+    bnd = used & (c["nelcon"] < 0)
+    tol = 1e-9 * side
+    left = bnd & (np.abs(a[..., 0]) < tol) & (np.abs(b[..., 0]) < tol)
+    right = bnd & (np.abs(a[..., 0] - side) < tol) & (np.abs(b[..., 0] - side) < tol)
+    pe = np.zeros((n, nsh + 1), np.int32)
+    se = np.zeros((n, nsh + 1))
+    pe[:, :nsh][left | right] = 1
+    se[:, :nsh][left] = t0 + 0.5 * dt_wall
+    se[:, :nsh][right] = t0 - 0.5 * dt_wall
+    c.update(pedgeE=pe, sedgeE=se, gravity=np.array([0.0, -g]), t0=t0, side=side, ra=ra)
+    c["e"][0, 1] = rho
+    return c

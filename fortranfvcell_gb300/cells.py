@@ -180,6 +180,34 @@ class SimpleLoop:
                    "fvc_simple_iterate")
         return res, its
 
+    def enable_energy(self, pedge_e, sedge_e, gravity, t0: float) -> None:
+        """Ideal-gas iteration with the energy equation (fvc_simple_energy)."""
+        pe = np.ascontiguousarray(pedge_e, np.int32)
+        se = np.ascontiguousarray(sedge_e, np.float64)
+        _lib.check(self._L.fvc_simple_energy(self._h, pe.ctypes.data_as(C.c_void_p),
+                                             se.ctypes.data_as(C.c_void_p), float(gravity[0]),
+                                             float(gravity[1]), float(t0)), "fvc_simple_energy")
+
+    def iterate_energy(self, nit: int):
+        """nit outer iterations of the energy loop: (residuals (nit,4),
+        solver iterations (nit,4)) for u1, u2, p' and the enthalpy."""
+        res = np.zeros((nit, 4))
+        its = np.zeros((nit, 4), np.int32)
+        _lib.check(self._L.fvc_simple_iterate_energy(self._h, nit,
+                                                     res.ctypes.data_as(C.c_void_p),
+                                                     its.ctypes.data_as(C.c_void_p)),
+                   "fvc_simple_iterate_energy")
+        return res, its
+
+    def energy_fields(self):
+        """(temperature, enthalpy, densities (numel,3))."""
+        t, h, ro = np.zeros(self.numel), np.zeros(self.numel), np.zeros((self.numel, 3))
+        _lib.check(self._L.fvc_simple_energy_fields(self._h, t.ctypes.data_as(C.c_void_p),
+                                                    h.ctypes.data_as(C.c_void_p),
+                                                    ro.ctypes.data_as(C.c_void_p)),
+                   "fvc_simple_energy_fields")
+        return t, h, ro
+
     def time_step(self) -> None:
         _lib.check(self._L.fvc_simple_time_step(self._h), "fvc_simple_time_step")
 

@@ -91,6 +91,16 @@ struct fvc_simple {
   double *b10 = nullptr, *b20 = nullptr, *adp = nullptr, *aup = nullptr, *bp = nullptr;
   double *rc1 = nullptr, *rc2 = nullptr, *rcp = nullptr, *xe = nullptr, *dots = nullptr;
   double *h_dots = nullptr;  // pinned
+  // ideal gas with the energy equation (fvc_simple_energy)
+  bool gas = false;
+  double grav[2] = {0.0, 0.0}, cp = 0.0, tref = 0.0;
+  int32_t *pedge_e = nullptr, *ia_e = nullptr, *ja_e = nullptr;
+  double *sedge_e = nullptr;
+  size_t nja_e = 0;
+  fvc_context *ctx_e = nullptr;
+  double *ro = nullptr, *en = nullptr, *en0 = nullptr, *temp = nullptr, *ge = nullptr;
+  double *ade = nullptr, *aue = nullptr, *be = nullptr, *be0 = nullptr, *rce = nullptr;
+  std::vector<int32_t> ident;
   std::vector<void *> owned;
 };
 
@@ -117,6 +127,7 @@ int32_t dcopy(fvc_simple *s, T *&ptr, const T *h, size_t n) {
 void release(fvc_simple *s) {
   if (s->ctx_u) fvc_context_destroy(s->ctx_u);
   if (s->ctx_pc) fvc_context_destroy(s->ctx_pc);
+  if (s->ctx_e) fvc_context_destroy(s->ctx_e);
   for (void *ptr : s->owned) cudaFree(ptr);
   if (s->h_dots) cudaFreeHost(s->h_dots);
   if (s->stream) cudaStreamDestroy(s->stream);
@@ -146,6 +157,53 @@ int32_t make_system(fvc_simple *s, const std::vector<int32_t> &ident, int matriz
   std::vector<double> ad(neq, 1.0), au((size_t)std::max<int64_t>(len, 1), 0.0);
   return fvc_matrix_set(*ctx, matriz, 1, neq, nad, ad.data(), au.data(), au.data(), ia.data(),
                         ja.data());
+}
+
+// start of a time step with the ideal gas (src/Simple.f:229-300): momentum
+// time terms from the densities of levels n-1 and n, w0 = w, the enthalpy's
+// time term and volume source, en0 = en
+int32_t time_term_gas(fvc_simple *s) {
+  const int n = s->numel;
+  fvc::split_w<<<fvc::g(n), fvc::kT, 0, s->stream>>>(n, s->w, s->u1, s->u2);
+  fvc::count_launch();
+  double *u0a = s->wp, *u0b = s->xe;  // the previous level (read only with bs)
+  fvc::split_w<<<fvc::g(n), fvc::kT, 0, s->stream>>>(n, s->w0, u0a, u0b);
+  fvc::count_launch();
+  const int mu = s->o.matriz_u;
+  int32_t rc;
+  for (int comp = 1; comp <= 2; ++comp) {
+    rc = fvc_cells_momentum_ideal_gas(&s->m, comp, 3, comp == 1 ? s->u1 : s->u2,
+                                      comp == 1 ? u0a : u0b, nullptr, nullptr, nullptr, nullptr,
+                                      s->ro, nullptr, s->grav[0], s->grav[1], s->o.dt, s->o.bs,
+                                      s->o.under_u, s->o.simple_c, mu, s->ia_u, s->ja_u, nullptr,
+                                      nullptr, comp == 1 ? s->b10 : s->b20, nullptr, nullptr,
+                                      nullptr, s->stream);
+    if (rc != FVC_OK) return rc;
+  }
+  if (cudaMemcpyAsync(s->w0, s->w, sizeof(double) * 2 * n, cudaMemcpyDeviceToDevice,
+                      s->stream) != cudaSuccess)
+    return FVC_ERR_CUDA;
+  rc = fvc_cells_energy(&s->m, 3, 4, s->pedge_e, s->sedge_e, s->en, s->en0, s->ro, nullptr,
+                        nullptr, s->o.dt, s->o.bs, 1, s->ia_e, s->ja_e, nullptr, nullptr, s->be0,
+                        nullptr, s->stream);
+  if (rc != FVC_OK) return rc;
+  return cudaMemcpyAsync(s->en0, s->en, sizeof(double) * n, cudaMemcpyDeviceToDevice,
+                         s->stream) == cudaSuccess
+             ? FVC_OK
+             : FVC_ERR_CUDA;
+}
+
+// massUpdate (src/Simple.f:1041-1050): ro(1) = ro(2), ro(2) = ro(3)
+__global__ void mass_update(int n, double *ro) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  ro[3 * (size_t)i] = ro[3 * (size_t)i + 1];
+  ro[3 * (size_t)i + 1] = ro[3 * (size_t)i + 2];
+}
+
+__global__ void fill(int n, double *x, double v) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) x[i] = v;
 }
 
 int32_t time_term(fvc_simple *s) {
@@ -265,8 +323,11 @@ int32_t fvc_simple_create(fvc_simple **out, int32_t device, int32_t numel, int32
   s->m.pedge = s->pedge;
   s->m.sedge = s->sedge;
   s->m.e = s->e;
-  std::vector<int32_t> ident((size_t)nshared * n);
+  std::vector<int32_t> &ident = s->ident;
+  ident.resize((size_t)nshared * n);
   if ((rc = fvc_mesh_numeq(num, nelcon, numel, nshared, ident.data())) != FVC_OK) return fail(rc);
+  s->cp = e[3];    // e(4,1), e(5,1): the reference's EnthalpyForTemp uses material 1
+  s->tref = e[4];
   if ((rc = make_system(s, ident, o.matriz_u, &s->ctx_u, &s->ia_u, &s->ja_u, &s->nja_u)) !=
       FVC_OK)
     return fail(rc);
@@ -294,6 +355,13 @@ int32_t fvc_simple_create(fvc_simple **out, int32_t device, int32_t numel, int32
 int32_t fvc_simple_time_step(fvc_simple *s) {
   if (!s) return FVC_ERR_ARG;
   cudaSetDevice(s->device);
+  if (s->gas) {
+    mass_update<<<fvc::g(s->numel), fvc::kT, 0, s->stream>>>(s->numel, s->ro);
+    fvc::count_launch();
+    int32_t rc = time_term_gas(s);
+    if (rc != FVC_OK) return rc;
+    return cudaStreamSynchronize(s->stream) == cudaSuccess ? FVC_OK : FVC_ERR_CUDA;
+  }
   int32_t rc = time_term(s);
   if (rc != FVC_OK) return rc;
   if (cudaMemcpyAsync(s->w0, s->w, sizeof(double) * 2 * s->numel, cudaMemcpyDeviceToDevice,
@@ -302,33 +370,51 @@ int32_t fvc_simple_time_step(fvc_simple *s) {
   return cudaStreamSynchronize(s->stream) == cudaSuccess ? FVC_OK : FVC_ERR_CUDA;
 }
 
-int32_t fvc_simple_iterate(fvc_simple *s, int32_t nit, double *res, int32_t *its) {
+}  // extern "C"
+
+namespace {
+
+int32_t iterate(fvc_simple *s, int32_t nit, double *res, int32_t *its, int nrep) {
   if (!s || nit < 0) return FVC_ERR_ARG;
   cudaSetDevice(s->device);
+  const bool gas = s->gas;
   const int n = s->numel, mu = s->o.matriz_u, mpc = s->o.matriz_pc;
   const fvc_cell_mesh *m = &s->m;
   cudaStream_t st = s->stream;
   int32_t rc;
   for (int it = 0; it < nit; ++it) {
-    int solver_its[3] = {0, 0, 0};
+    int solver_its[4] = {0, 0, 0, 0};
     // guess; gradients of u1, u2 (momentum ghost rules) and p
     fvc::split_w<<<fvc::g(n), fvc::kT, 0, st>>>(n, s->w, s->u1, s->u2);
     fvc::count_launch();
     if ((rc = fvc_cells_gradient(m, 1, 1, s->u1, s->gu1, st)) != FVC_OK) return rc;
     if ((rc = fvc_cells_gradient(m, 1, 2, s->u2, s->gu2, st)) != FVC_OK) return rc;
     if ((rc = fvc_cells_divergence(n, s->div, s->gu1, s->gu2, st)) != FVC_OK) return rc;
-    if ((rc = fvc_cells_gradient(m, 2, 3, s->p, s->gp, st)) != FVC_OK) return rc;
+    // the pressure's ghost rules: incompressible, or the ideal-gas cell's (p)
+    if ((rc = fvc_cells_gradient(m, gas ? 3 : 2, 3, s->p, s->gp, st)) != FVC_OK) return rc;
     // momentum systems (u0 = p), time term, cell residuals
-    if ((rc = fvc_cells_momentum(m, 1, 1, s->u1, s->p, s->w, s->gu1, s->gu2, s->gp, s->o.dt,
-                                 s->o.bs, s->o.under_u, s->o.simple_c, mu, s->ia_u, s->ja_u,
-                                 s->ad1, s->au1, s->b1, s->im, s->d, s->rc1, st)) != FVC_OK)
-      return rc;
+    if (gas)
+      rc = fvc_cells_momentum_ideal_gas(m, 1, 1, s->u1, s->p, s->w, s->gu1, s->gu2, s->gp, s->ro,
+                                        s->div, s->grav[0], s->grav[1], s->o.dt, s->o.bs,
+                                        s->o.under_u, s->o.simple_c, mu, s->ia_u, s->ja_u,
+                                        s->ad1, s->au1, s->b1, s->im, s->d, s->rc1, st);
+    else
+      rc = fvc_cells_momentum(m, 1, 1, s->u1, s->p, s->w, s->gu1, s->gu2, s->gp, s->o.dt,
+                              s->o.bs, s->o.under_u, s->o.simple_c, mu, s->ia_u, s->ja_u, s->ad1,
+                              s->au1, s->b1, s->im, s->d, s->rc1, st);
+    if (rc != FVC_OK) return rc;
     fvc::add_time_term<<<fvc::g(n), fvc::kT, 0, st>>>(n, s->num, s->b1, s->b10, s->rc1);
     fvc::count_launch();
-    if ((rc = fvc_cells_momentum(m, 2, 1, s->u2, s->p, s->w, s->gu2, s->gu1, s->gp, s->o.dt,
-                                 s->o.bs, s->o.under_u, s->o.simple_c, mu, s->ia_u, s->ja_u,
-                                 s->ad2, s->au2, s->b2, s->im, s->d, s->rc2, st)) != FVC_OK)
-      return rc;
+    if (gas)
+      rc = fvc_cells_momentum_ideal_gas(m, 2, 1, s->u2, s->p, s->w, s->gu2, s->gu1, s->gp, s->ro,
+                                        s->div, s->grav[0], s->grav[1], s->o.dt, s->o.bs,
+                                        s->o.under_u, s->o.simple_c, mu, s->ia_u, s->ja_u,
+                                        s->ad2, s->au2, s->b2, s->im, s->d, s->rc2, st);
+    else
+      rc = fvc_cells_momentum(m, 2, 1, s->u2, s->p, s->w, s->gu2, s->gu1, s->gp, s->o.dt,
+                              s->o.bs, s->o.under_u, s->o.simple_c, mu, s->ia_u, s->ja_u, s->ad2,
+                              s->au2, s->b2, s->im, s->d, s->rc2, st);
+    if (rc != FVC_OK) return rc;
     fvc::add_time_term<<<fvc::g(n), fvc::kT, 0, st>>>(n, s->num, s->b2, s->b20, s->rc2);
     fvc::count_launch();
     fvc::self_dots<<<2, fvc::kT, 0, st>>>(n, s->b1, s->b2, s->b2, s->dots);
@@ -345,10 +431,14 @@ int32_t fvc_simple_iterate(fvc_simple *s, int32_t nit, double *res, int32_t *its
     // updateVel, p' system and the residual norms
     fvc::join_w<<<fvc::g(n), fvc::kT, 0, st>>>(n, s->wp, s->u1, s->u2);
     fvc::count_launch();
-    if ((rc = fvc_cells_pressure_correction(m, s->wp, s->d, s->p, s->gp, s->o.int_vel, mpc,
-                                            s->ia_pc, s->ja_pc, s->adp, s->aup, s->bp, s->rcp,
-                                            st)) != FVC_OK)
-      return rc;
+    if (gas)
+      rc = fvc_cells_pressure_correction_ideal_gas(m, s->wp, s->d, s->p, s->gp, s->ro,
+                                                   s->o.int_vel, s->o.dt, s->o.bs, mpc, s->ia_pc,
+                                                   s->ja_pc, s->adp, s->aup, s->bp, s->rcp, st);
+    else
+      rc = fvc_cells_pressure_correction(m, s->wp, s->d, s->p, s->gp, s->o.int_vel, mpc,
+                                         s->ia_pc, s->ja_pc, s->adp, s->aup, s->bp, s->rcp, st);
+    if (rc != FVC_OK) return rc;
     fvc::self_dots<<<3, fvc::kT, 0, st>>>(n, s->rc1, s->rc2, s->rcp, s->dots);
     fvc::count_launch();
     cudaMemcpyAsync(s->h_dots, s->dots, 3 * sizeof(double), cudaMemcpyDeviceToHost, st);
@@ -359,20 +449,113 @@ int32_t fvc_simple_iterate(fvc_simple *s, int32_t nit, double *res, int32_t *its
       if ((rc = solve(s, s->ctx_pc, s->o.code_pc, s->adp, s->aup, s->bp, s->pc, s->o.tol_pc,
                       &solver_its[2])) != FVC_OK)
         return rc;
-      if ((rc = fvc_cells_gradient(m, 2, 2, s->pc, s->gpc, st)) != FVC_OK) return rc;
+      if ((rc = fvc_cells_gradient(m, gas ? 3 : 2, 2, s->pc, s->gpc, st)) != FVC_OK) return rc;
       if ((rc = fvc_cells_simple_update(n, s->w, s->p, s->u1, s->u2, s->pc, s->gpc, s->d,
                                         s->o.under_pc, st)) != FVC_OK)
         return rc;
     }
+    double re = 0.0;
+    if (gas) {  // energy (src/Simple.f:647-710)
+      if ((rc = fvc_cells_energy_gradient(m, 3, s->pedge_e, s->sedge_e, s->en, s->ge, st)) !=
+          FVC_OK)
+        return rc;
+      if ((rc = fvc_cells_energy(m, 3, 1, s->pedge_e, s->sedge_e, s->en, s->en, s->ro, s->w,
+                                 s->ge, s->o.dt, s->o.bs, 1, s->ia_e, s->ja_e, s->ade, s->aue,
+                                 s->be, s->rce, st)) != FVC_OK)
+        return rc;
+      fvc::add_time_term<<<fvc::g(n), fvc::kT, 0, st>>>(n, s->num, s->be, s->be0, s->rce);
+      fvc::count_launch();
+      fvc::self_dots<<<2, fvc::kT, 0, st>>>(n, s->be, s->rce, s->rce, s->dots);
+      fvc::count_launch();
+      cudaMemcpyAsync(s->h_dots, s->dots, 2 * sizeof(double), cudaMemcpyDeviceToHost, st);
+      if (cudaStreamSynchronize(st) != cudaSuccess) return FVC_ERR_CUDA;
+      re = std::sqrt(s->h_dots[0]);
+      if (re >= 1.0e-32) {
+        re = std::sqrt(s->h_dots[1]);
+        if ((rc = solve(s, s->ctx_e, 2, s->ade, s->aue, s->be, s->en, s->o.tol_u,
+                        &solver_its[3])) != FVC_OK)
+          return rc;
+        if ((rc = fvc_cells_enthalpy_temperature(n, s->en, s->temp, s->cp, s->tref, 1, st)) !=
+                FVC_OK ||
+            (rc = fvc_cells_ideal_gas_density(n, s->ro, s->temp, 1, 3, 1.0, 1.0, st)) != FVC_OK)
+          return rc;
+      }
+    }
     if (res) {
-      res[3 * it] = r1;
-      res[3 * it + 1] = r2;
-      res[3 * it + 2] = rpc;
+      res[nrep * it] = r1;
+      res[nrep * it + 1] = r2;
+      res[nrep * it + 2] = rpc;
+      if (nrep == 4) res[4 * it + 3] = re;
     }
     if (its)
-      for (int k = 0; k < 3; ++k) its[3 * it + k] = solver_its[k];
+      for (int k = 0; k < nrep; ++k) its[nrep * it + k] = solver_its[k];
   }
   return cudaStreamSynchronize(st) == cudaSuccess ? FVC_OK : FVC_ERR_CUDA;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t fvc_simple_iterate(fvc_simple *s, int32_t nit, double *res, int32_t *its) {
+  return iterate(s, nit, res, its, 3);
+}
+
+int32_t fvc_simple_iterate_energy(fvc_simple *s, int32_t nit, double *res, int32_t *its) {
+  if (!s || !s->gas) return FVC_ERR_ARG;
+  return iterate(s, nit, res, its, 4);
+}
+
+int32_t fvc_simple_energy(fvc_simple *s, const int32_t *pedge_e, const double *sedge_e,
+                          double gx, double gy, double t0) {
+  if (!s || !pedge_e || !sedge_e || s->gas || s->cp == 0.0) return FVC_ERR_ARG;
+  cudaSetDevice(s->device);
+  const size_t n = s->numel, ld = s->nshared + 1;
+  int32_t rc;
+  if ((rc = dcopy(s, s->pedge_e, pedge_e, ld * n)) != FVC_OK ||
+      (rc = dcopy(s, s->sedge_e, sedge_e, ld * n)) != FVC_OK ||
+      (rc = make_system(s, s->ident, 1, &s->ctx_e, &s->ia_e, &s->ja_e, &s->nja_e)) != FVC_OK)
+    return rc;
+  double **vec[] = {&s->en, &s->en0, &s->temp, &s->ade, &s->be, &s->be0, &s->rce};
+  for (double **v : vec)
+    if ((rc = dalloc(s, *v, n)) != FVC_OK) return rc;
+  if ((rc = dalloc(s, s->ro, 3 * n)) != FVC_OK || (rc = dalloc(s, s->ge, 2 * n)) != FVC_OK ||
+      (rc = dalloc(s, s->aue, s->nja_e)) != FVC_OK)
+    return rc;
+  s->grav[0] = gx;
+  s->grav[1] = gy;
+  // start-up of src/Main.f:815-837: T uniform, h from T, en0 = en, w0 = w,
+  // the three density levels from the ideal-gas law
+  fill<<<fvc::g((int)n), fvc::kT, 0, s->stream>>>((int)n, s->temp, t0);
+  fvc::count_launch();
+  if ((rc = fvc_cells_enthalpy_temperature((int)n, s->en, s->temp, s->cp, s->tref, 0,
+                                           s->stream)) != FVC_OK)
+    return rc;
+  cudaMemcpyAsync(s->en0, s->en, sizeof(double) * n, cudaMemcpyDeviceToDevice, s->stream);
+  cudaMemcpyAsync(s->w0, s->w, sizeof(double) * 2 * n, cudaMemcpyDeviceToDevice, s->stream);
+  for (int row = 1; row <= 3; ++row)
+    if ((rc = fvc_cells_ideal_gas_density((int)n, s->ro, s->temp, 1, row, 1.0, 1.0,
+                                          s->stream)) != FVC_OK)
+      return rc;
+  s->gas = true;
+  if ((rc = time_term_gas(s)) != FVC_OK) return rc;
+  return cudaStreamSynchronize(s->stream) == cudaSuccess ? FVC_OK : FVC_ERR_CUDA;
+}
+
+int32_t fvc_simple_energy_fields(const fvc_simple *s, double *temp, double *en, double *ro) {
+  if (!s || !s->gas) return FVC_ERR_ARG;
+  cudaSetDevice(s->device);
+  const size_t n = s->numel;
+  if (temp && cudaMemcpyAsync(temp, s->temp, sizeof(double) * n, cudaMemcpyDeviceToHost,
+                              s->stream) != cudaSuccess)
+    return FVC_ERR_CUDA;
+  if (en && cudaMemcpyAsync(en, s->en, sizeof(double) * n, cudaMemcpyDeviceToHost, s->stream) !=
+                cudaSuccess)
+    return FVC_ERR_CUDA;
+  if (ro && cudaMemcpyAsync(ro, s->ro, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost,
+                            s->stream) != cudaSuccess)
+    return FVC_ERR_CUDA;
+  return cudaStreamSynchronize(s->stream) == cudaSuccess ? FVC_OK : FVC_ERR_CUDA;
 }
 
 int32_t fvc_simple_fields(const fvc_simple *s, double *w, double *p) {

@@ -489,6 +489,33 @@ int32_t fvc_simple_iterate(fvc_simple *s, int32_t nit, double *res, int32_t *its
  * (src/Simple.f:229-266). */
 int32_t fvc_simple_time_step(fvc_simple *s);
 
+/* Switches the loop to the ideal-gas iteration with the energy equation
+ * (materials of type 53/55; src/Simple.f with sEnergy): momentum
+ * cell_si_eb_idg_ggl with buoyancy from gravity (gx, gy), p' cell_si_p_idg_ggl,
+ * then the enthalpy cell_e_eb_idg_ggl (CSRD, BiCGSTAB at tol_u) with
+ * pedge_e / sedge_e (HOST, nshared+1 per cell: 0 flux, 1 temperature,
+ * 2 inflow, 4 outflow; face nshared+1 a volume source), the temperature from
+ * the enthalpy and the current density level from the ideal-gas law of
+ * air.  Starts as src/Main.f:815-837 does: temperature t0 everywhere, the
+ * enthalpy cp (t0 - tRef) with cp = e(4,1), tRef = e(5,1), all three
+ * density levels from the ideal-gas law, and the time terms of a first
+ * step.  The domain is open (the closed-cavity pressure rescaling is not
+ * applied).  fvc_simple_time_step then shifts the density levels
+ * (massUpdate) before forming the new time terms. */
+int32_t fvc_simple_energy(fvc_simple *s, const int32_t *pedge_e,
+                          const double *sedge_e, double gx, double gy,
+                          double t0);
+
+/* As fvc_simple_iterate for a loop switched by fvc_simple_energy; res and
+ * its take 4 values per iteration: u1, u2, p', enthalpy. */
+int32_t fvc_simple_iterate_energy(fvc_simple *s, int32_t nit, double *res,
+                                  int32_t *its);
+
+/* Host copies of the temperature, enthalpy (numel) and densities (3,numel)
+ * of a loop switched by fvc_simple_energy; any may be NULL. */
+int32_t fvc_simple_energy_fields(const fvc_simple *s, double *temp, double *en,
+                                 double *ro);
+
 /* Host copies of the velocity w(2,numel) and pressure p(numel); either may
  * be NULL.  fvc_simple_set_fields uploads them (e.g. to restart). */
 int32_t fvc_simple_fields(const fvc_simple *s, double *w, double *p);

@@ -32,3 +32,14 @@ def cavity(orc, nx, kind="quad", nu=0.01, rho=1.0, lid=1.0, pin_cell=1, limiter=
     e[0, 0], e[0, 1], e[0, 5], e[0, 6] = nu, rho, cc, limiter
     return dict(coor=m.coor, ix=ix, nelcon=nelcon, num=num, ident=ident, pedge=pedge,
                 sedge=sedge, e=e, nshared=nsh, numel=numel, mesh=m)
+
+
+def hot_wall_nusselt(case, temp):
+    """Mean Nusselt number of the hot (x = 0) wall of a natural_convection_cavity
+    on uniform quads: (T_wall - T_P) / (h/2) L / dT averaged over the wall."""
+    nx = int(round(np.sqrt(case["numel"])))
+    side, dt_wall = case["side"], 1.0
+    h = side / nx
+    t_wall = case["t0"] + 0.5 * dt_wall
+    tp = temp.reshape(nx, nx)[:, 0]
+    return float(np.mean((t_wall - tp) / (0.5 * h)) * side / dt_wall)

@@ -83,3 +83,50 @@ def test_bad_inputs_rejected(orc):
         gpu_loop(case, int_vel=3)
     with pytest.raises(FvcError):
         gpu_loop(case, matriz_u=2)
+
+
+def gas_loop(case, **kw):
+    loop = gpu_loop(case, **kw)
+    loop.enable_energy(case["pedgeE"], case["sedgeE"], case["gravity"], case["t0"])
+    return loop
+
+
+@pytest.mark.parametrize("kind,nx", [("quad", 12), ("tri", 9)])
+def test_ideal_gas_loop_matches_reference(orc, kind, nx):
+    # transient natural convection (dt 0.5 s, two steps of 8 outer
+    # iterations): the GPU loop against the restated iteration, solver
+    # tolerances 1e-13 so that the two differ only in rounding
+    from oracle.simple_ref import GasSimpleRef
+    from fortranfvcell_gb300.cases import natural_convection_cavity
+    c = natural_convection_cavity(nx, ra=1e4, kind=kind, jitter=0.15 if kind == "tri" else 0.0)
+    ref = GasSimpleRef(orc, c, dt=0.5, tol_pcg=1e-13, tol_bcg=1e-13, matriz_u=1)
+    loop = gas_loop(c, dt=0.5, tol_u=1e-13, tol_pc=1e-13, matriz_u=1)
+    hist, res = [], []
+    for step in range(2):
+        if step:
+            ref.end_step()
+            ref.start_step()
+            loop.time_step()
+        hist += [ref.step() for _ in range(8)]
+        r, _ = loop.iterate_energy(8)
+        res.append(r)
+    res = np.concatenate(res)
+    np.testing.assert_allclose(res, np.array(hist), rtol=1e-7, atol=1e-18)
+    w, p = loop.fields()
+    t, h, ro = loop.energy_fields()
+    loop.close()
+    np.testing.assert_allclose(w, ref.w, rtol=0, atol=1e-9 * np.abs(ref.w).max())
+    np.testing.assert_allclose(t, ref.temp, rtol=0, atol=1e-10)
+    np.testing.assert_allclose(ro, ref.ro, rtol=1e-13)
+
+
+def test_ideal_gas_loop_reaches_steady_convection(orc):
+    from fortranfvcell_gb300.cases import natural_convection_cavity
+    from _simple_ref import hot_wall_nusselt
+    c = natural_convection_cavity(16, ra=1e3)
+    loop = gas_loop(c)
+    res, its = loop.iterate_energy(300)
+    t, _, _ = loop.energy_fields()
+    loop.close()
+    assert res[-1, :3].max() < 1e-12 and (its[:, 3] > 0).any()
+    assert abs(hot_wall_nusselt(c, t) - 1.118) < 0.02 * 1.118

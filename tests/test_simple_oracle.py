@@ -165,3 +165,23 @@ def test_ideal_gas_density_and_enthalpy(orc):
     t2 = np.zeros(3)
     orc.enthalpy_temp(h, t2, e, True)
     np.testing.assert_allclose(t2, t, rtol=1e-15)
+
+
+def test_natural_convection_nusselt(orc):
+    # differentially heated cavity, ideal gas with the energy equation:
+    # hot-wall Nusselt numbers near de Vahl Davis (1983), 1.118 at Ra = 1e3
+    # and 2.243 at Ra = 1e4 (coarse meshes: within 2% and 3%)
+    from oracle.simple_ref import GasSimpleRef
+    from fortranfvcell_gb300.cases import natural_convection_cavity
+    from _simple_ref import hot_wall_nusselt
+    for nx, ra, nit, nu_ref, tol in ((16, 1e3, 300, 1.118, 0.02), (24, 1e4, 400, 2.243, 0.03)):
+        c = natural_convection_cavity(nx, ra=ra)
+        s = GasSimpleRef(orc, c, dt=1e10)
+        for _ in range(nit):
+            r = s.step()
+        assert max(r[:3]) < 1e-12
+        nu = hot_wall_nusselt(c, s.temp)
+        assert abs(nu - nu_ref) < tol * nu_ref, (ra, nu)
+        # buoyancy turns the flow clockwise: up along the hot wall
+        v = s.w[:, 1].reshape(nx, nx)
+        assert v[nx // 2, 0] > 0 and v[nx // 2, -1] < 0
