@@ -364,6 +364,8 @@ def run_ours(args):
         line["simple_c1"] = run_simple_c1(args)
     if rank == 0 and args.c4_cases > 0:
         line["batched_c4"] = run_batched_c4(args)
+    if rank == 0 and args.c3_nx > 0:
+        line["gas_c3"] = run_gas_c3(args)
     return line
 
 
@@ -408,6 +410,74 @@ def run_simple_c1(args):
         out["cpu_port_s"] = round(cpu_s, 4)
         out["cpu_kind"] = "port (restated reference, sequential solvers, 1 core)"
         out["max_abs_w_difference"] = float(f"{np.abs(w - ref.w).max():.2e}")
+    return out
+
+
+def run_gas_c3(args):
+    """The C3 configuration: natural convection in a differentially heated
+    square cavity, ideal-gas SIMPLE loop with the energy equation (air,
+    Pr 0.72, dT 1 K around 20 C, adiabatic top and bottom, side set for
+    Ra = 1e6) on nx x nx quads, steady pseudo-time (dt 1e10), underU 0.7,
+    underPc 0.3, from rest at 20 C.  GPU: the device-resident loop with FP64
+    solves and with mixed FP32/FP64 solves, the same outer iterations;
+    per-field differences of the mixed run against the FP64 one.  CPU: the
+    same iteration restated (sequential solvers, one core), a bounded
+    sample of outer iterations."""
+    from fortranfvcell_gb300.cases import natural_convection_cavity
+    from fortranfvcell_gb300.cells import SimpleLoop, simple_opts
+
+    def loop_for(case, prec):
+        # mixed: the FP32-inner defect correction for the p' PCG; momentum and
+        # enthalpy stay on FP64 BiCGSTAB (the FP32-inner BiCGSTAB stalls on
+        # the 512^2 enthalpy system)
+        lp = SimpleLoop(case["coor"], case["ix"], case["nelcon"], case["num"], case["pedge"],
+                        case["sedge"], case["e"],
+                        opts=simple_opts(precision=prec, precision_u="fp64"))
+        lp.enable_energy(case["pedgeE"], case["sedgeE"], case["gravity"], case["t0"])
+        return lp
+
+    warm = natural_convection_cavity(32, ra=args.c3_ra)
+    for prec in ("fp64", "mixed"):
+        lp = loop_for(warm, prec)
+        lp.iterate_energy(3)
+        lp.close()
+    c = natural_convection_cavity(args.c3_nx, ra=args.c3_ra)
+    nit = args.c3_its
+    out = {"workload": f"natural convection, ideal gas + energy, {args.c3_nx}x{args.c3_nx} quads "
+                       f"({c['numel']} cells), Ra={args.c3_ra:g}, steady pseudo-time, "
+                       f"{nit} outer iterations from rest"}
+    fields = {}
+    for prec in ("fp64", "mixed"):
+        lp = loop_for(c, prec)
+        t0 = time.perf_counter()
+        res, its = lp.iterate_energy(nit)
+        el = time.perf_counter() - t0
+        w, p = lp.fields()
+        t, _, _ = lp.energy_fields()
+        lp.close()
+        fields[prec] = (w, p, t)
+        out[prec] = {"gpu_s": round(el, 3), "outer_its_per_s": round(nit / el, 2),
+                     "solver_iterations": [int(v) for v in its.sum(axis=0)],
+                     "final_residuals": [float(f"{v:.3e}") for v in res[-1]]}
+    (w64, p64, t64), (wmx, pmx, tmx) = fields["fp64"], fields["mixed"]
+    out["mixed_vs_fp64"] = {
+        "w_rel_max": float(f"{np.abs(wmx - w64).max() / np.abs(w64).max():.2e}"),
+        "p_rel_max": float(f"{np.abs(pmx - p64).max() / max(np.abs(p64).max(), 1e-300):.2e}"),
+        "t_max_K": float(f"{np.abs(tmx - t64).max():.2e}")}
+    if not args.no_cpu:
+        from oracle import oracle
+        from oracle.simple_ref import GasSimpleRef
+        ref = GasSimpleRef(oracle, c, dt=1e10)
+        t0 = time.perf_counter()
+        k = 0
+        while k < nit and (k == 0 or time.perf_counter() - t0 < args.cpu_seconds):
+            ref.step()
+            k += 1
+        per_it = (time.perf_counter() - t0) / k
+        out["cpu_port_s_per_outer_it"] = round(per_it, 3)
+        out["cpu_kind"] = (f"port (restated reference, sequential solvers, 1 core), first {k} "
+                           f"outer iterations timed")
+        out["gpu_fp64_over_cpu"] = round(per_it / (out["fp64"]["gpu_s"] / nit), 1)
     return out
 
 
@@ -633,6 +703,10 @@ def main():
     ap.add_argument("--no-simple", action="store_true", help="skip the C1 SIMPLE leg")
     ap.add_argument("--simple-nx", type=int, default=64)
     ap.add_argument("--simple-its", type=int, default=200)
+    ap.add_argument("--c3-nx", type=int, default=512,
+                    help="natural-convection C3 leg: cells per side (0 skips it)")
+    ap.add_argument("--c3-ra", type=float, default=1.0e6)
+    ap.add_argument("--c3-its", type=int, default=30)
     ap.add_argument("--c4-cases", type=int, default=256,
                     help="batched C4 leg: number of systems (0 skips it)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)

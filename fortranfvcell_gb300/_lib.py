@@ -98,6 +98,7 @@ class FvcSimpleOpts(C.Structure):
         ("tol_pc", F64),
         ("maxit", I32),
         ("precision", I32),
+        ("precision_u", I32),
     ]
 
 

@@ -143,7 +143,7 @@ def simple_opts(**kw):
     o = _lib.FvcSimpleOpts()
     _lib.load().fvc_simple_opts_default(C.byref(o))
     for k, v in kw.items():
-        if k == "precision":
+        if k in ("precision", "precision_u"):
             v = {"fp64": _lib.FVC_PREC_FP64, "mixed": _lib.FVC_PREC_MIXED}.get(v, v)
         setattr(o, k, v)
     return o

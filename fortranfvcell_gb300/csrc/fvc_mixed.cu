@@ -1097,6 +1097,8 @@ __global__ void __launch_bounds__(1024, 1) mixed_cg_staged_w4(MArgs a) {
 
 // The reference's Jacobi BiCGSTAB (Iterativos.f:140-234) in FP32 on the
 // correction equation A e = r, inside FP64 defect correction.
+constexpr int kBcgStall = 100;
+
 __global__ void __launch_bounds__(1024, 1) mixed_bicgstab(MArgs a) {
   __shared__ double red[kMaxNV * 32];
   const MPart P(a.A.nslices, a.A.n);
@@ -1132,7 +1134,8 @@ __global__ void __launch_bounds__(1024, 1) mixed_bicgstab(MArgs a) {
       e[row] = make_float2(0.0f, 0.0f);
     }
     if (!grid_barrier(a.gs, ep)) return;
-    int it = 0;
+    int it = 0, it_best = 0;
+    double best = fabs(d);
     for (;;) {
       ++it;
       // v = A z ; rr0 = s.r0 ; v.r0
@@ -1148,6 +1151,9 @@ __global__ void __launch_bounds__(1024, 1) mixed_bicgstab(MArgs a) {
       if (!grid_allreduce<2>(a.gs, ep, acc, red)) return;
       const double rr0 = acc[0];
       const float alpha = (float)(rr0 / acc[1]);
+      // breakdown (v.r0 or r0.s vanished in FP32): leave the correction as it
+      // is and restart from an FP64 residual in the next sweep
+      if (!isfinite(alpha) || alpha == 0.0f) break;
       // e += alpha z ; s -= alpha v ; z = s/m
       MFOR_ROWS(P) {
         e[row] = df_axpy(e[row], alpha, 0.0f, z[row]);
@@ -1168,6 +1174,7 @@ __global__ void __launch_bounds__(1024, 1) mixed_bicgstab(MArgs a) {
       acc[1] = c3.value();
       if (!grid_allreduce<2>(a.gs, ep, acc, red)) return;
       const float omega = (acc[1] > 0.0) ? (float)(acc[0] / acc[1]) : 0.0f;
+      if (!isfinite(omega)) break;
       // e += w z ; s -= w t ; s.z ; r0.s
       CSum c4, c5;
       MFOR_ROWS(P) {
@@ -1183,6 +1190,14 @@ __global__ void __launch_bounds__(1024, 1) mixed_bicgstab(MArgs a) {
       if (!(acc2[0] == acc2[0]) || fabs(acc2[0]) <= stop2 || inner_total + it >= a.maxit ||
           omega == 0.0f)
         break;
+      // restarted BiCGSTAB: an inner solve whose residual has not improved
+      // for kBcgStall iterations (FP32 stagnation) restarts from an FP64 one
+      if (fabs(acc2[0]) < 0.99 * best) {
+        best = fabs(acc2[0]);
+        it_best = it;
+      } else if (it - it_best > kBcgStall) {
+        break;
+      }
       const float beta = (float)((acc2[1] / rr0) * ((double)alpha / (double)omega));
       // p = s + beta (p - w v) ; z = p/m
       MFOR_ROWS(P) {

@@ -10,6 +10,7 @@
 // Only the few norms that steer the reference's control flow cross to the
 // host.
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <new>
 #include <vector>
@@ -231,18 +232,25 @@ int32_t time_term(fvc_simple *s) {
 
 // x (cells) -> equation order, solve, back to cells
 int32_t solve(fvc_simple *s, fvc_context *ctx, int code, const double *ad, const double *au,
-              const double *b, double *x_cells, double tol, int *its) {
+              const double *b, double *x_cells, double tol, int *its, const char *what) {
   const int n = s->numel;
   int32_t rc = fvc_getres(n, s->num, x_cells, s->xe, 1, s->stream);
   if (rc != FVC_OK) return rc;
   if ((rc = fvc_matrix_update_values(ctx, ad, au, au)) != FVC_OK) return rc;
   fvc_opts o;
   fvc_opts_default(&o);
-  o.precision = s->o.precision;
+  // p' (ctx_pc) takes precision; momentum and energy precision_u when set
+  o.precision = (ctx != s->ctx_pc && s->o.precision_u >= 0) ? s->o.precision_u : s->o.precision;
   fvc_stats st;
   rc = fvc_solve(ctx, code, b, s->xe, tol, s->o.maxit, &o, &st);
   if (its) *its = st.iterations;
-  if (rc != FVC_OK) return rc;
+  if (rc != FVC_OK) {
+    // the reference prints the failing solve before it stops
+    fprintf(stderr, "fvcgpu: SIMPLE %s solve (code %d, %s) ended with status %d after %d "
+                    "iterations\n", what, code, o.precision == FVC_PREC_MIXED ? "mixed" : "fp64",
+            rc, st.iterations);
+    return rc;
+  }
   return fvc_getres(n, s->num, x_cells, s->xe, 0, s->stream);
 }
 
@@ -265,6 +273,7 @@ void fvc_simple_opts_default(fvc_simple_opts *o) {
   o->tol_pc = 1.0e-8;
   o->maxit = 50000;
   o->precision = FVC_PREC_FP64;
+  o->precision_u = -1;
 }
 
 int32_t fvc_simple_create(fvc_simple **out, int32_t device, int32_t numel, int32_t nnode,
@@ -423,10 +432,10 @@ int32_t iterate(fvc_simple *s, int32_t nit, double *res, int32_t *its, int nrep)
     if (cudaStreamSynchronize(st) != cudaSuccess) return FVC_ERR_CUDA;
     const bool solve1 = s->h_dots[0] >= 1.0e-32, solve2 = s->h_dots[1] >= 1.0e-32;
     if (solve1 && (rc = solve(s, s->ctx_u, s->o.code_u, s->ad1, s->au1, s->b1, s->u1,
-                              s->o.tol_u, &solver_its[0])) != FVC_OK)
+                              s->o.tol_u, &solver_its[0], "u1")) != FVC_OK)
       return rc;
     if (solve2 && (rc = solve(s, s->ctx_u, s->o.code_u, s->ad2, s->au2, s->b2, s->u2,
-                              s->o.tol_u, &solver_its[1])) != FVC_OK)
+                              s->o.tol_u, &solver_its[1], "u2")) != FVC_OK)
       return rc;
     // updateVel, p' system and the residual norms
     fvc::join_w<<<fvc::g(n), fvc::kT, 0, st>>>(n, s->wp, s->u1, s->u2);
@@ -447,7 +456,7 @@ int32_t iterate(fvc_simple *s, int32_t nit, double *res, int32_t *its, int nrep)
     const double rpc = std::sqrt(s->h_dots[2]);
     if (rpc >= 1.0e-32) {
       if ((rc = solve(s, s->ctx_pc, s->o.code_pc, s->adp, s->aup, s->bp, s->pc, s->o.tol_pc,
-                      &solver_its[2])) != FVC_OK)
+                      &solver_its[2], "p'")) != FVC_OK)
         return rc;
       if ((rc = fvc_cells_gradient(m, gas ? 3 : 2, 2, s->pc, s->gpc, st)) != FVC_OK) return rc;
       if ((rc = fvc_cells_simple_update(n, s->w, s->p, s->u1, s->u2, s->pc, s->gpc, s->d,
@@ -473,7 +482,7 @@ int32_t iterate(fvc_simple *s, int32_t nit, double *res, int32_t *its, int nrep)
       if (re >= 1.0e-32) {
         re = std::sqrt(s->h_dots[1]);
         if ((rc = solve(s, s->ctx_e, 2, s->ade, s->aue, s->be, s->en, s->o.tol_u,
-                        &solver_its[3])) != FVC_OK)
+                        &solver_its[3], "energy")) != FVC_OK)
           return rc;
         if ((rc = fvc_cells_enthalpy_temperature(n, s->en, s->temp, s->cp, s->tref, 1, st)) !=
                 FVC_OK ||

@@ -462,6 +462,8 @@ typedef struct {
   double tol_pc;
   int32_t maxit;      /* per linear solve                                   */
   int32_t precision;  /* FVC_PREC_FP64 or FVC_PREC_MIXED for the solves     */
+  int32_t precision_u; /* -1: as precision; else FVC_PREC_* for the momentum
+                          and energy solves only (p' keeps precision)       */
 } fvc_simple_opts;
 
 /* Defaults: dt 1e10 (steady), underU 0.7, underPc 0.3, SIMPLE, intVel 5,
