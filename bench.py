@@ -711,11 +711,19 @@ def main():
                     help="batched C4 leg: number of systems (0 skips it)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--ref-sample-its", type=int, default=300)
+    ap.add_argument("--profile-leg", choices=["c1", "c3", "c4"], default=None,
+                    help="profiling: run only this leg (no CPU side) and print its JSON")
     ap.add_argument("--profile-its", type=int, default=0,
                     help="profiling case: run each solver once for this many iterations")
     args = ap.parse_args()
     if args.profile_its > 0:
         print(json.dumps(run_profile_case(args)), flush=True)
+        return
+    if args.profile_leg:
+        args.no_cpu = True
+        args.c4_batched_only = True
+        leg = {"c1": run_simple_c1, "c3": run_gas_c3, "c4": run_batched_c4}[args.profile_leg]
+        print(json.dumps(leg(args)), flush=True)
         return
     if args.warmup < 3:
         log("note: the timing rules want >= 3 warm-up steps")
