@@ -19,7 +19,7 @@ BUILD = os.path.join(HERE, "_build")
 LIBDIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIBDIR, "libfvcgpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["fvc_krylov.cu", "fvc_mixed.cu", "fvc_gather.cu", "fvc_assembly.cu",
+SOURCES = ["fvc_krylov.cu", "fvc_cluster.cu", "fvc_mixed.cu", "fvc_gather.cu", "fvc_assembly.cu",
            "fvc_noalloc.cu", "fvc_simple.cu", "fvc_simple_driver.cu", "fvc_api.cpp",
            "fvc_mesh.cpp"]
 # files whose kernels reproduce the reference's rounding: no FMA contraction

@@ -77,6 +77,11 @@ int32_t run_bicgstab(const DeviceMatrix &A, Scratch &S, const double *b,
 int32_t run_gmres(const DeviceMatrix &A, Scratch &S, const double *b, double *x,
                   double tol, int maxit, const fvc_opts &o, cudaStream_t stream,
                   fvc_stats *st);
+// PCG on one thread-block cluster (fvc_cluster.cu); FVC_ERR_UNSUPPORTED
+// when the system does not fit one cluster's shared memory
+int32_t run_pcg_cluster(const DeviceMatrix &A, Scratch &S, const double *b, double *x,
+                        double tol, int maxit, int init, const fvc_opts &o,
+                        cudaStream_t stream, fvc_stats *st);
 int32_t run_pcg_batched(const DeviceMatrix &A, Scratch &S, int nsys,
                         const int32_t *row_start, const double *b, double *x,
                         double tol, int maxit, int init, const fvc_opts &o,

@@ -754,6 +754,12 @@ int32_t run_persistent(K kernel, const DeviceMatrix &A, Scratch &S, const double
 
 int32_t run_pcg(const DeviceMatrix &A, Scratch &S, const double *b, double *x, double tol,
                 int maxit, int init, const fvc_opts &o, cudaStream_t stream, fvc_stats *st) {
+  // a system that fits one thread-block cluster runs there (fvc_cluster.cu)
+  // unless the caller fixed the launch shape of the grid-wide kernel
+  if (o.block_threads == 0 && o.blocks_per_sm == 0 && o.max_blocks == 0) {
+    const int32_t rc = run_pcg_cluster(A, S, b, x, tol, maxit, init, o, stream, st);
+    if (rc != FVC_ERR_UNSUPPORTED) return rc;
+  }
   return run_persistent(pcg_f64, A, S, b, x, tol, maxit, init, o, stream, st, 5, false);
 }
 

@@ -342,3 +342,33 @@ def test_single_equation_and_ragged_sizes(fvc, orc):
         st, so, sg, x_ref, x_gpu, _ = _solve_both(fvc, orc, s, 1, 1, True, 1e-12, b=b)
         assert st == 0
         assert np.linalg.norm(x_gpu - x_ref) <= REL_TOL * max(1.0, np.linalg.norm(x_ref))
+
+
+@pytest.mark.parametrize("kind,nx", [("quad", 1), ("quad", 3), ("tri", 14), ("quad", 64),
+                                     ("mixed", 70), ("quad", 170), ("quad", 200)])
+def test_cluster_pcg_matches_grid_and_reference(fvc, orc, kind, nx):
+    # systems up to 8192 rows run on one thread-block cluster (default
+    # launch shape); a fixed block size selects the grid-wide kernel; both
+    # against the restated PCG.  The larger systems take the grid kernel
+    # either way.
+    from fortranfvcell_gb300 import mesh
+    m = mesh.square_mesh(nx, kind=kind, jitter=0.2 if kind != "quad" else 0.0, seed=nx)
+    s = pressure(orc, m, 1, True)
+    n = s["n"]
+    b = np.random.default_rng(nx).uniform(-1, 1, n)
+    x_ref = np.zeros(n)
+    st, so = orc.solver(s["ad"].copy(), s["au"].copy(), s["au"].copy(), x_ref, b.copy(), s["ia"],
+                        s["ja"], n, s["nad"], True, 1e-10, 50000, 1, 1)
+    assert st == 0
+    out = {}
+    for name, opts in (("cluster", fvc.make_opts("fp64")),
+                       ("grid", fvc.make_opts("fp64", block_threads=128))):
+        x = np.zeros(n)
+        sg = fvc.solver(s["ad"], s["au"], s["au"], x, b, s["ia"], s["ja"], n, s["nad"], True,
+                        1e-10, 50000, 1, 1, opts=opts)
+        out[name] = (x, sg)
+        err = np.linalg.norm(x - x_ref) / max(np.linalg.norm(x_ref), 1e-300)
+        assert err <= REL_TOL, (name, n, err)
+        assert abs(sg.iterations - so.iterations) <= ITS_TOL, (name, n, sg.iterations,
+                                                               so.iterations)
+        assert abs(sg.energy - so.energy) <= 1e-9 * abs(so.energy), name
