@@ -156,6 +156,8 @@ SIGNATURES = {
     "fvc_simple_iterate_energy": ([P, I32, P, P], I32),
     "fvc_simple_energy": ([P, P, P, F64, F64, F64], I32),
     "fvc_simple_energy_fields": ([P, P, P, P], I32),
+    "fvc_simple_get_state": ([P, P, P, P, P, P, P], I32),
+    "fvc_simple_set_state": ([P, P, P, P, P, P, P], I32),
     "fvc_simple_time_step": ([P], I32),
     "fvc_simple_fields": ([P, P, P], I32),
     "fvc_simple_set_fields": ([P, P, P], I32),

@@ -208,6 +208,28 @@ class SimpleLoop:
                    "fvc_simple_energy_fields")
         return t, h, ro
 
+    def get_state(self, energy: bool = False) -> dict:
+        """w, w0, p (and en, en0, ro with the energy equation), as saveSimple
+        writes them."""
+        n = self.numel
+        st = dict(w=np.zeros((n, 2)), w0=np.zeros((n, 2)), p=np.zeros(n))
+        if energy:
+            st.update(en=np.zeros(n), en0=np.zeros(n), ro=np.zeros((n, 3)))
+        ptr = lambda k: st[k].ctypes.data_as(C.c_void_p) if k in st else None
+        _lib.check(self._L.fvc_simple_get_state(self._h, *[ptr(k) for k in
+                                                          ("w", "w0", "p", "en", "en0", "ro")]),
+                   "fvc_simple_get_state")
+        return st
+
+    def set_state(self, st: dict) -> None:
+        """Uploads a saved state and starts a step from it."""
+        arrs = {k: np.ascontiguousarray(v, np.float64) for k, v in st.items()
+                if k in ("w", "w0", "p", "en", "en0", "ro") and v is not None}
+        ptr = lambda k: arrs[k].ctypes.data_as(C.c_void_p) if k in arrs else None
+        _lib.check(self._L.fvc_simple_set_state(self._h, *[ptr(k) for k in
+                                                          ("w", "w0", "p", "en", "en0", "ro")]),
+                   "fvc_simple_set_state")
+
     def time_step(self) -> None:
         _lib.check(self._L.fvc_simple_time_step(self._h), "fvc_simple_time_step")
 

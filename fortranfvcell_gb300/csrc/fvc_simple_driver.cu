@@ -591,6 +591,56 @@ int32_t fvc_simple_set_fields(fvc_simple *s, const double *w, const double *p) {
   return cudaStreamSynchronize(s->stream) == cudaSuccess ? FVC_OK : FVC_ERR_CUDA;
 }
 
+int32_t fvc_simple_get_state(const fvc_simple *s, double *w, double *w0, double *p, double *en,
+                             double *en0, double *ro) {
+  if (!s || (!s->gas && (en || en0 || ro))) return FVC_ERR_ARG;
+  cudaSetDevice(s->device);
+  const size_t n = s->numel;
+  const struct {
+    double *h;
+    const double *d;
+    size_t k;
+  } cp[] = {{w, s->w, 2 * n}, {w0, s->w0, 2 * n}, {p, s->p, n},
+            {en, s->en, n},   {en0, s->en0, n}, {ro, s->ro, 3 * n}};
+  for (const auto &c : cp)
+    if (c.h && cudaMemcpyAsync(c.h, c.d, sizeof(double) * c.k, cudaMemcpyDeviceToHost,
+                               s->stream) != cudaSuccess)
+      return FVC_ERR_CUDA;
+  return cudaStreamSynchronize(s->stream) == cudaSuccess ? FVC_OK : FVC_ERR_CUDA;
+}
+
+int32_t fvc_simple_set_state(fvc_simple *s, const double *w, const double *w0, const double *p,
+                             const double *en, const double *en0, const double *ro) {
+  if (!s || (!s->gas && (en || en0 || ro))) return FVC_ERR_ARG;
+  cudaSetDevice(s->device);
+  const size_t n = s->numel;
+  const struct {
+    const double *h;
+    double *d;
+    size_t k;
+  } cp[] = {{w, s->w, 2 * n}, {w0, s->w0, 2 * n}, {p, s->p, n},
+            {en, s->en, n},   {en0, s->en0, n}, {ro, s->ro, 3 * n}};
+  for (const auto &c : cp)
+    if (c.h && cudaMemcpyAsync(c.d, c.h, sizeof(double) * c.k, cudaMemcpyHostToDevice,
+                               s->stream) != cudaSuccess)
+      return FVC_ERR_CUDA;
+  // the start of a step from the loaded levels: time terms (and w0 = w,
+  // en0 = en); with the energy equation the temperature from the enthalpy
+  int32_t rc;
+  if (s->gas) {
+    if ((rc = fvc_cells_enthalpy_temperature((int)n, s->en, s->temp, s->cp, s->tref, 1,
+                                             s->stream)) != FVC_OK ||
+        (rc = time_term_gas(s)) != FVC_OK)
+      return rc;
+  } else {
+    if ((rc = time_term(s)) != FVC_OK) return rc;
+    if (cudaMemcpyAsync(s->w0, s->w, sizeof(double) * 2 * n, cudaMemcpyDeviceToDevice,
+                        s->stream) != cudaSuccess)
+      return FVC_ERR_CUDA;
+  }
+  return cudaStreamSynchronize(s->stream) == cudaSuccess ? FVC_OK : FVC_ERR_CUDA;
+}
+
 int32_t fvc_simple_destroy(fvc_simple *s) {
   if (!s) return FVC_ERR_ARG;
   cudaSetDevice(s->device);

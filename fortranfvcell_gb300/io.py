@@ -321,3 +321,56 @@ def simple_case(deck):
                 pedge=np.ascontiguousarray(deck["pedgeF"], np.int32), sedge=sedge,
                 e=deck["e"], nshared=nen, numel=deck["params"]["numel"], mesh=m,
                 pedgeE=deck["pedgeE"], sedgeE=deck["sedgeE"], gravity=deck["gravity"])
+
+
+# ---------------------------------------------------------------- checkpoints
+def save_simple(path, istep, t, w, w0, p, ro, en=None, en0=None):
+    """Writes a SIMPLE restart file in the ASCII layout of the reference's
+    saveSimple (src/Simple.f:1307-1626): labelled blocks with the step
+    (i9), the time (f20.8), w and w0 (3f36.16, two values a line), p
+    (f36.16), with the energy equation en and en0 (f36.16), and the three
+    density levels (3f36.16)."""
+    f36 = lambda v: f"{float(v):36.16f}"
+    with open(path, "w") as f:
+        f.write("passo de tempo\n")
+        f.write(f"{int(istep):9d}\n")
+        f.write("tempo \n")
+        f.write(f"{float(t):20.8f}\n")
+        for label, a in (("Velocidade (n)", w), ("Velocidade (n-1)", w0)):
+            f.write(label + "\n")
+            f.writelines(f36(u) + f36(v) + "\n" for u, v in np.asarray(a).reshape(-1, 2))
+        f.write("pressao (n)\n")
+        f.writelines(f36(v) + "\n" for v in np.asarray(p).ravel())
+        if en is not None:
+            f.write("en (n)\n")
+            f.writelines(f36(v) + "\n" for v in np.asarray(en).ravel())
+            f.write("en (n-1)\n")
+            f.writelines(f36(v) + "\n" for v in np.asarray(en0).ravel())
+        f.write("ro      \n")
+        f.writelines(f36(a) + f36(b) + f36(c) + "\n" for a, b, c in np.asarray(ro).reshape(-1, 3))
+
+
+def load_simple(path, numel, energy=False):
+    """Reads a saveSimple restart file: dict(istep, t, w, w0, p, ro[, en,
+    en0]).  energy says whether the file holds the en blocks (the
+    reference's sEnergy at save time)."""
+    with open(path) as f:
+        lines = f.read().splitlines()
+    pos = 0
+
+    def block(ncols):
+        nonlocal pos
+        pos += 1                                      # label line
+        out = np.array([[float(x) for x in ln.split()] for ln in lines[pos:pos + numel]])
+        pos += numel
+        return out.reshape(numel, ncols) if ncols > 1 else out.ravel()
+    st = {"istep": int(lines[1]), "t": float(lines[3])}
+    pos = 4
+    st["w"] = block(2)
+    st["w0"] = block(2)
+    st["p"] = block(1)
+    if energy:
+        st["en"] = block(1)
+        st["en0"] = block(1)
+    st["ro"] = block(3)
+    return st

@@ -518,6 +518,20 @@ int32_t fvc_simple_iterate_energy(fvc_simple *s, int32_t nit, double *res,
 int32_t fvc_simple_energy_fields(const fvc_simple *s, double *temp, double *en,
                                  double *ro);
 
+/* The state a restart needs, as the reference's saveSimple writes it
+ * (src/Simple.f:1307-1626): w and w0 (2,numel), p, and with the energy
+ * equation en, en0 (numel) and ro (3,numel).  HOST arrays, any may be NULL;
+ * en/en0/ro need a loop switched by fvc_simple_energy.  fvc_simple_set_state
+ * uploads the given arrays and then starts a step from them, as the first
+ * simple macro after the reference's load does: the time terms from w, w0
+ * (and en, en0, ro), then w0 = w (and en0 = en); the temperature follows
+ * from en. */
+int32_t fvc_simple_get_state(const fvc_simple *s, double *w, double *w0,
+                             double *p, double *en, double *en0, double *ro);
+int32_t fvc_simple_set_state(fvc_simple *s, const double *w, const double *w0,
+                             const double *p, const double *en,
+                             const double *en0, const double *ro);
+
 /* Host copies of the velocity w(2,numel) and pressure p(numel); either may
  * be NULL.  fvc_simple_set_fields uploads them (e.g. to restart). */
 int32_t fvc_simple_fields(const fvc_simple *s, double *w, double *p);

@@ -169,3 +169,27 @@ def test_deck_drives_the_restated_simple_loop(orc, tmp_path):
     a, b = SimpleRef(orc, case), SimpleRef(orc, c)
     for _ in range(5):
         assert a.step() == b.step()
+
+
+def test_save_simple_round_trip(tmp_path):
+    rng = np.random.default_rng(7)
+    n = 13
+    st = dict(w=rng.uniform(-1, 1, (n, 2)), w0=rng.uniform(-1, 1, (n, 2)),
+              p=rng.uniform(-100, 100, n), en=rng.uniform(-500, 500, n),
+              en0=rng.uniform(-500, 500, n), ro=rng.uniform(1.1, 1.3, (n, 3)))
+    path = str(tmp_path / "save.dat")
+    io.save_simple(path, 42, 0.84, st["w"], st["w0"], st["p"], st["ro"], en=st["en"],
+                   en0=st["en0"])
+    lines = open(path).read().splitlines()
+    assert lines[:4] == ["passo de tempo", f"{42:9d}", "tempo ", f"{0.84:20.8f}"]
+    assert lines[4] == "Velocidade (n)" and len(lines[5]) == 72
+    assert "pressao (n)" in lines and "en (n)" in lines and "en (n-1)" in lines
+    assert lines[-n - 1] == "ro      " and len(lines[-1]) == 108
+    back = io.load_simple(path, n, energy=True)
+    assert back["istep"] == 42 and back["t"] == 0.84
+    for k, v in st.items():     # F36.16: 16 decimals
+        np.testing.assert_allclose(back[k], v, rtol=0, atol=5e-17 * 1000)
+    # without the energy blocks
+    io.save_simple(path, 1, 0.0, st["w"], st["w0"], st["p"], st["ro"])
+    back = io.load_simple(path, n)
+    assert "en" not in back and np.allclose(back["ro"], st["ro"], atol=1e-15)
