@@ -112,7 +112,15 @@ class Context:
                    "fvc_matrix_set")
 
     def update_values(self, ad, au=None, al=None) -> None:
-        _lib.check(self._L.fvc_matrix_update_values(self._h, _p(ad), _p(au), _p(al)),
+        """New values for the structure of the last set_matrix: host numpy
+        arrays or device buffers (torch CUDA float64 tensors)."""
+        def ptr(a):
+            if a is None:
+                return None
+            if hasattr(a, "data_ptr"):
+                return C.c_void_p(a.data_ptr())
+            return _p(a)
+        _lib.check(self._L.fvc_matrix_update_values(self._h, ptr(ad), ptr(au), ptr(al)),
                    "fvc_matrix_update_values")
 
     def info(self) -> dict:

@@ -1,0 +1,88 @@
+"""Differentiable GPU solves (fortranfvcell_gb300.autograd): the adjoint
+gradients of a scalar loss against central finite differences of the
+restated reference solver, and torch's gradcheck."""
+import numpy as np
+import pytest
+
+from _systems import pressure, unsymmetric
+
+pytestmark = pytest.mark.gpu
+
+
+def system(orc, sym):
+    from fortranfvcell_gb300 import mesh
+    s = pressure(orc, mesh.square_mesh(6, kind="mixed", jitter=0.2, seed=1), 1, True)
+    if not sym:
+        s = unsymmetric(s, seed=3)
+    else:
+        s["ad"] = s["ad"].copy()
+        s["ad"][s["ad"] > 1e30] = 4.0     # drop the pin: a plain SPD Laplacian + diagonal
+        s["ad"] = s["ad"] + 0.5
+    return s
+
+
+def ref_solve(orc, s, ad, au, b, code):
+    x = np.zeros(s["n"])
+    st, _ = orc.solver(ad.copy(), au.copy(), au.copy(), x, b.copy(), s["ia"], s["ja"], s["n"],
+                       s["nad"], True, 1e-14, 100000, code, 1)
+    assert st == 0
+    return x
+
+
+@pytest.mark.parametrize("sym,code", [(False, 2), (True, 1)])
+def test_adjoint_gradients_match_finite_differences(orc, sym, code):
+    import torch
+    from fortranfvcell_gb300.autograd import CsrdSystem, linear_solve
+    s = system(orc, sym)
+    n, nad = s["n"], s["nad"]
+    rng = np.random.default_rng(5)
+    b = rng.uniform(-1, 1, n)
+    wt = rng.uniform(-1, 1, n)
+    sysg = CsrdSystem(s["ia"], s["ja"], n, code=code, tol=1e-13)
+    dev = lambda a: torch.tensor(a, dtype=torch.float64, device="cuda", requires_grad=True)
+    ad_t, au_t, b_t = dev(s["ad"]), dev(s["au"][:nad]), dev(b)
+    x = linear_solve(ad_t, au_t, b_t, sysg)
+    loss = (x * torch.tensor(wt, device="cuda")).sum()
+    loss.backward()
+    g_ad, g_au, g_b = (t.grad.cpu().numpy() for t in (ad_t, au_t, b_t))
+    sysg.close()
+    loss_of = lambda ad, au, bb: float(wt @ ref_solve(orc, s, ad, au, bb, code))
+    ad0, au0 = s["ad"].copy(), s["au"][:nad].copy()
+    for i in rng.choice(n, 4, replace=False):
+        h = 1e-6 * max(1.0, abs(b[i]))
+        bp, bm = b.copy(), b.copy()
+        bp[i] += h
+        bm[i] -= h
+        fd = (loss_of(ad0, au0, bp) - loss_of(ad0, au0, bm)) / (2 * h)
+        assert abs(g_b[i] - fd) <= 1e-6 * max(1.0, abs(fd)), ("b", i)
+        h = 1e-6 * abs(ad0[i])
+        ap, am = ad0.copy(), ad0.copy()
+        ap[i] += h
+        am[i] -= h
+        fd = (loss_of(ap, au0, b) - loss_of(am, au0, b)) / (2 * h)
+        assert abs(g_ad[i] - fd) <= 1e-6 * max(1.0, abs(fd)), ("ad", i)
+    for k in rng.choice(nad, 4, replace=False):
+        h = 1e-6 * max(abs(au0[k]), 1e-3)
+        up, um = au0.copy(), au0.copy()
+        up[k] += h
+        um[k] -= h
+        fd = (loss_of(ad0, up, b) - loss_of(ad0, um, b)) / (2 * h)
+        assert abs(g_au[k] - fd) <= 1e-6 * max(1.0, abs(fd)), ("au", k)
+
+
+def test_gradcheck_small_system(orc):
+    import torch
+    from fortranfvcell_gb300 import mesh
+    from fortranfvcell_gb300.autograd import CsrdSystem, linear_solve
+    s = unsymmetric(pressure(orc, mesh.square_mesh(3, kind="tri", seed=2), 1, True), seed=4)
+    n, nad = s["n"], s["nad"]
+    # tol 1e-12: on 18 rows a tighter test drives BiCGSTAB to an exactly
+    # vanishing s, where omega = t.s / t.t is 0/0 (the reference's recurrence
+    # breaks down the same way; the solver reports it as NaN)
+    sysg = CsrdSystem(s["ia"], s["ja"], n, code=2, tol=1e-12)
+    dev = lambda a: torch.tensor(a, dtype=torch.float64, device="cuda", requires_grad=True)
+    b = np.random.default_rng(1).uniform(-1, 1, n)
+    inputs = (dev(s["ad"]), dev(s["au"][:nad]), dev(b))
+    assert torch.autograd.gradcheck(lambda ad, au, bb: linear_solve(ad, au, bb, sysg), inputs,
+                                    eps=1e-6, atol=1e-6, rtol=1e-5)
+    sysg.close()
