@@ -366,6 +366,8 @@ def run_ours(args):
         line["batched_c4"] = run_batched_c4(args)
     if rank == 0 and args.c3_nx > 0:
         line["gas_c3"] = run_gas_c3(args)
+    if rank == 0 and args.c5_nx > 0:
+        line["adjoint_c5"] = run_adjoint_c5(args)
     return line
 
 
@@ -478,6 +480,77 @@ def run_gas_c3(args):
         out["cpu_kind"] = (f"port (restated reference, sequential solvers, 1 core), first {k} "
                            f"outer iterations timed")
         out["gpu_fp64_over_cpu"] = round(per_it / (out["fp64"]["gpu_s"] / nit), 1)
+    return out
+
+
+def run_adjoint_c5(args):
+    """The C5 configuration: sensitivity of the mean hot-wall Nusselt number
+    to the hot-wall face temperatures of a natural-convection cavity (nx x nx
+    quads, Ra = 1e5, hot faces at T_cold + (1 + N(0, 0.05)) K, seed 11) at the
+    state the GPU loop reaches after c5_its outer iterations, with flow and
+    densities frozen.  Adjoint: one forward and one adjoint solve give all
+    the derivatives; checked against GPU central differences on 32 faces
+    (seed 12).  J is affine in the continuous wall enthalpy of the frozen
+    system, so the step (0.1 K) adds no truncation error; it is large so
+    that the differences stand well above the solver tolerance (a 1 mK step
+    leaves them at the 1e-2 level of the iterative solves' noise).  CPU: one solve of the same frozen system by
+    the restated BiCGSTAB, times the 2 x faces solves of full differences."""
+    import torch
+    from fortranfvcell_gb300 import sensitivity as sv
+    from fortranfvcell_gb300.cases import natural_convection_cavity
+    from fortranfvcell_gb300.cells import SimpleLoop, simple_opts
+    c = natural_convection_cavity(args.c5_nx, ra=1e5)
+    cells, faces, _, _ = sv.wall_faces(c, 0.0)
+    rng = np.random.default_rng(11)
+    c["sedgeE"][cells, faces] = (c["t0"] - 0.5) + 1.0 + rng.normal(0.0, 0.05, cells.size)
+    loop = SimpleLoop(c["coor"], c["ix"], c["nelcon"], c["num"], c["pedge"], c["sedge"], c["e"],
+                      opts=simple_opts())
+    loop.enable_energy(c["pedgeE"], c["sedgeE"], c["gravity"], c["t0"])
+    t0 = time.perf_counter()
+    res, _ = loop.iterate_energy(args.c5_its)
+    loop_s = time.perf_counter() - t0
+    sysd = sv.frozen_energy_system(c, loop)
+    loop.close()
+    prob = sv.NusseltProblem(c, sysd, tol=1e-12)
+    sv.nusselt_wall_gradient(prob, sysd["h_wall"])           # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    j, g = sv.nusselt_wall_gradient(prob, sysd["h_wall"])
+    torch.cuda.synchronize()
+    adj_s = time.perf_counter() - t0
+    idx = np.random.default_rng(12).choice(g.size, min(32, g.size), replace=False)
+    t0 = time.perf_counter()
+    fd = sv.nusselt_fd(prob, sysd["h_wall"], idx, step=sysd["cp"] * 0.1)
+    torch.cuda.synchronize()
+    fd_s = time.perf_counter() - t0
+    prob.close()
+    rel = np.abs(g[idx] - fd) / np.maximum(np.abs(fd), 1e-300)
+    out = {"workload": f"dJ/dT_wall, J = mean hot-wall Nu, natural convection {args.c5_nx}x"
+                       f"{args.c5_nx} quads, Ra=1e5, {g.size} hot-wall faces, state after "
+                       f"{args.c5_its} outer iterations (flow frozen)",
+           "loop_s": round(loop_s, 3), "final_residuals": [float(f"{v:.3e}") for v in res[-1]],
+           "J": round(j, 6), "adjoint_s": round(adj_s, 4),
+           "fd_subset": {"faces": int(idx.size), "s": round(fd_s, 3),
+                         "max_rel_diff_vs_adjoint": float(f"{rel.max():.2e}")},
+           "fd_all_faces_s_est": round(fd_s * g.size / idx.size, 3),
+           "adjoint_over_fd_all": round(fd_s * g.size / idx.size / adj_s, 1),
+           "dJ_dT_range": [float(f"{sysd['cp'] * g.min():.4e}"),
+                           float(f"{sysd['cp'] * g.max():.4e}")]}
+    if not args.no_cpu:
+        from oracle import oracle
+        n = c["numel"]
+        ad = sysd["ad"].cpu().numpy()
+        au = sysd["au"].cpu().numpy()
+        b = sysd["b"].cpu().numpy()
+        x = np.zeros(n)
+        t0 = time.perf_counter()
+        oracle.solver(ad, au.copy(), au.copy(), x, b.copy(), sysd["ia"], sysd["ja"], n,
+                      sysd["nad"], True, 1e-12, 100000, 2, 1)
+        cpu_solve = time.perf_counter() - t0
+        out["cpu_port_one_solve_s"] = round(cpu_solve, 3)
+        out["cpu_fd_all_faces_s_est"] = round(cpu_solve * 2 * g.size, 1)
+        out["cpu_kind"] = ("port: restated sequential BiCGSTAB (1 core), one solve of the frozen "
+                           "system, times 2 x faces for full central differences")
     return out
 
 
@@ -707,11 +780,14 @@ def main():
                     help="natural-convection C3 leg: cells per side (0 skips it)")
     ap.add_argument("--c3-ra", type=float, default=1.0e6)
     ap.add_argument("--c3-its", type=int, default=30)
+    ap.add_argument("--c5-nx", type=int, default=256,
+                    help="adjoint C5 leg: cells per side (0 skips it)")
+    ap.add_argument("--c5-its", type=int, default=200)
     ap.add_argument("--c4-cases", type=int, default=256,
                     help="batched C4 leg: number of systems (0 skips it)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--ref-sample-its", type=int, default=300)
-    ap.add_argument("--profile-leg", choices=["c1", "c3", "c4"], default=None,
+    ap.add_argument("--profile-leg", choices=["c1", "c3", "c4", "c5"], default=None,
                     help="profiling: run only this leg (no CPU side) and print its JSON")
     ap.add_argument("--profile-its", type=int, default=0,
                     help="profiling case: run each solver once for this many iterations")
@@ -722,7 +798,8 @@ def main():
     if args.profile_leg:
         args.no_cpu = True
         args.c4_batched_only = True
-        leg = {"c1": run_simple_c1, "c3": run_gas_c3, "c4": run_batched_c4}[args.profile_leg]
+        leg = {"c1": run_simple_c1, "c3": run_gas_c3, "c4": run_batched_c4,
+               "c5": run_adjoint_c5}[args.profile_leg]
         print(json.dumps(leg(args)), flush=True)
         return
     if args.warmup < 3:

@@ -84,6 +84,7 @@ def natural_convection_cavity(nx: int, ra: float = 1.0e6, dt_wall: float = 1.0,
     pe[:, :nsh][left | right] = 1
     se[:, :nsh][left] = t0 + 0.5 * dt_wall
     se[:, :nsh][right] = t0 - 0.5 * dt_wall
-    c.update(pedgeE=pe, sedgeE=se, gravity=np.array([0.0, -g]), t0=t0, side=side, ra=ra)
+    c.update(pedgeE=pe, sedgeE=se, gravity=np.array([0.0, -g]), t0=t0, side=side, ra=ra,
+             dt_wall=dt_wall)
     c["e"][0, 1] = rho
     return c
