@@ -139,6 +139,12 @@ __device__ __forceinline__ bool epilogue(const KArgs &a, unsigned int &ep, doubl
 // The iteration over the rows of P, synchronising through gs; the lead
 // block writes result / iresult.  pcg_f64 runs it over the whole matrix,
 // pcg_batched over one system of a batch per group of blocks.
+// kStoreP: p = z + beta p is formed once per row in place and published by a
+// grid barrier before the SpMV (one FP64 FMA per row instead of one per
+// gathered neighbour -- 4 of the 16 FP64 instructions of a row-iteration on
+// quadrilaterals); otherwise it is formed at every read from the previous p
+// and z, which saves the barrier.  Both give the same bits.
+template <bool kStoreP>
 __device__ __forceinline__ void pcg_run(const KArgs &a, const Part &P, const GridSync &gs,
                                         double *result, int *iresult, bool lead) {
   __shared__ double red[kMaxNV * 32];
@@ -186,7 +192,11 @@ __device__ __forceinline__ void pcg_run(const KArgs &a, const Part &P, const Gri
   for (j = 1; j <= a.maxit; ++j) {
     // q = A p  (p = z + beta*p formed on the fly for j >= 2); p.q
     double pq[1] = {0.0};
-    if (j == 1) {
+    if (kStoreP && j > 1) {
+      FOR_ROWS(P) pcur[row] = fma(beta, pcur[row], z[row]);
+      if (!grid_barrier(gs, ep)) return;
+    }
+    if (j == 1 || kStoreP) {
       FOR_ROWS(P) {
         const double *pc = pcur;
         const double qi = sell_row_fma(a.A, s_, P.lane, row, [&](int k) { return pc[k]; });
@@ -239,8 +249,10 @@ __device__ __forceinline__ void pcg_run(const KArgs &a, const Part &P, const Gri
     }
     if (sh.stop == 1) break;
     beta = sh.beta;
-    pprev = pcur;
-    pcur = (pcur == a.v2) ? a.v3 : a.v2;
+    if (!kStoreP) {
+      pprev = pcur;
+      pcur = (pcur == a.v2) ? a.v3 : a.v2;
+    }
   }
   if (j > a.maxit) {
     j = a.maxit;
@@ -250,8 +262,11 @@ __device__ __forceinline__ void pcg_run(const KArgs &a, const Part &P, const Gri
   epilogue_to(a, P, gs, result, lead, ep, red, false);
 }
 
+constexpr int kStorePRows = 262144;
+
+template <bool kStoreP>
 __global__ void __launch_bounds__(1024, 1) pcg_f64(KArgs a) {
-  pcg_run(a, Part(a.A.nslices, a.A.n), a.gs, a.result, a.iresult, blockIdx.x == 0);
+  pcg_run<kStoreP>(a, Part(a.A.nslices, a.A.n), a.gs, a.result, a.iresult, blockIdx.x == 0);
 }
 
 // One system of a batch: its slices, its synchronisation state (counter,
@@ -267,12 +282,13 @@ struct BatchSys {
 // slice boundary; every block belongs to one system (sys_of_block) and
 // synchronises only with that system's blocks, so each system iterates and
 // stops on its own inside one cooperative launch.
+template <bool kStoreP>
 __global__ void __launch_bounds__(1024, 1) pcg_batched(KArgs a, const BatchSys *__restrict__ sys,
                                                         const int *__restrict__ sys_of_block) {
   const BatchSys d = sys[sys_of_block[blockIdx.x]];
   const int rank = (int)(blockIdx.x - d.gs.base);
-  pcg_run(a, Part(d.s0, d.s1, a.A.n, rank, (int)d.gs.nblocks), d.gs, d.result, d.iresult,
-          rank == 0);
+  pcg_run<kStoreP>(a, Part(d.s0, d.s1, a.A.n, rank, (int)d.gs.nblocks), d.gs, d.result,
+                   d.iresult, rank == 0);
 }
 
 // ---------------------------------------------------------------------
@@ -760,7 +776,12 @@ int32_t run_pcg(const DeviceMatrix &A, Scratch &S, const double *b, double *x, d
     const int32_t rc = run_pcg_cluster(A, S, b, x, tol, maxit, init, o, stream, st);
     if (rc != FVC_ERR_UNSUPPORTED) return rc;
   }
-  return run_persistent(pcg_f64, A, S, b, x, tol, maxit, init, o, stream, st, 5, false);
+  // p stored from 262144 rows on: per iteration on GB300 (same bits either
+  // way) 98k rows 14.5 vs 13.0 us, 393k 23.0 vs 23.5, 1.57M 58.8 vs 66.2,
+  // 4.19M 146 vs 161 us (stored vs formed at every read)
+  if (A.n >= kStorePRows)
+    return run_persistent(pcg_f64<true>, A, S, b, x, tol, maxit, init, o, stream, st, 5, false);
+  return run_persistent(pcg_f64<false>, A, S, b, x, tol, maxit, init, o, stream, st, 5, false);
 }
 
 int32_t run_bicgstab(const DeviceMatrix &A, Scratch &S, const double *b, double *x, double tol,
@@ -784,7 +805,10 @@ int32_t run_pcg_batched(const DeviceMatrix &A, Scratch &S, int nsys, const int32
   // 256 cavities: 184 ms at 128 threads, 215 at 256, 386 at 512)
   const int threads = (o.block_threads > 0) ? block_threads_for(o.block_threads, 0, 1) : 128;
   int occ = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, pcg_batched, threads, 0);
+  // p stored: most groups of a batch are one block, where publishing p is a
+  // __syncthreads (C4 batch of 256 cavities: 159 ms vs 184 ms)
+  auto kern = pcg_batched<true>;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, threads, 0);
   if (occ <= 0) occ = 1;
   if (o.blocks_per_sm > 0 && o.blocks_per_sm < occ) occ = o.blocks_per_sm;
   int cap = occ * sm_count();
@@ -924,7 +948,7 @@ int32_t run_pcg_batched(const DeviceMatrix &A, Scratch &S, int nsys, const int32
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   cudaEventRecord(e0, stream);
-  cudaError_t ce = cudaLaunchCooperativeKernel((const void *)pcg_batched, dim3((unsigned)total),
+  cudaError_t ce = cudaLaunchCooperativeKernel((const void *)kern, dim3((unsigned)total),
                                                dim3(threads), args, 0, stream);
   count_launch();
   cudaEventRecord(e1, stream);

@@ -372,3 +372,26 @@ def test_cluster_pcg_matches_grid_and_reference(fvc, orc, kind, nx):
         assert abs(sg.iterations - so.iterations) <= ITS_TOL, (name, n, sg.iterations,
                                                                so.iterations)
         assert abs(sg.energy - so.energy) <= 1e-9 * abs(so.energy), name
+
+
+def test_stored_p_pcg_on_a_large_system(fvc):
+    # 512 x 512 cells = 262144 rows: the grid-wide PCG stores p before its
+    # SpMV (the size from which that is faster); against a direct solve
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spla
+    from fortranfvcell_gb300 import mesh
+    s = mesh.pressure_system(mesh.square_mesh(512, kind="quad"), matriz=1, unsym=True,
+                             pin_cell=1)
+    n = s.neq
+    assert n >= 262144
+    ad = s.ad.copy()
+    ad[ad > 1e30] = 4.0
+    ad = ad + 1e-3                        # SPD and well-posed for the direct solver
+    b = np.random.default_rng(9).uniform(-1, 1, n)
+    rows = np.repeat(np.arange(n), np.diff(s.ia))
+    A = sp.csr_matrix((s.au[:s.nad], (rows, s.ja[:s.nad] - 1)), shape=(n, n)) + sp.diags(ad)
+    x_ref = spla.spsolve(A.tocsc(), b)
+    x = np.zeros(n)
+    st = fvc.solver(ad, s.au, s.au, x, b, s.ia, s.ja, n, s.nad, True, 1e-11, 100000, 1, 1)
+    assert st.iterations > 0
+    assert np.linalg.norm(x - x_ref) / np.linalg.norm(x_ref) < 1e-8
