@@ -46,3 +46,32 @@ def test_no_gpu_context_errors_cleanly(fvc):
     h = C.c_void_p()
     rc = fvc.load().fvc_context_create(C.byref(h), 0)
     assert rc == 5  # FVC_ERR_CUDA: no device, no silent fallback
+
+
+def _f90():
+    src = open(os.path.join(ROOT, "include", "fvcgpu.f90")).read()
+    return re.sub(r"!.*", "", src)
+
+
+def test_fortran_module_binds_exported_symbols(fvc):
+    # every bind(C, name=...) of include/fvcgpu.f90 is declared in the C
+    # header (no Fortran compiler runs here; this keeps the module honest)
+    names = re.findall(r'bind\(C,\s*name="(\w+)"\)', _f90())
+    assert names and not set(names) - set(declared_functions())
+
+
+def test_fortran_derived_types_match_the_c_structs(fvc):
+    # field names, order and kinds of the bind(C) types against the ctypes
+    # structures that mirror fvcgpu.h
+    import ctypes as C
+    from fortranfvcell_gb300 import _lib
+    kind = {"real(c_double)": C.c_double, "integer(c_int32_t)": C.c_int32}
+    src = _f90()
+    for ftype, cls in (("fvc_opts", _lib.FvcOpts), ("fvc_stats", _lib.FvcStats),
+                       ("fvc_simple_opts", _lib.FvcSimpleOpts)):
+        body = re.search(r"type, bind\(C\) :: %s\n(.*?)end type" % ftype, src, re.S).group(1)
+        fields = []
+        for line in body.strip().splitlines():
+            t, names = line.split("::")
+            fields += [(n.strip(), kind[t.strip()]) for n in names.split(",")]
+        assert fields == [(n, t) for n, t in cls._fields_], ftype
