@@ -393,9 +393,26 @@ def run_simple_c1(args):
     gpu_s = time.perf_counter() - t0
     w, _ = loop.fields()
     loop.close()
+    # the same iterations as one CUDA graph launch each (captured before the clock)
+    loop = SimpleLoop(case["coor"], case["ix"], case["nelcon"], case["num"], case["pedge"],
+                      case["sedge"], case["e"])
+    loop.use_graph(True)
+    t0 = time.perf_counter()
+    loop.iterate(0)
+    capture_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    res_g, its_g = loop.iterate(nit)
+    graph_s = time.perf_counter() - t0
+    w_g, _ = loop.fields()
+    loop.close()
     out = {"workload": f"lid-driven cavity Re={1.0 / case['e'][0, 0]:g}, {args.simple_nx}x"
                        f"{args.simple_nx} quads, {nit} SIMPLE outer iterations",
            "gpu_s": round(gpu_s, 4), "outer_its_per_s": round(nit / gpu_s, 2),
+           "graph": {"gpu_s": round(graph_s, 4), "outer_its_per_s": round(nit / graph_s, 2),
+                     "capture_s": round(capture_s, 4),
+                     "same_as_uncaptured": bool(np.array_equal(res_g, res)
+                                                and np.array_equal(its_g, its)
+                                                and np.array_equal(w_g, w))},
            "solver_iterations": [int(v) for v in its.sum(axis=0)],
            "final_residuals": [float(f"{v:.3e}") for v in res[-1]],
            "u_min_centreline": float(np.round(np.min(0.5 * (

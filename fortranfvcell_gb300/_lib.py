@@ -114,6 +114,8 @@ SIGNATURES = {
     "fvc_context_set_stream": ([P, P], I32),
     "fvc_matrix_set": ([P, I32, I32, I32, I32, P, P, P, P, P], I32),
     "fvc_matrix_update_values": ([P, P, P, P], I32),
+    "fvc_matrix_update_values_async": ([P, P, P, P], I32),
+    "fvc_solve_async": ([P, I32, P, P, F64, I32, C.POINTER(FvcOpts), P], I32),
     "fvc_solve": ([P, I32, P, P, F64, I32, C.POINTER(FvcOpts), C.POINTER(FvcStats)], I32),
     "fvc_solve_batched": ([P, I32, P, P, P, F64, I32, C.POINTER(FvcOpts), P], I32),
     "fvc_spmv": ([P, P, P], I32),
@@ -153,6 +155,7 @@ SIGNATURES = {
     "fvc_simple_create": ([C.POINTER(P), I32, I32, I32, I32, I32, P, P, P, P, P, P, P,
                            C.POINTER(FvcSimpleOpts)], I32),
     "fvc_simple_iterate": ([P, I32, P, P], I32),
+    "fvc_simple_set_graph": ([P, I32], I32),
     "fvc_simple_iterate_energy": ([P, I32, P, P], I32),
     "fvc_simple_energy": ([P, P, P, F64, F64, F64], I32),
     "fvc_simple_energy_fields": ([P, P, P, P], I32),

@@ -233,6 +233,10 @@ class SimpleLoop:
     def time_step(self) -> None:
         _lib.check(self._L.fvc_simple_time_step(self._h), "fvc_simple_time_step")
 
+    def use_graph(self, on: bool = True) -> None:
+        """Run each outer iteration as one CUDA graph launch (same results)."""
+        _lib.check(self._L.fvc_simple_set_graph(self._h, int(bool(on))), "fvc_simple_set_graph")
+
     def fields(self):
         w = np.zeros((self.numel, 2))
         p = np.zeros(self.numel)

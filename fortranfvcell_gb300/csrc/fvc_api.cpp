@@ -208,9 +208,9 @@ int32_t upload_raw(fvc_context *c, const double *ad, const double *au, const dou
     rc = fvc::launch_gather_values(c->neq, c->d_jac_src, c->d_raw1, nullptr, c->A.jac, s);
     if (rc != FVC_OK) return rc;
   } else {
-    if (cudaMemcpyAsync(c->A.diag, ad, sizeof(double) * c->neq, cudaMemcpyHostToDevice, s) !=
+    if (cudaMemcpyAsync(c->A.diag, ad, sizeof(double) * c->neq, cudaMemcpyDefault, s) !=
             cudaSuccess ||
-        cudaMemcpyAsync(c->A.jac, ad, sizeof(double) * c->neq, cudaMemcpyHostToDevice, s) !=
+        cudaMemcpyAsync(c->A.jac, ad, sizeof(double) * c->neq, cudaMemcpyDefault, s) !=
             cudaSuccess)
       return FVC_ERR_CUDA;
   }
@@ -340,6 +340,7 @@ int32_t fvc_matrix_set(fvc_context *c, int32_t matriz, int32_t unsym, int32_t ne
   A.matriz = matriz;
   A.unsym = unsym;
   A.nad = nad;
+  A.cl_smax = fvc::cluster_slots_max(n, nslices, sptr.data());
   const size_t sl = (size_t)std::max<int64_t>(slots, 1);
   bool ok = cudaMalloc(&A.sptr, sizeof(int64_t) * (nslices + 1)) == cudaSuccess &&
             cudaMalloc(&A.col, sizeof(int32_t) * sl) == cudaSuccess &&
@@ -474,6 +475,33 @@ int32_t fvc_solve(fvc_context *c, int32_t code, const double *d_b, double *d_x, 
   }
   if (st && rc != st->status) st->status = rc;
   return rc;
+}
+
+int32_t fvc_matrix_update_values_async(fvc_context *c, const double *ad, const double *au,
+                                       const double *al) {
+  if (!c || !c->has_matrix) return FVC_ERR_ARG;
+  cudaSetDevice(c->device);
+  return upload_raw(c, ad, au, al);
+}
+
+int32_t fvc_solve_async(fvc_context *c, int32_t code, const double *d_b, double *d_x, double tol,
+                        int32_t maxit, const fvc_opts *opts, int32_t *d_status) {
+  if (!c || !c->has_matrix || !d_b || !d_x || !d_status || maxit < 1) return FVC_ERR_ARG;
+  fvc_opts o;
+  if (opts)
+    o = *opts;
+  else
+    fvc_opts_default(&o);
+  if (o.precision != FVC_PREC_FP64) return FVC_ERR_UNSUPPORTED;
+  const int matriz = c->matriz;
+  if (code < 1 || code > 3) return FVC_ERR_UNSUPPORTED;
+  if ((code == 2 || code == 3) && matriz == 2) return FVC_ERR_UNSUPPORTED;
+  if (code == 3 && matriz == 4) return FVC_ERR_UNSUPPORTED;
+  cudaSetDevice(c->device);
+  const int init = (o.init < 0) ? default_init(code, matriz) : (o.init ? 1 : 0);
+  int32_t rc = fvc::enqueue_solve(c->A, c->S, code, d_b, d_x, tol, maxit, init, o, c->stream, true);
+  if (rc != FVC_OK) return rc;
+  return fvc::launch_solve_status(c->S, d_status, c->stream);
 }
 
 int32_t fvc_solve_batched(fvc_context *c, int32_t nsys, const int32_t *row_start,
@@ -733,3 +761,14 @@ void solver_(double *ad, double *au, double *al, double *x, double *b, const int
 }
 
 }  // extern "C"
+
+namespace fvc {
+
+int32_t context_prepare(fvc_context *c, int code, const fvc_opts &o) {
+  if (!c || !c->has_matrix) return FVC_ERR_ARG;
+  if (o.precision != FVC_PREC_FP64) return FVC_ERR_UNSUPPORTED;
+  cudaSetDevice(c->device);
+  return enqueue_solve(c->A, c->S, code, nullptr, nullptr, 0.0, 1, 0, o, c->stream, false);
+}
+
+}  // namespace fvc

@@ -264,32 +264,53 @@ __global__ void __launch_bounds__(1024) pcg_cluster(ClArgs a) {
   cl.sync();  // no CTA leaves while another may still read its shared memory
 }
 
+// The cluster layout of an n-row system: CTAs, rows per CTA (a multiple of
+// 32, at most kClMaxRows, over at most kClMax CTAs).  False when the system
+// does not fit one cluster.
+bool cluster_shape(int n, int &nb, int &R) {
+  if (n <= 0 || n > kClMaxN) return false;
+  nb = std::min(kClMax, std::max(1, (n + 255) / 256));
+  R = ((n + nb - 1) / nb + 31) / 32 * 32;
+  if (R > kClMaxRows) return false;
+  nb = (n + R - 1) / R;
+  return true;
+}
+
 }  // namespace
 
-// Runs the cluster PCG when the system fits one cluster; returns
-// FVC_ERR_UNSUPPORTED (and launches nothing) when it does not, so the
-// caller falls back to the grid-wide kernel.
-int32_t run_pcg_cluster(const DeviceMatrix &A, Scratch &S, const double *b, double *x,
-                        double tol, int maxit, int init, const fvc_opts &o, cudaStream_t stream,
-                        fvc_stats *st) {
-  const int n = A.n;
-  if (n <= 0 || A.diag_mode == DIAG_NONE || !A.jinv) return FVC_ERR_UNSUPPORTED;
-  // rows per CTA: a multiple of 32, at most kClMaxRows, over at most 16 CTAs
-  if (n > kClMaxN) return FVC_ERR_UNSUPPORTED;
-  int nb = std::min(kClMax, std::max(1, (n + 255) / 256));
-  int R = ((n + nb - 1) / nb + 31) / 32 * 32;
-  if (R > kClMaxRows) return FVC_ERR_UNSUPPORTED;
-  nb = (n + R - 1) / R;
-  // slots per CTA from the slice pointers (a small host copy)
-  std::vector<int64_t> sptr((size_t)A.nslices + 1);
-  if (cudaMemcpyAsync(sptr.data(), A.sptr, sizeof(int64_t) * sptr.size(),
-                      cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
-      cudaStreamSynchronize(stream) != cudaSuccess)
-    return FVC_ERR_CUDA;
+// Largest number of stored slots of one CTA's rows under the cluster
+// layout, from the host copy of the slice pointers; -1 when the system does
+// not fit one cluster.
+int cluster_slots_max(int n, int nslices, const int64_t *sptr) {
+  int nb = 0, R = 0;
+  if (!sptr || !cluster_shape(n, nb, R)) return -1;
   int smax = 0;
   for (int c = 0; c < nb; ++c) {
-    const int s0 = c * R / 32, s1 = std::min(A.nslices, (c + 1) * R / 32);
+    const int s0 = c * R / 32, s1 = std::min(nslices, (c + 1) * R / 32);
     smax = std::max(smax, (int)(sptr[s1] - sptr[s0]));
+  }
+  return smax;
+}
+
+// Enqueues the cluster PCG when the system fits one cluster and returns
+// without waiting; FVC_ERR_UNSUPPORTED (and nothing enqueued) when it does
+// not, so the caller falls back to the grid-wide kernel.  launch = false
+// only checks the fit and prepares the scratch.
+int32_t enqueue_pcg_cluster(const DeviceMatrix &A, Scratch &S, const double *b, double *x,
+                            double tol, int maxit, int init, const fvc_opts &o,
+                            cudaStream_t stream, bool launch) {
+  const int n = A.n;
+  if (n <= 0 || A.diag_mode == DIAG_NONE || !A.jinv) return FVC_ERR_UNSUPPORTED;
+  int nb = 0, R = 0;
+  if (!cluster_shape(n, nb, R)) return FVC_ERR_UNSUPPORTED;
+  int smax = A.cl_smax;
+  if (smax < 0) {  // a matrix loaded without the host-side count
+    std::vector<int64_t> sptr((size_t)A.nslices + 1);
+    if (cudaMemcpyAsync(sptr.data(), A.sptr, sizeof(int64_t) * sptr.size(),
+                        cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
+        cudaStreamSynchronize(stream) != cudaSuccess)
+      return FVC_ERR_CUDA;
+    smax = cluster_slots_max(n, A.nslices, sptr.data());
   }
   const ClLayout L{R, smax};
   const size_t smem = L.bytes();
@@ -302,20 +323,6 @@ int32_t run_pcg_cluster(const DeviceMatrix &A, Scratch &S, const double *b, doub
   }
   const int threads = std::min(1024, std::max(128, (R + 127) / 128 * 128));
   if (ensure_sync(S, 1) != FVC_OK) return FVC_ERR_CUDA;
-  cudaMemsetAsync(S.iresult, 0, 16 * sizeof(int), stream);
-  cudaMemsetAsync(S.result, 0, 16 * sizeof(double), stream);
-  ClArgs a{};
-  a.A = SellView<double>{A.n, A.nslices, A.sptr, A.col, A.val, A.diag, A.diag_mode};
-  a.minv = A.jinv;
-  a.b = b;
-  a.x = x;
-  a.R = R;
-  a.tol = tol;
-  a.maxit = maxit;
-  a.init = init;
-  a.stop_rule = o.stop_rule;
-  a.result = S.result;
-  a.iresult = S.iresult;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)nb);
   cfg.blockDim = dim3((unsigned)threads);
@@ -334,24 +341,55 @@ int32_t run_pcg_cluster(const DeviceMatrix &A, Scratch &S, const double *b, doub
     cudaGetLastError();
     return FVC_ERR_UNSUPPORTED;
   }
+  if (!launch) return FVC_OK;
+  cudaMemsetAsync(S.err, 0, sizeof(int), stream);
+  cudaMemsetAsync(S.iresult, 0, 16 * sizeof(int), stream);
+  cudaMemsetAsync(S.result, 0, 16 * sizeof(double), stream);
+  ClArgs a{};
+  a.A = SellView<double>{A.n, A.nslices, A.sptr, A.col, A.val, A.diag, A.diag_mode};
+  a.minv = A.jinv;
+  a.b = b;
+  a.x = x;
+  a.R = R;
+  a.tol = tol;
+  a.maxit = maxit;
+  a.init = init;
+  a.stop_rule = o.stop_rule;
+  a.result = S.result;
+  a.iresult = S.iresult;
+  const cudaError_t ce = cudaLaunchKernelEx(&cfg, pcg_cluster, a);
+  count_launch();
+  if (ce != cudaSuccess) {
+    fprintf(stderr, "fvcgpu: cluster PCG launch failed: %s\n", cudaGetErrorString(ce));
+    cudaGetLastError();
+    return FVC_ERR_CUDA;
+  }
+  return FVC_OK;
+}
+
+// Runs the cluster PCG synchronously (FVC_ERR_UNSUPPORTED when the system
+// does not fit one cluster).
+int32_t run_pcg_cluster(const DeviceMatrix &A, Scratch &S, const double *b, double *x,
+                        double tol, int maxit, int init, const fvc_opts &o, cudaStream_t stream,
+                        fvc_stats *st) {
+  int32_t rc = enqueue_pcg_cluster(A, S, b, x, tol, maxit, init, o, stream, false);
+  if (rc != FVC_OK) return rc;
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   cudaEventRecord(e0, stream);
-  cudaError_t ce = cudaLaunchKernelEx(&cfg, pcg_cluster, a);
-  count_launch();
+  rc = enqueue_pcg_cluster(A, S, b, x, tol, maxit, init, o, stream, true);
   cudaEventRecord(e1, stream);
-  if (ce != cudaSuccess) {
-    cudaGetLastError();
+  if (rc != FVC_OK) {
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    return FVC_ERR_UNSUPPORTED;
+    return rc;
   }
   double res[16];
   int ires[16];
   cudaMemcpyAsync(res, S.result, sizeof(res), cudaMemcpyDeviceToHost, stream);
   cudaMemcpyAsync(ires, S.iresult, sizeof(ires), cudaMemcpyDeviceToHost, stream);
-  ce = cudaStreamSynchronize(stream);
+  const cudaError_t ce = cudaStreamSynchronize(stream);
   float ms = 0.f;
   cudaEventElapsedTime(&ms, e0, e1);
   cudaEventDestroy(e0);

@@ -35,6 +35,7 @@ struct DeviceMatrix {
   bool col16_ok = false;
   int ell_w = 0;             // FP32 copy padded to this uniform slice width (0: SELL)
   bool have32 = false;
+  int cl_smax = -1;          // cluster PCG: most slots of one CTA's rows (-1: unknown)
   // host-side description of the source layout, for value updates
   int matriz = 0, unsym = 0, nad = 0;
   int64_t *src_of_slot = nullptr;  // device map: slot -> source value index
@@ -82,6 +83,20 @@ int32_t run_gmres(const DeviceMatrix &A, Scratch &S, const double *b, double *x,
 int32_t run_pcg_cluster(const DeviceMatrix &A, Scratch &S, const double *b, double *x,
                         double tol, int maxit, int init, const fvc_opts &o,
                         cudaStream_t stream, fvc_stats *st);
+int32_t enqueue_pcg_cluster(const DeviceMatrix &A, Scratch &S, const double *b, double *x,
+                            double tol, int maxit, int init, const fvc_opts &o,
+                            cudaStream_t stream, bool launch);
+int cluster_slots_max(int n, int nslices, const int64_t *sptr);
+// An FP64 solve (code 1..3, the kernel run_pcg / run_bicgstab / run_gmres
+// would choose) enqueued on `stream` without waiting; its scalars stay on
+// the device (launch_solve_status copies them out).  launch = false only
+// allocates the scratch, so that a later call can be captured into a graph.
+int32_t enqueue_solve(const DeviceMatrix &A, Scratch &S, int code, const double *b, double *x,
+                      double tol, int maxit, int init, const fvc_opts &o, cudaStream_t stream,
+                      bool launch);
+// out[0..3] = status, iterations, inner iterations, timeout flag of the
+// solve enqueued last on S
+int32_t launch_solve_status(const Scratch &S, int32_t *out, cudaStream_t stream);
 int32_t run_pcg_batched(const DeviceMatrix &A, Scratch &S, int nsys,
                         const int32_t *row_start, const double *b, double *x,
                         double tol, int maxit, int init, const fvc_opts &o,
@@ -109,5 +124,15 @@ inline int block_threads_for(int requested, int nslices, int sms) {
   const int warps = (nslices + std::max(sms, 1) - 1) / std::max(sms, 1);
   return std::min(1024, std::max(128, (warps * 32 + 127) / 128 * 128));
 }
+
+namespace cells {
+// fvc_cells_gradient without the wait: an unsupported boundary code sets
+// *d_err (device) instead of being returned
+int32_t gradient_async(const fvc_cell_mesh *m, int kind, int comp, const double *u,
+                       double *grad, int *d_err, cudaStream_t s);
+}  // namespace cells
+
+// Allocates what fvc_solve_async needs for (code, opts) on this context.
+int32_t context_prepare(fvc_context *c, int code, const fvc_opts &o);
 
 }  // namespace fvc

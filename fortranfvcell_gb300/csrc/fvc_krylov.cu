@@ -10,7 +10,7 @@
 //   pcg        Iterativos.f:29-106   (2 grid barriers per iteration: the
 //              search-direction update p = z + beta*p of iteration j+1 is
 //              fused into the SpMV of iteration j+1, double-buffering p)
-//   pbicgstab  Iterativos.f:140-234  (5 barriers per iteration)
+//   pbicgstab  Iterativos.f:140-234  (3 grid reductions per iteration)
 //   gmres      Iterativos.f:271-446  (restarted, k = 15, modified
 //              Gram-Schmidt, Givens rotations)
 // The arithmetic follows the Fortran statements term by term, with two
@@ -691,14 +691,18 @@ int32_t ensure_vectors(Scratch &S, size_t n, int nvec, size_t nblocks, bool gmre
   return ensure_sync(S, nblocks);
 }
 
+// Enqueues one persistent solve on `stream` and returns without waiting:
+// the scratch exists afterwards, so a second call of the same shape makes
+// no allocation and may run inside a stream capture.  launch = false stops
+// after the allocations.
 template <typename K>
-int32_t run_persistent(K kernel, const DeviceMatrix &A, Scratch &S, const double *b, double *x,
-                       double tol, int maxit, int init, const fvc_opts &o, cudaStream_t stream,
-                       fvc_stats *st, int nvec, bool gmres) {
+int32_t enqueue_persistent(K kernel, const DeviceMatrix &A, Scratch &S, const double *b,
+                           double *x, double tol, int maxit, int init, const fvc_opts &o,
+                           cudaStream_t stream, int nvec, bool gmres, bool launch = true) {
   if (A.n <= 0) return FVC_ERR_ARG;
   Launch L = persistent_launch(kernel, A, o);
   int32_t rc = ensure_vectors(S, (size_t)A.n, nvec, (size_t)L.blocks, gmres);
-  if (rc != FVC_OK) return rc;
+  if (rc != FVC_OK || !launch) return rc;
   reset_sync(S, stream);
   KArgs a{};
   a.A = view64(A);
@@ -722,27 +726,26 @@ int32_t run_persistent(K kernel, const DeviceMatrix &A, Scratch &S, const double
   a.stop_rule = o.stop_rule;
   a.result = S.result;
   a.iresult = S.iresult;
-  cudaEvent_t e0, e1;
-  cudaEventCreate(&e0);
-  cudaEventCreate(&e1);
-  cudaEventRecord(e0, stream);
   void *args[] = {&a};
   cudaError_t ce = cudaLaunchCooperativeKernel((const void *)kernel, dim3(L.blocks), dim3(L.threads),
                                                args, 0, stream);
   count_launch();
-  cudaEventRecord(e1, stream);
   if (ce != cudaSuccess) {
     fprintf(stderr, "fvcgpu: cooperative launch failed: %s\n", cudaGetErrorString(ce));
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
     return FVC_ERR_CUDA;
   }
+  return FVC_OK;
+}
+
+// The solver's scalars after a synchronous solve (the kernel has ended).
+int32_t read_stats(const Scratch &S, cudaStream_t stream, cudaEvent_t e0, cudaEvent_t e1,
+                   bool have_err, fvc_stats *st) {
   double res[16];
   int ires[16], err = 0;
   cudaMemcpyAsync(res, S.result, sizeof(res), cudaMemcpyDeviceToHost, stream);
   cudaMemcpyAsync(ires, S.iresult, sizeof(ires), cudaMemcpyDeviceToHost, stream);
-  cudaMemcpyAsync(&err, S.err, sizeof(int), cudaMemcpyDeviceToHost, stream);
-  ce = cudaStreamSynchronize(stream);
+  if (have_err) cudaMemcpyAsync(&err, S.err, sizeof(int), cudaMemcpyDeviceToHost, stream);
+  cudaError_t ce = cudaStreamSynchronize(stream);
   float ms = 0.f;
   cudaEventElapsedTime(&ms, e0, e1);
   cudaEventDestroy(e0);
@@ -764,6 +767,34 @@ int32_t run_persistent(K kernel, const DeviceMatrix &A, Scratch &S, const double
     st->solve_ms = ms;
   }
   return ires[1];
+}
+
+template <typename K>
+int32_t run_persistent(K kernel, const DeviceMatrix &A, Scratch &S, const double *b, double *x,
+                       double tol, int maxit, int init, const fvc_opts &o, cudaStream_t stream,
+                       fvc_stats *st, int nvec, bool gmres) {
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventRecord(e0, stream);
+  const int32_t rc =
+      enqueue_persistent(kernel, A, S, b, x, tol, maxit, init, o, stream, nvec, gmres);
+  cudaEventRecord(e1, stream);
+  if (rc != FVC_OK) {
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return rc;
+  }
+  return read_stats(S, stream, e0, e1, true, st);
+}
+
+// status, iterations, inner iterations and the timeout flag of the solve
+// that ran last on this scratch, copied where a captured graph can read them
+__global__ void solve_status_kernel(const int *iresult, const int *err, int32_t *out) {
+  out[0] = (*err != 0) ? (int32_t)FVC_ERR_TIMEOUT : iresult[1];
+  out[1] = iresult[0];
+  out[2] = iresult[2];
+  out[3] = *err;
 }
 
 }  // namespace
@@ -792,6 +823,35 @@ int32_t run_bicgstab(const DeviceMatrix &A, Scratch &S, const double *b, double 
 int32_t run_gmres(const DeviceMatrix &A, Scratch &S, const double *b, double *x, double tol,
                   int maxit, const fvc_opts &o, cudaStream_t stream, fvc_stats *st) {
   return run_persistent(gmres_f64, A, S, b, x, tol, maxit, 1, o, stream, st, 0, true);
+}
+
+int32_t enqueue_solve(const DeviceMatrix &A, Scratch &S, int code, const double *b, double *x,
+                      double tol, int maxit, int init, const fvc_opts &o, cudaStream_t stream,
+                      bool launch) {
+  if (code == 1) {
+    if (o.block_threads == 0 && o.blocks_per_sm == 0 && o.max_blocks == 0) {
+      const int32_t rc = enqueue_pcg_cluster(A, S, b, x, tol, maxit, init, o, stream, launch);
+      if (rc != FVC_ERR_UNSUPPORTED) return rc;
+    }
+    if (A.n >= kStorePRows)
+      return enqueue_persistent(pcg_f64<true>, A, S, b, x, tol, maxit, init, o, stream, 5, false,
+                                launch);
+    return enqueue_persistent(pcg_f64<false>, A, S, b, x, tol, maxit, init, o, stream, 5, false,
+                              launch);
+  }
+  if (code == 2)
+    return enqueue_persistent(bicgstab_f64, A, S, b, x, tol, maxit, init, o, stream, 8, false,
+                              launch);
+  if (code == 3)
+    return enqueue_persistent(gmres_f64, A, S, b, x, tol, maxit, 1, o, stream, 0, true, launch);
+  return FVC_ERR_UNSUPPORTED;
+}
+
+int32_t launch_solve_status(const Scratch &S, int32_t *out, cudaStream_t stream) {
+  if (!S.iresult || !S.err || !out) return FVC_ERR_ARG;
+  solve_status_kernel<<<1, 1, 0, stream>>>(S.iresult, S.err, out);
+  count_launch();
+  return cudaPeekAtLastError() == cudaSuccess ? FVC_OK : FVC_ERR_CUDA;
 }
 
 int32_t run_pcg_batched(const DeviceMatrix &A, Scratch &S, int nsys, const int32_t *row_start,

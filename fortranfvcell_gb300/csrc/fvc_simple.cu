@@ -1007,6 +1007,16 @@ inline int grid(int n) { return (n + kThreads - 1) / kThreads; }
 
 }  // namespace
 
+int32_t gradient_async(const fvc_cell_mesh *m, int kind, int comp, const double *u,
+                       double *grad, int *d_err, cudaStream_t s) {
+  if (!mesh_ok(m) || !u || !grad || !d_err || kind < 1 || kind > 3 || comp < 1 || comp > 3 ||
+      (kind == 3 && comp == 1))
+    return FVC_ERR_ARG;
+  gradient_kernel<<<grid(m->numel), kThreads, 0, s>>>(view(m), kind, comp, u, grad, d_err);
+  count_launch();
+  return cudaPeekAtLastError() == cudaSuccess ? FVC_OK : FVC_ERR_CUDA;
+}
+
 int32_t gradient(const fvc_cell_mesh *m, int kind, int comp, const double *u, double *grad,
                  cudaStream_t s) {
   if (!mesh_ok(m) || !u || !grad || kind < 1 || kind > 3 || comp < 1 || comp > 3 ||

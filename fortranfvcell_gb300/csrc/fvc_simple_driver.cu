@@ -67,6 +67,51 @@ __global__ void self_dots(int n, const double *a, const double *b, const double 
 
 inline int g(int n) { return (n + kT - 1) / kT; }
 
+// One outer iteration of the captured loop (fvc_simple_set_graph): the
+// norms that steer it and what each solve (u1, u2, p', energy) returned.
+struct SimpleRec {
+  double dots[8];   // |b1|^2 |b2|^2, |rc1|^2 |rc2|^2 |rcp|^2, |be|^2 |rce|^2
+  int32_t st[4][4]; // status, iterations, inner iterations, timeout flag
+  int32_t ran[4];   // the solve ran
+  int32_t ok[4];    // ... and ended with FVC_OK
+};
+constexpr int kRecMax = 256;  // outer iterations per batch of graph launches
+
+// ctr[0]: the record of the running iteration; ctr[1]: a solve failed
+__global__ void rec_dots(const int32_t *ctr, SimpleRec *rec, const double *dots, int off,
+                         int k) {
+  SimpleRec &r = rec[ctr[0]];
+  for (int i = 0; i < k; ++i) r.dots[off + i] = dots[i];
+}
+
+// The reference's test before a solve (the norm, or its square root, at
+// least 1e-32), and no solve failed before it in this batch.
+__global__ void set_run(cudaGraphConditionalHandle h, const int32_t *ctr, SimpleRec *rec,
+                        int dot, int use_sqrt, int sys) {
+  SimpleRec &r = rec[ctr[0]];
+  const double v = use_sqrt ? sqrt(r.dots[dot]) : r.dots[dot];
+  const int run = (v >= 1.0e-32 && ctr[1] == 0) ? 1 : 0;
+  r.ran[sys] = run;
+  cudaGraphSetConditional(h, (unsigned)run);
+}
+
+// After a solve: its status into the record; a failure stops the solves of
+// the rest of the batch, as the uncaptured loop returns at the first one.
+__global__ void set_ok(cudaGraphConditionalHandle h, int32_t *ctr, SimpleRec *rec,
+                       const int32_t *st, int sys) {
+  SimpleRec &r = rec[ctr[0]];
+  int ok = 0;
+  if (r.ran[sys]) {
+    for (int k = 0; k < 4; ++k) r.st[sys][k] = st[k];
+    ok = (st[0] == 0) ? 1 : 0;
+    if (!ok) ctr[1] = 1;
+  }
+  r.ok[sys] = ok;
+  cudaGraphSetConditional(h, (unsigned)ok);
+}
+
+__global__ void next_rec(int32_t *ctr) { ctr[0] += 1; }
+
 }  // namespace
 }  // namespace fvc
 
@@ -103,6 +148,15 @@ struct fvc_simple {
   double *ade = nullptr, *aue = nullptr, *be = nullptr, *be0 = nullptr, *rce = nullptr;
   std::vector<int32_t> ident;
   std::vector<void *> owned;
+  int32_t *d_err = nullptr, *h_err = nullptr;  // gradient: unsupported boundary code
+  // one outer iteration as a CUDA graph (fvc_simple_set_graph)
+  bool use_graph = false, graph_gas = false;
+  cudaStream_t body = nullptr;  // captures the bodies of the conditional nodes
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  fvc::SimpleRec *rec = nullptr, *h_rec = nullptr;
+  int32_t *gctr = nullptr, *st_tmp = nullptr;
+  int64_t launches_top = 0, launches_run[4] = {0, 0, 0, 0}, launches_ok[4] = {0, 0, 0, 0};
 };
 
 namespace {
@@ -129,8 +183,13 @@ void release(fvc_simple *s) {
   if (s->ctx_u) fvc_context_destroy(s->ctx_u);
   if (s->ctx_pc) fvc_context_destroy(s->ctx_pc);
   if (s->ctx_e) fvc_context_destroy(s->ctx_e);
+  if (s->gexec) cudaGraphExecDestroy(s->gexec);
+  if (s->graph) cudaGraphDestroy(s->graph);
+  if (s->body) cudaStreamDestroy(s->body);
   for (void *ptr : s->owned) cudaFree(ptr);
   if (s->h_dots) cudaFreeHost(s->h_dots);
+  if (s->h_err) cudaFreeHost(s->h_err);
+  if (s->h_rec) cudaFreeHost(s->h_rec);
   if (s->stream) cudaStreamDestroy(s->stream);
 }
 
@@ -230,17 +289,22 @@ int32_t time_term(fvc_simple *s) {
                             s->stream);
 }
 
+// p' (ctx_pc) takes precision; momentum and energy precision_u when set
+fvc_opts solve_opts(const fvc_simple *s, const fvc_context *ctx) {
+  fvc_opts o;
+  fvc_opts_default(&o);
+  o.precision = (ctx != s->ctx_pc && s->o.precision_u >= 0) ? s->o.precision_u : s->o.precision;
+  return o;
+}
+
 // x (cells) -> equation order, solve, back to cells
 int32_t solve(fvc_simple *s, fvc_context *ctx, int code, const double *ad, const double *au,
               const double *b, double *x_cells, double tol, int *its, const char *what) {
   const int n = s->numel;
   int32_t rc = fvc_getres(n, s->num, x_cells, s->xe, 1, s->stream);
   if (rc != FVC_OK) return rc;
-  if ((rc = fvc_matrix_update_values(ctx, ad, au, au)) != FVC_OK) return rc;
-  fvc_opts o;
-  fvc_opts_default(&o);
-  // p' (ctx_pc) takes precision; momentum and energy precision_u when set
-  o.precision = (ctx != s->ctx_pc && s->o.precision_u >= 0) ? s->o.precision_u : s->o.precision;
+  if ((rc = fvc_matrix_update_values_async(ctx, ad, au, au)) != FVC_OK) return rc;
+  const fvc_opts o = solve_opts(s, ctx);
   fvc_stats st;
   rc = fvc_solve(ctx, code, b, s->xe, tol, s->o.maxit, &o, &st);
   if (its) *its = st.iterations;
@@ -354,7 +418,10 @@ int32_t fvc_simple_create(fvc_simple **out, int32_t device, int32_t numel, int32
       (rc = dalloc(s, s->au2, s->nja_u)) != FVC_OK ||
       (rc = dalloc(s, s->aup, s->nja_pc)) != FVC_OK || (rc = dalloc(s, s->dots, 4)) != FVC_OK)
     return fail(rc);
-  if (cudaMallocHost(&s->h_dots, 4 * sizeof(double)) != cudaSuccess) return fail(FVC_ERR_CUDA);
+  if ((rc = dalloc(s, s->d_err, 1)) != FVC_OK) return fail(rc);
+  if (cudaMallocHost(&s->h_dots, 4 * sizeof(double)) != cudaSuccess ||
+      cudaMallocHost(&s->h_err, sizeof(int32_t)) != cudaSuccess)
+    return fail(FVC_ERR_CUDA);
   if ((rc = time_term(s)) != FVC_OK) return fail(rc);
   if (cudaStreamSynchronize(s->stream) != cudaSuccess) return fail(FVC_ERR_CUDA);
   *out = s;
@@ -383,53 +450,120 @@ int32_t fvc_simple_time_step(fvc_simple *s) {
 
 namespace {
 
-int32_t iterate(fvc_simple *s, int32_t nit, double *res, int32_t *its, int nrep) {
-  if (!s || nit < 0) return FVC_ERR_ARG;
-  cudaSetDevice(s->device);
+// ---- stages of one outer iteration (src/Simple.f:299-710) ------------------
+// Each enqueues on st and returns without waiting; the loop below (or the
+// capture of a graph) reads the norms they leave in s->dots.
+
+// guess, the gradients of u1, u2 (momentum ghost rules) and p, divergente,
+// both momentum systems with the time term and cell residuals; dots =
+// |b1|^2, |b2|^2
+int32_t stage_momentum(fvc_simple *s, cudaStream_t st) {
   const bool gas = s->gas;
-  const int n = s->numel, mu = s->o.matriz_u, mpc = s->o.matriz_pc;
+  const int n = s->numel, mu = s->o.matriz_u;
   const fvc_cell_mesh *m = &s->m;
+  int32_t rc;
+  fvc::split_w<<<fvc::g(n), fvc::kT, 0, st>>>(n, s->w, s->u1, s->u2);
+  fvc::count_launch();
+  if ((rc = fvc::cells::gradient_async(m, 1, 1, s->u1, s->gu1, s->d_err, st)) != FVC_OK ||
+      (rc = fvc::cells::gradient_async(m, 1, 2, s->u2, s->gu2, s->d_err, st)) != FVC_OK)
+    return rc;
+  if ((rc = fvc_cells_divergence(n, s->div, s->gu1, s->gu2, st)) != FVC_OK) return rc;
+  // the pressure's ghost rules: incompressible, or the ideal-gas cell's (p)
+  if ((rc = fvc::cells::gradient_async(m, gas ? 3 : 2, 3, s->p, s->gp, s->d_err, st)) != FVC_OK)
+    return rc;
+  // momentum systems (u0 = p), time term, cell residuals
+  for (int comp = 1; comp <= 2; ++comp) {
+    double *u = comp == 1 ? s->u1 : s->u2, *ad = comp == 1 ? s->ad1 : s->ad2;
+    double *au = comp == 1 ? s->au1 : s->au2, *b = comp == 1 ? s->b1 : s->b2;
+    double *rcv = comp == 1 ? s->rc1 : s->rc2;
+    const double *ga = comp == 1 ? s->gu1 : s->gu2, *gb = comp == 1 ? s->gu2 : s->gu1;
+    if (gas)
+      rc = fvc_cells_momentum_ideal_gas(m, comp, 1, u, s->p, s->w, ga, gb, s->gp, s->ro, s->div,
+                                        s->grav[0], s->grav[1], s->o.dt, s->o.bs, s->o.under_u,
+                                        s->o.simple_c, mu, s->ia_u, s->ja_u, ad, au, b, s->im,
+                                        s->d, rcv, st);
+    else
+      rc = fvc_cells_momentum(m, comp, 1, u, s->p, s->w, ga, gb, s->gp, s->o.dt, s->o.bs,
+                              s->o.under_u, s->o.simple_c, mu, s->ia_u, s->ja_u, ad, au, b, s->im,
+                              s->d, rcv, st);
+    if (rc != FVC_OK) return rc;
+    fvc::add_time_term<<<fvc::g(n), fvc::kT, 0, st>>>(n, s->num, b, comp == 1 ? s->b10 : s->b20,
+                                                      rcv);
+    fvc::count_launch();
+  }
+  fvc::self_dots<<<2, fvc::kT, 0, st>>>(n, s->b1, s->b2, s->b2, s->dots);
+  fvc::count_launch();
+  return FVC_OK;
+}
+
+// updateVel, the p' system; dots = |rc1|^2, |rc2|^2, |rcp|^2
+int32_t stage_pressure(fvc_simple *s, cudaStream_t st) {
+  const int n = s->numel, mpc = s->o.matriz_pc;
+  int32_t rc;
+  fvc::join_w<<<fvc::g(n), fvc::kT, 0, st>>>(n, s->wp, s->u1, s->u2);
+  fvc::count_launch();
+  if (s->gas)
+    rc = fvc_cells_pressure_correction_ideal_gas(&s->m, s->wp, s->d, s->p, s->gp, s->ro,
+                                                 s->o.int_vel, s->o.dt, s->o.bs, mpc, s->ia_pc,
+                                                 s->ja_pc, s->adp, s->aup, s->bp, s->rcp, st);
+  else
+    rc = fvc_cells_pressure_correction(&s->m, s->wp, s->d, s->p, s->gp, s->o.int_vel, mpc,
+                                       s->ia_pc, s->ja_pc, s->adp, s->aup, s->bp, s->rcp, st);
+  if (rc != FVC_OK) return rc;
+  fvc::self_dots<<<3, fvc::kT, 0, st>>>(n, s->rc1, s->rc2, s->rcp, s->dots);
+  fvc::count_launch();
+  return FVC_OK;
+}
+
+// after the p' solve: its gradient and simpleUpdate
+int32_t after_pressure(fvc_simple *s, cudaStream_t st) {
+  int32_t rc = fvc::cells::gradient_async(&s->m, s->gas ? 3 : 2, 2, s->pc, s->gpc, s->d_err, st);
+  if (rc != FVC_OK) return rc;
+  return fvc_cells_simple_update(s->numel, s->w, s->p, s->u1, s->u2, s->pc, s->gpc, s->d,
+                                 s->o.under_pc, st);
+}
+
+// the enthalpy system (src/Simple.f:647-710); dots = |be|^2, |rce|^2
+int32_t stage_energy(fvc_simple *s, cudaStream_t st) {
+  const int n = s->numel;
+  const fvc_cell_mesh *m = &s->m;
+  int32_t rc;
+  if ((rc = fvc_cells_energy_gradient(m, 3, s->pedge_e, s->sedge_e, s->en, s->ge, st)) != FVC_OK)
+    return rc;
+  if ((rc = fvc_cells_energy(m, 3, 1, s->pedge_e, s->sedge_e, s->en, s->en, s->ro, s->w, s->ge,
+                             s->o.dt, s->o.bs, 1, s->ia_e, s->ja_e, s->ade, s->aue, s->be, s->rce,
+                             st)) != FVC_OK)
+    return rc;
+  fvc::add_time_term<<<fvc::g(n), fvc::kT, 0, st>>>(n, s->num, s->be, s->be0, s->rce);
+  fvc::count_launch();
+  fvc::self_dots<<<2, fvc::kT, 0, st>>>(n, s->be, s->rce, s->rce, s->dots);
+  fvc::count_launch();
+  return FVC_OK;
+}
+
+// after the energy solve: temperatures and the new density level
+int32_t after_energy(fvc_simple *s, cudaStream_t st) {
+  int32_t rc = fvc_cells_enthalpy_temperature(s->numel, s->en, s->temp, s->cp, s->tref, 1, st);
+  if (rc != FVC_OK) return rc;
+  return fvc_cells_ideal_gas_density(s->numel, s->ro, s->temp, 1, 3, 1.0, 1.0, st);
+}
+
+int32_t read_dots(fvc_simple *s, int k, bool err) {
+  cudaMemcpyAsync(s->h_dots, s->dots, k * sizeof(double), cudaMemcpyDeviceToHost, s->stream);
+  if (err) cudaMemcpyAsync(s->h_err, s->d_err, sizeof(int32_t), cudaMemcpyDeviceToHost, s->stream);
+  if (cudaStreamSynchronize(s->stream) != cudaSuccess) return FVC_ERR_CUDA;
+  return (err && *s->h_err) ? FVC_ERR_UNSUPPORTED : FVC_OK;  // a velocity code outside 0..4
+}
+
+// nit outer iterations with the norms read back where the reference tests
+// them; res/its get nrep entries per iteration
+int32_t iterate_plain(fvc_simple *s, int32_t nit, double *res, int32_t *its, int nrep) {
   cudaStream_t st = s->stream;
   int32_t rc;
   for (int it = 0; it < nit; ++it) {
     int solver_its[4] = {0, 0, 0, 0};
-    // guess; gradients of u1, u2 (momentum ghost rules) and p
-    fvc::split_w<<<fvc::g(n), fvc::kT, 0, st>>>(n, s->w, s->u1, s->u2);
-    fvc::count_launch();
-    if ((rc = fvc_cells_gradient(m, 1, 1, s->u1, s->gu1, st)) != FVC_OK) return rc;
-    if ((rc = fvc_cells_gradient(m, 1, 2, s->u2, s->gu2, st)) != FVC_OK) return rc;
-    if ((rc = fvc_cells_divergence(n, s->div, s->gu1, s->gu2, st)) != FVC_OK) return rc;
-    // the pressure's ghost rules: incompressible, or the ideal-gas cell's (p)
-    if ((rc = fvc_cells_gradient(m, gas ? 3 : 2, 3, s->p, s->gp, st)) != FVC_OK) return rc;
-    // momentum systems (u0 = p), time term, cell residuals
-    if (gas)
-      rc = fvc_cells_momentum_ideal_gas(m, 1, 1, s->u1, s->p, s->w, s->gu1, s->gu2, s->gp, s->ro,
-                                        s->div, s->grav[0], s->grav[1], s->o.dt, s->o.bs,
-                                        s->o.under_u, s->o.simple_c, mu, s->ia_u, s->ja_u,
-                                        s->ad1, s->au1, s->b1, s->im, s->d, s->rc1, st);
-    else
-      rc = fvc_cells_momentum(m, 1, 1, s->u1, s->p, s->w, s->gu1, s->gu2, s->gp, s->o.dt,
-                              s->o.bs, s->o.under_u, s->o.simple_c, mu, s->ia_u, s->ja_u, s->ad1,
-                              s->au1, s->b1, s->im, s->d, s->rc1, st);
-    if (rc != FVC_OK) return rc;
-    fvc::add_time_term<<<fvc::g(n), fvc::kT, 0, st>>>(n, s->num, s->b1, s->b10, s->rc1);
-    fvc::count_launch();
-    if (gas)
-      rc = fvc_cells_momentum_ideal_gas(m, 2, 1, s->u2, s->p, s->w, s->gu2, s->gu1, s->gp, s->ro,
-                                        s->div, s->grav[0], s->grav[1], s->o.dt, s->o.bs,
-                                        s->o.under_u, s->o.simple_c, mu, s->ia_u, s->ja_u,
-                                        s->ad2, s->au2, s->b2, s->im, s->d, s->rc2, st);
-    else
-      rc = fvc_cells_momentum(m, 2, 1, s->u2, s->p, s->w, s->gu2, s->gu1, s->gp, s->o.dt,
-                              s->o.bs, s->o.under_u, s->o.simple_c, mu, s->ia_u, s->ja_u, s->ad2,
-                              s->au2, s->b2, s->im, s->d, s->rc2, st);
-    if (rc != FVC_OK) return rc;
-    fvc::add_time_term<<<fvc::g(n), fvc::kT, 0, st>>>(n, s->num, s->b2, s->b20, s->rc2);
-    fvc::count_launch();
-    fvc::self_dots<<<2, fvc::kT, 0, st>>>(n, s->b1, s->b2, s->b2, s->dots);
-    fvc::count_launch();
-    cudaMemcpyAsync(s->h_dots, s->dots, 2 * sizeof(double), cudaMemcpyDeviceToHost, st);
-    if (cudaStreamSynchronize(st) != cudaSuccess) return FVC_ERR_CUDA;
+    if ((rc = stage_momentum(s, st)) != FVC_OK || (rc = read_dots(s, 2, true)) != FVC_OK)
+      return rc;
     const bool solve1 = s->h_dots[0] >= 1.0e-32, solve2 = s->h_dots[1] >= 1.0e-32;
     if (solve1 && (rc = solve(s, s->ctx_u, s->o.code_u, s->ad1, s->au1, s->b1, s->u1,
                               s->o.tol_u, &solver_its[0], "u1")) != FVC_OK)
@@ -437,56 +571,26 @@ int32_t iterate(fvc_simple *s, int32_t nit, double *res, int32_t *its, int nrep)
     if (solve2 && (rc = solve(s, s->ctx_u, s->o.code_u, s->ad2, s->au2, s->b2, s->u2,
                               s->o.tol_u, &solver_its[1], "u2")) != FVC_OK)
       return rc;
-    // updateVel, p' system and the residual norms
-    fvc::join_w<<<fvc::g(n), fvc::kT, 0, st>>>(n, s->wp, s->u1, s->u2);
-    fvc::count_launch();
-    if (gas)
-      rc = fvc_cells_pressure_correction_ideal_gas(m, s->wp, s->d, s->p, s->gp, s->ro,
-                                                   s->o.int_vel, s->o.dt, s->o.bs, mpc, s->ia_pc,
-                                                   s->ja_pc, s->adp, s->aup, s->bp, s->rcp, st);
-    else
-      rc = fvc_cells_pressure_correction(m, s->wp, s->d, s->p, s->gp, s->o.int_vel, mpc,
-                                         s->ia_pc, s->ja_pc, s->adp, s->aup, s->bp, s->rcp, st);
-    if (rc != FVC_OK) return rc;
-    fvc::self_dots<<<3, fvc::kT, 0, st>>>(n, s->rc1, s->rc2, s->rcp, s->dots);
-    fvc::count_launch();
-    cudaMemcpyAsync(s->h_dots, s->dots, 3 * sizeof(double), cudaMemcpyDeviceToHost, st);
-    if (cudaStreamSynchronize(st) != cudaSuccess) return FVC_ERR_CUDA;
+    if ((rc = stage_pressure(s, st)) != FVC_OK || (rc = read_dots(s, 3, false)) != FVC_OK)
+      return rc;
     const double r1 = std::sqrt(s->h_dots[0]), r2 = std::sqrt(s->h_dots[1]);
     const double rpc = std::sqrt(s->h_dots[2]);
     if (rpc >= 1.0e-32) {
       if ((rc = solve(s, s->ctx_pc, s->o.code_pc, s->adp, s->aup, s->bp, s->pc, s->o.tol_pc,
-                      &solver_its[2], "p'")) != FVC_OK)
-        return rc;
-      if ((rc = fvc_cells_gradient(m, gas ? 3 : 2, 2, s->pc, s->gpc, st)) != FVC_OK) return rc;
-      if ((rc = fvc_cells_simple_update(n, s->w, s->p, s->u1, s->u2, s->pc, s->gpc, s->d,
-                                        s->o.under_pc, st)) != FVC_OK)
+                      &solver_its[2], "p'")) != FVC_OK ||
+          (rc = after_pressure(s, st)) != FVC_OK)
         return rc;
     }
     double re = 0.0;
-    if (gas) {  // energy (src/Simple.f:647-710)
-      if ((rc = fvc_cells_energy_gradient(m, 3, s->pedge_e, s->sedge_e, s->en, s->ge, st)) !=
-          FVC_OK)
+    if (s->gas) {
+      if ((rc = stage_energy(s, st)) != FVC_OK || (rc = read_dots(s, 2, false)) != FVC_OK)
         return rc;
-      if ((rc = fvc_cells_energy(m, 3, 1, s->pedge_e, s->sedge_e, s->en, s->en, s->ro, s->w,
-                                 s->ge, s->o.dt, s->o.bs, 1, s->ia_e, s->ja_e, s->ade, s->aue,
-                                 s->be, s->rce, st)) != FVC_OK)
-        return rc;
-      fvc::add_time_term<<<fvc::g(n), fvc::kT, 0, st>>>(n, s->num, s->be, s->be0, s->rce);
-      fvc::count_launch();
-      fvc::self_dots<<<2, fvc::kT, 0, st>>>(n, s->be, s->rce, s->rce, s->dots);
-      fvc::count_launch();
-      cudaMemcpyAsync(s->h_dots, s->dots, 2 * sizeof(double), cudaMemcpyDeviceToHost, st);
-      if (cudaStreamSynchronize(st) != cudaSuccess) return FVC_ERR_CUDA;
       re = std::sqrt(s->h_dots[0]);
       if (re >= 1.0e-32) {
         re = std::sqrt(s->h_dots[1]);
         if ((rc = solve(s, s->ctx_e, 2, s->ade, s->aue, s->be, s->en, s->o.tol_u,
-                        &solver_its[3], "energy")) != FVC_OK)
-          return rc;
-        if ((rc = fvc_cells_enthalpy_temperature(n, s->en, s->temp, s->cp, s->tref, 1, st)) !=
-                FVC_OK ||
-            (rc = fvc_cells_ideal_gas_density(n, s->ro, s->temp, 1, 3, 1.0, 1.0, st)) != FVC_OK)
+                        &solver_its[3], "energy")) != FVC_OK ||
+            (rc = after_energy(s, st)) != FVC_OK)
           return rc;
       }
     }
@@ -502,9 +606,280 @@ int32_t iterate(fvc_simple *s, int32_t nit, double *res, int32_t *its, int nrep)
   return cudaStreamSynchronize(st) == cudaSuccess ? FVC_OK : FVC_ERR_CUDA;
 }
 
+// ---- one outer iteration as a CUDA graph -----------------------------------
+// The stages above, captured once.  The reference's host tests before each
+// solve become conditional (IF) nodes whose values kernels set from the
+// norms on the device, so one graph launch runs a whole outer iteration and
+// a batch of launches needs one host synchronisation at its end.
+
+// A failed CUDA call while the graph is captured: names the call
+bool cap_ok(cudaError_t e, const char *what) {
+  if (e == cudaSuccess) return true;
+  fprintf(stderr, "fvcgpu: graph capture: %s: %s\n", what, cudaGetErrorString(e));
+  return false;
+}
+
+// Adds an IF node on h to the capture running on s->stream and captures
+// body(stream) into the node's body graph on s->body.
+template <typename F>
+int32_t cap_if(fvc_simple *s, cudaGraphConditionalHandle h, int64_t *launches, F body) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaGraph_t g = nullptr;
+  const cudaGraphNode_t *deps = nullptr;
+  const cudaGraphEdgeData *ed = nullptr;
+  size_t nd = 0;
+  if (!cap_ok(cudaStreamGetCaptureInfo(s->stream, &cs, nullptr, &g, &deps, &ed, &nd),
+              "cudaStreamGetCaptureInfo"))
+    return FVC_ERR_CUDA;
+  if (cs != cudaStreamCaptureStatusActive) {
+    fprintf(stderr, "fvcgpu: graph capture: the capture was invalidated (status %d)\n",
+            (int)cs);
+    return FVC_ERR_CUDA;
+  }
+  cudaGraphNodeParams p = {cudaGraphNodeTypeConditional};
+  p.conditional.handle = h;
+  p.conditional.type = cudaGraphCondTypeIf;
+  p.conditional.size = 1;
+  cudaGraphNode_t node;
+  if (!cap_ok(cudaGraphAddNode(&node, g, deps, ed, nd, &p), "cudaGraphAddNode (IF)") ||
+      !cap_ok(cudaStreamUpdateCaptureDependencies(s->stream, &node, nullptr, 1,
+                                                  cudaStreamSetCaptureDependencies),
+              "cudaStreamUpdateCaptureDependencies"))
+    return FVC_ERR_CUDA;
+  if (!cap_ok(cudaStreamBeginCaptureToGraph(s->body, p.conditional.phGraph_out[0], nullptr,
+                                            nullptr, 0, cudaStreamCaptureModeRelaxed),
+              "cudaStreamBeginCaptureToGraph"))
+    return FVC_ERR_CUDA;
+  const int64_t l0 = fvc_kernel_launches();
+  const int32_t rc = body(s->body);
+  *launches = fvc_kernel_launches() - l0;
+  cudaGraph_t out = nullptr;  // the body graph itself, owned by the node
+  const bool ended = cap_ok(cudaStreamEndCapture(s->body, &out), "cudaStreamEndCapture (body)");
+  if (rc != FVC_OK) {
+    fprintf(stderr, "fvcgpu: graph capture: a body enqueue returned status %d\n", rc);
+    return rc;
+  }
+  return ended ? FVC_OK : FVC_ERR_CUDA;
+}
+
+// One system's solve inside the captured iteration: IF(run) { x to
+// equation order, the values, the solve, its status }, the status into the
+// record, IF(ok) { x back to the cells, then after(stream) }.
+template <typename F>
+int32_t cap_solve(fvc_simple *s, int sys, fvc_context *ctx, int code, const double *ad,
+                  const double *au, const double *b, double *x_cells, double tol,
+                  cudaGraphConditionalHandle hrun, cudaGraphConditionalHandle hok, F after) {
+  const int n = s->numel;
+  const fvc_opts o = solve_opts(s, ctx);
+  int32_t *stp = s->st_tmp + 4 * sys;
+  int32_t rc = cap_if(s, hrun, &s->launches_run[sys], [&](cudaStream_t bs) {
+    int32_t r = fvc_getres(n, s->num, x_cells, s->xe, 1, bs);
+    if (r != FVC_OK) return r;
+    fvc_context_set_stream(ctx, bs);
+    if ((r = fvc_matrix_update_values_async(ctx, ad, au, au)) == FVC_OK)
+      r = fvc_solve_async(ctx, code, b, s->xe, tol, s->o.maxit, &o, stp);
+    fvc_context_set_stream(ctx, s->stream);
+    return r;
+  });
+  if (rc != FVC_OK) return rc;
+  fvc::set_ok<<<1, 1, 0, s->stream>>>(hok, s->gctr, s->rec, stp, sys);
+  fvc::count_launch();
+  return cap_if(s, hok, &s->launches_ok[sys], [&](cudaStream_t bs) {
+    const int32_t r = fvc_getres(n, s->num, x_cells, s->xe, 0, bs);
+    return r != FVC_OK ? r : after(bs);
+  });
+}
+
+int32_t capture_iteration(fvc_simple *s, const cudaGraphConditionalHandle *h) {
+  cudaStream_t st = s->stream;
+  const int64_t l0 = fvc_kernel_launches();
+  int64_t body = 0;
+  auto none = [](cudaStream_t) { return (int32_t)FVC_OK; };
+  auto dots = [&](int off, int k) {
+    fvc::rec_dots<<<1, 1, 0, st>>>(s->gctr, s->rec, s->dots, off, k);
+    fvc::count_launch();
+  };
+  auto run = [&](int sys, int dot, int use_sqrt) {
+    fvc::set_run<<<1, 1, 0, st>>>(h[2 * sys], s->gctr, s->rec, dot, use_sqrt, sys);
+    fvc::count_launch();
+  };
+  int32_t rc;
+  if ((rc = stage_momentum(s, st)) != FVC_OK) {
+    fprintf(stderr, "fvcgpu: graph capture: the momentum stage returned status %d\n", rc);
+    return rc;
+  }
+  dots(0, 2);
+  run(0, 0, 0);
+  if ((rc = cap_solve(s, 0, s->ctx_u, s->o.code_u, s->ad1, s->au1, s->b1, s->u1, s->o.tol_u, h[0],
+                      h[1], none)) != FVC_OK)
+    return rc;
+  run(1, 1, 0);
+  if ((rc = cap_solve(s, 1, s->ctx_u, s->o.code_u, s->ad2, s->au2, s->b2, s->u2, s->o.tol_u, h[2],
+                      h[3], none)) != FVC_OK)
+    return rc;
+  if ((rc = stage_pressure(s, st)) != FVC_OK) return rc;
+  dots(2, 3);
+  run(2, 4, 1);
+  if ((rc = cap_solve(s, 2, s->ctx_pc, s->o.code_pc, s->adp, s->aup, s->bp, s->pc, s->o.tol_pc,
+                      h[4], h[5], [&](cudaStream_t bs) { return after_pressure(s, bs); })) !=
+      FVC_OK)
+    return rc;
+  if (s->gas) {
+    if ((rc = stage_energy(s, st)) != FVC_OK) return rc;
+    dots(5, 2);
+    run(3, 5, 1);
+    if ((rc = cap_solve(s, 3, s->ctx_e, 2, s->ade, s->aue, s->be, s->en, s->o.tol_u, h[6], h[7],
+                        [&](cudaStream_t bs) { return after_energy(s, bs); })) != FVC_OK)
+      return rc;
+  }
+  fvc::next_rec<<<1, 1, 0, st>>>(s->gctr);
+  fvc::count_launch();
+  for (int k = 0; k < 4; ++k) body += s->launches_run[k] + s->launches_ok[k];
+  s->launches_top = fvc_kernel_launches() - l0 - body;
+  return FVC_OK;
+}
+
+void drop_graph(fvc_simple *s) {
+  if (s->gexec) cudaGraphExecDestroy(s->gexec);
+  if (s->graph) cudaGraphDestroy(s->graph);
+  s->gexec = nullptr;
+  s->graph = nullptr;
+}
+
+int32_t build_graph(fvc_simple *s) {
+  drop_graph(s);
+  int32_t rc;
+  if (!s->rec) {
+    if ((rc = dalloc(s, s->rec, fvc::kRecMax)) != FVC_OK || (rc = dalloc(s, s->gctr, 2)) != FVC_OK ||
+        (rc = dalloc(s, s->st_tmp, 16)) != FVC_OK)
+      return rc;
+    if (cudaMallocHost(&s->h_rec, sizeof(fvc::SimpleRec) * fvc::kRecMax) != cudaSuccess)
+      return FVC_ERR_CUDA;
+  }
+  if (!s->body && cudaStreamCreateWithFlags(&s->body, cudaStreamNonBlocking) != cudaSuccess)
+    return FVC_ERR_CUDA;
+  // every solve's scratch exists before the capture
+  fvc_context *ctxs[3] = {s->ctx_u, s->ctx_pc, s->ctx_e};
+  const int codes[3] = {s->o.code_u, s->o.code_pc, 2};
+  for (int k = 0; k < (s->gas ? 3 : 2); ++k)
+    if ((rc = fvc::context_prepare(ctxs[k], codes[k], solve_opts(s, ctxs[k]))) != FVC_OK)
+      return rc;
+  if (cudaStreamSynchronize(s->stream) != cudaSuccess) return FVC_ERR_CUDA;
+  const int64_t l0 = fvc_kernel_launches();
+  if (!cap_ok(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeRelaxed),
+              "cudaStreamBeginCapture"))
+    return FVC_ERR_CUDA;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaGraph_t g = nullptr;
+  rc = FVC_OK;
+  // run/ok handles of u1, u2, p' (and the energy): every handle created
+  // must belong to a conditional node, or the instantiation fails
+  cudaGraphConditionalHandle h[8];
+  if (!cap_ok(cudaStreamGetCaptureInfo(s->stream, &cs, nullptr, &g), "cudaStreamGetCaptureInfo"))
+    rc = FVC_ERR_CUDA;
+  for (int k = 0; k < (s->gas ? 8 : 6) && rc == FVC_OK; ++k)
+    if (!cap_ok(cudaGraphConditionalHandleCreate(&h[k], g, 0, cudaGraphCondAssignDefault),
+                "cudaGraphConditionalHandleCreate"))
+      rc = FVC_ERR_CUDA;
+  if (rc == FVC_OK) rc = capture_iteration(s, h);
+  cudaGraph_t out = nullptr;
+  const bool ended = cap_ok(cudaStreamEndCapture(s->stream, &out), "cudaStreamEndCapture");
+  // launches were counted at the capture; they are counted per replay instead
+  fvc::count_launch(l0 - fvc_kernel_launches());
+  if (rc == FVC_OK && !ended) rc = FVC_ERR_CUDA;
+  if (rc == FVC_OK) {
+    cudaGraphInstantiateParams ip;
+    memset(&ip, 0, sizeof(ip));
+    if (!cap_ok(cudaGraphInstantiateWithParams(&s->gexec, out, &ip),
+                "cudaGraphInstantiateWithParams")) {
+      cudaGraphNodeType t = cudaGraphNodeTypeEmpty;
+      if (ip.errNode_out) cudaGraphNodeGetType(ip.errNode_out, &t);
+      fprintf(stderr, "fvcgpu: graph capture: instantiation result %d, node type %d\n",
+              (int)ip.result_out, ip.errNode_out ? (int)t : -1);
+      rc = FVC_ERR_CUDA;
+    }
+  }
+  if (rc != FVC_OK) {
+    if (out) cudaGraphDestroy(out);
+    cudaGetLastError();
+    fprintf(stderr, "fvcgpu: the SIMPLE iteration could not be captured as a CUDA graph "
+                    "(status %d)\n", rc);
+    return rc;
+  }
+  s->graph = out;
+  s->graph_gas = s->gas;
+  return FVC_OK;
+}
+
+const char *const kSysName[4] = {"u1", "u2", "p'", "energy"};
+
+// nit outer iterations as graph launches, in batches of at most kRecMax with
+// one synchronisation each; the same results as iterate_plain
+int32_t iterate_graph(fvc_simple *s, int32_t nit, double *res, int32_t *its, int nrep) {
+  int32_t rc;
+  if (!s->gexec || s->graph_gas != s->gas)
+    if ((rc = build_graph(s)) != FVC_OK) return rc;
+  cudaStream_t st = s->stream;
+  for (int done = 0; done < nit;) {
+    const int chunk = std::min(fvc::kRecMax, nit - done);
+    cudaMemsetAsync(s->rec, 0, sizeof(fvc::SimpleRec) * chunk, st);
+    cudaMemsetAsync(s->gctr, 0, 2 * sizeof(int32_t), st);
+    for (int c = 0; c < chunk; ++c)
+      if (cudaGraphLaunch(s->gexec, st) != cudaSuccess) return FVC_ERR_CUDA;
+    cudaMemcpyAsync(s->h_rec, s->rec, sizeof(fvc::SimpleRec) * chunk, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(s->h_err, s->d_err, sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) return FVC_ERR_CUDA;
+    if (*s->h_err) return FVC_ERR_UNSUPPORTED;  // a velocity boundary code outside 0..4
+    int64_t launched = s->launches_top * chunk;
+    for (int c = 0; c < chunk; ++c) {
+      const fvc::SimpleRec &r = s->h_rec[c];
+      for (int k = 0; k < 4; ++k) {
+        launched += (r.ran[k] ? s->launches_run[k] : 0) + (r.ok[k] ? s->launches_ok[k] : 0);
+        if (r.ran[k] && !r.ok[k]) {
+          fvc::count_launch(launched);
+          fprintf(stderr, "fvcgpu: SIMPLE %s solve (code %d, fp64) ended with status %d after %d "
+                          "iterations\n", kSysName[k],
+                  k < 2 ? s->o.code_u : k == 2 ? s->o.code_pc : 2, r.st[k][0], r.st[k][1]);
+          return r.st[k][0];
+        }
+      }
+      const int it = done + c;
+      if (res) {
+        res[nrep * it] = std::sqrt(r.dots[2]);
+        res[nrep * it + 1] = std::sqrt(r.dots[3]);
+        res[nrep * it + 2] = std::sqrt(r.dots[4]);
+        if (nrep == 4)
+          res[4 * it + 3] = r.ran[3] ? std::sqrt(r.dots[6]) : std::sqrt(r.dots[5]);
+      }
+      if (its)
+        for (int k = 0; k < nrep; ++k) its[nrep * it + k] = r.ran[k] ? r.st[k][1] : 0;
+    }
+    fvc::count_launch(launched);
+    done += chunk;
+  }
+  return FVC_OK;
+}
+
+int32_t iterate(fvc_simple *s, int32_t nit, double *res, int32_t *its, int nrep) {
+  if (!s || nit < 0) return FVC_ERR_ARG;
+  cudaSetDevice(s->device);
+  return s->use_graph ? iterate_graph(s, nit, res, its, nrep)
+                      : iterate_plain(s, nit, res, its, nrep);
+}
+
 }  // namespace
 
 extern "C" {
+
+int32_t fvc_simple_set_graph(fvc_simple *s, int32_t on) {
+  if (!s) return FVC_ERR_ARG;
+  const bool fp64 = s->o.precision == FVC_PREC_FP64 &&
+                    (s->o.precision_u < 0 || s->o.precision_u == FVC_PREC_FP64);
+  if (on && !fp64) return FVC_ERR_UNSUPPORTED;
+  s->use_graph = on != 0;
+  if (!on) drop_graph(s);
+  return FVC_OK;
+}
 
 int32_t fvc_simple_iterate(fvc_simple *s, int32_t nit, double *res, int32_t *its) {
   return iterate(s, nit, res, its, 3);

@@ -123,6 +123,17 @@ class Context:
         _lib.check(self._L.fvc_matrix_update_values(self._h, ptr(ad), ptr(au), ptr(al)),
                    "fvc_matrix_update_values")
 
+    def update_values_async(self, ad, au=None, al=None) -> None:
+        """update_values without the wait (device arrays: capturable)."""
+        def ptr(a):
+            if a is None:
+                return None
+            if hasattr(a, "data_ptr"):
+                return C.c_void_p(a.data_ptr())
+            return _p(a)
+        _lib.check(self._L.fvc_matrix_update_values_async(self._h, ptr(ad), ptr(au), ptr(al)),
+                   "fvc_matrix_update_values_async")
+
     def info(self) -> dict:
         n, slots, nnz, ns = C.c_int64(), C.c_int64(), C.c_int64(), C.c_int64()
         _lib.check(self._L.fvc_matrix_info(self._h, C.byref(n), C.byref(slots), C.byref(nnz),
@@ -143,6 +154,18 @@ class Context:
                                f"{_lib.STATUS_NAMES.get(rc, rc)}")
         st.status = rc
         return st
+
+    def solve_async(self, code: int, b_dev, x_dev, tol: float, maxit: int, status_dev,
+                    opts: FvcOpts | None = None) -> None:
+        """Enqueues an FP64 solve on the context's stream without waiting
+        (capturable into a CUDA graph).  status_dev: a device int32 buffer of
+        4 entries that receives status, iterations, inner iterations and the
+        timeout flag when the solve has run."""
+        o = opts if opts is not None else make_opts()
+        _lib.check(self._L.fvc_solve_async(self._h, int(code), C.c_void_p(_addr(b_dev)),
+                                           C.c_void_p(_addr(x_dev)), float(tol), int(maxit),
+                                           C.byref(o), C.c_void_p(_addr(status_dev))),
+                   "fvc_solve_async")
 
     def solve_batched(self, row_start, b_dev, x_dev, tol: float, maxit: int,
                       opts: FvcOpts | None = None, raise_on_error: bool = True):

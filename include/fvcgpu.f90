@@ -118,6 +118,14 @@ module fvcgpu
        integer(c_int32_t)        :: its(*)
      end function fvc_simple_iterate
 
+     ! on = 1: one CUDA graph launch per outer iteration (same results)
+     integer(c_int32_t) function fvc_simple_set_graph(s, on) &
+          bind(C, name="fvc_simple_set_graph")
+       import :: c_ptr, c_int32_t
+       type(c_ptr), value        :: s
+       integer(c_int32_t), value :: on
+     end function fvc_simple_set_graph
+
      integer(c_int32_t) function fvc_simple_time_step(s) &
           bind(C, name="fvc_simple_time_step")
        import :: c_ptr, c_int32_t

@@ -147,6 +147,26 @@ int32_t fvc_solve(fvc_context *ctx, int32_t code, const double *d_b, double *d_x
                   double tol, int32_t maxit, const fvc_opts *opts,
                   fvc_stats *stats);
 
+/* fvc_matrix_update_values without the wait: the copies and the value
+ * gather are enqueued on the context's stream.  With DEVICE value arrays the
+ * call can be recorded in a CUDA stream capture on that stream. */
+int32_t fvc_matrix_update_values_async(fvc_context *ctx, const double *ad,
+                                       const double *au, const double *al);
+
+/* fvc_solve without the wait, for CUDA graphs: the same FP64 kernels, and
+ * so the same results, enqueued on the context's stream.  The call makes no
+ * host-device copy and no synchronisation, so it can be recorded in a
+ * stream capture on that stream and replayed.  When the solve has run,
+ * d_status (DEVICE, 4 int32) holds the FVC_* status, the iterations, the
+ * inner iterations (GMRES steps) and 1 if an on-device wait gave up
+ * (status FVC_ERR_TIMEOUT).  The first call for a context and launch shape
+ * allocates work buffers, so it must not be the captured one.  Returns
+ * FVC_OK once the work is enqueued; FVC_ERR_UNSUPPORTED for FVC_PREC_MIXED
+ * and for the (code, matriz) pairs fvc_solve rejects. */
+int32_t fvc_solve_async(fvc_context *ctx, int32_t code, const double *d_b,
+                        double *d_x, double tol, int32_t maxit,
+                        const fvc_opts *opts, int32_t *d_status);
+
 /* Batched Jacobi-PCG (src/Iterativos.f:29-106) of nsys independent systems
  * in one persistent launch: the context's matrix holds them block-
  * diagonally, system s on rows row_start[s] .. row_start[s+1]-1 (host
@@ -486,6 +506,22 @@ int32_t fvc_simple_create(fvc_simple **s, int32_t device, int32_t numel,
  * reference's cell-residual norms (u1, u2, p') of each iteration; its
  * (host, 3*nit, may be NULL) the linear-solver iterations (0: not solved). */
 int32_t fvc_simple_iterate(fvc_simple *s, int32_t nit, double *res, int32_t *its);
+
+/* on = 1: later fvc_simple_iterate / fvc_simple_iterate_energy calls run
+ * each outer iteration as one CUDA graph launch.  The graph is captured at
+ * the first such call (and again after fvc_simple_energy).  The reference's
+ * host tests before each solve (a norm of at least 1e-32,
+ * src/Simple.f:445-446,475-476,578-579,680-681) become conditional graph nodes
+ * whose values are set on the device.  A batch of up to 256 iterations then
+ * needs one host synchronisation.  The kernels, their order, and so the
+ * results, the residual norms and the iteration counts are those of the
+ * uncaptured loop.  A failed solve stops the solves of the rest of the
+ * batch; the call returns its status with the fields as the failing
+ * iteration left them, as the uncaptured loop does.  on = 0 returns to
+ * individual launches.  FVC_ERR_UNSUPPORTED when a system is solved in
+ * FVC_PREC_MIXED.  No counterpart in the reference, whose outer loop runs
+ * on the host. */
+int32_t fvc_simple_set_graph(fvc_simple *s, int32_t on);
 
 /* Starts a new time step: w0 = w and the time term from the current fields
  * (src/Simple.f:229-266). */
