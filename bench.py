@@ -291,6 +291,16 @@ def run_ours(args):
     spmv_ref_ms = time_spmv(ctx.spmv)
     spmv_bytes = 12 * nnz + 24 * n
     spmv_gbs = spmv_bytes / (spmv_ms * 1e-3) / 1e9
+    # the FP32 operator of the mixed solves (difference form, built by them):
+    # a 4-byte weight and a 16-bit column offset per stored slot, e, x and y
+    # per row.  Its slices are padded to the widest (4 here), so at most
+    # 128 slots per slice: the larger of that and the FP64 slot count
+    x32 = bd.float()
+    y32 = torch.empty_like(x32)
+    spmv32_ms = time_spmv(lambda xv, yv: ctx.spmv_f32(x32, y32))
+    inf = ctx.info()
+    spmv32_bytes = 6 * max(inf["slots"], 128 * inf["nslices"]) + 12 * n
+    spmv32_gbs = spmv32_bytes / (spmv32_ms * 1e-3) / 1e9
 
     # end to end through the public host API, pinned host arrays
     pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
@@ -348,7 +358,11 @@ def run_ours(args):
                   "mixed_over_fp64": round(ms64 / ms_step, 3)},
         "spmv": {"gbs": round(spmv_gbs, 1), "ms": round(spmv_ms, 4), "bytes": spmv_bytes,
                  "frac_of_peak": round(spmv_gbs / hbm, 3),
-                 "ref_rounding_gbs": round(spmv_bytes / (spmv_ref_ms * 1e-3) / 1e9, 1)},
+                 "ref_rounding_gbs": round(spmv_bytes / (spmv_ref_ms * 1e-3) / 1e9, 1),
+                 "bound": "FP64 issue rate (FP64 pipe ~75% active), not HBM",
+                 "fp32": {"gbs": round(spmv32_gbs, 1), "ms": round(spmv32_ms, 4),
+                          "bytes": spmv32_bytes, "frac_of_peak": round(spmv32_gbs / hbm, 3),
+                          "kernel": "spmv_f32, the mixed solves' operator"}},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm,
                      "unit": "GB/s", "frac": round(achieved / hbm, 3), "traffic": traffic,
                      "kernel": "mixed_cg (persistent, one launch per solve)",
@@ -508,10 +522,11 @@ def run_adjoint_c5(args):
     densities frozen.  Adjoint: one forward and one adjoint solve give all
     the derivatives; checked against GPU central differences on 32 faces
     (seed 12).  J is affine in the continuous wall enthalpy of the frozen
-    system, so the step (0.1 K) adds no truncation error; it is large so
-    that the differences stand well above the solver tolerance (a 1 mK step
-    leaves them at the 1e-2 level of the iterative solves' noise).  CPU: one solve of the same frozen system by
-    the restated BiCGSTAB, times the 2 x faces solves of full differences."""
+    system, so no step adds truncation error, and a large one (c5_fd_step,
+    default 10 K) keeps the differences far above the iterative solves'
+    error: a 1 mK step leaves them at the 1e-2 level of that error, 0.1 K
+    at 1e-4.  CPU: one solve of the same frozen system by the restated
+    BiCGSTAB, times the 2 x faces solves of full differences."""
     import torch
     from fortranfvcell_gb300 import sensitivity as sv
     from fortranfvcell_gb300.cases import natural_convection_cavity
@@ -528,7 +543,7 @@ def run_adjoint_c5(args):
     loop_s = time.perf_counter() - t0
     sysd = sv.frozen_energy_system(c, loop)
     loop.close()
-    prob = sv.NusseltProblem(c, sysd, tol=1e-12)
+    prob = sv.NusseltProblem(c, sysd, tol=args.c5_tol)
     sv.nusselt_wall_gradient(prob, sysd["h_wall"])           # warm-up
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -537,7 +552,7 @@ def run_adjoint_c5(args):
     adj_s = time.perf_counter() - t0
     idx = np.random.default_rng(12).choice(g.size, min(32, g.size), replace=False)
     t0 = time.perf_counter()
-    fd = sv.nusselt_fd(prob, sysd["h_wall"], idx, step=sysd["cp"] * 0.1)
+    fd = sv.nusselt_fd(prob, sysd["h_wall"], idx, step=sysd["cp"] * args.c5_fd_step)
     torch.cuda.synchronize()
     fd_s = time.perf_counter() - t0
     prob.close()
@@ -548,6 +563,7 @@ def run_adjoint_c5(args):
            "loop_s": round(loop_s, 3), "final_residuals": [float(f"{v:.3e}") for v in res[-1]],
            "J": round(j, 6), "adjoint_s": round(adj_s, 4),
            "fd_subset": {"faces": int(idx.size), "s": round(fd_s, 3),
+                         "step_K": args.c5_fd_step, "solve_tol": args.c5_tol,
                          "max_rel_diff_vs_adjoint": float(f"{rel.max():.2e}")},
            "fd_all_faces_s_est": round(fd_s * g.size / idx.size, 3),
            "adjoint_over_fd_all": round(fd_s * g.size / idx.size / adj_s, 1),
@@ -800,6 +816,10 @@ def main():
     ap.add_argument("--c5-nx", type=int, default=256,
                     help="adjoint C5 leg: cells per side (0 skips it)")
     ap.add_argument("--c5-its", type=int, default=200)
+    ap.add_argument("--c5-fd-step", type=float, default=10.0,
+                    help="adjoint C5 leg: central-difference step of the wall temperatures (K)")
+    ap.add_argument("--c5-tol", type=float, default=1e-12,
+                    help="adjoint C5 leg: relative tolerance of the forward and adjoint solves")
     ap.add_argument("--c4-cases", type=int, default=256,
                     help="batched C4 leg: number of systems (0 skips it)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
