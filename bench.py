@@ -593,26 +593,54 @@ def c4_sides(ncases, seed=7):
     return np.rint(np.exp(rng.uniform(np.log(32.0), np.log(256.0), ncases))).astype(int)
 
 
+C4_WHICH = ((1, 2, "u"), (2, 2, "v"), (4, 2, "T"), (3, 1, "p'"))  # loop system, code, name
+
+
+def c4_systems(ncases, outer_its=3):
+    """The u, v, enthalpy and p' systems of ncases heated lid-driven
+    cavities of air (N x N quads, N log-uniform in [32, 256] seed 7, Re ~
+    U[50, 400] seed 8, side walls 1 K apart): each case runs outer_its
+    iterations of the GPU ideal-gas SIMPLE loop (CSRD for every system) and
+    hands over the systems its last iteration solved (ad, au, b), with the
+    solver iterations of the iteration before as each system's hint for
+    the batched launch's share of blocks."""
+    from fortranfvcell_gb300 import mesh
+    from fortranfvcell_gb300.cases import heated_lid_cavity
+    from fortranfvcell_gb300.cells import SimpleLoop, simple_opts
+    sides = c4_sides(ncases)
+    res = np.random.default_rng(8).uniform(50.0, 400.0, ncases)
+    systems, codes, hints = [], [], []
+    col = {1: 0, 2: 1, 3: 2, 4: 3}   # iterate_energy's columns: u1, u2, p', enthalpy
+    for nside, re in zip(sides, res):
+        c = heated_lid_cavity(int(nside), re=float(re))
+        loop = SimpleLoop(c["coor"], c["ix"], c["nelcon"], c["num"], c["pedge"], c["sedge"],
+                          c["e"], opts=simple_opts(matriz_u=1))
+        loop.enable_energy(c["pedgeE"], c["sedgeE"], c["gravity"], c["t0"])
+        _, its = loop.iterate_energy(outer_its)
+        ia, ja, nad = mesh.datastruc(c["ident"], 1, True)
+        for which, code, _ in C4_WHICH:
+            ad, au, b = loop.system(which)
+            systems.append(dict(ad=ad, au=au, ia=ia, ja=ja, n=ad.size, nad=nad, b=b))
+            codes.append(code)
+            hints.append(float(its[-2, col[which]]))
+        loop.close()
+    return sides, res, systems, np.array(codes, np.int32), np.array(hints)
+
+
 def run_batched_c4(args):
-    """The C4 configuration, pressure-correction field: ncases independent
-    p' systems of lid-driven cavities on N x N quads (N log-uniform in
-    [32, 256], seed 7; cell 1 pinned; b ~ U[-1,1], seed 1000+k), Jacobi-PCG
-    with the reference's stopping test at tol 1e-8 from x = 0.
-    GPU batched: one persistent launch for all systems (fvc_solve_batched),
-    CUDA-event time.  GPU sequential: the same systems one fvc_solve at a
-    time (matrices already on the device).  CPU: the restated OpenMP PCG
-    (pcg_omp) on whole systems of a seeded sample, extrapolated by
-    rows x iterations."""
+    """The C4 configuration: the u, v, enthalpy (BiCGSTAB) and p' (PCG)
+    systems of one outer iteration of each of ncases heated lid-driven
+    cavities (c4_systems), 4 x ncases systems of 1k..65k rows, solved from
+    x = 0 to the reference's stopping tests at tol 1e-8.  GPU batched: one
+    persistent launch for all systems (fvc_solve_batched_ex), CUDA-event
+    time.  GPU sequential: the same systems one fvc_solve at a time
+    (matrices already on the device).  CPU: the restated reference solvers
+    (OpenMP pcg_omp / pbicgstab_omp paths) on whole systems of a seeded
+    sample, extrapolated by rows x iterations."""
     import torch
-    from fortranfvcell_gb300 import Context, make_opts, mesh, pack_block_diagonal
-    sides = c4_sides(args.c4_cases)
+    from fortranfvcell_gb300 import Context, make_opts, pack_block_diagonal
     t0 = time.time()
-    systems = []
-    for k, nside in enumerate(sides):
-        s = mesh.pressure_system(mesh.square_mesh(int(nside), kind="quad"), matriz=1,
-                                 unsym=True, pin_cell=1)
-        systems.append(dict(ad=s.ad, au=s.au, ia=s.ia, ja=s.ja, n=s.neq, nad=s.nad,
-                            b=np.random.default_rng(1000 + k).uniform(-1.0, 1.0, s.neq)))
+    sides, res, systems, codes, hints = c4_systems(args.c4_cases)
     pk = pack_block_diagonal(systems)
     rows = int(sum(s["n"] for s in systems))
     log(f"C4 setup: {len(systems)} systems, {rows} rows, {time.time() - t0:.1f} s")
@@ -628,15 +656,20 @@ def run_batched_c4(args):
     xd = torch.zeros(pk["neq"], dtype=torch.float64, device="cuda")
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
-            ctx.solve_batched(pk["row_start"], bd, xd, C4_TOL, 50000, opts)
-        runs = [ctx.solve_batched(pk["row_start"], bd, xd, C4_TOL, 50000, opts)[1]
+            ctx.solve_batched(pk["row_start"], bd, xd, C4_TOL, 50000, opts, codes=codes,
+                              its_hint=hints)
+        runs = [ctx.solve_batched(pk["row_start"], bd, xd, C4_TOL, 50000, opts, codes=codes,
+                                  its_hint=hints)[1]
                 for _ in range(max(1, min(args.steps, 3)))]
+        nohint = ctx.solve_batched(pk["row_start"], bd, xd, C4_TOL, 50000, opts, codes=codes)[1]
     batch_ms = min(st[0].solve_ms for st in runs)
+    nohint_ms = nohint[0].solve_ms
     its = np.array([t.iterations for t in runs[-1]])
     worst_rel = max(t.rel_residual for t in runs[-1])
     ctx.close()
     if getattr(args, "c4_batched_only", False):
-        return {"batched_ms": round(batch_ms, 3), "iterations_max": int(its.max())}
+        return {"batched_ms": round(batch_ms, 3), "batched_ms_without_hints": round(nohint_ms, 3),
+                "iterations_max": int(its.max()), "systems": len(systems)}
     # the same systems one solve at a time
     opts = make_opts("fp64", init=1)
     ctxs = []
@@ -646,26 +679,35 @@ def run_batched_c4(args):
         ctxs.append((c, torch.from_numpy(s["b"]).cuda(),
                      torch.zeros(s["n"], dtype=torch.float64, device="cuda")))
     with torch.cuda.stream(stream):
-        for c, sb, sx in ctxs[:8]:
-            c.solve(1, sb, sx, C4_TOL, 50000, opts)
+        for (c, sb, sx), code in list(zip(ctxs, codes))[:8]:
+            c.solve(int(code), sb, sx, C4_TOL, 50000, opts)
         torch.cuda.synchronize()
         t1 = time.perf_counter()
-        seq_kernel_ms = sum(c.solve(1, sb, sx, C4_TOL, 50000, opts).solve_ms
-                            for c, sb, sx in ctxs)
+        seq_kernel_ms = sum(c.solve(int(code), sb, sx, C4_TOL, 50000, opts).solve_ms
+                            for (c, sb, sx), code in zip(ctxs, codes))
         torch.cuda.synchronize()
         seq_wall_ms = (time.perf_counter() - t1) * 1e3
     for c, _, _ in ctxs:
         c.close()
-    out = {"workload": f"{len(systems)} p' systems of N x N quad cavities, N = round(exp "
-                       f"U[ln 32, ln 256]) seed 7 ({int(sides.min())}..{int(sides.max())}), "
-                       f"{rows} rows in all, Jacobi-PCG, reference stopping test, tol {C4_TOL:g}",
+    by_field = {}
+    for k, (_, _, name) in enumerate(C4_WHICH):
+        f = its[k::len(C4_WHICH)]
+        by_field[name] = {"solver": "PCG" if C4_WHICH[k][1] == 1 else "BiCGSTAB",
+                          "iterations": {"min": int(f.min()), "median": int(np.median(f)),
+                                         "max": int(f.max())}}
+    out = {"workload": f"{len(systems)} systems: the u, v, T (BiCGSTAB) and p' (PCG) systems of "
+                       f"the 3rd GPU SIMPLE outer iteration of {args.c4_cases} heated lid-driven "
+                       f"cavities of air, N x N quads, N = round(exp U[ln 32, ln 256]) seed 7 "
+                       f"({int(sides.min())}..{int(sides.max())}), Re ~ U[50, 400] seed 8, "
+                       f"{rows} rows in all, reference stopping tests, tol {C4_TOL:g}, x0 = 0",
            "batched_ms": round(batch_ms, 3),
+           "batched_ms_without_hints": round(nohint_ms, 3),
+           "hints": "each system's solver iterations in the 2nd outer iteration",
            "systems_per_s": round(len(systems) / (batch_ms * 1e-3), 2),
            "sequential_gpu_kernel_ms": round(seq_kernel_ms, 3),
            "sequential_gpu_wall_ms": round(seq_wall_ms, 3),
            "batched_over_sequential": round(seq_kernel_ms / batch_ms, 2),
-           "iterations": {"min": int(its.min()), "median": int(np.median(its)),
-                          "max": int(its.max())},
+           "iterations": by_field,
            "worst_rel_residual_fp64": float(f"{worst_rel:.3e}")}
     if not args.no_cpu:
         from oracle import oracle
@@ -676,21 +718,23 @@ def run_batched_c4(args):
             s = systems[k]
             x = np.zeros(s["n"])
             t1 = time.perf_counter()
-            oracle.pcg_omp_sample(s["ad"], s["au"], x, s["b"].copy(), s["ia"], s["ja"], s["n"],
-                                  s["nad"], C4_TOL, 50000, 1, threads)
+            oracle.solver(s["ad"].copy(), s["au"].copy(), s["au"].copy(), x, s["b"].copy(),
+                          s["ia"], s["ja"], s["n"], s["nad"], True, C4_TOL, 50000,
+                          int(codes[k]), 1, omp_threads=threads)
             el += time.perf_counter() - t1
-            done += s["n"] * its[k]
+            done += s["n"] * its[k] * codes[k]     # a BiCGSTAB iteration: two SpMVs
             if el > args.cpu_seconds:
                 break
-        total = float((its * np.array([s["n"] for s in systems])).sum())
+        total = float((its * codes * np.array([s["n"] for s in systems])).sum())
         cpu_s = total / (done / el)
         out["cpu_port_s"] = round(cpu_s, 3)
         if done >= total:
-            out["cpu_kind"] = (f"port: pcg_omp on {threads} host threads, every system of the "
-                               f"batch solved in turn ({el:.1f} s)")
+            out["cpu_kind"] = (f"port: the reference's OpenMP solvers on {threads} host threads, "
+                               f"every system of the batch solved in turn ({el:.1f} s)")
         else:
-            out["cpu_kind"] = (f"port: pcg_omp on {threads} host threads, whole systems of a "
-                               f"seeded sample ({el:.1f} s), extrapolated by rows x iterations")
+            out["cpu_kind"] = (f"port: the reference's OpenMP solvers on {threads} host threads, "
+                               f"whole systems of a seeded sample ({el:.1f} s), extrapolated by "
+                               f"rows x iterations x SpMVs per iteration")
         out["batched_over_cpu"] = round(cpu_s / (batch_ms * 1e-3), 1)
     return out
 

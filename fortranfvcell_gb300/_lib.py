@@ -118,6 +118,8 @@ SIGNATURES = {
     "fvc_solve_async": ([P, I32, P, P, F64, I32, C.POINTER(FvcOpts), P], I32),
     "fvc_solve": ([P, I32, P, P, F64, I32, C.POINTER(FvcOpts), C.POINTER(FvcStats)], I32),
     "fvc_solve_batched": ([P, I32, P, P, P, F64, I32, C.POINTER(FvcOpts), P], I32),
+    "fvc_solve_batched_ex": ([P, I32, P, P, P, P, P, P, F64, I32, C.POINTER(FvcOpts), P],
+                             I32),
     "fvc_spmv": ([P, P, P], I32),
     "fvc_spmv_fast": ([P, P, P], I32),
     "fvc_spmv_f32": ([P, P, P], I32),
@@ -156,6 +158,7 @@ SIGNATURES = {
                            C.POINTER(FvcSimpleOpts)], I32),
     "fvc_simple_iterate": ([P, I32, P, P], I32),
     "fvc_simple_set_graph": ([P, I32], I32),
+    "fvc_simple_system": ([P, I32, P, P, P, P], I32),
     "fvc_simple_iterate_energy": ([P, I32, P, P], I32),
     "fvc_simple_energy": ([P, P, P, F64, F64, F64], I32),
     "fvc_simple_energy_fields": ([P, P, P, P], I32),

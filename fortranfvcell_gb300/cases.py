@@ -88,3 +88,33 @@ def natural_convection_cavity(nx: int, ra: float = 1.0e6, dt_wall: float = 1.0,
              dt_wall=dt_wall)
     c["e"][0, 1] = rho
     return c
+
+
+def heated_lid_cavity(nx: int, re: float = 100.0, side: float = 0.01, dt_wall: float = 1.0,
+                      t0: float = 20.0, kind: str = "quad") -> dict:
+    """Lid-driven cavity of air for the ideal-gas loop with the energy
+    equation: the top wall moves at U = Re nu / side (momentum pedge 1,
+    sedge (U, 0)), the other walls are at rest; the left wall is held at
+    t0 + dt_wall/2 and the right one at t0 - dt_wall/2, top and bottom are
+    adiabatic; no gravity, so the temperature is carried by the flow (forced
+    convection) and acts only through the ideal-gas density.  Keys as
+    natural_convection_cavity, plus re and lid."""
+    mu, rho, k, cp, _ = AIR
+    nu, alpha, g = mu / rho, k / (rho * cp), 9.81
+    beta = 1.0 / (t0 + 273.15)
+    ra = g * beta * dt_wall * side ** 3 / (nu * alpha)   # the side's Ra, for the builder
+    c = natural_convection_cavity(nx, ra=ra, dt_wall=dt_wall, t0=t0, kind=kind)
+    lid = re * nu / side
+    nsh = c["nshared"]
+    m = c["mesh"]
+    a = c["coor"][m.ix - 1]
+    nxt = np.take_along_axis(m.ix, (np.arange(nsh)[None, :] + 1) % m.nsides[:, None], axis=1)
+    b = c["coor"][nxt - 1]
+    used = np.arange(nsh)[None, :] < m.nsides[:, None]
+    tol = 1e-9 * c["side"]
+    top = (used & (c["nelcon"] < 0) & (np.abs(a[..., 1] - c["side"]) < tol)
+           & (np.abs(b[..., 1] - c["side"]) < tol))
+    c["pedge"][:, :nsh][top] = 1
+    c["sedge"][:, :nsh, 0][top] = lid
+    c.update(gravity=np.array([0.0, 0.0]), re=re, lid=lid)
+    return c

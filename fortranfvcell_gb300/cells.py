@@ -233,6 +233,22 @@ class SimpleLoop:
     def time_step(self) -> None:
         _lib.check(self._L.fvc_simple_time_step(self._h), "fvc_simple_time_step")
 
+    def system(self, which: int):
+        """(ad, au, b) of the last outer iteration's system: which = 1 u1,
+        2 u2, 3 p', 4 the enthalpy; equation order, the structure of
+        mesh.datastruc for the system's matriz."""
+        nja = C.c_int64()
+        _lib.check(self._L.fvc_simple_system(self._h, int(which), None, None, None,
+                                             C.byref(nja)), "fvc_simple_system")
+        ad = np.zeros(self.numel)
+        au = np.zeros(max(nja.value, 1))
+        b = np.zeros(self.numel)
+        _lib.check(self._L.fvc_simple_system(self._h, int(which), ad.ctypes.data_as(C.c_void_p),
+                                             au.ctypes.data_as(C.c_void_p),
+                                             b.ctypes.data_as(C.c_void_p), C.byref(nja)),
+                   "fvc_simple_system")
+        return ad, au[:nja.value], b
+
     def use_graph(self, on: bool = True) -> None:
         """Run each outer iteration as one CUDA graph launch (same results)."""
         _lib.check(self._L.fvc_simple_set_graph(self._h, int(bool(on))), "fvc_simple_set_graph")

@@ -504,9 +504,10 @@ int32_t fvc_solve_async(fvc_context *c, int32_t code, const double *d_b, double 
   return fvc::launch_solve_status(c->S, d_status, c->stream);
 }
 
-int32_t fvc_solve_batched(fvc_context *c, int32_t nsys, const int32_t *row_start,
-                          const double *d_b, double *d_x, double tol, int32_t maxit,
-                          const fvc_opts *opts, fvc_stats *st) {
+int32_t fvc_solve_batched_ex(fvc_context *c, int32_t nsys, const int32_t *row_start,
+                             const int32_t *codes, const double *tols, const double *its_hint,
+                             const double *d_b, double *d_x, double tol, int32_t maxit,
+                             const fvc_opts *opts, fvc_stats *st) {
   if (!c || !c->has_matrix || !d_b || !d_x || maxit < 1 || nsys < 1 || !row_start)
     return FVC_ERR_ARG;
   fvc_opts o;
@@ -515,10 +516,23 @@ int32_t fvc_solve_batched(fvc_context *c, int32_t nsys, const int32_t *row_start
   else
     fvc_opts_default(&o);
   if (o.precision != FVC_PREC_FP64) return FVC_ERR_UNSUPPORTED;
+  std::vector<int32_t> inits((size_t)nsys);
+  for (int s = 0; s < nsys; ++s) {
+    const int code = codes ? codes[s] : 1;
+    if (code != 1 && code != 2) return FVC_ERR_UNSUPPORTED;
+    if (code == 2 && c->matriz == 2) return FVC_ERR_UNSUPPORTED;  // Solver.f:224-227
+    inits[s] = (o.init < 0) ? default_init(code, c->matriz) : (o.init ? 1 : 0);
+  }
   cudaSetDevice(c->device);
-  const int init = (o.init < 0) ? default_init(1, c->matriz) : (o.init ? 1 : 0);
-  return fvc::run_pcg_batched(c->A, c->S, nsys, row_start, d_b, d_x, tol, maxit, init, o,
-                              c->stream, st);
+  return fvc::run_krylov_batched(c->A, c->S, nsys, row_start, codes, tols, its_hint,
+                                 inits.data(), d_b, d_x, tol, maxit, o, c->stream, st);
+}
+
+int32_t fvc_solve_batched(fvc_context *c, int32_t nsys, const int32_t *row_start,
+                          const double *d_b, double *d_x, double tol, int32_t maxit,
+                          const fvc_opts *opts, fvc_stats *st) {
+  return fvc_solve_batched_ex(c, nsys, row_start, nullptr, nullptr, nullptr, d_b, d_x, tol,
+                              maxit, opts, st);
 }
 
 }  // extern "C"

@@ -97,10 +97,15 @@ int32_t enqueue_solve(const DeviceMatrix &A, Scratch &S, int code, const double 
 // out[0..3] = status, iterations, inner iterations, timeout flag of the
 // solve enqueued last on S
 int32_t launch_solve_status(const Scratch &S, int32_t *out, cudaStream_t stream);
-int32_t run_pcg_batched(const DeviceMatrix &A, Scratch &S, int nsys,
-                        const int32_t *row_start, const double *b, double *x,
-                        double tol, int maxit, int init, const fvc_opts &o,
-                        cudaStream_t stream, fvc_stats *st);
+// Batched PCG / BiCGSTAB of the block-diagonal matrix A (fvc_krylov.cu):
+// codes (1 PCG, 2 BiCGSTAB), tols and its_hint (expected iterations, for
+// the share of blocks) per system may be null (all PCG, all tol, sqrt of
+// the rows); inits gives each system's warm-start rule.
+int32_t run_krylov_batched(const DeviceMatrix &A, Scratch &S, int nsys,
+                           const int32_t *row_start, const int32_t *codes, const double *tols,
+                           const double *its_hint, const int32_t *inits, const double *b,
+                           double *x, double tol, int maxit, const fvc_opts &o,
+                           cudaStream_t stream, fvc_stats *st);
 int32_t run_mixed(const DeviceMatrix &A, Scratch &S, int code, const double *b,
                   double *x, double tol, int maxit, int init, const fvc_opts &o,
                   cudaStream_t stream, fvc_stats *st);

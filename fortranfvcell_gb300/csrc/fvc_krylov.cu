@@ -144,11 +144,13 @@ __device__ __forceinline__ bool epilogue(const KArgs &a, unsigned int &ep, doubl
 // gathered neighbour -- 4 of the 16 FP64 instructions of a row-iteration on
 // quadrilaterals); otherwise it is formed at every read from the previous p
 // and z, which saves the barrier.  Both give the same bits.
-template <bool kStoreP>
+// kMaxT: the most threads per block the kernel is launched with (the
+// reductions' staging buffer holds that many values per reduced quantity).
+template <bool kStoreP, int kMaxT = 1024>
 __device__ __forceinline__ void pcg_run(const KArgs &a, const Part &P, const GridSync &gs,
                                         double *result, int *iresult, bool lead) {
   __shared__ double red[kMaxNV * 32];
-  __shared__ double buf[2 * 1024];
+  __shared__ double buf[2 * kMaxT];
   // scalars of the recurrence, updated by lane 0 of warp 0 inside the
   // all-reduces and read by every thread after them
   __shared__ struct {
@@ -269,27 +271,17 @@ __global__ void __launch_bounds__(1024, 1) pcg_f64(KArgs a) {
   pcg_run<kStoreP>(a, Part(a.A.nslices, a.A.n), a.gs, a.result, a.iresult, blockIdx.x == 0);
 }
 
-// One system of a batch: its slices, its synchronisation state (counter,
-// partials, nblocks and first block) and its result slots.
+// One system of a batch: its slices, its solver (1 PCG, 2 BiCGSTAB), its
+// stopping tolerance and warm-start rule, its synchronisation state
+// (counter, partials, nblocks and first block) and its result slots.
 struct BatchSys {
   int s0, s1;
+  int code, init;
+  double tol;
   GridSync gs;
   double *result;
   int *iresult;
 };
-
-// Batched PCG: the matrix is block diagonal, each system starting at a
-// slice boundary; every block belongs to one system (sys_of_block) and
-// synchronises only with that system's blocks, so each system iterates and
-// stops on its own inside one cooperative launch.
-template <bool kStoreP>
-__global__ void __launch_bounds__(1024, 1) pcg_batched(KArgs a, const BatchSys *__restrict__ sys,
-                                                        const int *__restrict__ sys_of_block) {
-  const BatchSys d = sys[sys_of_block[blockIdx.x]];
-  const int rank = (int)(blockIdx.x - d.gs.base);
-  pcg_run<kStoreP>(a, Part(d.s0, d.s1, a.A.n, rank, (int)d.gs.nblocks), d.gs, d.result,
-                   d.iresult, rank == 0);
-}
 
 // ---------------------------------------------------------------------
 
@@ -308,14 +300,15 @@ __global__ void __launch_bounds__(1024, 1) pcg_batched(KArgs a, const BatchSys *
 //            s''.(s'/m) ; r.s'' ; s''.s''                       -> beta, stop
 // v0 = r (shadow r0), v1/v2 = s, v3/v4 = p, v5/v6 = v, v7 = t.
 // ---------------------------------------------------------------------
-__global__ void __launch_bounds__(1024, 1) bicgstab_f64(KArgs a) {
+template <int kMaxT = 1024>
+__device__ __forceinline__ void bicgstab_run(const KArgs &a, const Part &P, const GridSync &gs,
+                                             double *result, int *iresult, bool lead) {
   __shared__ double red[kMaxNV * 32];
-  __shared__ double buf[3 * 1024];
+  __shared__ double buf[3 * kMaxT];
   __shared__ struct {
     double d, conv, rr0, alpha, w, beta, crit;
     int stop;  // 0 go on, 1 converged, 2 NaN/Inf
   } sh;
-  const Part P(a.A.nslices, a.A.n);
   double *r = a.v0, *t = a.v7, *x = a.x;
   double *scur = a.v1, *snxt = a.v2, *pold = a.v3, *pnew = a.v4, *vold = a.v5, *vnew = a.v6;
   const double *minv = a.minv, *b = a.b;
@@ -339,7 +332,7 @@ __global__ void __launch_bounds__(1024, 1) bicgstab_f64(KArgs a) {
     acc[0] = fma(ri, ri * minv[row], acc[0]);
     acc[1] = fma(b[row], b[row], acc[1]);
   }
-  if (!grid_allreduce_d<2>(a.gs, ep, acc, buf, [&](const double *q) {
+  if (!grid_allreduce_d<2>(gs, ep, acc, buf, [&](const double *q) {
         sh.d = q[0];
         sh.conv = rule0 ? a.tol * sqrt(fabs(q[0])) : a.tol * sqrt(q[1]);
         sh.crit = 0.0;
@@ -375,7 +368,7 @@ __global__ void __launch_bounds__(1024, 1) bicgstab_f64(KArgs a) {
         acc[1] = fma(vi, ri, acc[1]);
       }
     }
-    if (!grid_allreduce_d<2>(a.gs, ep, acc, buf, [&](const double *q) {
+    if (!grid_allreduce_d<2>(gs, ep, acc, buf, [&](const double *q) {
           sh.rr0 = q[0];
           sh.alpha = q[0] / q[1];
         }))
@@ -394,7 +387,7 @@ __global__ void __launch_bounds__(1024, 1) bicgstab_f64(KArgs a) {
       acc[0] = fma(ti, snxt[row], acc[0]);
       acc[1] = fma(ti, ti, acc[1]);
     }
-    if (!grid_allreduce_d<2>(a.gs, ep, acc, buf,
+    if (!grid_allreduce_d<2>(gs, ep, acc, buf,
                              [&](const double *q) { sh.w = q[0] / q[1]; }))
       return;
     w = sh.w;
@@ -414,7 +407,7 @@ __global__ void __launch_bounds__(1024, 1) bicgstab_f64(KArgs a) {
       acc3[1] = fma(r[row], si, acc3[1]);
       acc3[2] = fma(si, si, acc3[2]);
     }
-    if (!grid_allreduce_d<3>(a.gs, ep, acc3, buf, [&](const double *q) {
+    if (!grid_allreduce_d<3>(gs, ep, acc3, buf, [&](const double *q) {
           const double b0 = q[0] / sh.d;
           sh.crit = rule0 ? sqrt(fabs(b0)) : sqrt(q[2]);
           sh.stop = (!(sh.crit == sh.crit) || !(sh.w == sh.w)) ? 2 : (sh.crit < sh.conv ? 1 : 0);
@@ -441,8 +434,33 @@ __global__ void __launch_bounds__(1024, 1) bicgstab_f64(KArgs a) {
     j = a.maxit;
     status = FVC_ERR_NOCONV;
   }
-  finish(a, j, status, sh.conv, sh.crit, 0);
-  epilogue(a, ep, red, false);
+  finish_to(result, iresult, lead, j, status, sh.conv, sh.crit, 0);
+  epilogue_to(a, P, gs, result, lead, ep, red, false);
+}
+
+__global__ void __launch_bounds__(1024, 1) bicgstab_f64(KArgs a) {
+  bicgstab_run(a, Part(a.A.nslices, a.A.n), a.gs, a.result, a.iresult, blockIdx.x == 0);
+}
+
+// Batched PCG / BiCGSTAB: the matrix is block diagonal, each system
+// starting at a slice boundary; every block belongs to one system
+// (sys_of_block) and synchronises only with that system's blocks, so each
+// system iterates with its own solver and stops on its own inside one
+// cooperative launch.  PCG stores p (most groups are one block, where
+// publishing p is a __syncthreads).
+template <int kMaxT>
+__global__ void __launch_bounds__(kMaxT, 1024 / kMaxT) krylov_batched(KArgs a, const BatchSys *__restrict__ sys,
+                                                        const int *__restrict__ sys_of_block) {
+  const BatchSys d = sys[sys_of_block[blockIdx.x]];
+  const int rank = (int)(blockIdx.x - d.gs.base);
+  const Part P(d.s0, d.s1, a.A.n, rank, (int)d.gs.nblocks);
+  KArgs ak = a;
+  ak.tol = d.tol;
+  ak.init = d.init;
+  if (d.code == 2)
+    bicgstab_run<kMaxT>(ak, P, d.gs, d.result, d.iresult, rank == 0);
+  else
+    pcg_run<true, kMaxT>(ak, P, d.gs, d.result, d.iresult, rank == 0);
 }
 
 // ---------------------------------------------------------------------
@@ -854,20 +872,28 @@ int32_t launch_solve_status(const Scratch &S, int32_t *out, cudaStream_t stream)
   return cudaPeekAtLastError() == cudaSuccess ? FVC_OK : FVC_ERR_CUDA;
 }
 
-int32_t run_pcg_batched(const DeviceMatrix &A, Scratch &S, int nsys, const int32_t *row_start,
-                        const double *b, double *x, double tol, int maxit, int init,
-                        const fvc_opts &o, cudaStream_t stream, fvc_stats *st) {
-  if (nsys < 1 || !row_start || row_start[0] != 0 || row_start[nsys] != A.n) return FVC_ERR_ARG;
-  for (int s = 0; s < nsys; ++s)
+int32_t run_krylov_batched(const DeviceMatrix &A, Scratch &S, int nsys,
+                           const int32_t *row_start, const int32_t *codes, const double *tols,
+                           const double *its_hint, const int32_t *inits, const double *b,
+                           double *x, double tol, int maxit, const fvc_opts &o,
+                           cudaStream_t stream, fvc_stats *st) {
+  if (nsys < 1 || !row_start || !inits || row_start[0] != 0 || row_start[nsys] != A.n)
+    return FVC_ERR_ARG;
+  bool any_bicg = false;
+  for (int s = 0; s < nsys; ++s) {
     if (row_start[s] % 32 != 0 || row_start[s + 1] <= row_start[s]) return FVC_ERR_ARG;
+    const int code = codes ? codes[s] : 1;
+    if (code != 1 && code != 2) return FVC_ERR_UNSUPPORTED;
+    any_bicg = any_bicg || code == 2;
+  }
   // 128-thread blocks by default: twice the co-resident blocks of 256, so the
   // one-block minimum of the small systems takes a smaller share (C4 batch of
   // 256 cavities: 184 ms at 128 threads, 215 at 256, 386 at 512)
   const int threads = (o.block_threads > 0) ? block_threads_for(o.block_threads, 0, 1) : 128;
   int occ = 0;
-  // p stored: most groups of a batch are one block, where publishing p is a
-  // __syncthreads (C4 batch of 256 cavities: 159 ms vs 184 ms)
-  auto kern = pcg_batched<true>;
+  // PCG stores p: most groups of a batch are one block, where publishing p
+  // is a __syncthreads (C4 batch of 256 cavities: 159 ms vs 184 ms)
+  auto kern = threads <= 128 ? krylov_batched<128> : krylov_batched<1024>;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, threads, 0);
   if (occ <= 0) occ = 1;
   if (o.blocks_per_sm > 0 && o.blocks_per_sm < occ) occ = o.blocks_per_sm;
@@ -878,9 +904,10 @@ int32_t run_pcg_batched(const DeviceMatrix &A, Scratch &S, int nsys, const int32
             cap);
     return FVC_ERR_ARG;
   }
-  // blocks per system in proportion to slices x sqrt(rows) (work per
-  // iteration x the growth of the iteration count with the mesh size),
-  // at most one slice per warp.  Water-filling: a system whose share is
+  // blocks per system in proportion to its work: slices x the expected
+  // iterations (the caller's hint, else sqrt(rows), the growth of the
+  // iteration count with the mesh size) x the SpMVs per iteration (2 for
+  // BiCGSTAB); at most one slice per warp.  Water-filling: a system whose share is
   // below one block gets one, the others share the rest, and blocks left
   // over by rounding go to the largest remainders.
   const int warps = threads / 32;
@@ -892,7 +919,8 @@ int32_t run_pcg_batched(const DeviceMatrix &A, Scratch &S, int nsys, const int32
     const int rows = row_start[s + 1] - row_start[s];
     slices[s] = (rows + 31) / 32;
     most[s] = (slices[s] + warps - 1) / warps;
-    wt[s] = slices[s] * std::sqrt((double)rows);
+    const double its = (its_hint && its_hint[s] > 0.0) ? its_hint[s] : std::sqrt((double)rows);
+    wt[s] = slices[s] * its * ((codes && codes[s] == 2) ? 2.0 : 1.0);
     wleft += wt[s];
   }
   long capleft = cap;
@@ -964,6 +992,9 @@ int32_t run_pcg_batched(const DeviceMatrix &A, Scratch &S, int nsys, const int32
     BatchSys &d = hsys[s];
     d.s0 = row_start[s] / 32;
     d.s1 = d.s0 + slices[s];
+    d.code = codes ? codes[s] : 1;
+    d.init = inits[s];
+    d.tol = tols ? tols[s] : tol;
     d.gs.count = ctr + (size_t)s * 16;
     d.gs.flag = ctr + (size_t)s * 16 + 8;
     d.gs.err = err;
@@ -977,7 +1008,7 @@ int32_t run_pcg_batched(const DeviceMatrix &A, Scratch &S, int nsys, const int32
     for (int k = 0; k < nb[s]; ++k) hsob[(size_t)b0 + k] = s;
     b0 += nb[s];
   }
-  int32_t rc = ensure_vectors(S, (size_t)A.n, 5, 1, false);
+  int32_t rc = ensure_vectors(S, (size_t)A.n, any_bicg ? 8 : 5, 1, false);
   if (rc != FVC_OK) {
     cudaFreeAsync(buf, stream);
     return rc;
@@ -997,9 +1028,12 @@ int32_t run_pcg_batched(const DeviceMatrix &A, Scratch &S, int nsys, const int32
   a.v2 = S.v[2];
   a.v3 = S.v[3];
   a.v4 = S.v[4];
+  a.v5 = S.v[5];
+  a.v6 = S.v[6];
+  a.v7 = S.v[7];
   a.tol = tol;
   a.maxit = maxit;
-  a.init = init;
+  a.init = 1;
   a.stop_rule = o.stop_rule;
   const BatchSys *psys = dsys;
   const int *psob = dsob;

@@ -966,6 +966,28 @@ int32_t fvc_simple_set_fields(fvc_simple *s, const double *w, const double *p) {
   return cudaStreamSynchronize(s->stream) == cudaSuccess ? FVC_OK : FVC_ERR_CUDA;
 }
 
+int32_t fvc_simple_system(const fvc_simple *s, int32_t which, double *ad, double *au, double *b,
+                          int64_t *nja) {
+  if (!s || which < 1 || which > 4 || (which == 4 && !s->gas)) return FVC_ERR_ARG;
+  cudaSetDevice(s->device);
+  const double *dad = which == 1 ? s->ad1 : which == 2 ? s->ad2 : which == 3 ? s->adp : s->ade;
+  const double *dau = which == 1 ? s->au1 : which == 2 ? s->au2 : which == 3 ? s->aup : s->aue;
+  const double *db = which == 1 ? s->b1 : which == 2 ? s->b2 : which == 3 ? s->bp : s->be;
+  const size_t na = which <= 2 ? s->nja_u : which == 3 ? s->nja_pc : s->nja_e;
+  const size_t n = (size_t)s->numel;
+  if (nja) *nja = (int64_t)na;
+  if (ad && cudaMemcpyAsync(ad, dad, sizeof(double) * n, cudaMemcpyDeviceToHost, s->stream) !=
+                cudaSuccess)
+    return FVC_ERR_CUDA;
+  if (au && cudaMemcpyAsync(au, dau, sizeof(double) * na, cudaMemcpyDeviceToHost, s->stream) !=
+                cudaSuccess)
+    return FVC_ERR_CUDA;
+  if (b && cudaMemcpyAsync(b, db, sizeof(double) * n, cudaMemcpyDeviceToHost, s->stream) !=
+               cudaSuccess)
+    return FVC_ERR_CUDA;
+  return cudaStreamSynchronize(s->stream) == cudaSuccess ? FVC_OK : FVC_ERR_CUDA;
+}
+
 int32_t fvc_simple_get_state(const fvc_simple *s, double *w, double *w0, double *p, double *en,
                              double *en0, double *ro) {
   if (!s || (!s->gas && (en || en0 || ro))) return FVC_ERR_ARG;

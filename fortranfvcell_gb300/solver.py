@@ -168,21 +168,31 @@ class Context:
                    "fvc_solve_async")
 
     def solve_batched(self, row_start, b_dev, x_dev, tol: float, maxit: int,
-                      opts: FvcOpts | None = None, raise_on_error: bool = True):
-        """Batched PCG of the block-diagonal matrix on this context (see
+                      opts: FvcOpts | None = None, raise_on_error: bool = True,
+                      codes=None, tols=None, its_hint=None):
+        """Batched solves of the block-diagonal matrix on this context (see
         pack_block_diagonal): one persistent launch, each system on its own
-        blocks with its own stopping test.  Returns (status, [FvcStats] per
-        system)."""
+        blocks with its own stopping test.  codes: per system 1 (PCG, the
+        default) or 2 (BiCGSTAB); tols: per-system tolerances (default tol);
+        its_hint: expected iterations per system, for the share of blocks.
+        Returns (status, [FvcStats] per system)."""
         rs = np.ascontiguousarray(row_start, np.int32)
         nsys = rs.size - 1
         st = (FvcStats * nsys)()
         o = opts if opts is not None else make_opts()
-        rc = self._L.fvc_solve_batched(self._h, nsys, rs.ctypes.data_as(C.c_void_p),
-                                       C.c_void_p(_addr(b_dev)), C.c_void_p(_addr(x_dev)),
-                                       float(tol), int(maxit), C.byref(o),
-                                       C.cast(st, C.c_void_p))
+        cd = None if codes is None else np.ascontiguousarray(codes, np.int32)
+        td = None if tols is None else np.ascontiguousarray(tols, np.float64)
+        hd = None if its_hint is None else np.ascontiguousarray(its_hint, np.float64)
+        for arr in (cd, td, hd):
+            if arr is not None and arr.size != nsys:
+                raise ValueError("codes, tols and its_hint need one entry per system")
+        ptr = lambda arr: None if arr is None else arr.ctypes.data_as(C.c_void_p)
+        rc = self._L.fvc_solve_batched_ex(
+            self._h, nsys, rs.ctypes.data_as(C.c_void_p), ptr(cd), ptr(td), ptr(hd),
+            C.c_void_p(_addr(b_dev)), C.c_void_p(_addr(x_dev)), float(tol), int(maxit),
+            C.byref(o), C.cast(st, C.c_void_p))
         if raise_on_error and rc != _lib.FVC_OK:
-            raise FvcError(rc, f"batched PCG ended with status {_lib.STATUS_NAMES.get(rc, rc)}")
+            raise FvcError(rc, f"batched solve ended with status {_lib.STATUS_NAMES.get(rc, rc)}")
         return rc, list(st)
 
     def trace(self, max_records: int = 256):

@@ -186,6 +186,24 @@ int32_t fvc_solve_batched(fvc_context *ctx, int32_t nsys, const int32_t *row_sta
                           const double *d_b, double *d_x, double tol,
                           int32_t maxit, const fvc_opts *opts, fvc_stats *st);
 
+/* fvc_solve_batched with a solver and a tolerance per system, so that the
+ * u, v, T and p' systems of a SIMPLE outer iteration (of one case or of many)
+ * go into one launch: codes[s] = 1 (Jacobi-PCG, src/Iterativos.f:29-106) or
+ * 2 (Jacobi-BiCGSTAB, src/Iterativos.f:140-234); tols[s] the system's
+ * stopping tolerance; its_hint[s] the iterations the system is expected to
+ * take (in a SIMPLE loop, its count in the previous outer iteration), which
+ * sets its share of the launch's blocks: work = slices x iterations x SpMVs
+ * per iteration.  Host arrays of nsys entries; NULL codes = all PCG, NULL
+ * tols = tol for all, NULL its_hint (or an entry <= 0) = sqrt(rows).  The
+ * hint moves only the speed, never the results beyond rounding.  Each
+ * system takes the warm-start rule of its solver (src/Solver.f) unless opts
+ * sets init.  FVC_ERR_UNSUPPORTED for BiCGSTAB on matriz 2, as fvc_solve. */
+int32_t fvc_solve_batched_ex(fvc_context *ctx, int32_t nsys, const int32_t *row_start,
+                             const int32_t *codes, const double *tols,
+                             const double *its_hint, const double *d_b, double *d_x,
+                             double tol, int32_t maxit, const fvc_opts *opts,
+                             fvc_stats *st);
+
 /* y = A x with DEVICE vectors, the reference's summation order, FP64
  * (bit-identical to src/Matvec.f for the loaded format).  Asynchronous on
  * the context's stream. */
@@ -562,6 +580,18 @@ int32_t fvc_simple_energy_fields(const fvc_simple *s, double *temp, double *en,
  * simple macro after the reference's load does: the time terms from w, w0
  * (and en, en0, ro), then w0 = w (and en0 = en); the temperature follows
  * from en. */
+/* The system the last outer iteration solved (or would have solved) for
+ * which = 1 u1, 2 u2, 3 p', 4 the enthalpy (a loop switched by
+ * fvc_simple_energy): HOST copies, in equation order, of the diagonal ad
+ * (numel), the off-diagonal values au (*nja entries) and the right-hand
+ * side b (numel, the time term included), as the reference passes them to
+ * `solver` (src/Simple.f:488-489,499-500,590-591,693-694).  The structure is
+ * fvc_mesh_datastruc's for the system's matriz (matriz_u, matriz_pc, 1 for
+ * the enthalpy).  Any pointer may be NULL; call with au NULL first to learn
+ * *nja. */
+int32_t fvc_simple_system(const fvc_simple *s, int32_t which, double *ad,
+                          double *au, double *b, int64_t *nja);
+
 int32_t fvc_simple_get_state(const fvc_simple *s, double *w, double *w0,
                              double *p, double *en, double *en0, double *ro);
 int32_t fvc_simple_set_state(fvc_simple *s, const double *w, const double *w0,

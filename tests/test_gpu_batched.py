@@ -1,11 +1,13 @@
-"""Batched PCG (fvc_solve_batched): many independent pressure-correction
-systems of different sizes and cell shapes in one persistent launch, each
-checked against the restated reference PCG (src/Iterativos.f:29-106) run
-on that system alone."""
+"""Batched solves (fvc_solve_batched, fvc_solve_batched_ex): many
+independent systems of different sizes and cell shapes in one persistent
+launch -- pressure-correction systems by PCG, and convection-like
+unsymmetric systems by BiCGSTAB beside them -- each checked against the
+restated reference solver (src/Iterativos.f:29-106, 140-234) run on that
+system alone."""
 import numpy as np
 import pytest
 
-from _systems import pressure
+from _systems import pressure, unsymmetric
 
 pytestmark = pytest.mark.gpu
 
@@ -26,7 +28,7 @@ def batch(orc):
     return systems
 
 
-def solve_batch(systems, tol, maxit, raise_on_error=True):
+def solve_batch(systems, tol, maxit, raise_on_error=True, codes=None, tols=None, its_hint=None):
     import torch
     from fortranfvcell_gb300 import Context, make_opts, pack_block_diagonal
     pk = pack_block_diagonal(systems)
@@ -39,7 +41,8 @@ def solve_batch(systems, tol, maxit, raise_on_error=True):
     bd = torch.from_numpy(b).cuda()
     xd = torch.zeros(pk["neq"], dtype=torch.float64, device="cuda")
     rc, st = ctx.solve_batched(pk["row_start"], bd, xd, tol, maxit, make_opts("fp64", init=1),
-                               raise_on_error=raise_on_error)
+                               raise_on_error=raise_on_error, codes=codes, tols=tols,
+                               its_hint=its_hint)
     x = xd.cpu().numpy()
     ctx.close()
     return rc, st, [x[r] for r in pk["rows"]]
@@ -90,3 +93,51 @@ def test_batched_rejects_unaligned_layout(orc):
     with pytest.raises(FvcError):
         ctx.solve_batched(bad, bd, xd, 1e-8, 100)
     ctx.close()
+
+
+def test_batched_mixed_solvers_match_reference_per_system(orc):
+    # the u, v, T and p' pattern of a SIMPLE iteration: unsymmetric systems
+    # by BiCGSTAB beside p' systems by PCG, with a tolerance per system
+    systems = batch(orc)
+    codes, tols = [], []
+    for k, s in enumerate(systems):
+        if k % 2:
+            u = unsymmetric(s, seed=k)
+            s.update(ad=u["ad"], au=u["au"])
+            codes.append(2)
+            tols.append(1e-11)
+        else:
+            codes.append(1)
+            tols.append(1e-10)
+    rc, st, xs = solve_batch(systems, 0.0, 20000, codes=codes, tols=tols)
+    assert rc == 0
+    for s, t, x, code, tol in zip(systems, st, xs, codes, tols):
+        x_ref = np.zeros(s["n"])
+        status, so = orc.solver(s["ad"].copy(), s["au"].copy(), s["au"].copy(), x_ref,
+                                s["b"].copy(), s["ia"], s["ja"], s["n"], s["nad"], True, tol,
+                                20000, code, 1)
+        assert status == 0 and t.status == 0
+        err = np.linalg.norm(x - x_ref) / np.linalg.norm(x_ref)
+        assert err <= (REL_TOL if code == 1 else 1e-9), (code, s["n"], err)
+        # BiCGSTAB's exit iteration moves with the summation order (15%)
+        bar = ITS_TOL if code == 1 else max(2, int(0.15 * so.iterations))
+        assert abs(t.iterations - so.iterations) <= bar, (code, s["n"], t.iterations,
+                                                          so.iterations)
+
+
+def test_batched_iteration_hints_move_only_the_speed(orc):
+    # hints change each system's share of blocks, so only the reductions'
+    # summation order: the same solutions to rounding, counts within 2
+    systems = batch(orc)
+    codes = [2 if k % 3 == 0 else 1 for k in range(len(systems))]
+    for k, s in enumerate(systems):
+        if codes[k] == 2:
+            u = unsymmetric(s, seed=k)
+            s.update(ad=u["ad"], au=u["au"])
+    _, st0, x0 = solve_batch(systems, 1e-10, 20000, codes=codes)
+    hints = [5.0 if k % 2 else 500.0 for k in range(len(systems))]
+    _, st1, x1 = solve_batch(systems, 1e-10, 20000, codes=codes, its_hint=hints)
+    for a, b, t0, t1 in zip(x0, x1, st0, st1):
+        assert t0.status == 0 and t1.status == 0
+        assert np.linalg.norm(a - b) <= 1e-9 * max(np.linalg.norm(a), 1e-300)
+        assert abs(t0.iterations - t1.iterations) <= 2
