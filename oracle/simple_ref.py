@@ -69,7 +69,10 @@ class SimpleRef:
         sx = np.zeros(n)
         orc.lib().oref_getres(orc._p(np.ascontiguousarray(x_cells)), orc._p(sx),
                               orc._p(m["num"]), n, n, 1)
-        st = orc.solver(ad, au, au, sx, b, ia, ja, n, nad, True, tol, self.maxit, code, matriz)
+        # the solver overwrites b (as p or s, src/Iterativos.f); the system
+        # stays as assembled for whoever inspects it afterwards
+        st = orc.solver(ad, au, au, sx, b.copy(), ia, ja, n, nad, True, tol, self.maxit, code,
+                        matriz)
         out = np.zeros(n)
         orc.lib().oref_getres(orc._p(out), orc._p(sx), orc._p(m["num"]), n, n, 0)
         return out, st

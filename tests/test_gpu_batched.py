@@ -128,8 +128,10 @@ def test_batched_mixed_solvers_match_reference_per_system(orc):
 def test_batched_iteration_hints_move_only_the_speed(orc):
     # hints change each system's share of blocks, so only the reductions'
     # summation order: the same solutions to rounding, counts within 2
+    # (BiCGSTAB not on the one-cell system 0: its first half-step zeroes the
+    # residual and the reference's omega = 0/0 breaks down)
     systems = batch(orc)
-    codes = [2 if k % 3 == 0 else 1 for k in range(len(systems))]
+    codes = [2 if k % 3 == 1 else 1 for k in range(len(systems))]
     for k, s in enumerate(systems):
         if codes[k] == 2:
             u = unsymmetric(s, seed=k)

@@ -167,3 +167,23 @@ def test_restart_from_saved_state(orc, tmp_path):
     rf, _ = f.iterate_energy(6)
     f.close()
     np.testing.assert_allclose(rf, rb, rtol=1e-6)
+
+
+def test_loop_exports_the_systems_it_solves(orc):
+    # fvc_simple_system: the u1, u2 and p' systems of the last outer
+    # iteration against those the restated iteration assembled; iteration 1
+    # starts from the same state, so they agree to the assembly's rounding
+    case = cavity(orc, 12)
+    ref = SimpleRef(orc, case, tol_pcg=1e-13, tol_bcg=1e-13, matriz_u=1)
+    loop = gpu_loop(case, tol_u=1e-13, tol_pc=1e-13, matriz_u=1)
+    ref.step()
+    loop.iterate(1)
+    for which, key in ((1, "u1"), (2, "u2"), (3, "pc")):
+        ad, au, b = loop.system(which)
+        rad, rau, rb = ref.systems[key]
+        np.testing.assert_allclose(ad, rad, rtol=1e-13, atol=0)
+        np.testing.assert_allclose(au, rau[:au.size], rtol=1e-13, atol=1e-300)
+        np.testing.assert_allclose(b, rb, rtol=1e-13, atol=1e-13 * np.abs(rb).max())
+    with pytest.raises(Exception):
+        loop.system(4)                     # no energy equation in this loop
+    loop.close()
