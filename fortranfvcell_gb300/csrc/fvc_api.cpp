@@ -515,7 +515,7 @@ int32_t fvc_solve_batched_ex(fvc_context *c, int32_t nsys, const int32_t *row_st
     o = *opts;
   else
     fvc_opts_default(&o);
-  if (o.precision != FVC_PREC_FP64) return FVC_ERR_UNSUPPORTED;
+  if (o.precision != FVC_PREC_FP64 && o.precision != FVC_PREC_MIXED) return FVC_ERR_UNSUPPORTED;
   std::vector<int32_t> inits((size_t)nsys);
   for (int s = 0; s < nsys; ++s) {
     const int code = codes ? codes[s] : 1;

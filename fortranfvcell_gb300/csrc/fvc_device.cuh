@@ -387,6 +387,19 @@ __device__ __forceinline__ double sell_row_fma(const SellView<double> &A, int s,
   return t;
 }
 
+// One system of a batch: its slices, its solver (1 PCG, 2 BiCGSTAB), its
+// stopping tolerance, inner tolerance (mixed precision) and warm-start
+// rule, its synchronisation state (counter, partials, nblocks and first
+// block) and its result slots.
+struct BatchSys {
+  int s0, s1;
+  int code, init;
+  double tol, inner_tol;
+  GridSync gs;
+  double *result;
+  int *iresult;
+};
+
 // Host side: scratch for the grid synchronisation of a persistent launch.
 inline int32_t ensure_sync(Scratch &S, size_t nblocks) {
   const size_t need = 4 * kMaxNV * nblocks + 4 * kMaxNV;

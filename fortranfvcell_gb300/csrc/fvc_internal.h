@@ -58,6 +58,13 @@ struct Scratch {
 };
 
 constexpr int kTraceMax = 256;
+// Mixed precision: the FP32 iterations reduce the residual by this factor
+// between two FP64 recomputations (CG: a reliable update; BiCGSTAB: a
+// defect-correction sweep).  For BiCGSTAB, 0.1 rather than a deep inner
+// solve: a restarted FP32 BiCGSTAB stalls near FP32's limit on the
+// enthalpy systems (C4 enthalpy batch, 256 systems: 198 ms at 0.1, 291 ms
+// at 1e-2, 693 ms at 1e-4; FP64 251 ms).
+constexpr double kInnerTolDefault = 0.1;
 constexpr int kHistoryMax = 16384;
 
 struct Launch {
@@ -101,7 +108,7 @@ int32_t launch_solve_status(const Scratch &S, int32_t *out, cudaStream_t stream)
 // codes (1 PCG, 2 BiCGSTAB), tols and its_hint (expected iterations, for
 // the share of blocks) per system may be null (all PCG, all tol, sqrt of
 // the rows); inits gives each system's warm-start rule.
-int32_t run_krylov_batched(const DeviceMatrix &A, Scratch &S, int nsys,
+int32_t run_krylov_batched(DeviceMatrix &A, Scratch &S, int nsys,
                            const int32_t *row_start, const int32_t *codes, const double *tols,
                            const double *its_hint, const int32_t *inits, const double *b,
                            double *x, double tol, int maxit, const fvc_opts &o,
@@ -115,6 +122,15 @@ int32_t launch_reciprocal(const DeviceMatrix &A, cudaStream_t stream);
 int32_t launch_spmv_f32(const DeviceMatrix &A, const float *x, float *y,
                         cudaStream_t stream);
 int32_t build_f32_copy(DeviceMatrix &A, cudaStream_t stream);
+int32_t ensure_f32_vectors(Scratch &S, size_t n);
+// batched mixed-precision solves (fvc_mixed.cu): the kernel for the block
+// size (for occupancy queries) and its cooperative launch over the batch
+// descriptors (device BatchSys array) and the block-to-system map
+struct BatchSys;
+const void *mixed_batched_kernel(int threads);
+int32_t launch_mixed_batched(const DeviceMatrix &A, const Scratch &S, const BatchSys *dsys,
+                             const int *dsob, int blocks, int threads, const double *b, double *x,
+                             int maxit, const fvc_opts &o, cudaStream_t stream);
 
 // Threads per block of a persistent solver launch when the caller sets
 // none (or a multiple of 128 it asked for, clamped to 128..1024).  The

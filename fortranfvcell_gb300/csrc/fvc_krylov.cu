@@ -271,17 +271,6 @@ __global__ void __launch_bounds__(1024, 1) pcg_f64(KArgs a) {
   pcg_run<kStoreP>(a, Part(a.A.nslices, a.A.n), a.gs, a.result, a.iresult, blockIdx.x == 0);
 }
 
-// One system of a batch: its slices, its solver (1 PCG, 2 BiCGSTAB), its
-// stopping tolerance and warm-start rule, its synchronisation state
-// (counter, partials, nblocks and first block) and its result slots.
-struct BatchSys {
-  int s0, s1;
-  int code, init;
-  double tol;
-  GridSync gs;
-  double *result;
-  int *iresult;
-};
 
 // ---------------------------------------------------------------------
 
@@ -872,7 +861,7 @@ int32_t launch_solve_status(const Scratch &S, int32_t *out, cudaStream_t stream)
   return cudaPeekAtLastError() == cudaSuccess ? FVC_OK : FVC_ERR_CUDA;
 }
 
-int32_t run_krylov_batched(const DeviceMatrix &A, Scratch &S, int nsys,
+int32_t run_krylov_batched(DeviceMatrix &A, Scratch &S, int nsys,
                            const int32_t *row_start, const int32_t *codes, const double *tols,
                            const double *its_hint, const int32_t *inits, const double *b,
                            double *x, double tol, int maxit, const fvc_opts &o,
@@ -890,10 +879,18 @@ int32_t run_krylov_batched(const DeviceMatrix &A, Scratch &S, int nsys,
   // one-block minimum of the small systems takes a smaller share (C4 batch of
   // 256 cavities: 184 ms at 128 threads, 215 at 256, 386 at 512)
   const int threads = (o.block_threads > 0) ? block_threads_for(o.block_threads, 0, 1) : 128;
+  const bool mixed = o.precision == FVC_PREC_MIXED;
+  if (mixed) {
+    int32_t rc = build_f32_copy(A, stream);
+    if (rc == FVC_OK) rc = ensure_f32_vectors(S, (size_t)A.n);
+    if (rc != FVC_OK) return rc;
+  }
   int occ = 0;
   // PCG stores p: most groups of a batch are one block, where publishing p
   // is a __syncthreads (C4 batch of 256 cavities: 159 ms vs 184 ms)
-  auto kern = threads <= 128 ? krylov_batched<128> : krylov_batched<1024>;
+  const void *kern = mixed ? mixed_batched_kernel(threads)
+                           : (threads <= 128 ? (const void *)krylov_batched<128>
+                                             : (const void *)krylov_batched<1024>);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, threads, 0);
   if (occ <= 0) occ = 1;
   if (o.blocks_per_sm > 0 && o.blocks_per_sm < occ) occ = o.blocks_per_sm;
@@ -995,6 +992,9 @@ int32_t run_krylov_batched(const DeviceMatrix &A, Scratch &S, int nsys,
     d.code = codes ? codes[s] : 1;
     d.init = inits[s];
     d.tol = tols ? tols[s] : tol;
+    // mixed precision: FP32 reduction per reliable update (CG) or per
+    // defect-correction sweep (BiCGSTAB), as in a single solve
+    d.inner_tol = (o.inner_tol > 0) ? o.inner_tol : kInnerTolDefault;
     d.gs.count = ctr + (size_t)s * 16;
     d.gs.flag = ctr + (size_t)s * 16 + 8;
     d.gs.err = err;
@@ -1008,7 +1008,7 @@ int32_t run_krylov_batched(const DeviceMatrix &A, Scratch &S, int nsys,
     for (int k = 0; k < nb[s]; ++k) hsob[(size_t)b0 + k] = s;
     b0 += nb[s];
   }
-  int32_t rc = ensure_vectors(S, (size_t)A.n, any_bicg ? 8 : 5, 1, false);
+  int32_t rc = mixed ? FVC_OK : ensure_vectors(S, (size_t)A.n, any_bicg ? 8 : 5, 1, false);
   if (rc != FVC_OK) {
     cudaFreeAsync(buf, stream);
     return rc;
@@ -1042,9 +1042,15 @@ int32_t run_krylov_batched(const DeviceMatrix &A, Scratch &S, int nsys,
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   cudaEventRecord(e0, stream);
-  cudaError_t ce = cudaLaunchCooperativeKernel((const void *)kern, dim3((unsigned)total),
-                                               dim3(threads), args, 0, stream);
-  count_launch();
+  cudaError_t ce = cudaSuccess;
+  if (mixed) {
+    if (launch_mixed_batched(A, S, psys, psob, (int)total, threads, b, x, maxit, o, stream) !=
+        FVC_OK)
+      ce = cudaErrorLaunchFailure;
+  } else {
+    ce = cudaLaunchCooperativeKernel(kern, dim3((unsigned)total), dim3(threads), args, 0, stream);
+    count_launch();
+  }
   cudaEventRecord(e1, stream);
   std::vector<double> hres((size_t)nsys * 16);
   std::vector<int> hires((size_t)nsys * 16);
@@ -1053,7 +1059,7 @@ int32_t run_krylov_batched(const DeviceMatrix &A, Scratch &S, int nsys,
     cudaMemcpyAsync(hres.data(), res, res_bytes, cudaMemcpyDeviceToHost, stream);
     cudaMemcpyAsync(hires.data(), ires, ires_bytes, cudaMemcpyDeviceToHost, stream);
     cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, stream);
-  } else {
+  } else if (!mixed) {  // (the mixed launcher reports its own failure)
     fprintf(stderr, "fvcgpu: batched launch failed: %s\n", cudaGetErrorString(ce));
   }
   cudaFreeAsync(buf, stream);
@@ -1074,8 +1080,11 @@ int32_t run_krylov_batched(const DeviceMatrix &A, Scratch &S, int nsys,
       fvc_stats &t = st[s];
       memset(&t, 0, sizeof(t));
       t.status = ir[1];
-      t.iterations = ir[0];
-      t.energy = r[0];
+      // mixed: inner FP32 iterations, and reliable updates / sweeps
+      t.iterations = mixed ? ir[2] : ir[0];
+      t.inner_iterations = mixed ? ir[2] : 0;
+      t.refinements = mixed ? ir[0] : 0;
+      t.energy = mixed ? 0.0 : r[0];
       t.conv = r[1];
       t.final_crit = r[2];
       t.rel_residual = (r[4] > 0) ? std::sqrt(r[3] / r[4]) : std::sqrt(r[3]);

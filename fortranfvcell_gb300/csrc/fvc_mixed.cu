@@ -30,7 +30,7 @@
 // BiCGSTAB (code 2): the reference's Jacobi BiCGSTAB (src/Iterativos.f:
 // 140-234) in FP32 on the correction equation, restarted from the FP64
 // residual (defect correction) after each inner reduction by inner_tol
-// (default 1e-4).
+// (default 0.1).
 // Both stop on ||b - A x||2 <= refine_tol * ||b||2 recomputed in FP64.  Dot
 // products and norms: each thread sums its rows with compensated FP32
 // (TwoSum), the per-thread pairs are combined in FP64.  GB300 executes FP64
@@ -279,9 +279,17 @@ struct MArgs {
   int init;
   double *result;
   int *iresult;
-  double *trace;        // (iteration, relres) per residual replacement
-  float *history;       // recursive relres per iteration
+  double *trace;        // (iteration, relres) per residual replacement (may be null)
+  float *history;       // recursive relres per iteration (may be null)
+  // one system of a batch: its slices [grp_s0, grp_s1) over grp_nb blocks
+  // from block grp_base (grp_nb = 0: the whole matrix over the grid)
+  int grp_s0 = 0, grp_s1 = 0, grp_nb = 0, grp_base = 0;
 };
+
+// the block that writes the system's results
+__device__ __forceinline__ bool mlead(const MArgs &a) {
+  return blockIdx.x == (a.grp_nb > 0 ? (unsigned)a.grp_base : 0u);
+}
 
 // (A y)_row in FP32 difference form, y supplied by a functor.
 template <typename YF>
@@ -320,14 +328,20 @@ __device__ __forceinline__ float arow32(const MArgs &a, int s, int lane, int row
 
 struct MPart {
   int lane, warp, nwarps, sb, se, n;
-  __device__ MPart(int nslices, int nrows) {
+  // this block's slices: of the whole matrix over the grid, or of the
+  // batch system a belongs to over that system's blocks
+  __device__ explicit MPart(const MArgs &a) {
     lane = threadIdx.x & 31;
     warp = threadIdx.x >> 5;
     nwarps = blockDim.x >> 5;
-    const int spb = (nslices + gridDim.x - 1) / gridDim.x;
-    sb = blockIdx.x * spb;
-    se = min(nslices, sb + spb);
-    n = nrows;
+    const int s0 = a.grp_nb > 0 ? a.grp_s0 : 0;
+    const int s1 = a.grp_nb > 0 ? a.grp_s1 : a.A.nslices;
+    const int nb = a.grp_nb > 0 ? a.grp_nb : (int)gridDim.x;
+    const int rank = (int)blockIdx.x - (a.grp_nb > 0 ? a.grp_base : 0);
+    const int spb = (s1 - s0 + nb - 1) / nb;
+    sb = s0 + rank * spb;
+    se = min(s1, sb + spb);
+    n = a.A.n;
   }
 };
 
@@ -340,7 +354,7 @@ struct MPart {
 // (FP64 sums).
 __device__ __forceinline__ bool residual_sweep(const MArgs &a, unsigned int &ep, bool zero_x,
                                                double (&out)[4], double *red) {
-  const MPart P(a.A.nslices, a.A.n);
+  const MPart P(a);
   double acc[4] = {0.0, 0.0, 0.0, 0.0};
   const double *x = a.x;
   MFOR_ROWS(P) {
@@ -374,7 +388,7 @@ __device__ __forceinline__ bool residual_sweep(const MArgs &a, unsigned int &ep,
 __device__ __forceinline__ void fold_correction(const MArgs &a, const float *ppend = nullptr,
                                                 const float *ppend_lo = nullptr,
                                                 double apend = 0.0) {
-  const MPart P(a.A.nslices, a.A.n);
+  const MPart P(a);
   MFOR_ROWS(P) {
     const float2 ev = a.e[row];
     double dx = (double)ev.x + (double)ev.y;
@@ -913,7 +927,7 @@ template <bool kStaged, int kW>
 __device__ __forceinline__ void mixed_cg_body(const MArgs &a) {
   __shared__ double red[kMaxNV * 32];
   extern __shared__ __align__(128) unsigned char st_smem[];
-  const MPart P(a.A.nslices, a.A.n);
+  const MPart P(a);
   StCount gch;  // staged copies issued so far, per ring
   if (kStaged) {
     if (threadIdx.x == 0) {
@@ -1010,7 +1024,8 @@ __device__ __forceinline__ void mixed_cg_body(const MArgs &a) {
           if (!was_pending) sh.pend_alpha = sh.alpha;
           const double rz_new = t[0];
           sh.rz_new = rz_new;
-          if (blockIdx.x == 0 && it <= kHistoryMax) a.history[it - 1] = (float)sqrt(t[1] / sh.scale);
+          if (mlead(a) && a.history && it <= kHistoryMax)
+            a.history[it - 1] = (float)sqrt(t[1] / sh.scale);
           if (!(rz_new == rz_new)) {
             sh.status = FVC_ERR_NAN;
             sh.action = kStop;
@@ -1038,7 +1053,7 @@ __device__ __forceinline__ void mixed_cg_body(const MArgs &a) {
         const double relres = sqrt(res[0] / sh.scale);
         sh.res0 = res[0];
         sh.relres = relres;
-        if (blockIdx.x == 0 && u <= kTraceMax) {
+        if (mlead(a) && a.trace && u <= kTraceMax) {
           a.trace[2 * (u - 1)] = (double)it;
           a.trace[2 * (u - 1) + 1] = relres;
         }
@@ -1071,7 +1086,7 @@ __device__ __forceinline__ void mixed_cg_body(const MArgs &a) {
     bl = sh.beta_lo;
     flip = !flip;
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
+  if (mlead(a) && threadIdx.x == 0) {
     a.iresult[0] = sh.updates;
     a.iresult[1] = (status == FVC_ERR_NOCONV) ? sh.status : status;
     a.iresult[2] = it;
@@ -1099,9 +1114,9 @@ __global__ void __launch_bounds__(1024, 1) mixed_cg_staged_w4(MArgs a) {
 // correction equation A e = r, inside FP64 defect correction.
 constexpr int kBcgStall = 100;
 
-__global__ void __launch_bounds__(1024, 1) mixed_bicgstab(MArgs a) {
+__device__ __forceinline__ void mixed_bicgstab_body(const MArgs &a) {
   __shared__ double red[kMaxNV * 32];
-  const MPart P(a.A.nslices, a.A.n);
+  const MPart P(a);
   unsigned int ep = 0;
   int sweep = 0, inner_total = 0, status = FVC_ERR_NOCONV;
   double res[4];
@@ -1211,7 +1226,7 @@ __global__ void __launch_bounds__(1024, 1) mixed_bicgstab(MArgs a) {
     fold_correction(a);
     if (!grid_barrier(a.gs, ep)) return;
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
+  if (mlead(a) && threadIdx.x == 0) {
     a.iresult[0] = sweep;
     a.iresult[1] = status;
     a.iresult[2] = inner_total;
@@ -1219,6 +1234,71 @@ __global__ void __launch_bounds__(1024, 1) mixed_bicgstab(MArgs a) {
     a.result[3] = res[0];
     a.result[4] = bnorm2;
   }
+}
+
+__global__ void __launch_bounds__(1024, 1) mixed_bicgstab(MArgs a) { mixed_bicgstab_body(a); }
+
+// Batched mixed-precision solves: every block runs the mixed CG (code 1)
+// or the mixed BiCGSTAB (code 2) of its system of the block-diagonal
+// matrix, on that system's slices and synchronisation state.
+template <int kMaxT>
+__global__ void __launch_bounds__(kMaxT, 1024 / kMaxT)
+    mixed_batched(MArgs a, const BatchSys *__restrict__ sys, const int *__restrict__ sob) {
+  const BatchSys d = sys[sob[blockIdx.x]];
+  MArgs am = a;
+  am.gs = d.gs;
+  am.grp_s0 = d.s0;
+  am.grp_s1 = d.s1;
+  am.grp_nb = (int)d.gs.nblocks;
+  am.grp_base = (int)d.gs.base;
+  am.target = d.tol;
+  am.inner_tol = d.inner_tol;
+  am.init = d.init;
+  am.result = d.result;
+  am.iresult = d.iresult;
+  am.trace = nullptr;
+  am.history = nullptr;
+  if (d.code == 2) {
+    am.rsl = nullptr;
+    mixed_bicgstab_body(am);
+  } else {
+    mixed_cg_body<false, 0>(am);
+  }
+}
+
+// The launch-wide arguments of the mixed kernels over matrix A and the
+// FP32 vectors of S (rsl, gs and the solve's scalars are the caller's).
+MArgs mixed_args(const DeviceMatrix &A, const Scratch &S, const double *b, double *x) {
+  MArgs a{};
+  a.A.n = A.n;
+  a.A.nslices = A.nslices;
+  a.A.sptr = A.sptr;
+  a.A.col = A.col;
+  a.A.val = A.val;
+  a.A.diag = A.diag;
+  a.A.diag_mode = A.diag_mode;
+  a.w32 = A.val32;
+  a.e32 = A.diag32;
+  a.minv = A.minv32;
+  a.col16 = A.col16_ok ? A.col16 : nullptr;
+  a.ell_w = A.ell_w;
+  a.sflag = A.sflag;
+  a.jac = A.jac;
+  a.b = b;
+  a.x = x;
+  a.rs = S.f[0];
+  a.pa = S.f[1];
+  a.pb = S.f[2];
+  a.q = S.f[3];
+  a.e = reinterpret_cast<float2 *>(S.f[4]);
+  a.r0 = S.f[5];
+  a.t = S.f[6];
+  a.v = S.f[7];
+  a.z = S.f[8];
+  a.rsl = S.f[9];
+  a.pal = S.f[5];  // CG only (BiCGSTAB uses these buffers as r0 and t)
+  a.pbl = S.f[6];
+  return a;
 }
 
 int sm_count_m() {
@@ -1233,6 +1313,46 @@ int sm_count_m() {
 }
 
 }  // namespace
+
+int32_t ensure_f32_vectors(Scratch &S, size_t n) {
+  if (S.nf < n) {
+    for (int i = 0; i < 10; ++i) {
+      if (S.f[i]) cudaFree(S.f[i]);
+      S.f[i] = nullptr;
+    }
+    S.nf = n;
+  }
+  for (int i = 0; i < 10; ++i)  // f[4] holds the float2 correction
+    if (!S.f[i] && cudaMalloc(&S.f[i], sizeof(float) * (i == 4 ? 2 : 1) * (n + 64)) != cudaSuccess)
+      return FVC_ERR_CUDA;
+  return FVC_OK;
+}
+
+const void *mixed_batched_kernel(int threads) {
+  return threads <= 128 ? (const void *)mixed_batched<128> : (const void *)mixed_batched<1024>;
+}
+
+int32_t launch_mixed_batched(const DeviceMatrix &A, const Scratch &S, const BatchSys *dsys,
+                             const int *dsob, int blocks, int threads, const double *b, double *x,
+                             int maxit, const fvc_opts &o, cudaStream_t stream) {
+  MArgs a = mixed_args(A, S, b, x);
+  a.max_refine = (o.max_refine > 0) ? o.max_refine : 30;
+  a.update_beta = o.update_beta;
+  a.maxit = maxit;
+  // (the shared-memory carveout stays at its default: the caller sized the
+  // grid by the occupancy under it)
+  const void *kern = mixed_batched_kernel(threads);
+  void *args[] = {&a, &dsys, &dsob};
+  const cudaError_t ce =
+      cudaLaunchCooperativeKernel(kern, dim3((unsigned)blocks), dim3((unsigned)threads), args, 0,
+                                  stream);
+  count_launch();
+  if (ce != cudaSuccess) {
+    fprintf(stderr, "fvcgpu: batched mixed launch failed: %s\n", cudaGetErrorString(ce));
+    return FVC_ERR_CUDA;
+  }
+  return FVC_OK;
+}
 
 int32_t build_f32_copy(DeviceMatrix &A, cudaStream_t stream) {
   if (A.have32) return FVC_OK;
@@ -1280,17 +1400,7 @@ int32_t run_mixed(const DeviceMatrix &A0, Scratch &S, int code, const double *b,
   if (code != 1 && code != 2) return FVC_ERR_UNSUPPORTED;
   int32_t rc = build_f32_copy(A, stream);
   if (rc != FVC_OK) return rc;
-  const size_t n = (size_t)A.n;
-  if (S.nf < n) {
-    for (int i = 0; i < 10; ++i) {
-      if (S.f[i]) cudaFree(S.f[i]);
-      S.f[i] = nullptr;
-    }
-    S.nf = n;
-  }
-  for (int i = 0; i < 10; ++i)  // f[4] holds the float2 correction
-    if (!S.f[i] && cudaMalloc(&S.f[i], sizeof(float) * (i == 4 ? 2 : 1) * (n + 64)) != cudaSuccess)
-      return FVC_ERR_CUDA;
+  if ((rc = ensure_f32_vectors(S, (size_t)A.n)) != FVC_OK) return rc;
   const int threads = block_threads_for(o.block_threads, A.nslices, sm_count_m());
   // CG streams through shared-memory stages when its layout allows
   const bool staged = code == 1 && threads == kStRows && A.col16_ok && o.staging == 0;
@@ -1317,38 +1427,11 @@ int32_t run_mixed(const DeviceMatrix &A0, Scratch &S, int code, const double *b,
   if (o.max_blocks > 0) blocks = std::min(blocks, o.max_blocks);
   if (ensure_sync(S, (size_t)blocks) != FVC_OK) return FVC_ERR_CUDA;
   reset_sync(S, stream);
-  MArgs a{};
-  a.A.n = A.n;
-  a.A.nslices = A.nslices;
-  a.A.sptr = A.sptr;
-  a.A.col = A.col;
-  a.A.val = A.val;
-  a.A.diag = A.diag;
-  a.A.diag_mode = A.diag_mode;
-  a.w32 = A.val32;
-  a.e32 = A.diag32;
-  a.minv = A.minv32;
-  a.col16 = A.col16_ok ? A.col16 : nullptr;
-  a.ell_w = A.ell_w;
-  a.sflag = A.sflag;
-  a.jac = A.jac;
-  a.b = b;
-  a.x = x;
-  a.rs = S.f[0];
-  a.pa = S.f[1];
-  a.pb = S.f[2];
-  a.q = S.f[3];
-  a.e = reinterpret_cast<float2 *>(S.f[4]);
-  a.r0 = S.f[5];
-  a.t = S.f[6];
-  a.v = S.f[7];
-  a.z = S.f[8];
+  MArgs a = mixed_args(A, S, b, x);
   a.rsl = (code == 1) ? S.f[9] : nullptr;
-  a.pal = S.f[5];  // CG only (BiCGSTAB uses these buffers as r0 and t)
-  a.pbl = S.f[6];
   a.gs = make_sync(S, blocks);
   a.target = (o.refine_tol > 0) ? o.refine_tol : tol;
-  a.inner_tol = (o.inner_tol > 0) ? o.inner_tol : (code == 1 ? 0.1 : 1e-4);
+  a.inner_tol = (o.inner_tol > 0) ? o.inner_tol : kInnerTolDefault;
   a.max_refine = (o.max_refine > 0) ? o.max_refine : 30;
   a.update_beta = o.update_beta;
   a.maxit = maxit;

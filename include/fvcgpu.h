@@ -78,7 +78,8 @@ typedef struct {
   int32_t init;        /* -1: the reference's rule for (code,matriz); 0: warm
                           start from x; 1: start from x = 0               */
   double refine_tol;   /* MIXED: target ||b-Ax||/||b|| (0 -> derived: tol)  */
-  double inner_tol;    /* MIXED: inner FP32 reduction per sweep (0 -> 1e-4)*/
+  double inner_tol;    /* MIXED: FP32 reduction of the residual between two
+                          FP64 residual recomputations (0 -> 0.1)      */
   int32_t max_refine;  /* MIXED: max outer sweeps (0 -> 30)                */
   int32_t block_threads; /* 0 -> autotuned                                 */
   int32_t blocks_per_sm; /* 0 -> autotuned                                 */
@@ -179,8 +180,11 @@ int32_t fvc_solve_async(fvc_context *ctx, int32_t code, const double *d_b,
  * one launch (FVC_ERR_ARG beyond).  st (host, nsys entries, may be NULL)
  * receives each system's statistics; solve_ms is the launch's time.
  * Returns FVC_OK when every system converged, else FVC_ERR_NAN if one broke
- * down or the first other failure.  FP64 only (FVC_ERR_UNSUPPORTED for
- * FVC_PREC_MIXED).  No counterpart in the reference, which solves one
+ * down or the first other failure.  With FVC_PREC_MIXED each system runs
+ * the mixed-precision solve of fvc_solve (FP32 iterations inside FP64
+ * residual replacement or defect correction, stopping on the FP64
+ * ||b-Ax||/||b|| <= tol); its statistics then count the FP32 iterations
+ * and the refinements.  No counterpart in the reference, which solves one
  * system per call (src/Solver.f:28-346). */
 int32_t fvc_solve_batched(fvc_context *ctx, int32_t nsys, const int32_t *row_start,
                           const double *d_b, double *d_x, double tol,

@@ -143,3 +143,43 @@ def test_batched_iteration_hints_move_only_the_speed(orc):
         assert t0.status == 0 and t1.status == 0
         assert np.linalg.norm(a - b) <= 1e-9 * max(np.linalg.norm(a), 1e-300)
         assert abs(t0.iterations - t1.iterations) <= 2
+
+
+def test_batched_mixed_precision_reaches_tolerance(orc):
+    # mixed precision per system (FP32 iterations, FP64 residual
+    # replacement / defect correction): every system of a PCG + BiCGSTAB
+    # batch reaches ||b - Ax|| / ||b|| <= 1e-8 recomputed in FP64, and its
+    # solution agrees with the FP64 one within that residual times the
+    # condition number of these systems (at most ~1e4)
+    import torch
+    from fortranfvcell_gb300 import Context, make_opts, pack_block_diagonal
+    systems = batch(orc)[1:]                 # no one-cell system (BiCGSTAB breakdown)
+    codes = []
+    for k, s in enumerate(systems):
+        if k % 2:
+            u = unsymmetric(s, seed=k)
+            s.update(ad=u["ad"], au=u["au"])
+        codes.append(2 if k % 2 else 1)
+    pk = pack_block_diagonal(systems)
+    ctx = Context(device=0)
+    ctx.set_matrix(1, True, pk["neq"], pk["nad"], pk["ad"], pk["au"], pk["au"], pk["ia"],
+                   pk["ja"])
+    b = np.zeros(pk["neq"])
+    for s, r in zip(systems, pk["rows"]):
+        b[r] = s["b"]
+    bd = torch.from_numpy(b).cuda()
+    xs = {}
+    for prec in ("mixed", "fp64"):
+        xd = torch.zeros(pk["neq"], dtype=torch.float64, device="cuda")
+        o = make_opts(prec, init=1, stop_rule=1)
+        rc, st = ctx.solve_batched(pk["row_start"], bd, xd, 1e-8 if prec == "mixed" else 1e-12,
+                                   50000, o, codes=codes)
+        assert rc == 0, prec
+        xs[prec] = xd.cpu().numpy()
+        if prec == "mixed":
+            for t in st:
+                assert t.status == 0 and t.rel_residual <= 1e-8 and t.iterations > 0
+    ctx.close()
+    for s, r in zip(systems, pk["rows"]):
+        xm, x64 = xs["mixed"][r], xs["fp64"][r]
+        assert np.linalg.norm(xm - x64) <= 1e-4 * np.linalg.norm(x64), s["n"]
