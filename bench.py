@@ -302,6 +302,20 @@ def run_ours(args):
     spmv32_bytes = 6 * max(inf["slots"], 128 * inf["nslices"]) + 12 * n
     spmv32_gbs = spmv32_bytes / (spmv32_ms * 1e-3) / 1e9
 
+    # the launch-shape autotuner on this matrix: its pick against the
+    # automatic shape, per iteration over the same trial length
+    tuned = {}
+    for name, code, prec in (("pcg_fp64", 1, "fp64"), ("pcg_mixed", 1, "mixed")):
+        o_best, us_best = ctx.autotune(code, prec, 50)
+        o_def = make_opts(prec, init=1)
+        xt = torch.zeros_like(bd)
+        ctx.solve(code, bd, xt, 1e-300, 50, o_def, raise_on_error=False)
+        st_def = ctx.solve(code, bd, xt, 1e-300, 50, o_def, raise_on_error=False)
+        us_def = st_def.solve_ms * 1e3 / max(st_def.iterations, 1)
+        tuned[name] = {"block_threads": o_best.block_threads, "max_blocks": o_best.max_blocks,
+                       "staging": o_best.staging, "us_per_iteration": round(us_best, 2),
+                       "automatic_us_per_iteration": round(us_def, 2)}
+
     # end to end through the public host API, pinned host arrays
     pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
     h_ad, h_au, h_b = pin(s.ad), pin(s.au), pin(b)
@@ -368,6 +382,7 @@ def run_ours(args):
                      "kernel": "mixed_cg (persistent, one launch per solve)",
                      "peak_kind": peak_kind,
                      "alg_bytes_per_launch": int(alg_bytes)},
+        "autotune": tuned,
         "e2e": {"value": round(1.0 / e2e_s, 4), "unit": "solves/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "gpu_launches": int(launches),

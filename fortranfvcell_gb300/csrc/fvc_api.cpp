@@ -504,6 +504,82 @@ int32_t fvc_solve_async(fvc_context *c, int32_t code, const double *d_b, double 
   return fvc::launch_solve_status(c->S, d_status, c->stream);
 }
 
+int32_t fvc_autotune(fvc_context *c, int32_t code, int32_t precision, int32_t trial_its,
+                     fvc_opts *best, double *best_us) {
+  if (!c || !c->has_matrix || !best || trial_its < 1) return FVC_ERR_ARG;
+  if (code < 1 || code > 3 || (precision != FVC_PREC_FP64 && precision != FVC_PREC_MIXED))
+    return FVC_ERR_UNSUPPORTED;
+  if ((code == 2 || code == 3) && c->matriz == 2) return FVC_ERR_UNSUPPORTED;
+  if (code == 3 && c->matriz == 4) return FVC_ERR_UNSUPPORTED;
+  if (precision == FVC_PREC_MIXED && code == 3) return FVC_ERR_UNSUPPORTED;
+  cudaSetDevice(c->device);
+  const int n = c->neq;
+  double *d_b = nullptr, *d_x = nullptr;
+  if (cudaMalloc(&d_b, sizeof(double) * n) != cudaSuccess ||
+      cudaMalloc(&d_x, sizeof(double) * n) != cudaSuccess) {
+    cudaFree(d_b);
+    return FVC_ERR_CUDA;
+  }
+  {  // b = 1: any right-hand side serves, the iterations run to trial_its
+    std::vector<double> ones((size_t)n, 1.0);
+    cudaMemcpy(d_b, ones.data(), sizeof(double) * n, cudaMemcpyHostToDevice);
+  }
+  // the launch shapes the kernels take: the automatic one (a cluster for
+  // small PCG systems, else one block per SM with the fewest warps), block
+  // sizes, caps on the grid, and for mixed CG the staged or plain loads
+  std::vector<fvc_opts> cand;
+  fvc_opts base;
+  fvc_opts_default(&base);
+  base.precision = precision;
+  base.init = 1;
+  cand.push_back(base);
+  for (int t : {128, 256, 512, 1024}) {
+    fvc_opts o = base;
+    o.block_threads = t;
+    cand.push_back(o);
+  }
+  for (int mb : {16, 38, 76}) {
+    fvc_opts o = base;
+    o.block_threads = 1024;
+    o.max_blocks = mb;
+    cand.push_back(o);
+  }
+  if (precision == FVC_PREC_MIXED && code == 1) {
+    fvc_opts o = base;
+    o.block_threads = 1024;
+    o.staging = 1;
+    cand.push_back(o);
+  }
+  int32_t rc = FVC_OK;
+  double best_t = 0.0;
+  int best_k = -1;
+  for (size_t k = 0; k < cand.size() && rc == FVC_OK; ++k) {
+    double t_k = 0.0;
+    for (int rep = 0; rep < 2; ++rep) {  // the better of two runs
+      fvc_stats st;
+      const int32_t r = fvc_solve(c, code, d_b, d_x, 1e-300, trial_its, &cand[k], &st);
+      if (r != FVC_OK && r != FVC_ERR_NOCONV) {
+        t_k = -1.0;  // this shape does not run here (e.g. not co-resident)
+        break;
+      }
+      const int its = st.iterations > 0 ? st.iterations : 1;
+      const double us = 1e3 * st.solve_ms / its;
+      t_k = (rep == 0) ? us : std::min(t_k, us);
+    }
+    if (t_k > 0.0 && (best_k < 0 || t_k < best_t)) {
+      best_t = t_k;
+      best_k = (int)k;
+    }
+  }
+  cudaFree(d_b);
+  cudaFree(d_x);
+  if (best_k < 0) return FVC_ERR_CUDA;
+  *best = cand[(size_t)best_k];
+  best->init = -1;  // the tuned shape keeps the reference's warm-start rule
+  if (best_us) *best_us = best_t;
+  return FVC_OK;
+}
+
 int32_t fvc_solve_batched_ex(fvc_context *c, int32_t nsys, const int32_t *row_start,
                              const int32_t *codes, const double *tols, const double *its_hint,
                              const double *d_b, double *d_x, double tol, int32_t maxit,

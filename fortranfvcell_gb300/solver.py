@@ -167,6 +167,16 @@ class Context:
                                            C.byref(o), C.c_void_p(_addr(status_dev))),
                    "fvc_solve_async")
 
+    def autotune(self, code: int, precision: str = "fp64", trial_its: int = 50):
+        """The fastest launch shape for this matrix and method (fvc_autotune):
+        (FvcOpts to pass to solve, microseconds per iteration)."""
+        o = FvcOpts()
+        us = C.c_double()
+        prec = {"fp64": 0, "mixed": 1}[precision]
+        _lib.check(self._L.fvc_autotune(self._h, int(code), prec, int(trial_its), C.byref(o),
+                                        C.byref(us)), "fvc_autotune")
+        return o, us.value
+
     def solve_batched(self, row_start, b_dev, x_dev, tol: float, maxit: int,
                       opts: FvcOpts | None = None, raise_on_error: bool = True,
                       codes=None, tols=None, its_hint=None):

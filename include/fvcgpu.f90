@@ -126,6 +126,18 @@ module fvcgpu
        integer(c_int32_t), value :: on
      end function fvc_simple_set_graph
 
+     ! the system the last outer iteration solved: which 1 u1, 2 u2, 3 p',
+     ! 4 enthalpy; ad(numel), au(nja), b(numel) in equation order (c_loc of
+     ! the arrays, or c_null_ptr); nja receives the length of au
+     integer(c_int32_t) function fvc_simple_system(s, which, ad, au, b, nja) &
+          bind(C, name="fvc_simple_system")
+       import :: c_ptr, c_int32_t, c_int64_t
+       type(c_ptr), value        :: s
+       integer(c_int32_t), value :: which
+       type(c_ptr), value        :: ad, au, b
+       integer(c_int64_t)        :: nja
+     end function fvc_simple_system
+
      integer(c_int32_t) function fvc_simple_time_step(s) &
           bind(C, name="fvc_simple_time_step")
        import :: c_ptr, c_int32_t

@@ -168,6 +168,23 @@ int32_t fvc_solve_async(fvc_context *ctx, int32_t code, const double *d_b,
                         double *d_x, double tol, int32_t maxit,
                         const fvc_opts *opts, int32_t *d_status);
 
+/* Launch-shape autotuner: times trial solves of trial_its iterations (b =
+ * 1, x = 0, no early stop) of the context's matrix with code and precision
+ * over the shapes the kernels support -- the automatic choice (a thread-
+ * block cluster for a PCG system of at most 8192 rows, else one block per
+ * SM with the fewest warps that cover the rows), 128..1024 threads per
+ * block, a cap of 16/38/76 blocks, and for mixed CG plain loads instead of
+ * the staged copies -- and writes the fastest per iteration to *best (init
+ * -1, the rest as fvc_opts_default) and its time to *best_us (may be NULL).
+ * Pass *best to fvc_solve for later solves of this matrix and method.  The
+ * shape changes only the summation order of the reductions, so results
+ * move at rounding level.  Rows are one lane each in 32-row slices, the
+ * form every kernel is written for; that is not tuned.  Returns FVC_OK, or
+ * an FVC_* error; FVC_ERR_UNSUPPORTED for the (code, matriz) pairs
+ * fvc_solve rejects and for mixed GMRES. */
+int32_t fvc_autotune(fvc_context *ctx, int32_t code, int32_t precision,
+                     int32_t trial_its, fvc_opts *best, double *best_us);
+
 /* Batched Jacobi-PCG (src/Iterativos.f:29-106) of nsys independent systems
  * in one persistent launch: the context's matrix holds them block-
  * diagonally, system s on rows row_start[s] .. row_start[s+1]-1 (host

@@ -395,3 +395,33 @@ def test_stored_p_pcg_on_a_large_system(fvc):
     st = fvc.solver(ad, s.au, s.au, x, b, s.ia, s.ja, n, s.nad, True, 1e-11, 100000, 1, 1)
     assert st.iterations > 0
     assert np.linalg.norm(x - x_ref) / np.linalg.norm(x_ref) < 1e-8
+
+
+@pytest.mark.parametrize("code,prec", [(1, "fp64"), (2, "fp64"), (3, "fp64"), (1, "mixed")])
+def test_autotune_returns_a_shape_that_solves(fvc, code, prec):
+    # fvc_autotune picks among launch shapes by timing; whichever it picks
+    # solves the system to the same answer as the default shape (the shape
+    # moves only the summation order of the reductions)
+    import torch
+    from fortranfvcell_gb300 import mesh
+    s = mesh.pressure_system(mesh.square_mesh(70, kind="mixed", jitter=0.2, seed=5), matriz=1,
+                             unsym=True, pin_cell=1)
+    n = s.neq
+    ctx = fvc.Context()
+    ctx.set_matrix(1, True, n, s.nad, s.ad, s.au, s.au, s.ia, s.ja)
+    o, us = ctx.autotune(code, prec, 20)
+    assert us > 0.0 and o.precision == (1 if prec == "mixed" else 0)
+    b = torch_dev(np.random.default_rng(4).uniform(-1, 1, n))
+    xs = []
+    for opts in (o, fvc.make_opts(prec)):
+        x = torch.zeros_like(b)
+        st = ctx.solve(code, b, x, {1: 1e-10, 2: 1e-10, 3: 1e-8}[code] if prec == "fp64"
+                       else 1e-9, 50000, opts)
+        assert st.status == 0
+        xs.append(x.cpu().numpy())
+    ctx.close()
+    # the stopping tests bound the preconditioned residual, so two launch
+    # shapes stop a few iterations apart with errors of tol x cond(A)
+    # (BiCGSTAB, GMRES: about 1e-6 relative on this pinned p' system)
+    tol = {1: 1e-8, 2: 1e-5, 3: 1e-5}[code] if prec == "fp64" else 1e-5
+    assert np.linalg.norm(xs[0] - xs[1]) <= tol * np.linalg.norm(xs[1])
