@@ -138,7 +138,7 @@ __device__ __forceinline__ bool epilogue(const KArgs &a, unsigned int &ep, doubl
 // ---------------------------------------------------------------------
 // The iteration over the rows of P, synchronising through gs; the lead
 // block writes result / iresult.  pcg_f64 runs it over the whole matrix,
-// pcg_batched over one system of a batch per group of blocks.
+// krylov_batched over one system of a batch per group of blocks.
 // kStoreP: p = z + beta p is formed once per row in place and published by a
 // grid barrier before the SpMV (one FP64 FMA per row instead of one per
 // gathered neighbour -- 4 of the 16 FP64 instructions of a row-iteration on
