@@ -17,6 +17,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <climits>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -82,6 +83,7 @@ void free_matrix(fvc_context *c) {
   cudaFree(c->d_raw1);
   cudaFree(c->d_raw2);
   cudaFree(c->d_jac_src);
+  cudaFree(A.mirror);
   A = DeviceMatrix();
   c->d_src = nullptr;
   c->d_raw1 = c->d_raw2 = nullptr;
@@ -217,6 +219,55 @@ int32_t upload_raw(fvc_context *c, const double *ad, const double *au, const dou
   rc = fvc::launch_reciprocal(c->A, s);
   if (rc != FVC_OK) return rc;
   c->A.have32 = false;  // FP32 copy is rebuilt lazily from the new values
+  return FVC_OK;
+}
+
+// The mirror map of the SELL slots (the slot of entry (j, i) for the slot
+// of (i, j)), built once per structure from a host copy of the columns.
+// FVC_ERR_UNSUPPORTED when the off-diagonal pattern is not symmetric.
+int32_t build_mirror(fvc_context *c) {
+  fvc::DeviceMatrix &A = c->A;
+  if (A.mirror) return FVC_OK;
+  if (A.slots >= (int64_t)INT32_MAX) return FVC_ERR_UNSUPPORTED;
+  const int n = A.n, ns = A.nslices;
+  std::vector<int64_t> sptr((size_t)ns + 1);
+  std::vector<int32_t> col((size_t)std::max<int64_t>(A.slots, 1));
+  if (cudaMemcpy(sptr.data(), A.sptr, sizeof(int64_t) * sptr.size(), cudaMemcpyDeviceToHost) !=
+          cudaSuccess ||
+      cudaMemcpy(col.data(), A.col, sizeof(int32_t) * (size_t)A.slots, cudaMemcpyDeviceToHost) !=
+          cudaSuccess)
+    return FVC_ERR_CUDA;
+  std::vector<int32_t> mir(col.size());
+  for (int s = 0; s < ns; ++s) {
+    const int w = (int)((sptr[s + 1] - sptr[s]) / 32);
+    for (int l = 0; l < 32; ++l) {
+      const int i = s * 32 + l;
+      for (int k = 0; k < w; ++k) {
+        const int64_t q = sptr[s] + 32 * k + l;
+        const int j = col[q];
+        if (i >= n || j == i) {  // padding (column = row, value 0) or a diagonal slot
+          mir[q] = (int32_t)q;
+          continue;
+        }
+        const int sj = j / 32, lj = j % 32;
+        const int wj = (int)((sptr[sj + 1] - sptr[sj]) / 32);
+        int64_t found = -1;
+        for (int kk = 0; kk < wj && found < 0; ++kk) {
+          const int64_t qq = sptr[sj] + 32 * kk + lj;
+          if (col[qq] == i) found = qq;
+        }
+        if (found < 0) return FVC_ERR_UNSUPPORTED;
+        mir[q] = (int32_t)found;
+      }
+    }
+  }
+  if (cudaMalloc(&A.mirror, sizeof(int32_t) * mir.size()) != cudaSuccess) return FVC_ERR_CUDA;
+  if (cudaMemcpy(A.mirror, mir.data(), sizeof(int32_t) * mir.size(), cudaMemcpyHostToDevice) !=
+      cudaSuccess) {
+    cudaFree(A.mirror);
+    A.mirror = nullptr;
+    return FVC_ERR_CUDA;
+  }
   return FVC_OK;
 }
 
@@ -473,6 +524,25 @@ int32_t fvc_solve(fvc_context *c, int32_t code, const double *d_b, double *d_x, 
   } else {
     rc = fvc::run_gmres(c->A, c->S, d_b, d_x, tol, maxit, o, c->stream, st);
   }
+  if (st && rc != st->status) st->status = rc;
+  return rc;
+}
+
+int32_t fvc_solve_transposed(fvc_context *c, int32_t code, const double *d_b, double *d_x,
+                             double tol, int32_t maxit, const fvc_opts *opts, fvc_stats *st) {
+  if (!c || !c->has_matrix || !d_b || !d_x || maxit < 1) return FVC_ERR_ARG;
+  fvc_opts o;
+  if (opts)
+    o = *opts;
+  else
+    fvc_opts_default(&o);
+  if (st) memset(st, 0, sizeof(*st));
+  if (code != 2 || o.precision != FVC_PREC_FP64 || c->matriz == 2) return FVC_ERR_UNSUPPORTED;
+  cudaSetDevice(c->device);
+  int32_t rc = build_mirror(c);
+  if (rc != FVC_OK) return rc;
+  const int init = (o.init < 0) ? default_init(code, c->matriz) : (o.init ? 1 : 0);
+  rc = fvc::run_bicgstab_transposed(c->A, c->S, d_b, d_x, tol, maxit, init, o, c->stream, st);
   if (st && rc != st->status) st->status = rc;
   return rc;
 }

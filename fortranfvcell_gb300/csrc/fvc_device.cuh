@@ -30,6 +30,8 @@ struct SellView {
   const V *val;          // values (negated off-diagonals, as stored)
   const V *diag;         // n (null for DIAG_NONE)
   int diag_mode;
+  const int *mirror = nullptr;  // per slot: the slot of the transposed entry
+                                // (symmetric patterns; transposed solves only)
 };
 
 // Grid synchronisation state of one persistent launch.  `count` is a
@@ -399,6 +401,43 @@ struct BatchSys {
   double *result;
   int *iresult;
 };
+
+// y_row = (A^T x)_row over the stored matrix of a symmetric pattern: the
+// entry (row, col(slot)) of A^T is the stored value of the mirror slot
+// (col(slot), row); the diagonal is A's.  Terms in slot order, with FMA.
+template <typename XF>
+__device__ __forceinline__ double sell_row_fma_t(const SellView<double> &A, int s, int lane,
+                                                 int row, XF xf) {
+  const int64_t base = A.sptr[s];
+  const int w = (int)((A.sptr[s + 1] - base) >> 5);
+  const int *cp = A.col + base + lane;
+  const int *mp = A.mirror + base + lane;
+  const bool has_diag = A.diag_mode != DIAG_NONE;
+  const double dv = has_diag ? ld_stream(A.diag + row) : 0.0;
+  double t = has_diag ? dv * xf(row) : 0.0;
+  if (w <= 4) {
+    int c[4], m[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      c[k] = (k < w) ? ld_stream(cp + 32 * k) : 0;
+      m[k] = (k < w) ? ld_stream(mp + 32 * k) : 0;
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      if (k < w) t = fma(A.val[m[k]], xf(c[k]), t);
+  } else {
+    for (int k = 0; k < w; ++k) t = fma(A.val[ld_stream(mp + 32 * k)], xf(ld_stream(cp + 32 * k)), t);
+  }
+  return t;
+}
+
+// A x (kT false) or A^T x (kT true) for one row
+template <bool kT, typename XF>
+__device__ __forceinline__ double row_fma(const SellView<double> &A, int s, int lane, int row,
+                                          XF xf) {
+  if (kT) return sell_row_fma_t(A, s, lane, row, xf);
+  return sell_row_fma(A, s, lane, row, xf);
+}
 
 // Host side: scratch for the grid synchronisation of a persistent launch.
 inline int32_t ensure_sync(Scratch &S, size_t nblocks) {

@@ -36,6 +36,7 @@ struct DeviceMatrix {
   int ell_w = 0;             // FP32 copy padded to this uniform slice width (0: SELL)
   bool have32 = false;
   int cl_smax = -1;          // cluster PCG: most slots of one CTA's rows (-1: unknown)
+  int *mirror = nullptr;     // per slot: the slot of the transposed entry (built on demand)
   // host-side description of the source layout, for value updates
   int matriz = 0, unsym = 0, nad = 0;
   int64_t *src_of_slot = nullptr;  // device map: slot -> source value index
@@ -82,6 +83,10 @@ int32_t run_pcg(const DeviceMatrix &A, Scratch &S, const double *b, double *x,
 int32_t run_bicgstab(const DeviceMatrix &A, Scratch &S, const double *b,
                      double *x, double tol, int maxit, int init,
                      const fvc_opts &o, cudaStream_t stream, fvc_stats *st);
+// BiCGSTAB on A^T x = b over A's storage (A.mirror built): FVC_ERR_UNSUPPORTED without it
+int32_t run_bicgstab_transposed(const DeviceMatrix &A, Scratch &S, const double *b, double *x,
+                                double tol, int maxit, int init, const fvc_opts &o,
+                                cudaStream_t stream, fvc_stats *st);
 int32_t run_gmres(const DeviceMatrix &A, Scratch &S, const double *b, double *x,
                   double tol, int maxit, const fvc_opts &o, cudaStream_t stream,
                   fvc_stats *st);

@@ -104,13 +104,14 @@ __device__ __forceinline__ void finish(const KArgs &a, int iters, int status,
 // Energy norm x.Ax and the FP64 residual ||b-Ax||^2, ||b||^2 in one pass
 // over the rows of P (x must be complete at every row: called right after
 // a synchronisation of gs); the lead block writes result[0, 3, 4].
+template <bool kT = false>
 __device__ __forceinline__ bool epilogue_to(const KArgs &a, const Part &P, const GridSync &gs,
                                             double *result, bool lead, unsigned int &ep,
                                             double *red, bool energy_xb) {
   double acc[3] = {0.0, 0.0, 0.0};
   const double *x = a.x;
   FOR_ROWS(P) {
-    double ax = sell_row_fma(a.A, s_, P.lane, row, [&](int k) { return x[k]; });
+    double ax = row_fma<kT>(a.A, s_, P.lane, row, [&](int k) { return x[k]; });
     double xi = x[row], bi = a.b[row];
     double rr = bi - ax;
     acc[0] = fma(xi, energy_xb ? bi : ax, acc[0]);
@@ -289,7 +290,8 @@ __global__ void __launch_bounds__(1024, 1) pcg_f64(KArgs a) {
 //            s''.(s'/m) ; r.s'' ; s''.s''                       -> beta, stop
 // v0 = r (shadow r0), v1/v2 = s, v3/v4 = p, v5/v6 = v, v7 = t.
 // ---------------------------------------------------------------------
-template <int kMaxT = 1024>
+// kT: solve A^T x = b through the transposed row sums (sell_row_fma_t)
+template <int kMaxT = 1024, bool kT = false>
 __device__ __forceinline__ void bicgstab_run(const KArgs &a, const Part &P, const GridSync &gs,
                                              double *result, int *iresult, bool lead) {
   __shared__ double red[kMaxNV * 32];
@@ -312,7 +314,7 @@ __device__ __forceinline__ void bicgstab_run(const KArgs &a, const Part &P, cons
       ax = 0.0;
       x[row] = 0.0;
     } else {
-      ax = sell_row_fma(a.A, s_, P.lane, row, [&](int k) { return x[k]; });
+      ax = row_fma<kT>(a.A, s_, P.lane, row, [&](int k) { return x[k]; });
     }
     const double ri = b[row] - ax;
     r[row] = ri;
@@ -338,7 +340,7 @@ __device__ __forceinline__ void bicgstab_run(const KArgs &a, const Part &P, cons
       FOR_ROWS(P) {
         const double *pc = pnew;
         const double vi =
-            sell_row_fma(a.A, s_, P.lane, row, [&](int k) { return pc[k] * minv[k]; });
+            row_fma<kT>(a.A, s_, P.lane, row, [&](int k) { return pc[k] * minv[k]; });
         vnew[row] = vi;
         const double ri = r[row];
         acc[0] = fma(scur[row], ri, acc[0]);
@@ -350,7 +352,7 @@ __device__ __forceinline__ void bicgstab_run(const KArgs &a, const Part &P, cons
         auto pf = [&](int k) { return fma(beta, fma(-w, vo[k], po[k]), sc[k]); };
         pnew[row] = pf(row);
         const double vi =
-            sell_row_fma(a.A, s_, P.lane, row, [&](int k) { return pf(k) * minv[k]; });
+            row_fma<kT>(a.A, s_, P.lane, row, [&](int k) { return pf(k) * minv[k]; });
         vnew[row] = vi;
         const double ri = r[row];
         acc[0] = fma(sc[row], ri, acc[0]);
@@ -371,7 +373,7 @@ __device__ __forceinline__ void bicgstab_run(const KArgs &a, const Part &P, cons
       auto sf = [&](int k) { return fma(-alpha, vn[k], sc[k]); };
       snxt[row] = sf(row);
       const double ti =
-          sell_row_fma(a.A, s_, P.lane, row, [&](int k) { return sf(k) * minv[k]; });
+          row_fma<kT>(a.A, s_, P.lane, row, [&](int k) { return sf(k) * minv[k]; });
       t[row] = ti;
       acc[0] = fma(ti, snxt[row], acc[0]);
       acc[1] = fma(ti, ti, acc[1]);
@@ -424,11 +426,17 @@ __device__ __forceinline__ void bicgstab_run(const KArgs &a, const Part &P, cons
     status = FVC_ERR_NOCONV;
   }
   finish_to(result, iresult, lead, j, status, sh.conv, sh.crit, 0);
-  epilogue_to(a, P, gs, result, lead, ep, red, false);
+  epilogue_to<kT>(a, P, gs, result, lead, ep, red, false);
 }
 
 __global__ void __launch_bounds__(1024, 1) bicgstab_f64(KArgs a) {
   bicgstab_run(a, Part(a.A.nslices, a.A.n), a.gs, a.result, a.iresult, blockIdx.x == 0);
+}
+
+// BiCGSTAB on A^T x = b over A's storage (a.A.mirror set)
+__global__ void __launch_bounds__(1024, 1) bicgstab_f64_t(KArgs a) {
+  bicgstab_run<1024, true>(a, Part(a.A.nslices, a.A.n), a.gs, a.result, a.iresult,
+                           blockIdx.x == 0);
 }
 
 // Batched PCG / BiCGSTAB: the matrix is block diagonal, each system
@@ -647,6 +655,7 @@ SellView<double> view64(const DeviceMatrix &A) {
   v.val = A.val;
   v.diag = A.diag;
   v.diag_mode = A.diag_mode;
+  v.mirror = A.mirror;
   return v;
 }
 
@@ -825,6 +834,13 @@ int32_t run_pcg(const DeviceMatrix &A, Scratch &S, const double *b, double *x, d
 int32_t run_bicgstab(const DeviceMatrix &A, Scratch &S, const double *b, double *x, double tol,
                      int maxit, int init, const fvc_opts &o, cudaStream_t stream, fvc_stats *st) {
   return run_persistent(bicgstab_f64, A, S, b, x, tol, maxit, init, o, stream, st, 8, false);
+}
+
+int32_t run_bicgstab_transposed(const DeviceMatrix &A, Scratch &S, const double *b, double *x,
+                                double tol, int maxit, int init, const fvc_opts &o,
+                                cudaStream_t stream, fvc_stats *st) {
+  if (!A.mirror) return FVC_ERR_UNSUPPORTED;
+  return run_persistent(bicgstab_f64_t, A, S, b, x, tol, maxit, init, o, stream, st, 8, false);
 }
 
 int32_t run_gmres(const DeviceMatrix &A, Scratch &S, const double *b, double *x, double tol,

@@ -167,6 +167,21 @@ class Context:
                                            C.byref(o), C.c_void_p(_addr(status_dev))),
                    "fvc_solve_async")
 
+    def solve_transposed(self, b_dev, x_dev, tol: float, maxit: int,
+                         opts: FvcOpts | None = None, raise_on_error: bool = True) -> FvcStats:
+        """A^T x = b by BiCGSTAB over this context's matrix (no transposed
+        copy); device buffers as in solve."""
+        st = FvcStats()
+        o = opts if opts is not None else make_opts()
+        rc = self._L.fvc_solve_transposed(self._h, 2, C.c_void_p(_addr(b_dev)),
+                                          C.c_void_p(_addr(x_dev)), float(tol), int(maxit),
+                                          C.byref(o), C.byref(st))
+        if raise_on_error and rc != _lib.FVC_OK:
+            raise FvcError(rc, f"transposed BiCGSTAB ended with status "
+                               f"{_lib.STATUS_NAMES.get(rc, rc)}")
+        st.status = rc
+        return st
+
     def autotune(self, code: int, precision: str = "fp64", trial_its: int = 50):
         """The fastest launch shape for this matrix and method (fvc_autotune):
         (FvcOpts to pass to solve, microseconds per iteration)."""

@@ -148,6 +148,20 @@ int32_t fvc_solve(fvc_context *ctx, int32_t code, const double *d_b, double *d_x
                   double tol, int32_t maxit, const fvc_opts *opts,
                   fvc_stats *stats);
 
+/* Solve the transposed system A^T x = b (DEVICE vectors, as fvc_solve)
+ * with the reference's Jacobi BiCGSTAB (code 2; src/Iterativos.f:140-234)
+ * over the context's stored matrix: the SpMV reads entry (i, j) of A^T as
+ * the stored value of (j, i) through a per-slot mirror index built at the
+ * first call for a structure.  There is no transposed copy of the values,
+ * so a value update of A serves both A and A^T.  The Jacobi preconditioner
+ * is A's diagonal, which A^T shares.  The adjoint solves of
+ * fortranfvcell_gb300.autograd use it.  FVC_ERR_UNSUPPORTED for other
+ * codes, FVC_PREC_MIXED, matriz 2, or an off-diagonal pattern that is not
+ * symmetric (every cell-adjacency structure of the reference is). */
+int32_t fvc_solve_transposed(fvc_context *ctx, int32_t code, const double *d_b,
+                             double *d_x, double tol, int32_t maxit,
+                             const fvc_opts *opts, fvc_stats *stats);
+
 /* fvc_matrix_update_values without the wait: the copies and the value
  * gather are enqueued on the context's stream.  With DEVICE value arrays the
  * call can be recorded in a CUDA stream capture on that stream. */

@@ -86,3 +86,34 @@ def test_gradcheck_small_system(orc):
     assert torch.autograd.gradcheck(lambda ad, au, bb: linear_solve(ad, au, bb, sysg), inputs,
                                     eps=1e-6, atol=1e-6, rtol=1e-5)
     sysg.close()
+
+
+@pytest.mark.parametrize("kind,nx", [("mixed", 6), ("tri", 20), ("quad", 40)])
+def test_transposed_solve_over_stored_matrix(orc, kind, nx):
+    # fvc_solve_transposed: A^T x = b by BiCGSTAB through the mirror slots
+    # of A's own storage, against a direct solve of the transposed matrix
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spla
+    import torch
+    from fortranfvcell_gb300 import Context, make_opts, mesh
+    s = unsymmetric(pressure(orc, mesh.square_mesh(nx, kind=kind, jitter=0.2, seed=nx), 1, True),
+                    seed=nx)
+    n, nad = s["n"], s["nad"]
+    rows = np.repeat(np.arange(n), np.diff(s["ia"]))
+    A = sp.csr_matrix((s["au"][:nad], (rows, s["ja"][:nad] - 1)), shape=(n, n)) + sp.diags(s["ad"])
+    b = np.random.default_rng(nx).uniform(-1, 1, n)
+    x_ref = spla.spsolve(A.T.tocsc(), b)
+    ctx = Context()
+    ctx.set_matrix(1, True, n, nad, s["ad"], s["au"], s["au"], s["ia"], s["ja"])
+    x = torch.zeros(n, dtype=torch.float64, device="cuda")
+    st = ctx.solve_transposed(torch.from_numpy(b).cuda(), x, 1e-12, 10000,
+                              make_opts("fp64", init=1))
+    assert st.status == 0 and st.iterations > 0
+    err = np.linalg.norm(x.cpu().numpy() - x_ref) / np.linalg.norm(x_ref)
+    assert err < 1e-9, err
+    # the same context still solves A x = b
+    x2 = torch.zeros_like(x)
+    ctx.solve(2, torch.from_numpy(b).cuda(), x2, 1e-12, 10000, make_opts("fp64", init=1))
+    x2_ref = spla.spsolve(A.tocsc(), b)
+    assert np.linalg.norm(x2.cpu().numpy() - x2_ref) <= 1e-9 * np.linalg.norm(x2_ref)
+    ctx.close()
