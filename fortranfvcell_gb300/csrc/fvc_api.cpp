@@ -562,16 +562,20 @@ int32_t fvc_solve_async(fvc_context *c, int32_t code, const double *d_b, double 
     o = *opts;
   else
     fvc_opts_default(&o);
-  if (o.precision != FVC_PREC_FP64) return FVC_ERR_UNSUPPORTED;
+  const bool mixed = o.precision == FVC_PREC_MIXED;
+  if (o.precision != FVC_PREC_FP64 && !mixed) return FVC_ERR_UNSUPPORTED;
   const int matriz = c->matriz;
   if (code < 1 || code > 3) return FVC_ERR_UNSUPPORTED;
   if ((code == 2 || code == 3) && matriz == 2) return FVC_ERR_UNSUPPORTED;
-  if (code == 3 && matriz == 4) return FVC_ERR_UNSUPPORTED;
+  if (code == 3 && (matriz == 4 || mixed)) return FVC_ERR_UNSUPPORTED;
   cudaSetDevice(c->device);
   const int init = (o.init < 0) ? default_init(code, matriz) : (o.init ? 1 : 0);
-  int32_t rc = fvc::enqueue_solve(c->A, c->S, code, d_b, d_x, tol, maxit, init, o, c->stream, true);
+  int32_t rc = mixed ? fvc::enqueue_mixed(c->A, c->S, code, d_b, d_x, tol, maxit, init, o,
+                                          c->stream, true)
+                     : fvc::enqueue_solve(c->A, c->S, code, d_b, d_x, tol, maxit, init, o,
+                                          c->stream, true);
   if (rc != FVC_OK) return rc;
-  return fvc::launch_solve_status(c->S, d_status, c->stream);
+  return fvc::launch_solve_status(c->S, d_status, c->stream, mixed);
 }
 
 int32_t fvc_autotune(fvc_context *c, int32_t code, int32_t precision, int32_t trial_its,
@@ -926,8 +930,10 @@ namespace fvc {
 
 int32_t context_prepare(fvc_context *c, int code, const fvc_opts &o) {
   if (!c || !c->has_matrix) return FVC_ERR_ARG;
-  if (o.precision != FVC_PREC_FP64) return FVC_ERR_UNSUPPORTED;
   cudaSetDevice(c->device);
+  if (o.precision == FVC_PREC_MIXED)
+    return enqueue_mixed(c->A, c->S, code, nullptr, nullptr, 0.0, 1, 0, o, c->stream, false);
+  if (o.precision != FVC_PREC_FP64) return FVC_ERR_UNSUPPORTED;
   return enqueue_solve(c->A, c->S, code, nullptr, nullptr, 0.0, 1, 0, o, c->stream, false);
 }
 

@@ -35,6 +35,7 @@ struct DeviceMatrix {
   bool col16_ok = false;
   int ell_w = 0;             // FP32 copy padded to this uniform slice width (0: SELL)
   bool have32 = false;
+  bool layout32 = false;     // the FP32 layout (col16_ok, ell_w, buffers) is decided
   int cl_smax = -1;          // cluster PCG: most slots of one CTA's rows (-1: unknown)
   int *mirror = nullptr;     // per slot: the slot of the transposed entry (built on demand)
   // host-side description of the source layout, for value updates
@@ -107,8 +108,9 @@ int32_t enqueue_solve(const DeviceMatrix &A, Scratch &S, int code, const double 
                       double tol, int maxit, int init, const fvc_opts &o, cudaStream_t stream,
                       bool launch);
 // out[0..3] = status, iterations, inner iterations, timeout flag of the
-// solve enqueued last on S
-int32_t launch_solve_status(const Scratch &S, int32_t *out, cudaStream_t stream);
+// solve enqueued last on S (mixed: the iterations are the FP32 ones)
+int32_t launch_solve_status(const Scratch &S, int32_t *out, cudaStream_t stream,
+                            bool mixed = false);
 // Batched PCG / BiCGSTAB of the block-diagonal matrix A (fvc_krylov.cu):
 // codes (1 PCG, 2 BiCGSTAB), tols and its_hint (expected iterations, for
 // the share of blocks) per system may be null (all PCG, all tol, sqrt of
@@ -118,6 +120,11 @@ int32_t run_krylov_batched(DeviceMatrix &A, Scratch &S, int nsys,
                            const double *its_hint, const int32_t *inits, const double *b,
                            double *x, double tol, int maxit, const fvc_opts &o,
                            cudaStream_t stream, fvc_stats *st);
+// A mixed solve enqueued without waiting (launch = false: allocations,
+// the FP32 layout and operator only, for a later captured call)
+int32_t enqueue_mixed(const DeviceMatrix &A, Scratch &S, int code, const double *b, double *x,
+                      double tol, int maxit, int init, const fvc_opts &o, cudaStream_t stream,
+                      bool launch);
 int32_t run_mixed(const DeviceMatrix &A, Scratch &S, int code, const double *b,
                   double *x, double tol, int maxit, int init, const fvc_opts &o,
                   cudaStream_t stream, fvc_stats *st);

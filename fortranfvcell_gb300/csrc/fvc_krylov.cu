@@ -806,9 +806,9 @@ int32_t run_persistent(K kernel, const DeviceMatrix &A, Scratch &S, const double
 
 // status, iterations, inner iterations and the timeout flag of the solve
 // that ran last on this scratch, copied where a captured graph can read them
-__global__ void solve_status_kernel(const int *iresult, const int *err, int32_t *out) {
+__global__ void solve_status_kernel(const int *iresult, const int *err, int32_t *out, int mixed) {
   out[0] = (*err != 0) ? (int32_t)FVC_ERR_TIMEOUT : iresult[1];
-  out[1] = iresult[0];
+  out[1] = mixed ? iresult[2] : iresult[0];
   out[2] = iresult[2];
   out[3] = *err;
 }
@@ -870,9 +870,9 @@ int32_t enqueue_solve(const DeviceMatrix &A, Scratch &S, int code, const double 
   return FVC_ERR_UNSUPPORTED;
 }
 
-int32_t launch_solve_status(const Scratch &S, int32_t *out, cudaStream_t stream) {
+int32_t launch_solve_status(const Scratch &S, int32_t *out, cudaStream_t stream, bool mixed) {
   if (!S.iresult || !S.err || !out) return FVC_ERR_ARG;
-  solve_status_kernel<<<1, 1, 0, stream>>>(S.iresult, S.err, out);
+  solve_status_kernel<<<1, 1, 0, stream>>>(S.iresult, S.err, out, mixed ? 1 : 0);
   count_launch();
   return cudaPeekAtLastError() == cudaSuccess ? FVC_OK : FVC_ERR_CUDA;
 }

@@ -837,9 +837,11 @@ int32_t iterate_graph(fvc_simple *s, int32_t nit, double *res, int32_t *its, int
         launched += (r.ran[k] ? s->launches_run[k] : 0) + (r.ok[k] ? s->launches_ok[k] : 0);
         if (r.ran[k] && !r.ok[k]) {
           fvc::count_launch(launched);
-          fprintf(stderr, "fvcgpu: SIMPLE %s solve (code %d, fp64) ended with status %d after %d "
+          const fvc_opts so = solve_opts(s, k == 2 ? s->ctx_pc : s->ctx_u);
+          fprintf(stderr, "fvcgpu: SIMPLE %s solve (code %d, %s) ended with status %d after %d "
                           "iterations\n", kSysName[k],
-                  k < 2 ? s->o.code_u : k == 2 ? s->o.code_pc : 2, r.st[k][0], r.st[k][1]);
+                  k < 2 ? s->o.code_u : k == 2 ? s->o.code_pc : 2,
+                  so.precision == FVC_PREC_MIXED ? "mixed" : "fp64", r.st[k][0], r.st[k][1]);
           return r.st[k][0];
         }
       }
@@ -873,9 +875,6 @@ extern "C" {
 
 int32_t fvc_simple_set_graph(fvc_simple *s, int32_t on) {
   if (!s) return FVC_ERR_ARG;
-  const bool fp64 = s->o.precision == FVC_PREC_FP64 &&
-                    (s->o.precision_u < 0 || s->o.precision_u == FVC_PREC_FP64);
-  if (on && !fp64) return FVC_ERR_UNSUPPORTED;
   s->use_graph = on != 0;
   if (!on) drop_graph(s);
   return FVC_OK;

@@ -168,16 +168,18 @@ int32_t fvc_solve_transposed(fvc_context *ctx, int32_t code, const double *d_b,
 int32_t fvc_matrix_update_values_async(fvc_context *ctx, const double *ad,
                                        const double *au, const double *al);
 
-/* fvc_solve without the wait, for CUDA graphs: the same FP64 kernels, and
- * so the same results, enqueued on the context's stream.  The call makes no
+/* fvc_solve without the wait, for CUDA graphs: the same kernels, and so
+ * the same results, enqueued on the context's stream.  The call makes no
  * host-device copy and no synchronisation, so it can be recorded in a
  * stream capture on that stream and replayed.  When the solve has run,
  * d_status (DEVICE, 4 int32) holds the FVC_* status, the iterations, the
  * inner iterations (GMRES steps) and 1 if an on-device wait gave up
- * (status FVC_ERR_TIMEOUT).  The first call for a context and launch shape
- * allocates work buffers, so it must not be the captured one.  Returns
- * FVC_OK once the work is enqueued; FVC_ERR_UNSUPPORTED for FVC_PREC_MIXED
- * and for the (code, matriz) pairs fvc_solve rejects. */
+ * (status FVC_ERR_TIMEOUT); with FVC_PREC_MIXED the iterations are the FP32
+ * ones.  The first call for a context, precision and launch shape allocates
+ * work buffers (and lays out the FP32 operator), so it must not be the
+ * captured one.  Returns FVC_OK once the work is enqueued;
+ * FVC_ERR_UNSUPPORTED for mixed GMRES and for the (code, matriz) pairs
+ * fvc_solve rejects. */
 int32_t fvc_solve_async(fvc_context *ctx, int32_t code, const double *d_b,
                         double *d_x, double tol, int32_t maxit,
                         const fvc_opts *opts, int32_t *d_status);
@@ -571,9 +573,8 @@ int32_t fvc_simple_iterate(fvc_simple *s, int32_t nit, double *res, int32_t *its
  * uncaptured loop.  A failed solve stops the solves of the rest of the
  * batch; the call returns its status with the fields as the failing
  * iteration left them, as the uncaptured loop does.  on = 0 returns to
- * individual launches.  FVC_ERR_UNSUPPORTED when a system is solved in
- * FVC_PREC_MIXED.  No counterpart in the reference, whose outer loop runs
- * on the host. */
+ * individual launches.  No counterpart in the reference, whose outer loop
+ * runs on the host. */
 int32_t fvc_simple_set_graph(fvc_simple *s, int32_t on);
 
 /* Starts a new time step: w0 = w and the time term from the current fields
