@@ -117,3 +117,40 @@ def test_transposed_solve_over_stored_matrix(orc, kind, nx):
     x2_ref = spla.spsolve(A.tocsc(), b)
     assert np.linalg.norm(x2.cpu().numpy() - x2_ref) <= 1e-9 * np.linalg.norm(x2_ref)
     ctx.close()
+
+
+def test_transposed_and_batched_edge_cases(orc):
+    # unsupported requests return FVC_ERR_UNSUPPORTED without touching x:
+    # a transposed solve on a pattern that is not symmetric, or by PCG or
+    # mixed precision; a batched solver code other than PCG / BiCGSTAB.
+    # The autotuner runs on a one-row system.
+    import torch
+    from fortranfvcell_gb300 import Context, FvcError, _lib, make_opts
+    # 3 rows, entries (1,2) and (2,3) only: no mirror for either
+    ia = np.array([1, 2, 3, 3], np.int32)
+    ja = np.array([2, 3], np.int32)
+    ad, au = np.array([4.0, 4.0, 4.0]), np.array([-1.0, -1.0])
+    ctx = Context()
+    ctx.set_matrix(1, True, 3, 2, ad, au, au, ia, ja)
+    b = torch.ones(3, dtype=torch.float64, device="cuda")
+    x = torch.full((3,), 7.0, dtype=torch.float64, device="cuda")
+    for opts in (make_opts("fp64", init=1), make_opts("mixed", init=1)):
+        with pytest.raises(FvcError) as e:
+            ctx.solve_transposed(b, x, 1e-10, 100, opts)
+        assert e.value.status == _lib.FVC_ERR_UNSUPPORTED
+    assert bool(torch.all(x == 7.0))
+    # the forward solve of the same matrix still works
+    st = ctx.solve(2, b, x, 1e-12, 100, make_opts("fp64", init=1))
+    assert st.status == 0
+    rs = np.array([0, 32], np.int32)     # one system padded to 32 rows is not this matrix
+    with pytest.raises(FvcError):
+        ctx.solve_batched(np.array([0, 3], np.int32), b, x, 1e-10, 100, codes=[3])
+    with pytest.raises(ValueError):
+        ctx.solve_batched(rs, b, x, 1e-10, 100, codes=[1, 2])
+    ctx.close()
+    one = Context()
+    one.set_matrix(1, True, 1, 0, np.array([2.0]), np.zeros(1), np.zeros(1),
+                   np.array([1, 1], np.int32), np.zeros(1, np.int32))
+    o, us = one.autotune(1, "fp64", 5)
+    assert us > 0.0
+    one.close()

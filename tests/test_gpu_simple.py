@@ -184,6 +184,8 @@ def test_loop_exports_the_systems_it_solves(orc):
         np.testing.assert_allclose(ad, rad, rtol=1e-13, atol=0)
         np.testing.assert_allclose(au, rau[:au.size], rtol=1e-13, atol=1e-300)
         np.testing.assert_allclose(b, rb, rtol=1e-13, atol=1e-13 * np.abs(rb).max())
-    with pytest.raises(Exception):
-        loop.system(4)                     # no energy equation in this loop
+    from fortranfvcell_gb300 import FvcError
+    for bad in (4, 0, 5):                  # 4: no energy equation in this loop
+        with pytest.raises(FvcError):
+            loop.system(bad)
     loop.close()
