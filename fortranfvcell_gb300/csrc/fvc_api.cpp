@@ -619,10 +619,12 @@ int32_t fvc_autotune(fvc_context *c, int32_t code, int32_t precision, int32_t tr
     cand.push_back(o);
   }
   if (precision == FVC_PREC_MIXED && code == 1) {
-    fvc_opts o = base;
-    o.block_threads = 1024;
-    o.staging = 1;
-    cand.push_back(o);
+    for (int stg : {1, 2}) {  // plain loads; staged copies at any size
+      fvc_opts o = base;
+      o.block_threads = 1024;
+      o.staging = stg;
+      cand.push_back(o);
+    }
   }
   int32_t rc = FVC_OK;
   double best_t = 0.0;

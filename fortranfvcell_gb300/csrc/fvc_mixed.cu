@@ -534,6 +534,7 @@ __device__ __forceinline__ void cg_phase_b(const MArgs &a, const MPart &P, float
 // them).  A chunk with more than kStSlotCap slots (mean row width above 5)
 // reads its weights and offsets from global memory instead.
 constexpr int kStChunkSlices = 32;
+constexpr int kStagedRows = 524288;              // staged CG from this many rows
 constexpr int kStRows = kStChunkSlices * kSlice;  // = threads per block
 constexpr int kStSlotCap = kStRows * 5;
 constexpr int kWinHalo = 3;                      // gathers from chunks i-3 .. i+3
@@ -1415,8 +1416,13 @@ int32_t enqueue_mixed(const DeviceMatrix &A0, Scratch &S, int code, const double
   if (rc != FVC_OK) return rc;
   if ((rc = ensure_f32_vectors(S, (size_t)A.n)) != FVC_OK) return rc;
   const int threads = block_threads_for(o.block_threads, A.nslices, sm_count_m());
-  // CG streams through shared-memory stages when its layout allows
-  const bool staged = code == 1 && threads == kStRows && A.col16_ok && o.staging == 0;
+  // CG streams through shared-memory stages when its layout allows and
+  // each block owns enough 1024-row chunks to fill the pipeline beside its
+  // +-3-chunk window; below, plain loads are faster (per iteration on
+  // GB300, staged vs plain: 262k rows 16.5 vs 14.1 us, 1.05M 28.9 vs
+  // 28.6 us, 4.19M 87 vs 122 us)
+  const bool staged = code == 1 && threads == kStRows && A.col16_ok &&
+                      (o.staging == 2 || (o.staging == 0 && A.n >= kStagedRows));
   auto kern = (code != 1) ? mixed_bicgstab
               : !staged        ? mixed_cg
               : A.ell_w == 4   ? mixed_cg_staged_w4

@@ -92,7 +92,9 @@ typedef struct {
   int32_t staging;     /* MIXED CG: 0 streams the iteration's arrays through
                           shared memory with bulk asynchronous copies when
                           the layout allows (1024 threads, 16-bit column
-                          offsets); 1: plain loads                        */
+                          offsets) and the system has 524288 rows or more;
+                          1: plain loads; 2: staged whenever the layout
+                          allows                                           */
   int32_t max_blocks;  /* cap on the persistent grid (0 -> automatic)      */
 } fvc_opts;
 
@@ -189,8 +191,8 @@ int32_t fvc_solve_async(fvc_context *ctx, int32_t code, const double *d_b,
  * over the shapes the kernels support -- the automatic choice (a thread-
  * block cluster for a PCG system of at most 8192 rows, else one block per
  * SM with the fewest warps that cover the rows), 128..1024 threads per
- * block, a cap of 16/38/76 blocks, and for mixed CG plain loads instead of
- * the staged copies -- and writes the fastest per iteration to *best (init
+ * block, a cap of 16/38/76 blocks, and for mixed CG plain loads or the
+ * staged copies at 1024 threads -- and writes the fastest per iteration to *best (init
  * -1, the rest as fvc_opts_default) and its time to *best_us (may be NULL).
  * Pass *best to fvc_solve for later solves of this matrix and method.  The
  * shape changes only the summation order of the reductions, so results

@@ -1,7 +1,8 @@
 """Mixed-precision CG: the kernel that streams its arrays through shared
-memory with bulk asynchronous copies (the default) against the plain-load
-kernel of the same arithmetic.  Both must give the same iterates bit for
-bit: the staging changes where the operands come from, not the sums."""
+memory with bulk asynchronous copies (staging 2 here; the default from
+524288 rows) against the plain-load kernel of the same arithmetic.  Both
+must give the same iterates bit for bit: the staging changes where the
+operands come from, not the sums."""
 import numpy as np
 import pytest
 
@@ -40,7 +41,7 @@ def _solve_both(s, b, tol=1e-8):
     ctx = Context()
     ctx.set_matrix(1, True, n, s["nad"], s["ad"], s["au"], s["au"], s["ia"], s["ja"])
     out = []
-    for staging in (1, 0):
+    for staging in (1, 2):
         bd, xd = torch_dev(b), torch_dev(np.zeros(n))
         st = ctx.solve(1, bd, xd, tol, 200000, make_opts("mixed", init=1, staging=staging))
         out.append((st, xd.cpu().numpy()))
