@@ -881,20 +881,44 @@ __device__ __forceinline__ void issue_b(const MArgs &a, const MPart &P, unsigned
   }
 }
 
+// Lane 0 of warp 0: the first phase-B stages.  Every array they copy holds
+// this block's own rows (written by this block before the __syncthreads
+// that ended phase A) or constants, so they may be issued before the grid
+// reduction that separates the phases, which then hides their latency.
+template <bool kPair, bool kUpdE>
+__device__ __forceinline__ void prefetch_b(const MArgs &a, const MPart &P, const Dir &d,
+                                           unsigned char *smem, const StCount &cnt) {
+  if (P.warp == 0 && P.lane == 0) {
+    fence_proxy_async_global();
+    fence_proxy_async_smem();
+    const int nch = st_chunks(P);
+    for (int j = 0; j < kBStages - 1 && j < nch; ++j)
+      issue_b<kPair, kUpdE>(a, P, smem, cnt.sb + j, j, d);
+  }
+}
+
+// The prefetched stages complete before the block may leave (a grid
+// reduction that gave up): a bounded wait on each.
+__device__ __forceinline__ void drain_prefetch_b(const MPart &P, unsigned char *smem,
+                                                 const StCount &cnt) {
+  StHdr *H = reinterpret_cast<StHdr *>(smem);
+  const int nch = st_chunks(P);
+  for (int j = 0; j < kBStages - 1 && j < nch; ++j) {
+    const uint32_t seq = cnt.sb + (uint32_t)j;
+    mbar_drain(&H->sb[seq % kBStages], (seq / kBStages) & 1u);
+  }
+}
+
 // Staged phase B: the arithmetic of cg_phase_b, one row per thread.
+// pre: prefetch_b has issued the first stages already
 template <bool kPair, bool kUpdE>
 __device__ __forceinline__ void cg_phase_b_st(const MArgs &a, const MPart &P, float a1,
                                               float a1_lo, float alpha, float alpha_lo,
                                               const Dir &d, CSum &crz, CSum &crr,
-                                              unsigned char *smem, StCount &cnt) {
+                                              unsigned char *smem, StCount &cnt, bool pre) {
   StHdr *H = reinterpret_cast<StHdr *>(smem);
   const int nch = st_chunks(P);
-  if (P.warp == 0 && P.lane == 0) {
-    fence_proxy_async_global();
-    fence_proxy_async_smem();
-    for (int j = 0; j < kBStages - 1 && j < nch; ++j)
-      issue_b<kPair, kUpdE>(a, P, smem, cnt.sb + j, j, d);
-  }
+  if (!pre) prefetch_b<kPair, kUpdE>(a, P, d, smem, cnt);
   for (int i = 0; i < nch; ++i) {
     if (P.warp == 0 && P.lane == 0 && i + kBStages - 1 < nch)
       issue_b<kPair, kUpdE>(a, P, smem, cnt.sb + i + kBStages - 1, i + kBStages - 1, d);
@@ -992,6 +1016,12 @@ __device__ __forceinline__ void mixed_cg_body(const MArgs &a) {
                         : cg_phase_a_st<false, kW>(a, P, bh, bl, d, st_smem, gch);
     else
       pq[0] = (it == 1) ? cg_phase_a<true>(a, P, bh, bl, d) : cg_phase_a<false>(a, P, bh, bl, d);
+    if (kStaged) {  // phase B's first copies before the wait
+      if (pending)
+        prefetch_b<true, true>(a, P, d, st_smem, gch);
+      else
+        prefetch_b<true, false>(a, P, d, st_smem, gch);
+    }
     if (!grid_allreduce_ff<1>(a.gs, ep, pq, red2, [&](const double *t) {
           const double alpha_d = sh.rz / t[0];
           sh.alpha = alpha_d;
@@ -999,8 +1029,10 @@ __device__ __forceinline__ void mixed_cg_body(const MArgs &a) {
           sh.alpha_lo = (float)(alpha_d - (double)sh.alpha_f);
           sh.a1 = (float)sh.pend_alpha;
           sh.a1_lo = (float)(sh.pend_alpha - (double)sh.a1);
-        }))
+        })) {
+      if (kStaged) drain_prefetch_b(P, st_smem, gch);
       return;
+    }
     const float alpha = sh.alpha_f, alpha_lo = sh.alpha_lo;
     const float a1 = sh.a1, a1_lo = sh.a1_lo;
     // rs -= alpha q ; z = rs/m ; rs.z ; rs.rs ; every second iteration also
@@ -1009,10 +1041,10 @@ __device__ __forceinline__ void mixed_cg_body(const MArgs &a) {
     if (kStaged) {
       if (pending)
         cg_phase_b_st<true, true>(a, P, a1, a1_lo, alpha, alpha_lo, d, acc[0], acc[1], st_smem,
-                                  gch);
+                                  gch, true);
       else
         cg_phase_b_st<true, false>(a, P, a1, a1_lo, alpha, alpha_lo, d, acc[0], acc[1], st_smem,
-                                   gch);
+                                   gch, true);
     } else if (pending) {
       cg_phase_b<true, true>(a, P, a1, a1_lo, alpha, alpha_lo, d, acc[0], acc[1]);
     } else {

@@ -81,6 +81,17 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *e
   }
 }
 
+// Waits for the copies an mbarrier phase counts even when the error word is
+// set (before a block leaves with copies in flight); bounded by the same
+// time limit.  Returns false if they did not arrive in time.
+__device__ __forceinline__ bool mbar_drain(uint64_t *bar, uint32_t parity) {
+  const uint64_t t0 = global_ns();
+  for (unsigned int spins = 0;; ++spins) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((spins & 63u) == 63u && global_ns() - t0 > kBarrierTimeoutNs) return false;
+  }
+}
+
 // Orders this thread's earlier (generic-proxy) view of global memory --
 // including what the last grid barrier acquired -- before its later bulk
 // copies.
