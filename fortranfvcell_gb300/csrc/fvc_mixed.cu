@@ -678,13 +678,41 @@ __device__ __forceinline__ void p_form(float *ring, int r, int R0, int Rend, int
   }
 }
 
+// Lane 0 of warp 0: the first phase-A stages of a uniform-width layout.
+// They copy matrix weights and offsets only (constants), so they may be
+// issued before the grid reduction that ends phase B; the next phase A
+// then finds them in flight (pre = true).
+template <int kW>
+__device__ __forceinline__ void prefetch_a(const MArgs &a, const MPart &P, unsigned char *smem,
+                                           const StCount &cnt) {
+  if (P.warp == 0 && P.lane == 0) {
+    fence_proxy_async_smem();
+    const int nch = st_chunks(P);
+    for (int j = 0; j < kAStages - 1 && j < nch; ++j)
+      issue_slots_u<kW>(a, P, smem, cnt.sa + (uint32_t)j, j);
+  }
+}
+
+// The prefetched phase-A stages complete before the block leaves the loop
+// without a phase A to consume them (stop, maxit, a reduction that gave up).
+__device__ __forceinline__ void drain_prefetch_a(const MPart &P, unsigned char *smem,
+                                                 const StCount &cnt) {
+  StHdr *H = reinterpret_cast<StHdr *>(smem);
+  const int nch = st_chunks(P);
+  for (int j = 0; j < kAStages - 1 && j < nch; ++j) {
+    const uint32_t seq = cnt.sa + (uint32_t)j;
+    mbar_drain(&H->sa[seq % kAStages], (seq / kAStages) & 1u);
+  }
+}
+
 // Staged phase A: p = z + beta p_prev, q = A p_hi, returns p_hi.q.  Same
 // arithmetic, in the same order, as cg_phase_a.  kW > 0: every slice has
 // width kW (slot offsets follow from the slice index; no slice-pointer
 // loads, no capacity check, fixed unrolled row loop); kW == 0: general.
 template <bool kFirst, int kW>
 __device__ __forceinline__ CSum cg_phase_a_st(const MArgs &a, const MPart &P, float bh, float bl,
-                                              const Dir &d, unsigned char *smem, StCount &cnt) {
+                                              const Dir &d, unsigned char *smem, StCount &cnt,
+                                              bool pre = false) {
   StHdr *H = reinterpret_cast<StHdr *>(smem);
   CSum cpq;
   const int nch = st_chunks(P);
@@ -703,7 +731,7 @@ __device__ __forceinline__ CSum cg_phase_a_st(const MArgs &a, const MPart &P, fl
       for (int j = kWinHalo + 1; j <= jlast && j <= kWinHalo + kLandAhead; ++j)
         issue_land<kFirst>(a, P, smem, cnt.land + (j - kWinHalo - 1), j, nrows, d);
     }
-    for (int j = 0; j < kAStages - 1 && j < nch; ++j) {
+    for (int j = 0; j < kAStages - 1 && j < nch && !(kW > 0 && pre); ++j) {
       if (kW > 0) {
         if (P.lane == 0) issue_slots_u<kW>(a, P, smem, cnt.sa + j, j);
       } else {
@@ -1002,6 +1030,7 @@ __device__ __forceinline__ void mixed_cg_body(const MArgs &a) {
   float bh = 0.0f, bl = 0.0f;  // beta as an FP32 pair
   bool flip = false;           // which buffers hold p_prev / p this iteration
   bool pending = false;        // an alpha*p not yet added to e
+  bool a_pre = false;          // the next phase A's first stages are in flight
   while (status == FVC_ERR_NOCONV && it < a.maxit) {
     ++it;
     Dir d;
@@ -1012,10 +1041,11 @@ __device__ __forceinline__ void mixed_cg_body(const MArgs &a) {
     // p = z + beta p_prev (an FP32 pair); q = A p_hi; p_hi.q
     CSum pq[1];
     if (kStaged)
-      pq[0] = (it == 1) ? cg_phase_a_st<true, kW>(a, P, bh, bl, d, st_smem, gch)
-                        : cg_phase_a_st<false, kW>(a, P, bh, bl, d, st_smem, gch);
+      pq[0] = (it == 1) ? cg_phase_a_st<true, kW>(a, P, bh, bl, d, st_smem, gch, a_pre)
+                        : cg_phase_a_st<false, kW>(a, P, bh, bl, d, st_smem, gch, a_pre);
     else
       pq[0] = (it == 1) ? cg_phase_a<true>(a, P, bh, bl, d) : cg_phase_a<false>(a, P, bh, bl, d);
+    a_pre = false;
     if (kStaged) {  // phase B's first copies before the wait
       if (pending)
         prefetch_b<true, true>(a, P, d, st_smem, gch);
@@ -1052,6 +1082,10 @@ __device__ __forceinline__ void mixed_cg_body(const MArgs &a) {
     }
     const bool was_pending = pending;
     pending = !pending;
+    if (kStaged && kW > 0) {  // the next phase A's first matrix stages before the wait
+      prefetch_a<kW>(a, P, st_smem, gch);
+      a_pre = true;
+    }
     if (!grid_allreduce_ff<2>(a.gs, ep, acc, red2, [&](const double *t) {
           // the alpha*p of an iteration that did not update e is added later
           if (!was_pending) sh.pend_alpha = sh.alpha;
@@ -1071,16 +1105,20 @@ __device__ __forceinline__ void mixed_cg_body(const MArgs &a) {
             sh.rz = rz_new;
             sh.action = kContinue;
           }
-        }))
+        })) {
+      if (a_pre) drain_prefetch_a(P, st_smem, gch);
       return;
+    }
     int action = sh.action;
     if (action == kUpdate) {
       // reliable update: fold e (and a deferred alpha p) into x, recompute
       // the true residual in FP64
       fold_correction(a, pending ? d.ch : nullptr, pending ? d.cl : nullptr, sh.pend_alpha);
       pending = false;
-      if (!grid_barrier(a.gs, ep)) return;
-      if (!residual_sweep(a, ep, false, res, red)) return;
+      if (!grid_barrier(a.gs, ep) || !residual_sweep(a, ep, false, res, red)) {
+        if (a_pre) drain_prefetch_a(P, st_smem, gch);
+        return;
+      }
       if (threadIdx.x == 0) {
         const int u = ++sh.updates;
         const double relres = sqrt(res[0] / sh.scale);
@@ -1119,6 +1157,7 @@ __device__ __forceinline__ void mixed_cg_body(const MArgs &a) {
     bl = sh.beta_lo;
     flip = !flip;
   }
+  if (a_pre) drain_prefetch_a(P, st_smem, gch);
   if (mlead(a) && threadIdx.x == 0) {
     a.iresult[0] = sh.updates;
     a.iresult[1] = (status == FVC_ERR_NOCONV) ? sh.status : status;
