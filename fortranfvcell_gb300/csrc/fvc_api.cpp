@@ -59,9 +59,11 @@ struct fvc_context {
   // host-array solve buffers
   double *d_b = nullptr, *d_x = nullptr;
   size_t nvec = 0;
-  // drop-in structure cache key
+  // drop-in structure cache key: the arrays' addresses and host copies of
+  // their contents (compared with memcmp on every call)
   const void *key_iax = nullptr, *key_ja = nullptr;
-  uint64_t key_hash = 0;
+  std::vector<int32_t> key_ia_copy, key_ja_copy;
+  uint64_t key_shape = 0;
 };
 
 namespace {
@@ -691,13 +693,15 @@ int32_t fvc_solve_batched(fvc_context *c, int32_t nsys, const int32_t *row_start
 
 namespace {
 
-uint64_t fnv_hash(const int32_t *a, size_t n, uint64_t h) {
-  const uint64_t prime = 1099511628211ull;
-  for (size_t i = 0; i < n; ++i) {
-    h ^= (uint32_t)a[i];
-    h *= prime;
-  }
-  return h;
+// The cached structure is the caller's current one: same addresses, shape
+// and contents (an exact comparison; 18M indices of a 4M-cell system take a
+// few ms, where a serial hash of them took ~20 ms per call).
+bool same_structure(const fvc_context *c, const int32_t *iax, size_t ialen, const int32_t *ja,
+                    size_t jalen, uint64_t shape) {
+  return c->has_matrix && c->key_iax == iax && c->key_ja == ja && c->key_shape == shape &&
+         c->key_ia_copy.size() == ialen && c->key_ja_copy.size() == jalen &&
+         std::memcmp(c->key_ia_copy.data(), iax, sizeof(int32_t) * ialen) == 0 &&
+         (jalen == 0 || std::memcmp(c->key_ja_copy.data(), ja, sizeof(int32_t) * jalen) == 0);
 }
 
 std::mutex g_mutex;
@@ -714,17 +718,18 @@ int32_t solver_ex_ctx(fvc_context *c, double *ad, double *au, double *al, double
   // structure cache: same arrays and same contents -> only values move
   const size_t ialen = (matriz == 4) ? 2 : (size_t)neq + 1;
   const size_t jalen = (matriz == 4) ? (size_t)neq * (size_t)iax[0] : (size_t)std::max(nad, 0);
-  uint64_t h = fnv_hash(iax, ialen, 1469598103934665603ull);
-  h = fnv_hash(ja, jalen, h);
-  h ^= ((uint64_t)matriz << 56) ^ ((uint64_t)(unsym != 0) << 55) ^ ((uint64_t)neq << 20) ^ (uint64_t)nad;
+  const uint64_t shape = ((uint64_t)matriz << 56) ^ ((uint64_t)(unsym != 0) << 55) ^
+                         ((uint64_t)neq << 20) ^ (uint64_t)(uint32_t)nad;
   int32_t rc;
-  if (c->has_matrix && c->key_iax == iax && c->key_ja == ja && c->key_hash == h) {
+  if (same_structure(c, iax, ialen, ja, jalen, shape)) {
     rc = fvc_matrix_update_values(c, ad, au, al);
   } else {
     rc = fvc_matrix_set(c, matriz, unsym, neq, nad, ad, au, al, iax, ja);
     c->key_iax = iax;
     c->key_ja = ja;
-    c->key_hash = h;
+    c->key_shape = shape;
+    c->key_ia_copy.assign(iax, iax + ialen);
+    c->key_ja_copy.assign(ja, ja + jalen);
   }
   if (rc != FVC_OK) {
     c->key_iax = c->key_ja = nullptr;
