@@ -425,3 +425,39 @@ def test_autotune_returns_a_shape_that_solves(fvc, code, prec):
     # (BiCGSTAB, GMRES: about 1e-6 relative on this pinned p' system)
     tol = {1: 1e-8, 2: 1e-5, 3: 1e-5}[code] if prec == "fp64" else 1e-5
     assert np.linalg.norm(xs[0] - xs[1]) <= tol * np.linalg.norm(xs[1])
+
+
+def test_dropin_structure_cache_sees_in_place_changes(fvc, orc):
+    # the drop-in keeps a system's structure on the device between calls;
+    # a structure rewritten in place (same arrays, other contents) must be
+    # reloaded: solve system 1, overwrite its index arrays with system 2's
+    # (same sizes: two jittered meshes of one topology renumbered
+    # differently), solve again from the same buffers
+    from fortranfvcell_gb300 import mesh
+    m1 = mesh.square_mesh(12, kind="tri", jitter=0.2, seed=1)
+    s1 = pressure(orc, m1, 1, True)
+    rng = np.random.default_rng(0)
+    perm = rng.permutation(s1["n"])
+    # system 2: system 1 with its unknowns permuted (same nad, other ia/ja)
+    import scipy.sparse as sp
+    n, nad = s1["n"], s1["nad"]
+    rows = np.repeat(np.arange(n), np.diff(s1["ia"]))
+    A = sp.csr_matrix((s1["au"][:nad], (rows, s1["ja"][:nad] - 1)), shape=(n, n))
+    P = sp.csr_matrix((np.ones(n), (np.arange(n), perm)), shape=(n, n))
+    B = (P @ A @ P.T).tocsr()
+    B.sort_indices()
+    ia2 = (B.indptr + 1).astype(np.int32)
+    ja2 = (B.indices + 1).astype(np.int32)
+    au2 = B.data.copy()
+    ad2 = s1["ad"][perm].copy()
+    assert ja2.size == nad and not np.array_equal(ja2, s1["ja"][:nad])
+    b = rng.uniform(-1, 1, n)
+    ia, ja = s1["ia"].copy(), s1["ja"][:nad].copy()
+    ad, au = s1["ad"].copy(), s1["au"][:nad].copy()
+    x1 = np.zeros(n)
+    fvc.solver(ad, au, au, x1, b, ia, ja, n, nad, True, 1e-12, 50000, 1, 1)
+    ia[:], ja[:], ad[:], au[:] = ia2, ja2, ad2, au2     # in place: the same buffers
+    x2 = np.zeros(n)
+    fvc.solver(ad, au, au, x2, b[perm], ia, ja, n, nad, True, 1e-12, 50000, 1, 1)
+    # system 2 is system 1 renumbered: x2 = x1 permuted
+    assert np.linalg.norm(x2 - x1[perm]) <= 1e-9 * np.linalg.norm(x1)
