@@ -167,3 +167,36 @@ def test_solve_async_and_capture(nx, code):
     assert torch.equal(x3, x4)
     assert status.tolist()[:2] == [0, st4.iterations]
     ctx.close()
+
+
+def test_solve_async_mixed_and_tuner_rejections():
+    # fvc_solve_async with mixed precision equals fvc_solve (the FP32
+    # operator rebuilt by a stream-ordered kernel after a value upload);
+    # mixed GMRES is rejected by the async solve and by the tuner
+    import torch
+    from fortranfvcell_gb300 import FvcError, _lib, mesh
+    from fortranfvcell_gb300.solver import Context, make_opts
+    s = mesh.pressure_system(mesh.square_mesh(90, kind="mixed", jitter=0.2, seed=3), matriz=1,
+                             unsym=True, pin_cell=1)
+    n = s.neq
+    ctx = Context()
+    ctx.set_matrix(1, True, n, s.nad, s.ad, s.au, s.au, s.ia, s.ja)
+    b = torch.from_numpy(np.random.default_rng(2).uniform(-1, 1, n)).cuda()
+    o = make_opts("mixed", init=1)
+    x1, x2 = torch.zeros_like(b), torch.zeros_like(b)
+    st = ctx.solve(1, b, x1, 1e-9, 50000, o)
+    status = torch.zeros(4, dtype=torch.int32, device="cuda")
+    ad = torch.from_numpy(s.ad).cuda()
+    au = torch.from_numpy(s.au[:max(s.nad, 1)]).cuda()
+    ctx.update_values_async(ad, au, au)
+    ctx.solve_async(1, b, x2, 1e-9, 50000, status, o)
+    torch.cuda.synchronize()
+    assert torch.equal(x1, x2)
+    assert status.tolist()[:2] == [0, st.iterations]
+    with pytest.raises(FvcError) as e:
+        ctx.solve_async(3, b, x2, 1e-9, 100, status, o)
+    assert e.value.status == _lib.FVC_ERR_UNSUPPORTED
+    with pytest.raises(FvcError) as e:
+        ctx.autotune(3, "mixed", 5)
+    assert e.value.status == _lib.FVC_ERR_UNSUPPORTED
+    ctx.close()
