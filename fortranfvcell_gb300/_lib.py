@@ -117,6 +117,8 @@ SIGNATURES = {
     "fvc_matrix_update_values_async": ([P, P, P, P], I32),
     "fvc_solve_async": ([P, I32, P, P, F64, I32, C.POINTER(FvcOpts), P], I32),
     "fvc_autotune": ([P, I32, I32, I32, C.POINTER(FvcOpts), P], I32),
+    "fvc_set_solver_log": ([P, P], None),
+    "fvc_format_solver_log": ([I32, I32, F64, F64, P, I32], I32),
     "fvc_solve_transposed": ([P, I32, P, P, F64, I32, C.POINTER(FvcOpts),
                               C.POINTER(FvcStats)], I32),
     "fvc_solve": ([P, I32, P, P, F64, I32, C.POINTER(FvcOpts), C.POINTER(FvcStats)], I32),

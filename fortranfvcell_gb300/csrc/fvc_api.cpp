@@ -273,6 +273,49 @@ int32_t build_mirror(fvc_context *c) {
   return FVC_OK;
 }
 
+// v in Fortran Dw.d form (0.ddd...D+xx right-justified to w; a three-digit
+// exponent drops the D, as Fortran does)
+std::string fortran_d(double v, int w, int d) {
+  std::string body;
+  if (v == 0.0) {
+    body = std::string(std::signbit(v) ? "-" : "") + "0." + std::string((size_t)d, '0') + "D+00";
+  } else if (v != v) {
+    body = "NaN";
+  } else if (std::isinf(v)) {
+    body = v > 0 ? "Infinity" : "-Infinity";
+  } else {
+    char tmp[64];
+    std::snprintf(tmp, sizeof(tmp), "%.*e", d - 1, std::fabs(v));  // m.mmm e+XX
+    std::string m(tmp);
+    const size_t epos = m.find('e');
+    std::string digits = m.substr(0, epos);
+    digits.erase(std::remove(digits.begin(), digits.end(), '.'), digits.end());
+    const int e = std::atoi(m.c_str() + epos + 1) + 1;  // 0.ddd x 10^e
+    char ex[16];
+    if (std::abs(e) <= 99)
+      std::snprintf(ex, sizeof(ex), "D%c%02d", e >= 0 ? '+' : '-', std::abs(e));
+    else
+      std::snprintf(ex, sizeof(ex), "%c%03d", e >= 0 ? '+' : '-', std::abs(e));
+    body = std::string(v < 0 ? "-" : "") + "0." + digits + ex;
+  }
+  if ((int)body.size() < w) body.insert(0, (size_t)(w - (int)body.size()), ' ');
+  return body;
+}
+
+// The line src/Iterativos.f writes to unit 13 after a solve (:91-93,
+// :216-218, :429-431), format (a,a,i9,a,d20.10,a,d20.10)
+std::string solver_log_line(int code, int its, double energy, double tol) {
+  const char *label = code == 1 ? "PCG:       " : code == 2 ? "PBICGSTAB: " : "GMRES: ";
+  char it[16];
+  std::snprintf(it, sizeof(it), "%9d", its);
+  return std::string(label) + "it" + it + " energy norm " + fortran_d(energy, 20, 10) + " tol " +
+         fortran_d(tol, 20, 10);
+}
+
+std::mutex g_log_mutex;
+fvc_log_fn g_log_fn = nullptr;
+void *g_log_user = nullptr;
+
 int default_init(int code, int matriz) {
   // src/Solver.f with openmpSolver = .false. (or the OpenMP rule, below)
   static int omp = -1;
@@ -502,8 +545,10 @@ int32_t fvc_spmv_f32(fvc_context *c, const float *d_x, float *d_y) {
 }
 
 int32_t fvc_solve(fvc_context *c, int32_t code, const double *d_b, double *d_x, double tol,
-                  int32_t maxit, const fvc_opts *opts, fvc_stats *st) {
+                  int32_t maxit, const fvc_opts *opts, fvc_stats *st_out) {
   if (!c || !c->has_matrix || !d_b || !d_x || maxit < 1) return FVC_ERR_ARG;
+  fvc_stats local;
+  fvc_stats *st = st_out ? st_out : &local;
   fvc_opts o;
   if (opts)
     o = *opts;
@@ -527,7 +572,32 @@ int32_t fvc_solve(fvc_context *c, int32_t code, const double *d_b, double *d_x, 
     rc = fvc::run_gmres(c->A, c->S, d_b, d_x, tol, maxit, o, c->stream, st);
   }
   if (st && rc != st->status) st->status = rc;
+  fvc_log_fn fn;
+  void *user;
+  {
+    std::lock_guard<std::mutex> lk(g_log_mutex);
+    fn = g_log_fn;
+    user = g_log_user;
+  }
+  if (fn && rc != FVC_ERR_CUDA && rc != FVC_ERR_ARG)
+    fn(solver_log_line(code, st->iterations, st->energy, tol).c_str(), user);
   return rc;
+}
+
+void fvc_set_solver_log(fvc_log_fn fn, void *user) {
+  std::lock_guard<std::mutex> lk(g_log_mutex);
+  g_log_fn = fn;
+  g_log_user = user;
+}
+
+int32_t fvc_format_solver_log(int32_t code, int32_t iterations, double energy, double tol,
+                              char *buf, int32_t len) {
+  if (!buf || len < 1 || code < 1 || code > 3) return -FVC_ERR_ARG;
+  const std::string line = solver_log_line(code, iterations, energy, tol);
+  const int32_t n = (int32_t)std::min<size_t>(line.size(), (size_t)(len - 1));
+  std::memcpy(buf, line.data(), (size_t)n);
+  buf[n] = '\0';
+  return n;
 }
 
 int32_t fvc_solve_transposed(fvc_context *c, int32_t code, const double *d_b, double *d_x,
@@ -783,35 +853,6 @@ int32_t fvc_solver_ex(double *ad, double *au, double *al, double *x, const doubl
 // ---- drop-in entry: messages and STOP behaviour of the reference ---------
 namespace {
 
-// Fortran Dw.d edit descriptor (gfortran style: 0.ddddddD+ee, right-justified).
-std::string fortran_d(double v, int w, int d) {
-  char buf[64];
-  if (!std::isfinite(v)) {
-    snprintf(buf, sizeof buf, "%*s", w, std::isnan(v) ? "NaN" : (v > 0 ? "Infinity" : "-Infinity"));
-    return buf;
-  }
-  int e = 0;
-  double m = v;
-  if (v != 0.0) {
-    e = (int)std::floor(std::log10(std::fabs(v))) + 1;
-    m = v / std::pow(10.0, e);
-    // rounding may push |m| to 1.0: renormalise
-    double r = std::round(std::fabs(m) * std::pow(10.0, d)) / std::pow(10.0, d);
-    if (r >= 1.0) {
-      e += 1;
-      m = v / std::pow(10.0, e);
-    }
-  }
-  char mant[48];
-  snprintf(mant, sizeof mant, "%.*f", d, std::fabs(m));
-  std::string s = (v < 0 ? "-" : "");
-  s += mant;
-  char ex[16];
-  snprintf(ex, sizeof ex, "D%c%02d", e < 0 ? '-' : '+', std::abs(e));
-  s += ex;
-  if ((int)s.size() < w) s = std::string(w - s.size(), ' ') + s;
-  return s;
-}
 
 bool stop_on_error() {
   const char *e = getenv("FVC_STOP_ON_ERROR");

@@ -261,6 +261,33 @@ def _addr(t) -> int:
     return int(t)
 
 
+_LOG_FN = C.CFUNCTYPE(None, C.c_char_p, C.c_void_p)
+_log_keep = None
+
+
+def set_solver_log(fn=None) -> None:
+    """fn(line: str) receives, after every solve, the line the reference
+    writes to its unit-13 solver log (src/Iterativos.f:91-93); None stops."""
+    global _log_keep
+    L = _lib.load()
+    if fn is None:
+        L.fvc_set_solver_log(None, None)
+        _log_keep = None
+        return
+    _log_keep = _LOG_FN(lambda line, user: fn(line.decode()))
+    L.fvc_set_solver_log(C.cast(_log_keep, C.c_void_p), None)
+
+
+def format_solver_log(code: int, iterations: int, energy: float, tol: float) -> str:
+    """The reference's unit-13 line for the given values."""
+    buf = C.create_string_buffer(128)
+    n = _lib.load().fvc_format_solver_log(int(code), int(iterations), float(energy), float(tol),
+                                          buf, 128)
+    if n < 0:
+        raise FvcError(-n, "fvc_format_solver_log failed")
+    return buf.value.decode()
+
+
 def kernel_launches() -> int:
     return int(_lib.load().fvc_kernel_launches())
 

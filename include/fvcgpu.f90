@@ -87,6 +87,14 @@ module fvcgpu
        type(fvc_stats)    :: stats
      end function fvc_solver_ex
 
+     ! after each solve fn(line, user) receives the reference's unit-13
+     ! line (a NUL-terminated C string); c_null_funptr turns it off
+     subroutine fvc_set_solver_log(fn, user) bind(C, name="fvc_set_solver_log")
+       import :: c_funptr, c_ptr
+       type(c_funptr), value :: fn
+       type(c_ptr), value    :: user
+     end subroutine fvc_set_solver_log
+
      ! ---- the SIMPLE outer iteration on the GPU (fvc_simple_* of fvcgpu.h)
      subroutine fvc_simple_opts_default(opts) bind(C, name="fvc_simple_opts_default")
        import :: fvc_simple_opts

@@ -273,6 +273,22 @@ int32_t fvc_solve_history(const fvc_context *ctx, int32_t max, float *relres);
 int32_t fvc_matrix_info(const fvc_context *ctx, int64_t *n, int64_t *slots,
                         int64_t *nnz_off, int64_t *nslices);
 
+/* ---- the reference's solver log --------------------------------------- */
+/* After each solve (fvc_solver, solver_, fvc_solver_ex, fvc_solve) fn
+ * receives the line the reference writes to its unit-13 solver log
+ * (src/Iterativos.f:91-93, 216-218, 429-431; format
+ * (a,a,i9,a,d20.10,a,d20.10)), e.g.
+ * "PCG:       it      123 energy norm   0.1234567890D+01 tol   0.1000000000D-07".
+ * The iterations and energy are those of fvc_stats.  NULL turns it off.
+ * The callback runs on the calling thread, after the solve has ended. */
+typedef void (*fvc_log_fn)(const char *line, void *user);
+void fvc_set_solver_log(fvc_log_fn fn, void *user);
+
+/* The same line for given values into buf (len bytes, NUL-terminated;
+ * 96 suffice).  Returns its length, or -FVC_ERR_ARG. */
+int32_t fvc_format_solver_log(int32_t code, int32_t iterations, double energy,
+                              double tol, char *buf, int32_t len);
+
 /* Number of kernels this library launched since load (instrumentation). */
 int64_t fvc_kernel_launches(void);
 

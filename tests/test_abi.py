@@ -75,3 +75,18 @@ def test_fortran_derived_types_match_the_c_structs(fvc):
             t, names = line.split("::")
             fields += [(n.strip(), kind[t.strip()]) for n in names.split(",")]
         assert fields == [(n, t) for n, t in cls._fields_], ftype
+
+
+def test_solver_log_line_matches_fortran_format(fvc):
+    # the reference's unit-13 line, format (a,a,i9,a,d20.10,a,d20.10)
+    # (src/Iterativos.f:91-93): labels, an i9 count and two D20.10 fields,
+    # checked against an independent Fortran E-format writer
+    from fortranfvcell_gb300.io import fortran_e
+    from fortranfvcell_gb300.solver import format_solver_log
+    labels = {1: "PCG:       ", 2: "PBICGSTAB: ", 3: "GMRES: "}
+    for code, its, energy, tol in [(1, 123, 1.234567890123, 1e-8), (2, 7, -0.0, 1e-12),
+                                   (3, 45, 9.99999999996e99, 1e-10), (1, 0, 0.5, 1.0),
+                                   (2, 123456789, -3.0e-200, 5e-324)]:
+        d = lambda v: fortran_e(v, 20, 10).replace("E", "D")
+        want = f"{labels[code]}it{its:9d} energy norm {d(energy)} tol {d(tol)}"
+        assert format_solver_log(code, its, energy, tol) == want

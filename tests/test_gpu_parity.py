@@ -461,3 +461,29 @@ def test_dropin_structure_cache_sees_in_place_changes(fvc, orc):
     fvc.solver(ad, au, au, x2, b[perm], ia, ja, n, nad, True, 1e-12, 50000, 1, 1)
     # system 2 is system 1 renumbered: x2 = x1 permuted
     assert np.linalg.norm(x2 - x1[perm]) <= 1e-9 * np.linalg.norm(x1)
+
+
+def test_solver_log_callback(fvc, orc, meshes):
+    # every solve hands the callback the reference's unit-13 line, with the
+    # iterations and energy norm of the solve's statistics
+    from fortranfvcell_gb300.solver import format_solver_log, set_solver_log
+    s = pressure(orc, meshes["quad"], 1, True)
+    n = s["n"]
+    b = np.random.default_rng(1).uniform(-1, 1, n)
+    lines = []
+    set_solver_log(lines.append)
+    try:
+        stats = []
+        for code in (1, 2, 3):
+            x = np.zeros(n)
+            stats.append(fvc.solver(s["ad"], s["au"], s["au"], x, b, s["ia"], s["ja"], n,
+                                    s["nad"], True, 1e-8, 50000, code, 1))
+    finally:
+        set_solver_log(None)
+    assert len(lines) == 3
+    for code, st, line in zip((1, 2, 3), stats, lines):
+        assert line == format_solver_log(code, st.iterations, st.energy, 1e-8)
+    x = np.zeros(n)
+    fvc.solver(s["ad"], s["au"], s["au"], x, b, s["ia"], s["ja"], n, s["nad"], True, 1e-8,
+               50000, 1, 1)
+    assert len(lines) == 3                 # off again
