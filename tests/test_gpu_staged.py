@@ -95,3 +95,19 @@ def test_staged_matches_plain_beyond_window():
     assert st1.iterations == st0.iterations
     assert np.array_equal(x1, x0)
     assert _relres(s, x1, b) <= 1e-8
+
+
+def test_staged_matches_plain_with_long_blocks():
+    # 1.21M cells: every block walks about eight 1024-row chunks, so the
+    # copy window wraps within one phase and the prefetched stages of the
+    # next phase are drained and issued again after each reliable update
+    from fortranfvcell_gb300 import mesh
+    m = mesh.square_mesh(1100, kind="quad", jitter=0.1, seed=7)
+    ps = mesh.pressure_system(m, 1, True, pin_cell=1)
+    s = dict(n=ps.neq, ia=ps.ia, ja=ps.ja, au=ps.au, ad=ps.ad, nad=ps.nad)
+    assert s["n"] >= 152 * 7 * 1024
+    b = np.random.default_rng(11).uniform(-1, 1, s["n"])
+    (st1, x1), (st0, x0) = _solve_both(s, b)
+    assert st1.status == 0 and st0.status == 0 and st0.refinements >= 2
+    assert st1.iterations == st0.iterations
+    assert np.array_equal(x1, x0)
