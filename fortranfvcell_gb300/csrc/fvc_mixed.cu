@@ -1185,6 +1185,7 @@ __global__ void __launch_bounds__(1024, 1) mixed_cg_staged_w4(MArgs a) {
 // The reference's Jacobi BiCGSTAB (Iterativos.f:140-234) in FP32 on the
 // correction equation A e = r, inside FP64 defect correction.
 constexpr int kBcgStall = 100;
+constexpr int kSweepStall = 3;
 
 __device__ __forceinline__ void mixed_bicgstab_body(const MArgs &a) {
   __shared__ double red[kMaxNV * 32];
@@ -1192,7 +1193,8 @@ __device__ __forceinline__ void mixed_bicgstab_body(const MArgs &a) {
   unsigned int ep = 0;
   int sweep = 0, inner_total = 0, status = FVC_ERR_NOCONV;
   double res[4];
-  double relres = 0.0, bnorm2 = 0.0;
+  double relres = 0.0, bnorm2 = 0.0, best_rel = 0.0;
+  int flat = 0;
   bool zero_x = a.init != 0;
   float *sv = a.rs, *p = a.pa, *v = a.q, *t = a.t, *r0 = a.r0, *z = a.z;
   float2 *e = a.e;
@@ -1210,6 +1212,16 @@ __device__ __forceinline__ void mixed_bicgstab_body(const MArgs &a) {
       status = FVC_OK;
       break;
     }
+    // sweeps that no longer cut the FP64 residual by a tenth (the FP32
+    // operator's rounding outweighs the correction): after kSweepStall of
+    // them in a row the solve stops early with FVC_ERR_NOCONV, below both
+    // max_refine and maxit (every block sees the same relres)
+    if (sweep == 0 || relres <= 0.9 * best_rel) {
+      flat = 0;
+    } else if (++flat >= kSweepStall) {
+      break;
+    }
+    best_rel = (sweep == 0) ? relres : fmin(best_rel, relres);
     if (sweep == a.max_refine || inner_total >= a.maxit) break;
     const double d = res[2];  // r.z with z = r/m
     const double stop2 = a.inner_tol * a.inner_tol * fabs(d);
@@ -1582,6 +1594,26 @@ int32_t run_mixed(const DeviceMatrix &A, Scratch &S, int code, const double *b, 
     st->final_crit = res[2];
     st->rel_residual = res[2];
     st->solve_ms = ms;
+  }
+  const int max_refine = (o.max_refine > 0) ? o.max_refine : 30;
+  if (code == 2 && ires[1] == FVC_ERR_NOCONV && ires[0] < max_refine && ires[2] < maxit) {
+    // the defect-correction sweeps stalled (stopped early by the kernel):
+    // FP64 BiCGSTAB finishes from the current iterate, to the same target
+    // on ||r||2/||b||2, with the iterations left
+    fvc_opts fo = o;
+    fo.precision = FVC_PREC_FP64;
+    fo.stop_rule = 1;
+    fo.want_residual = 1;
+    fvc_stats s2{};
+    const int32_t rc2 = run_bicgstab(A, S, b, x, target, maxit - ires[2], 0, fo, stream, &s2);
+    if (st) {
+      st->status = rc2;
+      st->iterations = ires[2] + s2.iterations;
+      st->final_crit = s2.final_crit;
+      st->rel_residual = s2.rel_residual;
+      st->solve_ms = ms + s2.solve_ms;
+    }
+    return rc2;
   }
   return ires[1];
 }

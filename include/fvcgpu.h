@@ -71,6 +71,11 @@ void solver_(double *ad, double *au, double *al, double *x, double *b,
 enum {
   FVC_PREC_FP64 = 0,  /* reference arithmetic: FP64 everywhere             */
   FVC_PREC_MIXED = 1  /* FP32 SpMV + Jacobi inside FP64 defect correction  */
+  /* A mixed BiCGSTAB whose sweeps stop cutting the FP64 residual (three in a
+   * row each below a tenth) ends its FP32 part early; fvc_solve and the
+   * drop-in then finish in FP64 BiCGSTAB from that iterate (stats: the
+   * iterations of both parts, the FP32 ones in inner_iterations).  The
+   * enqueued and batched solves report that stall as FVC_ERR_NOCONV. */
 };
 
 typedef struct {
@@ -177,7 +182,7 @@ int32_t fvc_matrix_update_values_async(fvc_context *ctx, const double *ad,
  * d_status (DEVICE, 4 int32) holds the FVC_* status, the iterations, the
  * inner iterations (GMRES steps) and 1 if an on-device wait gave up
  * (status FVC_ERR_TIMEOUT); with FVC_PREC_MIXED the iterations are the FP32
- * ones.  The first call for a context, precision and launch shape allocates
+ * ones. A stalled mixed BiCGSTAB is not finished in FP64 here.  The first call for a context, precision and launch shape allocates
  * work buffers (and lays out the FP32 operator), so it must not be the
  * captured one.  Returns FVC_OK once the work is enqueued;
  * FVC_ERR_UNSUPPORTED for mixed GMRES and for the (code, matriz) pairs
