@@ -38,6 +38,9 @@ struct DeviceMatrix {
   bool layout32 = false;     // the FP32 layout (col16_ok, ell_w, buffers) is decided
   int cl_smax = -1;          // cluster PCG: most slots of one CTA's rows (-1: unknown)
   int *mirror = nullptr;     // per slot: the slot of the transposed entry (built on demand)
+  // a mixed BiCGSTAB on this structure stalled: its later mixed BiCGSTAB
+  // solves (new values, same structure) run in FP64 from the start
+  mutable bool bcg32_stalled = false;
   // host-side description of the source layout, for value updates
   int matriz = 0, unsym = 0, nad = 0;
   int64_t *src_of_slot = nullptr;  // device map: slot -> source value index

@@ -1557,6 +1557,28 @@ int32_t enqueue_mixed(const DeviceMatrix &A0, Scratch &S, int code, const double
 int32_t run_mixed(const DeviceMatrix &A, Scratch &S, int code, const double *b, double *x,
                   double tol, int maxit, int init, const fvc_opts &o, cudaStream_t stream,
                   fvc_stats *st) {
+  // FP64 BiCGSTAB to the mixed solve's target on ||r||2/||b||2 (stats: the
+  // FP32 part's iterations and sweeps kept, both parts' times summed)
+  const double target = (o.refine_tol > 0) ? o.refine_tol : tol;
+  auto fp64_bicgstab = [&](int from_init, int its_left, int fp32_its, int sweeps, float ms0) {
+    fvc_opts fo = o;
+    fo.precision = FVC_PREC_FP64;
+    fo.stop_rule = 1;
+    fo.want_residual = 1;
+    fvc_stats s2{};
+    const int32_t rc2 = run_bicgstab(A, S, b, x, target, its_left, from_init, fo, stream, &s2);
+    if (st) {
+      *st = s2;
+      st->status = rc2;
+      st->iterations = fp32_its + s2.iterations;
+      st->inner_iterations = fp32_its;
+      st->refinements = sweeps;
+      st->conv = target;
+      st->solve_ms = ms0 + s2.solve_ms;
+    }
+    return rc2;
+  };
+  if (code == 2 && A.bcg32_stalled) return fp64_bicgstab(init, maxit, 0, 0, 0.f);
   // allocations (and the FP32 layout) before the timed launch
   int32_t rc = enqueue_mixed(A, S, code, b, x, tol, maxit, init, o, stream, false);
   if (rc != FVC_OK) return rc;
@@ -1571,7 +1593,6 @@ int32_t run_mixed(const DeviceMatrix &A, Scratch &S, int code, const double *b, 
     cudaEventDestroy(e1);
     return rc;
   }
-  const double target = (o.refine_tol > 0) ? o.refine_tol : tol;
   double res[16];
   int ires[16], err = 0;
   cudaMemcpyAsync(res, S.result, sizeof(res), cudaMemcpyDeviceToHost, stream);
@@ -1598,22 +1619,10 @@ int32_t run_mixed(const DeviceMatrix &A, Scratch &S, int code, const double *b, 
   const int max_refine = (o.max_refine > 0) ? o.max_refine : 30;
   if (code == 2 && ires[1] == FVC_ERR_NOCONV && ires[0] < max_refine && ires[2] < maxit) {
     // the defect-correction sweeps stalled (stopped early by the kernel):
-    // FP64 BiCGSTAB finishes from the current iterate, to the same target
-    // on ||r||2/||b||2, with the iterations left
-    fvc_opts fo = o;
-    fo.precision = FVC_PREC_FP64;
-    fo.stop_rule = 1;
-    fo.want_residual = 1;
-    fvc_stats s2{};
-    const int32_t rc2 = run_bicgstab(A, S, b, x, target, maxit - ires[2], 0, fo, stream, &s2);
-    if (st) {
-      st->status = rc2;
-      st->iterations = ires[2] + s2.iterations;
-      st->final_crit = s2.final_crit;
-      st->rel_residual = s2.rel_residual;
-      st->solve_ms = ms + s2.solve_ms;
-    }
-    return rc2;
+    // FP64 finishes from the current iterate with the iterations left, and
+    // later mixed BiCGSTAB solves of this structure start in FP64
+    A.bcg32_stalled = true;
+    return fp64_bicgstab(0, maxit - ires[2], ires[2], ires[0], ms);
   }
   return ires[1];
 }

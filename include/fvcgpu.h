@@ -74,8 +74,10 @@ enum {
   /* A mixed BiCGSTAB whose sweeps stop cutting the FP64 residual (three in a
    * row each below a tenth) ends its FP32 part early; fvc_solve and the
    * drop-in then finish in FP64 BiCGSTAB from that iterate (stats: the
-   * iterations of both parts, the FP32 ones in inner_iterations).  The
-   * enqueued and batched solves report that stall as FVC_ERR_NOCONV. */
+   * iterations of both parts, the FP32 ones in inner_iterations), and the
+   * context's later mixed BiCGSTAB solves run in FP64 from the start until
+   * fvc_matrix_set gives it another structure.  The enqueued and batched
+   * solves report that stall as FVC_ERR_NOCONV. */
 };
 
 typedef struct {
