@@ -15,9 +15,14 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
-BUILD = os.path.join(HERE, "_build")
 LIBDIR = os.path.join(HERE, "lib")
-LIB = os.path.join(LIBDIR, "libfvcgpu.so")
+# FVC_CHECK=1 in the environment selects the check variant: every
+# translation unit compiled with -DFVC_CHECK (device bounds checks that
+# record a code and redirect the access, see csrc/fvc_device.cuh) into
+# lib/libfvcgpu_check.so, which the package then loads instead.
+CHECK = os.environ.get("FVC_CHECK", "0") not in ("", "0")
+BUILD = os.path.join(HERE, "_build_check" if CHECK else "_build")
+LIB = os.path.join(LIBDIR, "libfvcgpu_check.so" if CHECK else "libfvcgpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["fvc_krylov.cu", "fvc_cluster.cu", "fvc_mixed.cu", "fvc_gather.cu", "fvc_assembly.cu",
            "fvc_noalloc.cu", "fvc_simple.cu", "fvc_simple_driver.cu", "fvc_api.cpp",
@@ -38,6 +43,8 @@ def _compile(src: str, verbose_ptxas: bool) -> str:
     obj = os.path.join(BUILD, src + ".o")
     cmd = [nvcc(), "-c", path, "-o", obj, "-O3", "-std=c++17", "-lineinfo",
            "-Xcompiler", "-fPIC,-O3,-Wall", *ARCH]
+    if CHECK:
+        cmd.append("-DFVC_CHECK")
     if src.endswith(".cu"):
         cmd += ["--expt-relaxed-constexpr"]
         if src in NO_FMAD:

@@ -81,6 +81,7 @@ void free_matrix(fvc_context *c) {
   cudaFree(A.minv32);
   cudaFree(A.col16);
   cudaFree(A.sflag);
+  cudaFree(A.f32_bad);
   cudaFree(c->d_src);
   cudaFree(c->d_raw1);
   cudaFree(c->d_raw2);
@@ -642,6 +643,20 @@ int32_t fvc_solve_async(fvc_context *c, int32_t code, const double *d_b, double 
   if (code == 3 && (matriz == 4 || mixed)) return FVC_ERR_UNSUPPORTED;
   cudaSetDevice(c->device);
   const int init = (o.init < 0) ? default_init(code, matriz) : (o.init ? 1 : 0);
+  if (mixed && code == 2 && c->A.bcg32_stalled) {
+    // a mixed BiCGSTAB on this structure stalled in an fvc_solve, which
+    // finished it in FP64 and sends the later ones to FP64 from the start;
+    // so does this path: FP64 BiCGSTAB to the mixed solve's target on
+    // ||r||2 / ||b||2 (its buffers exist: that FP64 finish allocated them)
+    fvc_opts fo = o;
+    fo.precision = FVC_PREC_FP64;
+    fo.stop_rule = 1;
+    const double target = (o.refine_tol > 0) ? o.refine_tol : tol;
+    const int32_t rc = fvc::enqueue_solve(c->A, c->S, 2, d_b, d_x, target, maxit, init, fo,
+                                          c->stream, true);
+    if (rc != FVC_OK) return rc;
+    return fvc::launch_solve_status(c->S, d_status, c->stream, false);
+  }
   int32_t rc = mixed ? fvc::enqueue_mixed(c->A, c->S, code, d_b, d_x, tol, maxit, init, o,
                                           c->stream, true)
                      : fvc::enqueue_solve(c->A, c->S, code, d_b, d_x, tol, maxit, init, o,

@@ -122,10 +122,19 @@ __global__ void __launch_bounds__(1024) pcg_cluster(ClArgs a) {
   int *col = reinterpret_cast<int *>(val + S);  // (owner << 16) | local row
   int *sp = col + S;                            // slot offset of each local slice
   const bool has_diag = a.A.diag_mode != DIAG_NONE;
+#ifdef FVC_CHECK
+  // check builds: columns outside [0, n) (whose owner CTA would not be in
+  // the cluster) are counted here, redirected to this CTA's first row, and
+  // end the solve uniformly after the first reduction
+  __shared__ int s_bad;
+  if (threadIdx.x == 0) s_bad = 0;
+  __syncthreads();
+#endif
   // load the rows' slices (columns re-coded as owner CTA and local row)
   for (int i = threadIdx.x; i <= ns; i += blockDim.x) sp[i] = (int)(a.A.sptr[s0 + i] - sbase);
   for (int k = threadIdx.x; k < S; k += blockDim.x) {
-    const int c = a.A.col[sbase + k];
+    int c = a.A.col[sbase + k];
+    FVC_CHK((unsigned)c < (unsigned)n, &s_bad, kChkCluster, c = r0);
     const int owner = c / R;
     col[k] = (owner << 16) | (c - owner * R);
     val[k] = a.A.val[sbase + k];
@@ -178,7 +187,11 @@ __global__ void __launch_bounds__(1024) pcg_cluster(ClArgs a) {
   unsigned int ep = 0;
   const bool rule0 = a.stop_rule == 0;
   // r = b - A x ; z = r/m ; p = z ; d = r.z
+#ifdef FVC_CHECK
+  double acc[3] = {0.0, 0.0, (threadIdx.x == 0 && s_bad != 0) ? 1.0 : 0.0};
+#else
   double acc[2] = {0.0, 0.0};
+#endif
   for (int i = threadIdx.x; i < rows; i += blockDim.x) {
     const double ax = a.init ? 0.0 : spmv_row(i, xread);
     const double bi = a.b[r0 + i];
@@ -190,15 +203,22 @@ __global__ void __launch_bounds__(1024) pcg_cluster(ClArgs a) {
     acc[0] = fma(ri, zi, acc[0]);
     acc[1] = fma(bi, bi, acc[1]);
   }
+#ifdef FVC_CHECK
+  cluster_allreduce<3>(cl, ep, acc, part, red, [&](const double *t) {
+    sh.stop = (t[2] > 0.0) ? 3 : 0;
+#else
   cluster_allreduce<2>(cl, ep, acc, part, red, [&](const double *t) {
+    sh.stop = 0;
+#endif
     sh.d = t[0];
     sh.conv = rule0 ? a.tol * sqrt(fabs(t[0])) : a.tol * sqrt(t[1]);
     sh.crit = 0.0;
-    sh.stop = 0;
   });
   int j, status = FVC_OK;
   double beta = 0.0;
-  for (j = 1; j <= a.maxit; ++j) {
+  const int jmax = (sh.stop == 3) ? 0 : a.maxit;  // 3: a failed check (check builds)
+  if (sh.stop == 3) status = FVC_ERR_ARG;
+  for (j = 1; j <= jmax; ++j) {
     if (j > 1) {  // p = z + beta p on the own rows, then visible to the cluster
       for (int i = threadIdx.x; i < rows; i += blockDim.x) p[i] = fma(beta, p[i], z[i]);
       cl.sync();
@@ -234,10 +254,11 @@ __global__ void __launch_bounds__(1024) pcg_cluster(ClArgs a) {
     if (sh.stop == 1) break;
     beta = sh.beta;
   }
-  if (j > a.maxit) {
+  if (j > a.maxit && status == FVC_OK) {
     j = a.maxit;
     status = FVC_ERR_NOCONV;
   }
+  if (status == FVC_ERR_ARG) j = 0;
   // x.Ax, |b - Ax|^2, |b|^2 (x complete in every CTA after the barrier)
   cl.sync();
   double e3[3] = {0.0, 0.0, 0.0};
@@ -342,7 +363,7 @@ int32_t enqueue_pcg_cluster(const DeviceMatrix &A, Scratch &S, const double *b, 
     return FVC_ERR_UNSUPPORTED;
   }
   if (!launch) return FVC_OK;
-  cudaMemsetAsync(S.err, 0, sizeof(int), stream);
+  cudaMemsetAsync(S.err, 0, 64, stream);  // the whole error block (wait and check words)
   cudaMemsetAsync(S.iresult, 0, 16 * sizeof(int), stream);
   cudaMemsetAsync(S.result, 0, 16 * sizeof(double), stream);
   ClArgs a{};
@@ -398,6 +419,11 @@ int32_t run_pcg_cluster(const DeviceMatrix &A, Scratch &S, const double *b, doub
     fprintf(stderr, "fvcgpu: cluster PCG failed: %s\n", cudaGetErrorString(ce));
     return FVC_ERR_CUDA;
   }
+#ifdef FVC_CHECK
+  if (ires[1] == FVC_ERR_ARG)
+    fprintf(stderr, "fvcgpu: device check failed: cluster PCG column outside [0, n) (code %d); "
+                    "the solve's result is void\n", (int)kChkCluster);
+#endif
   if (st) {
     st->status = ires[1];
     st->iterations = ires[0];

@@ -32,7 +32,39 @@ struct SellView {
   int diag_mode;
   const int *mirror = nullptr;  // per slot: the slot of the transposed entry
                                 // (symmetric patterns; transposed solves only)
+  int *chk = nullptr;           // check builds: the launch's error word
 };
+
+// Opt-in device checks (compiled with -DFVC_CHECK, the library's check
+// variant; see build.py).  A column, slice width, offset or mirror index
+// outside its array is recorded in an error word -- the first failing
+// check's code, kept by atomicCAS -- and the access is redirected to a safe
+// index (the row itself, or an empty slice), so nothing is read out of
+// bounds and nothing traps.  The word is the launch's grid-wait error word:
+// every grid wait sees it and returns, so the launch ends through its
+// normal error path, and the host reports FVC_ERR_ARG with the check's
+// name (check_status).  Without FVC_CHECK the checks compile to nothing.
+enum CheckCode : int {
+  kChkColumn = 101,      // SELL column outside [0, n)
+  kChkSliceWidth = 102,  // slice width negative or above n
+  kChkOffset = 103,      // FP32 operator: row + 16-bit offset outside [0, n)
+  kChkMirror = 104,      // transposed solves: mirror slot outside the slots
+  kChkCluster = 105,     // cluster PCG: a column whose owner CTA is not in the cluster
+};
+#ifdef FVC_CHECK
+#define FVC_CHK(cond, word, code, fix)                        \
+  do {                                                        \
+    if (!(cond)) {                                            \
+      int *w_ = (word);                                       \
+      if (w_) atomicCAS(w_, 0, (int)(code));                  \
+      fix;                                                    \
+    }                                                         \
+  } while (0)
+#else
+#define FVC_CHK(cond, word, code, fix) \
+  do {                                 \
+  } while (0)
+#endif
 
 // Grid synchronisation state of one persistent launch.  `count` is a
 // monotonically increasing arrival counter (episode e completes when it
@@ -300,6 +332,27 @@ __device__ __forceinline__ float ld_stream(const float *p) {
   asm volatile("ld.global.nc.L1::no_allocate.f32 %0, [%1];" : "=f"(v) : "l"(p));
   return v;
 }
+// 16-byte and 8-byte streaming loads (p aligned to 16 / 8 bytes): one
+// row's four FP32 weights, one row's four 16-bit column offsets.
+__device__ __forceinline__ float4 ld_stream4(const float *p) {
+  float4 v;
+  asm volatile("ld.global.nc.L1::no_allocate.v4.f32 {%0, %1, %2, %3}, [%4];"
+               : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+               : "l"(p));
+  return v;
+}
+__device__ __forceinline__ uint2 ld_stream_u2(const int16_t *p) {
+  uint2 v;
+  asm volatile("ld.global.nc.L1::no_allocate.v2.u32 {%0, %1}, [%2];"
+               : "=r"(v.x), "=r"(v.y)
+               : "l"(p));
+  return v;
+}
+// The k-th signed 16-bit offset of four packed in (lo, hi) words.
+__device__ __forceinline__ int off16(uint2 v, int k) {
+  const unsigned int w = (k < 2) ? v.x : v.y;
+  return (int)(int16_t)(uint16_t)((k & 1) ? (w >> 16) : (w & 0xffffu));
+}
 
 __device__ __forceinline__ float warp_sum(float v) {
 #pragma unroll
@@ -319,7 +372,8 @@ template <typename XF>
 __device__ __forceinline__ double sell_row_f64(const SellView<double> &A, int s,
                                                int lane, int row, XF xf) {
   const int64_t base = A.sptr[s];
-  const int w = (int)((A.sptr[s + 1] - base) >> 5);
+  int w = (int)((A.sptr[s + 1] - base) >> 5);
+  FVC_CHK(w >= 0 && w <= A.n, A.chk, kChkSliceWidth, w = 0);
   const int *cp = A.col + base + lane;
   const double *vp = A.val + base + lane;
   double xd = 0.0;
@@ -332,6 +386,7 @@ __device__ __forceinline__ double sell_row_f64(const SellView<double> &A, int s,
     for (int k = 0; k < 4; ++k) {
       c[k] = (k < w) ? ld_stream(cp + 32 * k) : 0;
       a[k] = (k < w) ? ld_stream(vp + 32 * k) : 0.0;
+      FVC_CHK(k >= w || (unsigned)c[k] < (unsigned)A.n, A.chk, kChkColumn, c[k] = row);
     }
     if (A.diag_mode == DIAG_LAST) {
       // the reference's ELLPACK sums t1+t2+...+tw+t_diag left to right
@@ -346,14 +401,17 @@ __device__ __forceinline__ double sell_row_f64(const SellView<double> &A, int s,
       if (k < w) t = __dadd_rn(t, __dmul_rn(a[k], xf(c[k])));
     return t;
   }
+  auto colk = [&](int k) {
+    int c = ld_stream(cp + 32 * k);
+    FVC_CHK((unsigned)c < (unsigned)A.n, A.chk, kChkColumn, c = row);
+    return c;
+  };
   if (A.diag_mode == DIAG_LAST) {
-    t = __dmul_rn(ld_stream(vp), xf(ld_stream(cp)));
-    for (int k = 1; k < w; ++k)
-      t = __dadd_rn(t, __dmul_rn(ld_stream(vp + 32 * k), xf(ld_stream(cp + 32 * k))));
+    t = __dmul_rn(ld_stream(vp), xf(colk(0)));
+    for (int k = 1; k < w; ++k) t = __dadd_rn(t, __dmul_rn(ld_stream(vp + 32 * k), xf(colk(k))));
     return __dadd_rn(t, xd);
   }
-  for (int k = 0; k < w; ++k)
-    t = __dadd_rn(t, __dmul_rn(ld_stream(vp + 32 * k), xf(ld_stream(cp + 32 * k))));
+  for (int k = 0; k < w; ++k) t = __dadd_rn(t, __dmul_rn(ld_stream(vp + 32 * k), xf(colk(k))));
   return t;
 }
 
@@ -364,7 +422,8 @@ template <typename XF>
 __device__ __forceinline__ double sell_row_fma(const SellView<double> &A, int s, int lane,
                                                int row, XF xf) {
   const int64_t base = A.sptr[s];
-  const int w = (int)((A.sptr[s + 1] - base) >> 5);
+  int w = (int)((A.sptr[s + 1] - base) >> 5);
+  FVC_CHK(w >= 0 && w <= A.n, A.chk, kChkSliceWidth, w = 0);
   const int *cp = A.col + base + lane;
   const double *vp = A.val + base + lane;
   const bool has_diag = A.diag_mode != DIAG_NONE;
@@ -378,12 +437,17 @@ __device__ __forceinline__ double sell_row_fma(const SellView<double> &A, int s,
     for (int k = 0; k < 4; ++k) {
       c[k] = (k < w) ? ld_stream(cp + 32 * k) : 0;
       a[k] = (k < w) ? ld_stream(vp + 32 * k) : 0.0;
+      FVC_CHK(k >= w || (unsigned)c[k] < (unsigned)A.n, A.chk, kChkColumn, c[k] = row);
     }
 #pragma unroll
     for (int k = 0; k < 4; ++k)
       if (k < w) t = fma(a[k], xf(c[k]), t);
   } else {
-    for (int k = 0; k < w; ++k) t = fma(ld_stream(vp + 32 * k), xf(ld_stream(cp + 32 * k)), t);
+    for (int k = 0; k < w; ++k) {
+      int c = ld_stream(cp + 32 * k);
+      FVC_CHK((unsigned)c < (unsigned)A.n, A.chk, kChkColumn, c = row);
+      t = fma(ld_stream(vp + 32 * k), xf(c), t);
+    }
   }
   if (A.diag_mode == DIAG_LAST) t = fma(dv, xi, t);
   return t;
@@ -400,7 +464,24 @@ struct BatchSys {
   GridSync gs;
   double *result;
   int *iresult;
+  // per-system mask (may be null: always solve).  *run == 0: the system is
+  // not solved in this launch -- the reference's test before a solve
+  // (the right-hand side's norm below 1e-32) skipped it -- and x keeps its
+  // rows' values
+  const int32_t *run = nullptr;
 };
+
+// A masked system's blocks leave at once; its lead block reports status
+// FVC_OK after 0 iterations.  Every block of the group reads the same flag.
+__device__ __forceinline__ bool batch_masked(const BatchSys &d, bool lead) {
+  if (d.run == nullptr || *d.run != 0) return false;
+  if (lead && threadIdx.x == 0) {
+    d.iresult[0] = 0;
+    d.iresult[1] = FVC_OK;
+    d.iresult[2] = 0;
+  }
+  return true;
+}
 
 // y_row = (A^T x)_row over the stored matrix of a symmetric pattern: the
 // entry (row, col(slot)) of A^T is the stored value of the mirror slot
@@ -409,24 +490,35 @@ template <typename XF>
 __device__ __forceinline__ double sell_row_fma_t(const SellView<double> &A, int s, int lane,
                                                  int row, XF xf) {
   const int64_t base = A.sptr[s];
-  const int w = (int)((A.sptr[s + 1] - base) >> 5);
+  int w = (int)((A.sptr[s + 1] - base) >> 5);
+  FVC_CHK(w >= 0 && w <= A.n, A.chk, kChkSliceWidth, w = 0);
   const int *cp = A.col + base + lane;
   const int *mp = A.mirror + base + lane;
   const bool has_diag = A.diag_mode != DIAG_NONE;
   const double dv = has_diag ? ld_stream(A.diag + row) : 0.0;
   double t = has_diag ? dv * xf(row) : 0.0;
+#ifdef FVC_CHECK
+  const int64_t nslots = A.sptr[A.nslices];
+#endif
   if (w <= 4) {
     int c[4], m[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
       c[k] = (k < w) ? ld_stream(cp + 32 * k) : 0;
       m[k] = (k < w) ? ld_stream(mp + 32 * k) : 0;
+      FVC_CHK(k >= w || (unsigned)c[k] < (unsigned)A.n, A.chk, kChkColumn, c[k] = row);
+      FVC_CHK(k >= w || (m[k] >= 0 && m[k] < nslots), A.chk, kChkMirror, m[k] = (int)(base + lane));
     }
 #pragma unroll
     for (int k = 0; k < 4; ++k)
       if (k < w) t = fma(A.val[m[k]], xf(c[k]), t);
   } else {
-    for (int k = 0; k < w; ++k) t = fma(A.val[ld_stream(mp + 32 * k)], xf(ld_stream(cp + 32 * k)), t);
+    for (int k = 0; k < w; ++k) {
+      int c = ld_stream(cp + 32 * k), m = ld_stream(mp + 32 * k);
+      FVC_CHK((unsigned)c < (unsigned)A.n, A.chk, kChkColumn, c = row);
+      FVC_CHK(m >= 0 && m < nslots, A.chk, kChkMirror, m = (int)(base + lane));
+      t = fma(A.val[m], xf(c), t);
+    }
   }
   return t;
 }
@@ -450,7 +542,8 @@ inline int32_t ensure_sync(Scratch &S, size_t nblocks) {
   }
   if (!S.sync) {
     if (cudaMalloc(&S.sync, 64) != cudaSuccess) return FVC_ERR_CUDA;
-    if (cudaMalloc(&S.err, 64) != cudaSuccess) return FVC_ERR_CUDA;
+    if (cudaMalloc(&S.err, 64) != cudaSuccess || cudaMemset(S.err, 0, 64) != cudaSuccess)
+      return FVC_ERR_CUDA;
     if (cudaMalloc(&S.result, 16 * sizeof(double)) != cudaSuccess) return FVC_ERR_CUDA;
     if (cudaMalloc(&S.iresult, 16 * sizeof(int)) != cudaSuccess) return FVC_ERR_CUDA;
     if (cudaMalloc(&S.trace, 2 * kTraceMax * sizeof(double)) != cudaSuccess) return FVC_ERR_CUDA;
@@ -470,6 +563,15 @@ inline GridSync make_sync(const Scratch &S, int nblocks) {
   g.base = 0;
   return g;
 }
+
+// The word a failed device check records into (check builds): the second
+// 32-byte sector of the launch's 64-byte error block, zeroed with it.  A
+// separate word from the wait error, so that no wait gives up early (the
+// staged kernels must see every bulk copy land); the launch runs to its end
+// on the redirected indices and the host reads the word afterwards
+// (check_word_status).
+inline int *check_word(const Scratch &S) { return S.err ? S.err + 8 : nullptr; }
+int32_t check_word_status(const Scratch &S, cudaStream_t stream);
 
 inline void reset_sync(Scratch &S, cudaStream_t stream) {
   cudaMemsetAsync(S.sync, 0, 64, stream);

@@ -32,6 +32,10 @@ struct DeviceMatrix {
   float *minv32 = nullptr;  // Jacobi 1/m per row (0 for |m| beyond FP32)
   int16_t *col16 = nullptr; // column - row per slot (when every one fits)
   uint8_t *sflag = nullptr; // per slice: 1 if some row has e_i != 0
+  // set by the FP32 build when a slot that held 0 when the layout was
+  // chosen (and so was given offset 0) holds a value whose offset needs
+  // more than 16 bits; the mixed kernels then refuse to run
+  int *f32_bad = nullptr;
   bool col16_ok = false;
   int ell_w = 0;             // FP32 copy padded to this uniform slice width (0: SELL)
   bool have32 = false;
@@ -123,6 +127,35 @@ int32_t run_krylov_batched(DeviceMatrix &A, Scratch &S, int nsys,
                            const double *its_hint, const int32_t *inits, const double *b,
                            double *x, double tol, int maxit, const fvc_opts &o,
                            cudaStream_t stream, fvc_stats *st);
+// A batched launch planned once for a fixed block-diagonal structure
+// (plan_batched): the systems' descriptors, their block shares and the
+// launch's counters and result slots in one device buffer.  Each
+// enqueue_batched zeroes the counters and results and launches, with no
+// host transfer, so the launch can be captured in a CUDA graph.  run (may
+// be null) is a device array of one int32 per system: 0 skips that
+// system in the launch (x keeps its rows' values).
+struct BatchSys;
+struct BatchPlan {
+  int nsys = 0, total = 0, threads = 0;
+  bool mixed = false, persistent = false;
+  const void *kern = nullptr;
+  char *buf = nullptr;
+  size_t ctr_bytes = 0, res_bytes = 0, ires_bytes = 0;
+  int *err = nullptr;
+  double *res = nullptr;  // 16 per system: [1] conv [2] crit [3] |b-Ax|^2 [4] |b|^2
+  int *ires = nullptr;    // 16 per system: [0] iterations (mixed: updates) [1] status
+                          // [2] inner iterations
+  BatchSys *dsys = nullptr;
+  int *dsob = nullptr;
+  double tol = 0.0;
+};
+int32_t plan_batched(DeviceMatrix &A, Scratch &S, int nsys, const int32_t *row_start,
+                     const int32_t *codes, const double *tols, const double *its_hint,
+                     const int32_t *inits, const int32_t *run, double tol, const fvc_opts &o,
+                     cudaStream_t stream, bool persistent, BatchPlan &P);
+int32_t enqueue_batched(DeviceMatrix &A, Scratch &S, const BatchPlan &P, const double *b,
+                        double *x, int maxit, const fvc_opts &o, cudaStream_t stream);
+void free_batched(BatchPlan &P, cudaStream_t stream);
 // A mixed solve enqueued without waiting (launch = false: allocations,
 // the FP32 layout and operator only, for a later captured call)
 int32_t enqueue_mixed(const DeviceMatrix &A, Scratch &S, int code, const double *b, double *x,

@@ -450,6 +450,7 @@ __global__ void __launch_bounds__(kMaxT, 1024 / kMaxT) krylov_batched(KArgs a, c
                                                         const int *__restrict__ sys_of_block) {
   const BatchSys d = sys[sys_of_block[blockIdx.x]];
   const int rank = (int)(blockIdx.x - d.gs.base);
+  if (batch_masked(d, rank == 0)) return;
   const Part P(d.s0, d.s1, a.A.n, rank, (int)d.gs.nblocks);
   KArgs ak = a;
   ak.tol = d.tol;
@@ -608,13 +609,16 @@ __global__ void __launch_bounds__(256) spmv_f64(SellView<double> A, const double
   }
 }
 
-// FP32 difference form: y_i = e_i x_i + sum_k w_ik (x_i - x_k)
-// y = A x in the FP32 difference form.  ell_w > 0: the weights and 16-bit
-// column offsets are laid out ell_w slots per slice (padding slots add 0);
-// otherwise SELL-32 with the FP64 matrix's columns.
+// y = A x in the FP32 difference form, y_i = e_i x_i + sum_k w_ik (x_i - x_k).
+// kW = 4: the weights and 16-bit column offsets laid out 4 slots per slice
+// row-major (one 16-byte and one 8-byte load per row); kW = 3: 3 slots per
+// slice column-major (three coalesced 4-byte and three 2-byte loads, all
+// issued before the gathers); kW = 0: SELL-32 with the FP64 matrix's
+// columns.  Padding slots have weight 0 and add exactly 0.
+template <int kW>
 __global__ void __launch_bounds__(256) spmv_f32(int n, int nslices, const int64_t *__restrict__ sptr,
                                                 const int *__restrict__ col,
-                                                const int16_t *__restrict__ col16, int ell_w,
+                                                const int16_t *__restrict__ col16,
                                                 const float *__restrict__ w32,
                                                 const float *__restrict__ e32,
                                                 const float *__restrict__ x, float *__restrict__ y) {
@@ -625,17 +629,43 @@ __global__ void __launch_bounds__(256) spmv_f32(int n, int nslices, const int64_
     if (row >= n) continue;
     const float xi = __ldg(x + row);
     float t = ld_stream(e32 + row) * xi;
-    if (ell_w > 0) {
-      const int64_t base = (int64_t)s * 32 * ell_w + lane;
-      for (int kk = 0; kk < ell_w; ++kk)
-        t = fmaf(ld_stream(w32 + base + 32 * kk),
-                 xi - __ldg(x + row + (int)ld_stream16(col16 + base + 32 * kk)), t);
+    if (kW == 4) {
+      const int64_t base = (int64_t)s * 128 + 4 * lane;
+      const float4 w = ld_stream4(w32 + base);
+      const uint2 c = ld_stream_u2(col16 + base);
+      int k4[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        k4[k] = row + off16(c, k);
+        FVC_CHK((unsigned)k4[k] < (unsigned)n, (int *)nullptr, kChkOffset, k4[k] = row);
+      }
+      t = fmaf(w.x, xi - __ldg(x + k4[0]), t);
+      t = fmaf(w.y, xi - __ldg(x + k4[1]), t);
+      t = fmaf(w.z, xi - __ldg(x + k4[2]), t);
+      t = fmaf(w.w, xi - __ldg(x + k4[3]), t);
+    } else if (kW == 3) {
+      const int64_t base = (int64_t)s * 96 + lane;
+      float w[3];
+      int c[3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        w[k] = ld_stream(w32 + base + 32 * k);
+        c[k] = row + (int)ld_stream16(col16 + base + 32 * k);
+        FVC_CHK((unsigned)c[k] < (unsigned)n, (int *)nullptr, kChkOffset, c[k] = row);
+      }
+      float xv[3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) xv[k] = __ldg(x + c[k]);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) t = fmaf(w[k], xi - xv[k], t);
     } else {
       const int64_t base = sptr[s];
       const int w = (int)((sptr[s + 1] - base) >> 5);
-      for (int kk = 0; kk < w; ++kk)
-        t = fmaf(ld_stream(w32 + base + 32 * kk + lane),
-                 xi - __ldg(x + ld_stream(col + base + 32 * kk + lane)), t);
+      for (int kk = 0; kk < w; ++kk) {
+        int c = ld_stream(col + base + 32 * kk + lane);
+        FVC_CHK((unsigned)c < (unsigned)n, (int *)nullptr, kChkColumn, c = row);
+        t = fmaf(ld_stream(w32 + base + 32 * kk + lane), xi - __ldg(x + c), t);
+      }
     }
     y[row] = t;
   }
@@ -722,6 +752,7 @@ int32_t enqueue_persistent(K kernel, const DeviceMatrix &A, Scratch &S, const do
   reset_sync(S, stream);
   KArgs a{};
   a.A = view64(A);
+  a.A.chk = check_word(S);
   a.m = A.jac;
   a.minv = A.jinv;
   a.b = b;
@@ -771,6 +802,7 @@ int32_t read_stats(const Scratch &S, cudaStream_t stream, cudaEvent_t e0, cudaEv
     return FVC_ERR_CUDA;
   }
   if (err != 0) return FVC_ERR_TIMEOUT;
+  if (const int32_t c = check_word_status(S, stream); c != FVC_OK) return c;
   if (st) {
     st->status = ires[1];
     st->iterations = ires[0];
@@ -807,6 +839,15 @@ int32_t run_persistent(K kernel, const DeviceMatrix &A, Scratch &S, const double
 // status, iterations, inner iterations and the timeout flag of the solve
 // that ran last on this scratch, copied where a captured graph can read them
 __global__ void solve_status_kernel(const int *iresult, const int *err, int32_t *out, int mixed) {
+#ifdef FVC_CHECK
+  if (err[0] == 0 && err[8] != 0) {  // a failed device check (check builds)
+    out[0] = FVC_ERR_ARG;
+    out[1] = 0;
+    out[2] = 0;
+    out[3] = err[8];
+    return;
+  }
+#endif
   out[0] = (*err != 0) ? (int32_t)FVC_ERR_TIMEOUT : iresult[1];
   out[1] = mixed ? iresult[2] : iresult[0];
   out[2] = iresult[2];
@@ -814,6 +855,32 @@ __global__ void solve_status_kernel(const int *iresult, const int *err, int32_t 
 }
 
 }  // namespace
+
+int32_t check_word_status(const Scratch &S, cudaStream_t stream) {
+#ifdef FVC_CHECK
+  int w = 0;
+  int *cw = check_word(S);
+  if (!cw) return FVC_OK;
+  if (cudaMemcpyAsync(&w, cw, sizeof(int), cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
+      cudaStreamSynchronize(stream) != cudaSuccess)
+    return FVC_ERR_CUDA;
+  if (w != 0) {
+    const char *what = w == kChkColumn       ? "SELL column outside [0, n)"
+                       : w == kChkSliceWidth ? "slice width outside [0, n]"
+                       : w == kChkOffset     ? "FP32 operator row + offset outside [0, n)"
+                       : w == kChkMirror     ? "transposed-solve mirror slot outside the slots"
+                       : w == kChkCluster    ? "cluster PCG column outside [0, n)"
+                                             : "unknown check";
+    fprintf(stderr, "fvcgpu: device check failed: %s (code %d); the solve's result is void\n",
+            what, w);
+    return FVC_ERR_ARG;
+  }
+#else
+  (void)S;
+  (void)stream;
+#endif
+  return FVC_OK;
+}
 
 int32_t run_pcg(const DeviceMatrix &A, Scratch &S, const double *b, double *x, double tol,
                 int maxit, int init, const fvc_opts &o, cudaStream_t stream, fvc_stats *st) {
@@ -877,11 +944,10 @@ int32_t launch_solve_status(const Scratch &S, int32_t *out, cudaStream_t stream,
   return cudaPeekAtLastError() == cudaSuccess ? FVC_OK : FVC_ERR_CUDA;
 }
 
-int32_t run_krylov_batched(DeviceMatrix &A, Scratch &S, int nsys,
-                           const int32_t *row_start, const int32_t *codes, const double *tols,
-                           const double *its_hint, const int32_t *inits, const double *b,
-                           double *x, double tol, int maxit, const fvc_opts &o,
-                           cudaStream_t stream, fvc_stats *st) {
+int32_t plan_batched(DeviceMatrix &A, Scratch &S, int nsys, const int32_t *row_start,
+                     const int32_t *codes, const double *tols, const double *its_hint,
+                     const int32_t *inits, const int32_t *run, double tol, const fvc_opts &o,
+                     cudaStream_t stream, bool persistent, BatchPlan &P) {
   if (nsys < 1 || !row_start || !inits || row_start[0] != 0 || row_start[nsys] != A.n)
     return FVC_ERR_ARG;
   bool any_bicg = false;
@@ -989,7 +1055,9 @@ int32_t run_krylov_batched(DeviceMatrix &A, Scratch &S, int nsys,
   const size_t bytes =
       ctr_bytes + part_doubles * sizeof(double) + res_bytes + ires_bytes + sys_bytes + sob_bytes;
   char *buf = nullptr;
-  if (cudaMallocAsync((void **)&buf, bytes, stream) != cudaSuccess) return FVC_ERR_CUDA;
+  if (persistent ? cudaMalloc((void **)&buf, bytes) != cudaSuccess
+                 : cudaMallocAsync((void **)&buf, bytes, stream) != cudaSuccess)
+    return FVC_ERR_CUDA;
   unsigned int *ctr = reinterpret_cast<unsigned int *>(buf);
   int *err = reinterpret_cast<int *>(buf + (size_t)nsys * 64);
   double *part = reinterpret_cast<double *>(buf + ctr_bytes);
@@ -1020,21 +1088,65 @@ int32_t run_krylov_batched(DeviceMatrix &A, Scratch &S, int nsys,
     d.gs.base = (unsigned int)b0;
     d.result = res + (size_t)s * 16;
     d.iresult = ires + (size_t)s * 16;
+    d.run = run ? run + s : nullptr;
     poff += (size_t)4 * kMaxNV * (nb[s] + 1);
     for (int k = 0; k < nb[s]; ++k) hsob[(size_t)b0 + k] = s;
     b0 += nb[s];
   }
   int32_t rc = mixed ? FVC_OK : ensure_vectors(S, (size_t)A.n, any_bicg ? 8 : 5, 1, false);
+#ifdef FVC_CHECK
+  // the check word lives in the scratch's error block (check builds)
+  if (rc == FVC_OK) rc = ensure_sync(S, 1);
+  if (rc == FVC_OK) cudaMemsetAsync(S.err, 0, 64, stream);
+#endif
   if (rc != FVC_OK) {
-    cudaFreeAsync(buf, stream);
+    if (persistent)
+      cudaFree(buf);
+    else
+      cudaFreeAsync(buf, stream);
     return rc;
   }
-  cudaMemsetAsync(buf, 0, ctr_bytes, stream);
-  cudaMemsetAsync(res, 0, res_bytes + ires_bytes, stream);
   cudaMemcpyAsync(dsys, hsys.data(), sys_bytes, cudaMemcpyHostToDevice, stream);
   cudaMemcpyAsync(dsob, hsob.data(), sob_bytes, cudaMemcpyHostToDevice, stream);
+  if (persistent && cudaStreamSynchronize(stream) != cudaSuccess) {  // host vectors die here
+    cudaFree(buf);
+    return FVC_ERR_CUDA;
+  }
+  P.nsys = nsys;
+  P.total = (int)total;
+  P.threads = threads;
+  P.mixed = mixed;
+  P.kern = kern;
+  P.buf = buf;
+  P.persistent = persistent;
+  P.ctr_bytes = ctr_bytes;
+  P.res_bytes = res_bytes;
+  P.ires_bytes = ires_bytes;
+  P.err = err;
+  P.res = res;
+  P.ires = ires;
+  P.dsys = dsys;
+  P.dsob = dsob;
+  P.tol = tol;
+  return FVC_OK;
+}
+
+int32_t enqueue_batched(DeviceMatrix &A, Scratch &S, const BatchPlan &P, const double *b,
+                        double *x, int maxit, const fvc_opts &o, cudaStream_t stream) {
+  // counters, the error word and every system's result slots start at zero
+  if (cudaMemsetAsync(P.buf, 0, P.ctr_bytes, stream) != cudaSuccess ||
+      cudaMemsetAsync(P.res, 0, P.res_bytes + P.ires_bytes, stream) != cudaSuccess)
+    return FVC_ERR_CUDA;
+  if (P.mixed) {
+    // the FP32 operator of the current values (stream-ordered once its
+    // layout is decided, which planning did)
+    int32_t rc = build_f32_copy(A, stream);
+    if (rc != FVC_OK) return rc;
+    return launch_mixed_batched(A, S, P.dsys, P.dsob, P.total, P.threads, b, x, maxit, o, stream);
+  }
   KArgs a{};
   a.A = view64(A);
+  a.A.chk = check_word(S);
   a.m = A.jac;
   a.minv = A.jinv;
   a.b = b;
@@ -1047,45 +1159,67 @@ int32_t run_krylov_batched(DeviceMatrix &A, Scratch &S, int nsys,
   a.v5 = S.v[5];
   a.v6 = S.v[6];
   a.v7 = S.v[7];
-  a.tol = tol;
+  a.tol = P.tol;
   a.maxit = maxit;
   a.init = 1;
   a.stop_rule = o.stop_rule;
-  const BatchSys *psys = dsys;
-  const int *psob = dsob;
+  const BatchSys *psys = P.dsys;
+  const int *psob = P.dsob;
   void *args[] = {&a, &psys, &psob};
+  const cudaError_t ce =
+      cudaLaunchCooperativeKernel(P.kern, dim3((unsigned)P.total), dim3(P.threads), args, 0, stream);
+  count_launch();
+  if (ce != cudaSuccess) {
+    fprintf(stderr, "fvcgpu: batched launch failed: %s\n", cudaGetErrorString(ce));
+    return FVC_ERR_CUDA;
+  }
+  return FVC_OK;
+}
+
+void free_batched(BatchPlan &P, cudaStream_t stream) {
+  if (P.buf) {
+    if (P.persistent)
+      cudaFree(P.buf);
+    else
+      cudaFreeAsync(P.buf, stream);
+  }
+  P = BatchPlan();
+}
+
+int32_t run_krylov_batched(DeviceMatrix &A, Scratch &S, int nsys,
+                           const int32_t *row_start, const int32_t *codes, const double *tols,
+                           const double *its_hint, const int32_t *inits, const double *b,
+                           double *x, double tol, int maxit, const fvc_opts &o,
+                           cudaStream_t stream, fvc_stats *st) {
+  BatchPlan P;
+  int32_t rc = plan_batched(A, S, nsys, row_start, codes, tols, its_hint, inits, nullptr, tol, o,
+                            stream, false, P);
+  if (rc != FVC_OK) return rc;
+  const bool mixed = P.mixed;
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   cudaEventRecord(e0, stream);
-  cudaError_t ce = cudaSuccess;
-  if (mixed) {
-    if (launch_mixed_batched(A, S, psys, psob, (int)total, threads, b, x, maxit, o, stream) !=
-        FVC_OK)
-      ce = cudaErrorLaunchFailure;
-  } else {
-    ce = cudaLaunchCooperativeKernel(kern, dim3((unsigned)total), dim3(threads), args, 0, stream);
-    count_launch();
-  }
+  rc = enqueue_batched(A, S, P, b, x, maxit, o, stream);
   cudaEventRecord(e1, stream);
   std::vector<double> hres((size_t)nsys * 16);
   std::vector<int> hires((size_t)nsys * 16);
   int herr = 0;
-  if (ce == cudaSuccess) {
-    cudaMemcpyAsync(hres.data(), res, res_bytes, cudaMemcpyDeviceToHost, stream);
-    cudaMemcpyAsync(hires.data(), ires, ires_bytes, cudaMemcpyDeviceToHost, stream);
-    cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, stream);
-  } else if (!mixed) {  // (the mixed launcher reports its own failure)
-    fprintf(stderr, "fvcgpu: batched launch failed: %s\n", cudaGetErrorString(ce));
+  if (rc == FVC_OK) {
+    cudaMemcpyAsync(hres.data(), P.res, P.res_bytes, cudaMemcpyDeviceToHost, stream);
+    cudaMemcpyAsync(hires.data(), P.ires, P.ires_bytes, cudaMemcpyDeviceToHost, stream);
+    cudaMemcpyAsync(&herr, P.err, sizeof(int), cudaMemcpyDeviceToHost, stream);
   }
-  cudaFreeAsync(buf, stream);
+  free_batched(P, stream);
   cudaError_t ce2 = cudaStreamSynchronize(stream);
   float ms = 0.f;
   cudaEventElapsedTime(&ms, e0, e1);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  if (ce != cudaSuccess || ce2 != cudaSuccess) return FVC_ERR_CUDA;
+  if (rc != FVC_OK) return rc;
+  if (ce2 != cudaSuccess) return FVC_ERR_CUDA;
   if (herr != 0) return FVC_ERR_TIMEOUT;
+  if (const int32_t c = check_word_status(S, stream); c != FVC_OK) return c;
   int32_t worst = FVC_OK;
   for (int s = 0; s < nsys; ++s) {
     const double *r = &hres[(size_t)s * 16];
@@ -1129,8 +1263,15 @@ int32_t launch_spmv_f32(const DeviceMatrix &A, const float *x, float *y, cudaStr
   const int threads = 256;
   int blocks = (A.nslices + 7) / 8;
   blocks = std::max(1, std::min(blocks, sm_count() * 8));
-  spmv_f32<<<blocks, threads, 0, stream>>>(A.n, A.nslices, A.sptr, A.col, A.col16, A.ell_w,
-                                           A.val32, A.diag32, x, y);
+  if (A.ell_w == 4)
+    spmv_f32<4><<<blocks, threads, 0, stream>>>(A.n, A.nslices, A.sptr, A.col, A.col16,
+                                                A.val32, A.diag32, x, y);
+  else if (A.ell_w == 3)
+    spmv_f32<3><<<blocks, threads, 0, stream>>>(A.n, A.nslices, A.sptr, A.col, A.col16,
+                                                A.val32, A.diag32, x, y);
+  else
+    spmv_f32<0><<<blocks, threads, 0, stream>>>(A.n, A.nslices, A.sptr, A.col, A.col16,
+                                                A.val32, A.diag32, x, y);
   count_launch();
   return cudaPeekAtLastError() == cudaSuccess ? FVC_OK : FVC_ERR_CUDA;
 }

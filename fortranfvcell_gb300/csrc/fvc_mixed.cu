@@ -187,10 +187,15 @@ __device__ __forceinline__ float2 df_axpy(float2 e, float ah, float al, float p)
   return make_float2(hi, __fsub_rn(lo, __fsub_rn(hi, s)));
 }
 
-// Layout scan: flags[0] = 1 if some column offset (col - row) needs more
-// than 16 bits, flags[1] / flags[2] = smallest / largest slice width.
+// Layout scan: flags[0] = 1 if some column offset (col - row) of a slot
+// with a nonzero value needs more than 16 bits, flags[1] / flags[2] =
+// smallest / largest slice width.  Slots holding 0 (the reference's ELLPACK
+// padding: column 1, value 0, src/EllPack.f:19-42) add exactly 0 in the
+// difference form whatever column they name, so the FP32 operator points
+// them at their own row (offset 0) and they do not count here.
 __global__ void scan_slices(int n, int nslices, const int64_t *__restrict__ sptr,
-                            const int *__restrict__ col, int *__restrict__ flags) {
+                            const int *__restrict__ col, const double *__restrict__ val,
+                            int *__restrict__ flags) {
   const int lane = threadIdx.x & 31;
   const int nw = (gridDim.x * blockDim.x) >> 5;
   for (int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < nslices; s += nw) {
@@ -199,7 +204,8 @@ __global__ void scan_slices(int n, int nslices, const int64_t *__restrict__ sptr
     const int wd = (int)((sptr[s + 1] - base) >> 5);
     bool wide = false;
     for (int k = 0; k < wd; ++k) {
-      const int d = (row < n) ? col[base + 32 * k + lane] - row : 0;
+      const int64_t q = base + 32 * k + lane;
+      const int d = (row < n && val[q] != 0.0) ? col[q] - row : 0;
       if (d < -32768 || d > 32767) wide = true;
     }
     if (__any_sync(0xffffffffu, wide) && lane == 0) atomicExch(flags, 1);
@@ -210,17 +216,29 @@ __global__ void scan_slices(int n, int nslices, const int64_t *__restrict__ sptr
   }
 }
 
+// Slot of (lane, k) in a slice of the FP32 operator that starts at slot
+// dbase.  Width-4 uniform layout (ell_w == 4): row-major inside the slice,
+// a row's four slots contiguous (4 lane + k), so a lane reads its row's
+// weights with one 16-byte load and its offsets with one 8-byte load.
+// Otherwise column-major as in SELL-32 (32 k + lane): a warp's k-th slots
+// are one coalesced 128-byte line.
+__host__ __device__ __forceinline__ int64_t f32_slot(int64_t dbase, int ell_w, int lane, int k) {
+  return (ell_w == 4) ? dbase + 4 * lane + k : dbase + 32 * k + lane;
+}
+
 // e_i (FP64 sum, rounded once), Jacobi 1/m, the FP32 weights, the 16-bit
 // column offsets (col - row) and the per-slice "has excess" flags.  With
 // ell_w > 0 the weights and offsets are laid out with every slice ell_w
 // slots wide (slice s at slot 32 ell_w s); the slots a narrower slice lacks
 // get weight 0 and offset 0, which add exactly 0 to every row sum.
+// check16: the kernels read col16, so a nonzero slot whose offset does not
+// fit 16 bits (possible only where the layout scan saw a 0 there) sets *bad.
 __global__ void build_f32_operator(int n, int nslices, const int64_t *__restrict__ sptr,
                                    const int *__restrict__ col, const double *__restrict__ val,
                                    const double *__restrict__ jac, float *__restrict__ w32,
                                    float *__restrict__ e32, float *__restrict__ minv32,
                                    int16_t *__restrict__ col16, uint8_t *__restrict__ sflag,
-                                   int ell_w) {
+                                   int ell_w, int check16, int *__restrict__ bad) {
   const int lane = threadIdx.x & 31;
   const int nw = (gridDim.x * blockDim.x) >> 5;
   for (int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < nslices; s += nw) {
@@ -234,12 +252,16 @@ __global__ void build_f32_operator(int n, int nslices, const int64_t *__restrict
       const bool diag_slot = (row < n) && (col[q] == row);
       const double a = (row < n && !diag_slot) ? val[q] : 0.0;
       off += a;
-      w32[dbase + 32 * k + lane] = (float)(-a);
-      col16[dbase + 32 * k + lane] = (int16_t)((row < n) ? col[q] - row : 0);
+      const int64_t o = f32_slot(dbase, ell_w, lane, k);
+      const int d = (row < n && a != 0.0) ? col[q] - row : 0;
+      if (check16 && (d < -32768 || d > 32767)) atomicExch(bad, 1);
+      w32[o] = (a != 0.0) ? (float)(-a) : 0.0f;
+      col16[o] = (int16_t)d;
     }
     for (int k = wd; k < ell_w; ++k) {
-      w32[dbase + 32 * k + lane] = 0.0f;
-      col16[dbase + 32 * k + lane] = 0;
+      const int64_t o = f32_slot(dbase, ell_w, lane, k);
+      w32[o] = 0.0f;
+      col16[o] = 0;
     }
     float ev = 0.0f;
     if (row < n) {
@@ -263,6 +285,7 @@ struct MArgs {
   const int16_t *col16; // column offsets (col - row), when col16_ok
   int ell_w;            // > 0: w32/col16 hold every slice ell_w slots wide
   const uint8_t *sflag; // per slice: some row has e_i != 0
+  const int *f32_bad;   // nonzero: the 16-bit offsets no longer describe A
   const double *jac;    // m in FP64
   const double *b;
   double *x;
@@ -294,13 +317,38 @@ __device__ __forceinline__ bool mlead(const MArgs &a) {
 // (A y)_row in FP32 difference form, y supplied by a functor.
 template <typename YF>
 __device__ __forceinline__ float arow32(const MArgs &a, int s, int lane, int row, YF yf) {
-  if (a.ell_w > 0) {  // uniform layout: 16-bit offsets, padding slots add 0
-    const int64_t base = (int64_t)s * 32 * a.ell_w + lane;
+  if (a.ell_w == 4) {  // width 4, row-major in the slice: one 16-B and one 8-B load
+    const int64_t base = (int64_t)s * 128 + 4 * lane;
+    const float4 w = ld_stream4(a.w32 + base);
+    const uint2 c = ld_stream_u2(a.col16 + base);
     const float yi = yf(row);
     float t = ld_stream(a.e32 + row) * yi;
-    for (int k = 0; k < a.ell_w; ++k)
-      t = fmaf(ld_stream(a.w32 + base + 32 * k),
-               yi - yf(row + (int)ld_stream16(a.col16 + base + 32 * k)), t);
+    int k4[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      k4[k] = row + off16(c, k);
+      FVC_CHK((unsigned)k4[k] < (unsigned)a.A.n, a.A.chk, kChkOffset, k4[k] = row);
+    }
+    t = fmaf(w.x, yi - yf(k4[0]), t);
+    t = fmaf(w.y, yi - yf(k4[1]), t);
+    t = fmaf(w.z, yi - yf(k4[2]), t);
+    t = fmaf(w.w, yi - yf(k4[3]), t);
+    return t;
+  }
+  if (a.ell_w == 3) {  // width 3, column-major: the loads issued before the gathers
+    const int64_t base = (int64_t)s * 96 + lane;
+    float w[3];
+    int c[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      w[k] = ld_stream(a.w32 + base + 32 * k);
+      c[k] = row + (int)ld_stream16(a.col16 + base + 32 * k);
+      FVC_CHK((unsigned)c[k] < (unsigned)a.A.n, a.A.chk, kChkOffset, c[k] = row);
+    }
+    const float yi = yf(row);
+    float t = ld_stream(a.e32 + row) * yi;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) t = fmaf(w[k], yi - yf(c[k]), t);
     return t;
   }
   const int64_t base = a.A.sptr[s];
@@ -316,13 +364,18 @@ __device__ __forceinline__ float arow32(const MArgs &a, int s, int lane, int row
     for (int k = 0; k < 4; ++k) {
       c[k] = (k < w) ? ld_stream(cp + 32 * k) : row;
       v[k] = (k < w) ? ld_stream(vp + 32 * k) : 0.0f;
+      FVC_CHK((unsigned)c[k] < (unsigned)a.A.n, a.A.chk, kChkColumn, c[k] = row);
     }
 #pragma unroll
     for (int k = 0; k < 4; ++k)
       if (k < w) t = fmaf(v[k], yi - yf(c[k]), t);
     return t;
   }
-  for (int k = 0; k < w; ++k) t = fmaf(ld_stream(vp + 32 * k), yi - yf(ld_stream(cp + 32 * k)), t);
+  for (int k = 0; k < w; ++k) {
+    int c = ld_stream(cp + 32 * k);
+    FVC_CHK((unsigned)c < (unsigned)a.A.n, a.A.chk, kChkColumn, c = row);
+    t = fmaf(ld_stream(vp + 32 * k), yi - yf(c), t);
+  }
   return t;
 }
 
@@ -821,7 +874,7 @@ __device__ __forceinline__ CSum cg_phase_a_st(const MArgs &a, const MPart &P, fl
       const int16_t *cs;
       const unsigned char *b = st_region(smem) + kA_Base + stg * kA_Bytes;
       if (kW > 0) {
-        const int off = P.warp * kSlice * kW + P.lane;
+        const int off = P.warp * kSlice * kW + (kW == 4 ? 4 * P.lane : P.lane);
         ws = reinterpret_cast<const float *>(b) + off;
         cs = reinterpret_cast<const int16_t *>(b + kA_C) + off;
       } else if (H->ok[stg]) {
@@ -836,12 +889,22 @@ __device__ __forceinline__ CSum cg_phase_a_st(const MArgs &a, const MPart &P, fl
       // from global memory
       auto pat = [&](int k) -> float {
         if ((unsigned)(k - wlo) < (unsigned)kWinSpan) return ring[(k - R0) & (kPRingRows - 1)];
+        FVC_CHK((unsigned)k < (unsigned)P.n, a.A.chk, kChkOffset, k = row);
         return kFirst ? a.z[k] : p_update(a.z[k], bh, bl, d.ph[k], d.pl[k]).x;
       };
       if (row < P.n) {
         const float pi = ring[(row - R0) & (kPRingRows - 1)];
         float t = myex * pi;
-        if (kW > 0) {
+        if (kW == 4) {  // row-major stage: one 16-B and one 8-B shared load per row
+          const float4 w4 = *reinterpret_cast<const float4 *>(ws);
+          const uint2 c4 = *reinterpret_cast<const uint2 *>(cs);
+          const float w[4] = {w4.x, w4.y, w4.z, w4.w};
+          int c[4];
+#pragma unroll
+          for (int k = 0; k < 4; ++k) c[k] = row + off16(c4, k);
+#pragma unroll
+          for (int k = 0; k < 4; ++k) t = fmaf(w[k], pi - pat(c[k]), t);
+        } else if (kW > 0) {
           constexpr int W = kW > 0 ? kW : 1;
           int c[W];
           float w[W];
@@ -976,10 +1039,29 @@ __device__ __forceinline__ void cg_phase_b_st(const MArgs &a, const MPart &P, fl
   cnt.sb += (uint32_t)nch;
 }
 
+// The FP32 operator's 16-bit offsets no longer describe A (f32_bad, set
+// by the build when a slot that held 0 at layout time now holds a far
+// column's value): every block leaves before any work and the lead block
+// reports FVC_ERR_UNSUPPORTED.  Every block reads the same word, written
+// by the build earlier on the stream, so all take the same branch.
+__device__ __forceinline__ bool f32_refused(const MArgs &a) {
+  if (a.col16 == nullptr || a.f32_bad == nullptr || *a.f32_bad == 0) return false;
+  if (mlead(a) && threadIdx.x == 0) {
+    a.iresult[0] = 0;
+    a.iresult[1] = FVC_ERR_UNSUPPORTED;
+    a.iresult[2] = 0;
+    a.result[2] = 0.0;
+    a.result[3] = 0.0;
+    a.result[4] = 0.0;
+  }
+  return true;
+}
+
 template <bool kStaged, int kW>
 __device__ __forceinline__ void mixed_cg_body(const MArgs &a) {
   __shared__ double red[kMaxNV * 32];
   extern __shared__ __align__(128) unsigned char st_smem[];
+  if (f32_refused(a)) return;
   const MPart P(a);
   StCount gch;  // staged copies issued so far, per ring
   if (kStaged) {
@@ -1189,6 +1271,7 @@ constexpr int kSweepStall = 3;
 
 __device__ __forceinline__ void mixed_bicgstab_body(const MArgs &a) {
   __shared__ double red[kMaxNV * 32];
+  if (f32_refused(a)) return;
   const MPart P(a);
   unsigned int ep = 0;
   int sweep = 0, inner_total = 0, status = FVC_ERR_NOCONV;
@@ -1329,6 +1412,7 @@ template <int kMaxT>
 __global__ void __launch_bounds__(kMaxT, 1024 / kMaxT)
     mixed_batched(MArgs a, const BatchSys *__restrict__ sys, const int *__restrict__ sob) {
   const BatchSys d = sys[sob[blockIdx.x]];
+  if (batch_masked(d, blockIdx.x == d.gs.base)) return;
   MArgs am = a;
   am.gs = d.gs;
   am.grp_s0 = d.s0;
@@ -1366,7 +1450,9 @@ MArgs mixed_args(const DeviceMatrix &A, const Scratch &S, const double *b, doubl
   a.minv = A.minv32;
   a.col16 = A.col16_ok ? A.col16 : nullptr;
   a.ell_w = A.ell_w;
+  a.A.chk = check_word(S);
   a.sflag = A.sflag;
+  a.f32_bad = A.f32_bad;
   a.jac = A.jac;
   a.b = b;
   a.x = x;
@@ -1445,9 +1531,11 @@ int32_t build_f32_copy(DeviceMatrix &A, cudaStream_t stream) {
   if (A.have32) return FVC_OK;
   int blocks = std::max(1, std::min((A.nslices + 7) / 8, sm_count_m() * 8));
   if (A.layout32) {
+    if (cudaMemsetAsync(A.f32_bad, 0, sizeof(int), stream) != cudaSuccess) return FVC_ERR_CUDA;
     build_f32_operator<<<blocks, 256, 0, stream>>>(A.n, A.nslices, A.sptr, A.col, A.val, A.jac,
                                                    A.val32, A.diag32, A.minv32, A.col16,
-                                                   A.sflag, A.ell_w);
+                                                   A.sflag, A.ell_w, A.col16_ok ? 1 : 0,
+                                                   A.f32_bad);
     count_launch();
     if (cudaPeekAtLastError() != cudaSuccess) return FVC_ERR_CUDA;
     A.have32 = true;
@@ -1457,7 +1545,7 @@ int32_t build_f32_copy(DeviceMatrix &A, cudaStream_t stream) {
   if (cudaMalloc(&flags, 3 * sizeof(int)) != cudaSuccess) return FVC_ERR_CUDA;
   const int init[3] = {0, 1 << 30, 0};
   cudaMemcpyAsync(flags, init, sizeof(init), cudaMemcpyHostToDevice, stream);
-  scan_slices<<<blocks, 256, 0, stream>>>(A.n, A.nslices, A.sptr, A.col, flags);
+  scan_slices<<<blocks, 256, 0, stream>>>(A.n, A.nslices, A.sptr, A.col, A.val, flags);
   count_launch();
   int hf[3] = {1, 0, 0};
   cudaMemcpyAsync(hf, flags, sizeof(hf), cudaMemcpyDeviceToHost, stream);
@@ -1479,9 +1567,11 @@ int32_t build_f32_copy(DeviceMatrix &A, cudaStream_t stream) {
     return FVC_ERR_CUDA;
   if (!A.col16 && cudaMalloc(&A.col16, sizeof(int16_t) * sl) != cudaSuccess) return FVC_ERR_CUDA;
   if (!A.sflag && cudaMalloc(&A.sflag, (size_t)A.nslices + 1) != cudaSuccess) return FVC_ERR_CUDA;
+  if (!A.f32_bad && cudaMalloc(&A.f32_bad, sizeof(int)) != cudaSuccess) return FVC_ERR_CUDA;
+  if (cudaMemsetAsync(A.f32_bad, 0, sizeof(int), stream) != cudaSuccess) return FVC_ERR_CUDA;
   build_f32_operator<<<blocks, 256, 0, stream>>>(A.n, A.nslices, A.sptr, A.col, A.val, A.jac,
                                                  A.val32, A.diag32, A.minv32, A.col16, A.sflag,
-                                                 A.ell_w);
+                                                 A.ell_w, A.col16_ok ? 1 : 0, A.f32_bad);
   count_launch();
   ce = cudaStreamSynchronize(stream);
   if (ce != cudaSuccess) return FVC_ERR_CUDA;
@@ -1605,6 +1695,12 @@ int32_t run_mixed(const DeviceMatrix &A, Scratch &S, int code, const double *b, 
   cudaEventDestroy(e1);
   if (ce != cudaSuccess) return FVC_ERR_CUDA;
   if (err != 0) return FVC_ERR_TIMEOUT;
+  if (const int32_t c = check_word_status(S, stream); c != FVC_OK) return c;
+  if (ires[1] == FVC_ERR_UNSUPPORTED)
+    fprintf(stderr,
+            "fvcgpu: mixed solve refused: a matrix slot that held 0 when the FP32 layout was "
+            "chosen now holds a value whose column is more than 32767 rows away; set the "
+            "matrix again (fvc_matrix_set) to lay the FP32 operator out anew\n");
   if (st) {
     st->status = ires[1];
     st->iterations = ires[2];

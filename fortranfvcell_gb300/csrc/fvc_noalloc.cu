@@ -18,7 +18,6 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
-#include <mutex>
 
 #include "fvc_device.cuh"
 #include "fvc_internal.h"
@@ -43,7 +42,8 @@ constexpr size_t kResDoubles = 16;
 constexpr size_t kCtrDoubles = 16;  // count, flag, err, iresult (as 32-bit words)
 constexpr size_t kScratchDoubles = kVecDoubles + kPartDoubles + kTotDoubles + kResDoubles + kCtrDoubles;
 
-// Every GPU that loads the library holds this array (~5.0 MiB) until exit.
+// A device holds this array (~5.0 MiB) from the first call on it (the load
+// of this module on that device) until the process exits.
 static __device__ __align__(256) double g_noalloc_scratch[kScratchDoubles];
 
 struct NoAllocArgs {
@@ -83,10 +83,46 @@ __device__ __forceinline__ double csrd_row_f(const NoAllocArgs &a, int i, PF pf)
            end_ = min((n), (int)((blockIdx.x + 1) * (((n) + gridDim.x - 1) / gridDim.x))); \
        row < end_; row += blockDim.x)
 
+// Status the kernel reports when the structure check fails.
+constexpr int kBadStructure = -1;
+
 __global__ void __launch_bounds__(kNoAllocThreads, 1) pcg_csrd_noalloc_kernel(NoAllocArgs a) {
   __shared__ double red[kMaxNV * 32];
   const int n = a.n;
   unsigned int ep = 0;
+  // Structure check before any gather: ia(1) = 1, each row's length in
+  // [0, n-1], every column in [1, n]; and at least one entry above the
+  // diagonal when there are off-diagonals at all.  Symmetric CSRD keeps
+  // only the strictly lower triangle (src/Datastruct.f:77, matvec_csrd_sym
+  // src/Matvec.f:216-250); applied as unsymmetric CSRD it would be a
+  // different operator, so such input is refused rather than solved wrongly.
+  double chk[3] = {0.0, 0.0, 0.0};  // bad rows, entries above, off-diagonals
+  NA_FOR_ROWS(n) {
+    const int k0 = a.ia[row], k1 = a.ia[row + 1];
+    const bool ok_row = (row > 0 || k0 == 1) && k0 >= 1 && k1 >= k0 && k1 - k0 <= n - 1;
+    if (!ok_row) {
+      chk[0] += 1.0;
+      continue;
+    }
+    for (int k = k0 - 1; k < k1 - 1; ++k) {
+      const int c = a.ja[k];
+      if (c < 1 || c > n) {
+        chk[0] += 1.0;
+        break;
+      }
+      if (c - 1 > row) chk[1] += 1.0;
+    }
+    chk[2] += (double)(k1 - k0);
+  }
+  if (!grid_allreduce<3>(a.gs, ep, chk, red)) return;
+  if (chk[0] != 0.0 || (chk[2] > 0.0 && chk[1] == 0.0)) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      a.iresult[0] = 0;
+      a.iresult[1] = kBadStructure;
+      a.result[1] = chk[0];
+    }
+    return;
+  }
   double acc[2] = {0.0, 0.0};
   NA_FOR_ROWS(n) {
     double ax;
@@ -166,26 +202,24 @@ __global__ void __launch_bounds__(kNoAllocThreads, 1) pcg_csrd_noalloc_kernel(No
   }
 }
 
-// Device address of g_noalloc_scratch, looked up once per device with that
-// device current (host code cannot use the array's name as an address).
-constexpr int kMaxDevices = 64;
-std::mutex g_noalloc_mutex;
-double *g_noalloc_ptr[kMaxDevices] = {nullptr};
-
-int32_t noalloc_scratch(int dev, double **out) {
-  if (dev < 0 || dev >= kMaxDevices) return FVC_ERR_CUDA;
-  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-  if (!g_noalloc_ptr[dev]) {
-    void *p = nullptr;
-    const cudaError_t ce = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (ce != cudaSuccess || !p) {
-      fprintf(stderr, "fvc_pcg_csrd_noalloc: cudaGetSymbolAddress failed: %s\n",
-              cudaGetErrorString(ce));
-      return FVC_ERR_CUDA;
-    }
-    g_noalloc_ptr[dev] = static_cast<double *>(p);
+// Device address of g_noalloc_scratch on the current device.  Host code
+// cannot use the array's name as an address, so it asks the runtime, on
+// every call: the address belongs to the module loaded in the device's
+// current context, and a context that was reset and re-created (a
+// cudaDeviceReset in between) loads the module again, possibly elsewhere.
+// Once the module is loaded the look-up allocates nothing.  Under CUDA's
+// lazy module loading (CUDA_MODULE_LOADING=LAZY, the default since
+// CUDA 12.2) the first look-up on a device is what loads the module, and
+// with it places the array in device memory.
+int32_t noalloc_scratch(double **out) {
+  void *p = nullptr;
+  const cudaError_t ce = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (ce != cudaSuccess || !p) {
+    fprintf(stderr, "fvc_pcg_csrd_noalloc: cudaGetSymbolAddress failed: %s\n",
+            cudaGetErrorString(ce));
+    return FVC_ERR_CUDA;
   }
-  *out = g_noalloc_ptr[dev];
+  *out = static_cast<double *>(p);
   return FVC_OK;
 }
 
@@ -200,7 +234,8 @@ extern "C" int32_t fvc_pcg_csrd_noalloc(const double *d_ad, const double *d_au,
                                         void *stream, fvc_stats *stats) {
   using namespace fvc;
   if (stats) memset(stats, 0, sizeof(*stats));
-  if (!d_ad || !d_au || !d_ia || !d_ja || !d_b || !d_x || neq <= 0 || maxit < 1)
+  if (!d_ad || !d_au || !d_ia || !d_ja || !d_b || !d_x || neq <= 0 || maxit < 1 ||
+      (stop_rule != 0 && stop_rule != 1))
     return FVC_ERR_ARG;
   if (neq > kNoAllocMaxRows) {
     fprintf(stderr,
@@ -212,7 +247,7 @@ extern "C" int32_t fvc_pcg_csrd_noalloc(const double *d_ad, const double *d_au,
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return FVC_ERR_CUDA;
   double *base = nullptr;
-  int32_t rc = noalloc_scratch(dev, &base);
+  int32_t rc = noalloc_scratch(&base);
   if (rc != FVC_OK) return rc;
   cudaStream_t s = (cudaStream_t)stream;
   int sms = 1, occ = 0;
@@ -271,6 +306,14 @@ extern "C" int32_t fvc_pcg_csrd_noalloc(const double *d_ad, const double *d_au,
       cudaStreamSynchronize(s) != cudaSuccess)
     return FVC_ERR_CUDA;
   if (hctr[16] != 0) return FVC_ERR_TIMEOUT;
+  if (hctr[21] == kBadStructure) {
+    fprintf(stderr,
+            "fvc_pcg_csrd_noalloc: the CSRD structure is not unsymmetric CSRD "
+            "(%.0f rows with ia out of order or a column outside [1, %d], or no entry above "
+            "the diagonal: symmetric lower-only storage); nothing was solved\n",
+            hres[1], neq);
+    return FVC_ERR_ARG;
+  }
   if (stats) {
     stats->status = hctr[21];
     stats->iterations = hctr[20];

@@ -184,7 +184,12 @@ int32_t fvc_matrix_update_values_async(fvc_context *ctx, const double *ad,
  * d_status (DEVICE, 4 int32) holds the FVC_* status, the iterations, the
  * inner iterations (GMRES steps) and 1 if an on-device wait gave up
  * (status FVC_ERR_TIMEOUT); with FVC_PREC_MIXED the iterations are the FP32
- * ones. A stalled mixed BiCGSTAB is not finished in FP64 here.  The first call for a context, precision and launch shape allocates
+ * ones.  A mixed BiCGSTAB that stalls here is not finished in FP64: d_status
+ * holds FVC_ERR_NOCONV.  Once an fvc_solve on the context has met such a
+ * stall (and finished it in FP64), this call, like fvc_solve, runs the
+ * later mixed BiCGSTAB solves of that structure as FP64 BiCGSTAB to the
+ * mixed target on ||r||2/||b||2, until fvc_matrix_set gives it a new
+ * structure.  The first call for a context, precision and launch shape allocates
  * work buffers (and lays out the FP32 operator), so it must not be the
  * captured one.  Returns FVC_OK once the work is enqueued;
  * FVC_ERR_UNSUPPORTED for mixed GMRES and for the (code, matriz) pairs
@@ -308,13 +313,21 @@ int64_t fvc_kernel_launches(void);
  * (a fixed device budget handed out at start-up, allocations owned by a
  * pool outside the caller, or a time step that must not synchronise on a
  * cudaMalloc): it calls no cudaMalloc/cudaFree.  Its scratch is one static
- * device array of about 5.0 MiB that every GPU loading this library holds
- * until exit; neq above 131072 is rejected with FVC_ERR_ARG and a message.
- * The first call on each device looks up that array's device address; make
- * that first call before any stream capture.  All calls share the array, so
- * calls that overlap on the GPU (two streams, two host threads) race; the
- * call is synchronous on `stream` (a cudaStream_t, NULL = default stream).
- * stop_rule as in fvc_opts.  Returns an FVC_* status; stats may be NULL. */
+ * device array of about 5.0 MiB; neq above 131072 is rejected with
+ * FVC_ERR_ARG and a message.  The array is placed in a device's memory when
+ * this library's module is loaded on that device.  Under CUDA's lazy module
+ * loading (the default) that is the first call of this function there, so
+ * make one call per device during start-up, before the memory budget is
+ * handed out and before any stream capture; later calls allocate nothing.
+ * Every call looks the array's address up again (no cached address
+ * outlives a device reset).  The structure is checked on the device before
+ * any gather: ia(1) = 1, row lengths in [0, neq-1], columns in [1, neq],
+ * and some entry above the diagonal; a symmetric CSRD (strictly lower part
+ * only) or a broken structure returns FVC_ERR_ARG without solving.  All
+ * calls share the array, so calls that overlap on the GPU (two streams, two
+ * host threads) race; the call is synchronous on `stream` (a cudaStream_t,
+ * NULL = default stream).  stop_rule 0 or 1 as in fvc_opts.  Returns an
+ * FVC_* status; stats may be NULL. */
 int32_t fvc_pcg_csrd_noalloc(const double *d_ad, const double *d_au,
                              const int32_t *d_ia, const int32_t *d_ja,
                              int32_t neq, const double *d_b, double *d_x,

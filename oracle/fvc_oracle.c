@@ -1074,18 +1074,24 @@ static int32_t pcg_omp(int32_t neq, const int32_t *ia, const int32_t *ja,
                        const double *ad, const double *au, const double *al,
                        const double *m, double *b, double *x, double *z,
                        double *r, double tol, int32_t maxit, matvec_fn matvec,
-                       int32_t init, int32_t nthreads, oref_stats *st) {
-  /* Iterativos_omp.f:30-127 */
+                       int32_t init, int32_t nthreads, int32_t stop_rule,
+                       oref_stats *st) {
+  /* Iterativos_omp.f:30-127.  stop_rule 0 is the reference's test
+   * sqrt|r.z| < tol sqrt|r0.z0| (:57,:88).  stop_rule 1 (not in the
+   * reference) stops on ||r||2 < tol ||b||2 instead, the rule the GPU
+   * solves use with fvc_opts.stop_rule = 1; it adds one dot_ompL4(r, r)
+   * per iteration and changes nothing else. */
   int32_t status = OREF_OK, jout = 0;
   double energy = 0.0, dout = 0.0, convout = 0.0;
 #pragma omp parallel num_threads(nthreads)
   {
-    double d, conv, alpha, beta;
+    double d, conv, alpha, beta, crit = 0.0, bnorm = 0.0;
     int32_t i, j;
     if (init) {
 #pragma omp for schedule(static)
       for (i = 1; i <= neq; ++i) F1(x, i) = 0.0;
     }
+    if (stop_rule == 1) bnorm = sqrt(dot_ompL4(b, b, neq));
     matvec(ad, au, al, x, z, ia, ja, neq);
 #pragma omp for schedule(static)
     for (i = 1; i <= neq; ++i) {
@@ -1094,7 +1100,7 @@ static int32_t pcg_omp(int32_t neq, const int32_t *ia, const int32_t *ja,
       F1(b, i) = F1(z, i);
     }
     d = dot_ompL4(r, z, neq);
-    conv = tol * sqrt(fabs(d));
+    conv = (stop_rule == 1) ? tol * bnorm : tol * sqrt(fabs(d));
     for (j = 1; j <= maxit; ++j) {
       matvec(ad, au, al, b, z, ia, ja, neq);
       alpha = d / dot_ompL4(b, z, neq);
@@ -1108,7 +1114,8 @@ static int32_t pcg_omp(int32_t neq, const int32_t *ia, const int32_t *ja,
 #pragma omp for schedule(static)
       for (i = 1; i <= neq; ++i) F1(b, i) = F1(z, i) + beta * F1(b, i);
       d = beta * d;
-      if (sqrt(fabs(d)) < conv) break;
+      crit = (stop_rule == 1) ? sqrt(dot_ompL4(r, r, neq)) : sqrt(fabs(d));
+      if (crit < conv) break;
     }
     double en = 0.0;
     if (j <= maxit) {
@@ -1118,7 +1125,7 @@ static int32_t pcg_omp(int32_t neq, const int32_t *ia, const int32_t *ja,
 #pragma omp single
     {
       jout = j;
-      dout = d;
+      dout = crit;
       convout = conv;
       energy = en;
       if (j > maxit) status = OREF_NOCONV;
@@ -1127,7 +1134,7 @@ static int32_t pcg_omp(int32_t neq, const int32_t *ia, const int32_t *ja,
   st->iterations = (jout > maxit) ? maxit : jout;
   st->energy = energy;
   st->conv = convout;
-  st->final_crit = sqrt(fabs(dout));
+  st->final_crit = dout;
   st->status = status;
   return status;
 }
@@ -1255,10 +1262,10 @@ int32_t oref_solver(double *ad, double *au, double *al, double *x, double *b,
       if (openmp) {
         if (unsym)
           status = pcg_omp(neq, iax, ja, ad, au, al, m, b, x, z, r, tol, maxit,
-                           matvec_csrd_omp, 0, omp_threads, st);
+                           matvec_csrd_omp, 0, omp_threads, 0, st);
         else
           status = pcg_omp(neq, iax, ja, ad, au, al, m, b, x, z, r, tol, maxit,
-                           matvec_csrd_sym_omp, 0, omp_threads, st);
+                           matvec_csrd_sym_omp, 0, omp_threads, 0, st);
       } else {
         if (unsym)
           status = pcg(neq, iax, ja, ad, au, al, m, b, x, z, r, tol, maxit,
@@ -1279,7 +1286,7 @@ int32_t oref_solver(double *ad, double *au, double *al, double *x, double *b,
     } else if (matriz == 4) {
       if (openmp)
         status = pcg_omp(neq, iax, ja, ad, au, al, m, b, x, z, r, tol, maxit,
-                         matvec_ellpack_omp, 0, omp_threads, st);
+                         matvec_ellpack_omp, 0, omp_threads, 0, st);
       else
         status = pcg(neq, iax, ja, ad, au, al, m, b, x, z, r, tol, maxit,
                      oref_matvec_ellpack, 0, st);
@@ -1371,7 +1378,7 @@ int32_t oref_pcg_omp_sample(double *ad, double *au, double *al, double *x,
                             double *b, const int32_t *iax, const int32_t *ja,
                             int32_t neq, int32_t nad, double tol, int32_t maxit,
                             int32_t matriz, int32_t nthreads, int32_t init,
-                            oref_stats *st) {
+                            int32_t stop_rule, oref_stats *st) {
   (void)nad;
   memset(st, 0, sizeof(*st));
   double *r = (double *)calloc((size_t)neq, sizeof(double));
@@ -1381,10 +1388,10 @@ int32_t oref_pcg_omp_sample(double *ad, double *au, double *al, double *x,
   int32_t status;
   if (matriz == 4)
     status = pcg_omp(neq, iax, ja, ad, au, al, m, b, x, z, r, tol, maxit,
-                     matvec_ellpack_omp, init, nthreads, st);
+                     matvec_ellpack_omp, init, nthreads, stop_rule, st);
   else
     status = pcg_omp(neq, iax, ja, ad, au, al, m, b, x, z, r, tol, maxit,
-                     matvec_csrd_omp, init, nthreads, st);
+                     matvec_csrd_omp, init, nthreads, stop_rule, st);
   free(r);
   free(z);
   free(m);

@@ -129,12 +129,14 @@ int32_t oref_solver(double *ad, double *au, double *al, double *x, double *b,
 
 /* Iterativos_omp.f:30-127 pcg_omp with matvec_csrd_omp / matvec_ellpack_omp
  * and dot_ompL4, timed as the CPU baseline.  Runs at most maxit iterations
- * and reports (does not stop) non-convergence. */
+ * and reports (does not stop) non-convergence.  stop_rule 0: the
+ * reference's test on sqrt|r.z|; 1: ||r||2 < tol ||b||2 (the GPU solves'
+ * fvc_opts.stop_rule = 1), one extra dot_ompL4 per iteration. */
 int32_t oref_pcg_omp_sample(double *ad, double *au, double *al, double *x,
                             double *b, const int32_t *iax, const int32_t *ja,
                             int32_t neq, int32_t nad, double tol, int32_t maxit,
                             int32_t matriz, int32_t nthreads, int32_t init,
-                            oref_stats *st);
+                            int32_t stop_rule, oref_stats *st);
 
 /* src/Iterativos.f:450-462 */
 double oref_smachn(void);

@@ -73,7 +73,7 @@ def lib():
             "oref_matvec_ellpack": [vp] * 7 + [I],
             "oref_dot": [vp, vp, I],
             "oref_solver": [vp] * 7 + [I, I, I, D, I, I, I, I, C.POINTER(Stats)],
-            "oref_pcg_omp_sample": [vp] * 7 + [I, I, D, I, I, I, I, C.POINTER(Stats)],
+            "oref_pcg_omp_sample": [vp] * 7 + [I, I, D, I, I, I, I, I, C.POINTER(Stats)],
             "oref_smachn": [],
             "oref_getres": [vp, vp, vp, I, I, I],
             "oref_gform": [vp, vp, I, I, I, vp, vp, vp, I, I, vp, vp],
@@ -239,11 +239,14 @@ def solver(ad, au, al, x, b, iax, ja, neq, nad, unsym, tol, maxit, code, matriz,
 
 
 def pcg_omp_sample(ad, au, x, b, iax, ja, neq, nad, tol, maxit, matriz, nthreads,
-                   init=True):
+                   init=True, stop_rule=0):
+    """pcg_omp (Iterativos_omp.f:30-127) for at most maxit iterations; b is
+    clobbered.  stop_rule 0 is the reference's test, 1 stops on
+    ||r|| < tol ||b|| (the GPU solves' stop_rule 1)."""
     st = Stats()
     status = lib().oref_pcg_omp_sample(_p(ad), _p(au), _p(au), _p(x), _p(b), _p(iax),
                                        _p(ja), neq, nad, tol, maxit, matriz, nthreads,
-                                       int(init), C.byref(st))
+                                       int(init), int(stop_rule), C.byref(st))
     return status, st
 
 

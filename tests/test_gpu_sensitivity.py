@@ -34,11 +34,37 @@ def test_nusselt_wall_gradient_matches_finite_differences(orc):
     assert abs(j - hot_wall_nusselt_at(c, t_loop, h_t)) < 1e-4 * abs(j)
     idx = rng.choice(g.size, 4, replace=False)
     fd = sv.nusselt_fd(prob, sysd["h_wall"], idx, step=sysd["cp"] * 1e-3)
+    # the same differences through the restated reference BiCGSTAB
+    # (src/Iterativos.f:140-234) on the frozen system's host arrays
+    fd_ref = _oracle_fd(orc, prob, idx, sysd["cp"] * 1e-3, 1e-13)
     prob.close()
     # J is affine in the wall enthalpies: the differences are exact up to the
     # two iterative solves (each to 1e-13 of its own initial residual)
     np.testing.assert_allclose(g[idx], fd, rtol=1e-6)
+    np.testing.assert_allclose(g[idx], fd_ref, rtol=1e-6)
     assert (g > 0).all()          # a warmer hot-wall face raises the wall heat flux
+
+
+def _oracle_fd(orc, prob, idx, step, tol):
+    s = prob.s
+    n = int(s["ad"].numel())
+    ad, au, b_rest = s["ad"].cpu().numpy(), s["au"].cpu().numpy(), prob.b_rest.cpu().numpy()
+    hw0 = np.asarray(s["h_wall"], np.float64)
+
+    def jval(hw):
+        b = b_rest.copy()
+        np.add.at(b, s["rows"], s["ap"] * hw)
+        x = np.zeros(n)
+        st, _ = orc.solver(ad.copy(), au.copy(), au.copy(), x, b, s["ia"], s["ja"], n, s["nad"],
+                           True, tol, 100000, 2, 1)
+        assert st == 0
+        return float(np.mean((hw - x[s["rows"]]) / s["ca"]) * prob.scale)
+    out = []
+    for i in idx:
+        e = np.zeros_like(hw0)
+        e[i] = step
+        out.append((jval(hw0 + e) - jval(hw0 - e)) / (2 * step))
+    return np.array(out)
 
 
 def hot_wall_nusselt_at(c, temp, t_wall):
