@@ -173,6 +173,9 @@ SIGNATURES = {
     "fvc_simple_fields": ([P, P, P], I32),
     "fvc_simple_set_fields": ([P, P, P], I32),
     "fvc_simple_destroy": ([P], I32),
+    "fvc_simple_batch_create": ([P, I32, P, I32, I32], I32),
+    "fvc_simple_batch_iterate": ([P, I32, P, P], I32),
+    "fvc_simple_batch_destroy": ([P], I32),
 }
 
 _lib = None

@@ -118,3 +118,44 @@ def heated_lid_cavity(nx: int, re: float = 100.0, side: float = 0.01, dt_wall: f
     c["sedge"][:, :nsh, 0][top] = lid
     c.update(gravity=np.array([0.0, 0.0]), re=re, lid=lid)
     return c
+
+
+def heated_channel(nx: int, re: float = 100.0, side: float = 0.01, dt_wall: float = 1.0,
+                   t0: float = 20.0, kind: str = "quad") -> dict:
+    """A square section of a heated channel of air for the ideal-gas loop
+    with the energy equation: inflow at x = 0 with U = Re nu / side (momentum
+    pedge 2, sedge (U, 0)), outflow at x = side at the reference pressure
+    (pedge 3, pressure 0), no-slip walls at y = 0 and y = side; no pressure
+    pin, because the outflow fixes the pressure level; the air enters at
+    t0 - dt_wall/2 (energy pedge 2), the bottom wall is held at t0 + dt_wall/2
+    (energy pedge 1), the top wall is adiabatic and the outflow carries the
+    enthalpy out (energy pedge 4); no gravity (forced convection).  Keys as
+    heated_lid_cavity, plus u_in."""
+    c = heated_lid_cavity(nx, re=re, side=side, dt_wall=dt_wall, t0=t0, kind=kind)
+    mu, rho, _, _, _ = AIR
+    u_in = re * (mu / rho) / side
+    nsh, n = c["nshared"], c["numel"]
+    m = c["mesh"]
+    a = c["coor"][m.ix - 1]
+    nxt = np.take_along_axis(m.ix, (np.arange(nsh)[None, :] + 1) % m.nsides[:, None], axis=1)
+    b = c["coor"][nxt - 1]
+    used = np.arange(nsh)[None, :] < m.nsides[:, None]
+    bnd = used & (c["nelcon"] < 0)
+    tol = 1e-9 * c["side"]
+    on = lambda d, v: bnd & (np.abs(a[..., d] - v) < tol) & (np.abs(b[..., d] - v) < tol)
+    left, right = on(0, 0.0), on(0, c["side"])
+    bottom = on(1, 0.0)
+    pedge = np.zeros((n, nsh + 1), np.int32)          # walls, and no p' pin
+    sedge = np.zeros((n, nsh + 1, 3))
+    pedge[:, :nsh][left] = 2
+    sedge[:, :nsh, 0][left] = u_in
+    pedge[:, :nsh][right] = 3                          # pressure 0 on the outflow
+    pe = np.zeros((n, nsh + 1), np.int32)
+    se = np.zeros((n, nsh + 1))
+    pe[:, :nsh][left] = 2
+    se[:, :nsh][left] = t0 - 0.5 * dt_wall
+    pe[:, :nsh][bottom] = 1
+    se[:, :nsh][bottom] = t0 + 0.5 * dt_wall
+    pe[:, :nsh][right] = 4
+    c.update(pedge=pedge, sedge=sedge, pedgeE=pe, sedgeE=se, lid=0.0, u_in=u_in)
+    return c

@@ -277,3 +277,47 @@ class SimpleLoop:
             self.close()
         except Exception:
             pass
+
+
+class SimpleBatch:
+    """Many SimpleLoop cases advanced together (fvc_simple_batch_* of
+    include/fvcgpu.h): per outer iteration every stage's solves of all
+    cases in one persistent launch, the whole iteration one CUDA graph.
+    The loops must outlive the batch.  precision ("fp64" or "mixed") for the
+    p' solves, precision_u for u, v and the enthalpy (None: as precision)."""
+
+    def __init__(self, loops, precision: str = "fp64", precision_u: str | None = None):
+        self._L = _lib.load()
+        self.loops = list(loops)
+        handles = (C.c_void_p * len(self.loops))(*[lp._h.value for lp in self.loops])
+        h = C.c_void_p()
+        code = {"fp64": _lib.FVC_PREC_FP64, "mixed": _lib.FVC_PREC_MIXED}
+        prec_u = -1 if precision_u is None else code[precision_u]
+        _lib.check(self._L.fvc_simple_batch_create(C.byref(h), len(self.loops),
+                                                   C.cast(handles, C.c_void_p), code[precision],
+                                                   prec_u),
+                   "fvc_simple_batch_create")
+        self._h = h
+
+    def iterate(self, nit: int, nres: int):
+        """nit outer iterations of every case: (residuals (nit, ncases,
+        nres), solver iterations (nit, ncases, nres)); nres 3 (isothermal
+        loops) or 4 (loops with the energy equation)."""
+        nc = len(self.loops)
+        res = np.zeros((nit, nc, nres))
+        its = np.zeros((nit, nc, nres), np.int32)
+        _lib.check(self._L.fvc_simple_batch_iterate(self._h, nit, res.ctypes.data_as(C.c_void_p),
+                                                    its.ctypes.data_as(C.c_void_p)),
+                   "fvc_simple_batch_iterate")
+        return res, its
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._L.fvc_simple_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -991,6 +991,28 @@ void solver_(double *ad, double *au, double *al, double *x, double *b, const int
 
 namespace fvc {
 
+int32_t context_plan_batched(fvc_context *c, int nsys, const int32_t *row_start,
+                             const int32_t *codes, const double *tols, const double *its_hint,
+                             const int32_t *inits, const int32_t *run, double tol,
+                             const fvc_opts &o, BatchPlan &P) {
+  if (!c || !c->has_matrix) return FVC_ERR_ARG;
+  cudaSetDevice(c->device);
+  return plan_batched(c->A, c->S, nsys, row_start, codes, tols, its_hint, inits, run, tol, o,
+                      c->stream, true, P);
+}
+
+int32_t context_enqueue_batched(fvc_context *c, const BatchPlan &P, const double *b, double *x,
+                                int maxit, const fvc_opts &o) {
+  if (!c || !c->has_matrix) return FVC_ERR_ARG;
+  return enqueue_batched(c->A, c->S, P, b, x, maxit, o, c->stream);
+}
+
+void context_free_batched(fvc_context *c, BatchPlan &P) {
+  free_batched(P, c ? c->stream : nullptr);
+}
+
+int context_default_init(int code, int matriz) { return default_init(code, matriz); }
+
 int32_t context_prepare(fvc_context *c, int code, const fvc_opts &o) {
   if (!c || !c->has_matrix) return FVC_ERR_ARG;
   cudaSetDevice(c->device);

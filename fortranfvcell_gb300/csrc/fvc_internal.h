@@ -203,5 +203,16 @@ int32_t gradient_async(const fvc_cell_mesh *m, int kind, int comp, const double 
 
 // Allocates what fvc_solve_async needs for (code, opts) on this context.
 int32_t context_prepare(fvc_context *c, int code, const fvc_opts &o);
+// A persistent batched plan over the context's block-diagonal matrix, its
+// capturable launch on the context's stream, and its release (BatchPlan).
+int32_t context_plan_batched(fvc_context *c, int nsys, const int32_t *row_start,
+                             const int32_t *codes, const double *tols, const double *its_hint,
+                             const int32_t *inits, const int32_t *run, double tol,
+                             const fvc_opts &o, BatchPlan &P);
+int32_t context_enqueue_batched(fvc_context *c, const BatchPlan &P, const double *b, double *x,
+                                int maxit, const fvc_opts &o);
+void context_free_batched(fvc_context *c, BatchPlan &P);
+// src/Solver.f's warm-start rule for (code, matriz): 1 zeroes x first
+int context_default_init(int code, int matriz);
 
 }  // namespace fvc

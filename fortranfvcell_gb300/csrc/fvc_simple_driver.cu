@@ -1047,3 +1047,563 @@ int32_t fvc_simple_destroy(fvc_simple *s) {
 }
 
 }  // extern "C"
+
+// ---- many cases advanced together (fvc_simple_batch) -----------------------
+// The outer iterations of ncases independent SIMPLE loops (each an
+// fvc_simple, created by the caller), with every linear solve of a stage
+// in one persistent launch: all u1 and u2 systems together, then all p'
+// systems, then all enthalpy systems.  Each stage's systems are the
+// diagonal blocks of one matrix on one solver context (each system padded
+// with identity rows to a multiple of 32 rows); a pack kernel gathers the
+// cases' freshly assembled values, right-hand sides and unknowns into it,
+// the batched launch solves every system with its own convergence test and
+// status, an unpack kernel scatters the unknowns back.  The reference's
+// test before each solve (Simple.f: no solve when the right-hand side's or
+// the residual's norm is below 1e-32) becomes a per-system mask read by the
+// launch, and the work after a p' or enthalpy solve (its gradient and
+// simpleUpdate, the temperatures and densities) runs inside a conditional
+// graph node per case.  One outer iteration of all cases is one CUDA graph.
+
+namespace fvc {
+namespace {
+
+// One system of a stage: where its values and unknown live in its case,
+// where they go in the stage's block-diagonal arrays, and the reference's
+// test before its solve.
+struct StageSeg {
+  const double *ad, *au, *b;  // the case's system, equation order (au: nad values)
+  double *x;                  // the case's unknown, cell order
+  const int32_t *num;         // cell -> equation (1-based)
+  const double *dots;         // the case's norms of this stage
+  int n, nad, row0;           // rows, off-diagonals, first row in the stage matrix
+  int dot, use_sqrt;          // solve when dots[dot] (or its square root) >= 1e-32
+  long long au0;              // first off-diagonal in the stage matrix
+};
+
+// values, right-hand sides and unknowns (to equation order) into the stage
+// arrays; the mask from the reference's test.  blockIdx.y = system.
+__global__ void stage_pack(const StageSeg *segs, double *ad, double *au, double *b, double *x,
+                           int32_t *run) {
+  const StageSeg g = segs[blockIdx.y];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < g.n) {
+    ad[g.row0 + i] = g.ad[i];
+    b[g.row0 + i] = g.b[i];
+    x[g.row0 + g.num[i] - 1] = g.x[i];
+  }
+  if (i < g.nad) au[g.au0 + i] = g.au[i];
+  if (i == 0) {
+    const double v = g.use_sqrt ? sqrt(g.dots[g.dot]) : g.dots[g.dot];
+    run[blockIdx.y] = (v >= 1.0e-32) ? 1 : 0;
+  }
+}
+
+// the unknowns back to the cases (a masked system gives back what it got)
+__global__ void stage_unpack(const StageSeg *segs, const double *x) {
+  const StageSeg g = segs[blockIdx.y];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < g.n) g.x[i] = x[g.row0 + g.num[i] - 1];
+}
+
+// per case: run the work after its solve when the solve ran and ended with
+// FVC_OK (the batched launch's status slots: 16 ints per system, [1] status)
+struct CondSet {
+  const cudaGraphConditionalHandle *h;
+  const int32_t *run;
+  const int *ires;
+  int ncases;
+};
+__global__ void stage_conds(CondSet a) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= a.ncases) return;
+  const unsigned int go = (a.run[c] != 0 && a.ires[16 * c + 1] == FVC_OK) ? 1u : 0u;
+  cudaGraphSetConditional(a.h[c], go);
+}
+
+// each case's norms (k of them, from its dots) into its record slots
+__global__ void rec_case_dots(const double *const *dots, int ncases, int k, int off,
+                              double *rec) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncases) return;
+  for (int i = 0; i < k; ++i) rec[5 * (size_t)c + off + i] = dots[c][i];
+}
+
+// each system of a stage: run, status, iterations (mixed: the FP32 ones)
+__global__ void rec_stage(const int32_t *run, const int *ires, int nsys, int mixed,
+                          int32_t *rec) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nsys) return;
+  rec[4 * (size_t)s] = run[s];
+  rec[4 * (size_t)s + 1] = run[s] ? ires[16 * s + 1] : FVC_OK;
+  rec[4 * (size_t)s + 2] = run[s] ? (mixed ? ires[16 * s + 2] : ires[16 * s]) : 0;
+  rec[4 * (size_t)s + 3] = run[s] ? ires[16 * s + 2] : 0;
+}
+
+// the cases' gradient error words, or-ed
+__global__ void rec_errs(const int32_t *const *errs, int ncases, int32_t *out) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < ncases && *errs[c] != 0) atomicOr(out, 1);
+}
+
+}  // namespace
+}  // namespace fvc
+
+struct fvc_simple_batch {
+  int device = 0, ncases = 0;
+  cudaStream_t stream = nullptr, body = nullptr;
+  bool gas = false;
+  int precision = FVC_PREC_FP64;    // p'
+  int precision_u = FVC_PREC_FP64;  // u, v and the enthalpy
+  std::vector<fvc_simple *> cs;
+  struct Stage {
+    int nsys = 0, maxlen = 0;
+    fvc_context *ctx = nullptr;
+    std::vector<int32_t> row_start, codes, inits, sys_case, sys_which;
+    std::vector<double> tols, hints;
+    fvc::StageSeg *segs = nullptr;  // device
+    double *ad = nullptr, *au = nullptr, *b = nullptr, *x = nullptr;
+    int32_t *run = nullptr;
+    fvc::BatchPlan plan;
+    int32_t *rec = nullptr;  // device: 4 per system
+  } st[3];                   // 0 u1+u2, 1 p', 2 enthalpy
+  double **d_dots = nullptr;    // device array of the cases' dots pointers
+  int32_t **d_errs = nullptr;   // and of their gradient error words
+  double *rec_dots = nullptr;   // device: 5 per case
+  int32_t *rec_err = nullptr;
+  double *h_dots = nullptr;     // pinned copies
+  int32_t *h_sys = nullptr, *h_err = nullptr;
+  cudaGraphConditionalHandle *h_handles = nullptr;  // pinned
+  cudaGraphConditionalHandle *d_handles = nullptr;  // device: p' then enthalpy, per case
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  int64_t launches_top = 0;
+  std::vector<int64_t> launches_body[2];  // per case: after p', after the enthalpy
+  int iterations_done = 0;
+  bool hinted = false;
+  std::vector<void *> owned;
+};
+
+namespace {
+
+template <typename T>
+int32_t balloc(fvc_simple_batch *B, T *&p, size_t n) {
+  if (cudaMalloc(&p, sizeof(T) * std::max<size_t>(n, 1)) != cudaSuccess) return FVC_ERR_CUDA;
+  B->owned.push_back(p);
+  return cudaMemset(p, 0, sizeof(T) * std::max<size_t>(n, 1)) == cudaSuccess ? FVC_OK
+                                                                             : FVC_ERR_CUDA;
+}
+
+void batch_drop_graph(fvc_simple_batch *B) {
+  if (B->gexec) cudaGraphExecDestroy(B->gexec);
+  if (B->graph) cudaGraphDestroy(B->graph);
+  B->gexec = nullptr;
+  B->graph = nullptr;
+}
+
+void batch_release(fvc_simple_batch *B) {
+  batch_drop_graph(B);
+  for (auto &S : B->st) {
+    if (S.ctx) {
+      fvc::context_free_batched(S.ctx, S.plan);
+      fvc_context_destroy(S.ctx);
+    }
+  }
+  for (void *p : B->owned) cudaFree(p);
+  if (B->h_dots) cudaFreeHost(B->h_dots);
+  if (B->h_sys) cudaFreeHost(B->h_sys);
+  if (B->h_err) cudaFreeHost(B->h_err);
+  if (B->h_handles) cudaFreeHost(B->h_handles);
+  if (B->body) cudaStreamDestroy(B->body);
+  if (B->stream) cudaStreamDestroy(B->stream);
+}
+
+// A stage's block-diagonal structure on its context and its device arrays.
+// which: 1 u1, 2 u2 (stage 0), 3 p' (stage 1), 4 enthalpy (stage 2).
+int32_t batch_stage(fvc_simple_batch *B, int k, const std::vector<std::vector<int32_t>> &ia_c,
+                    const std::vector<std::vector<int32_t>> &ja_c) {
+  fvc_simple_batch::Stage &S = B->st[k];
+  const int per = (k == 0) ? 2 : 1;
+  S.nsys = B->ncases * per;
+  S.row_start.assign(S.nsys + 1, 0);
+  std::vector<fvc::StageSeg> h((size_t)S.nsys);
+  std::vector<int32_t> ia(1, 1), ja;
+  long long au0 = 0;
+  for (int c = 0; c < B->ncases; ++c) {
+    fvc_simple *s = B->cs[c];
+    const int n = s->numel;
+    const int nad = ia_c[c][n] - 1;
+    for (int q = 0; q < per; ++q) {
+      const int sys = per * c + q, which = (k == 0) ? 1 + q : (k == 1 ? 3 : 4);
+      const int row0 = S.row_start[sys];
+      const int rows = (n + 31) / 32 * 32;
+      S.row_start[sys + 1] = row0 + rows;
+      fvc::StageSeg &g = h[sys];
+      g.n = n;
+      g.nad = nad;
+      g.row0 = row0;
+      g.au0 = au0;
+      g.num = s->num;
+      g.dots = s->dots;
+      if (which == 1) {
+        g.ad = s->ad1; g.au = s->au1; g.b = s->b1; g.x = s->u1; g.dot = 0; g.use_sqrt = 0;
+      } else if (which == 2) {
+        g.ad = s->ad2; g.au = s->au2; g.b = s->b2; g.x = s->u2; g.dot = 1; g.use_sqrt = 0;
+      } else if (which == 3) {
+        g.ad = s->adp; g.au = s->aup; g.b = s->bp; g.x = s->pc; g.dot = 2; g.use_sqrt = 1;
+      } else {
+        g.ad = s->ade; g.au = s->aue; g.b = s->be; g.x = s->en; g.dot = 0; g.use_sqrt = 1;
+      }
+      S.maxlen = std::max(S.maxlen, std::max(n, nad));
+      // the case's rows (columns shifted), then identity rows to the slice
+      for (int i = 0; i < n; ++i) {
+        for (int q2 = ia_c[c][i] - 1; q2 < ia_c[c][i + 1] - 1; ++q2)
+          ja.push_back(ja_c[c][q2] + row0);
+        ia.push_back((int32_t)ja.size() + 1);
+      }
+      for (int i = n; i < rows; ++i) ia.push_back((int32_t)ja.size() + 1);
+      au0 += nad;
+      const int code = (which <= 2) ? s->o.code_u : (which == 3 ? s->o.code_pc : 2);
+      S.codes.push_back(code);
+      S.inits.push_back(fvc::context_default_init(code, 1));
+      S.tols.push_back(which == 3 ? s->o.tol_pc : s->o.tol_u);
+      S.sys_case.push_back(c);
+      S.sys_which.push_back(which);
+    }
+  }
+  const int N = S.row_start[S.nsys];
+  const long long NAD = au0;
+  if (NAD > INT32_MAX - 1) return FVC_ERR_ARG;
+  int32_t rc;
+  if ((rc = balloc(B, S.segs, (size_t)S.nsys)) != FVC_OK || (rc = balloc(B, S.ad, N)) != FVC_OK ||
+      (rc = balloc(B, S.au, (size_t)NAD)) != FVC_OK || (rc = balloc(B, S.b, N)) != FVC_OK ||
+      (rc = balloc(B, S.x, N)) != FVC_OK || (rc = balloc(B, S.run, (size_t)S.nsys)) != FVC_OK ||
+      (rc = balloc(B, S.rec, 4 * (size_t)S.nsys)) != FVC_OK)
+    return rc;
+  if (cudaMemcpy(S.segs, h.data(), sizeof(fvc::StageSeg) * S.nsys, cudaMemcpyHostToDevice) !=
+      cudaSuccess)
+    return FVC_ERR_CUDA;
+  // identity on the padding rows (the systems' own rows are packed later)
+  std::vector<double> ones((size_t)N, 1.0), zeros((size_t)std::max<long long>(NAD, 1), 0.0);
+  if (cudaMemcpy(S.ad, ones.data(), sizeof(double) * N, cudaMemcpyHostToDevice) != cudaSuccess)
+    return FVC_ERR_CUDA;
+  if ((rc = fvc_context_create(&S.ctx, B->device)) != FVC_OK) return rc;
+  fvc_context_set_stream(S.ctx, B->stream);
+  return fvc_matrix_set(S.ctx, 1, 1, N, (int32_t)NAD, ones.data(), zeros.data(), zeros.data(),
+                        ia.data(), ja.data());
+}
+
+// stage k's solver options: p' (stage 1) takes precision, u/v and the
+// enthalpy precision_u
+fvc_opts batch_opts(const fvc_simple_batch *B, int k) {
+  fvc_opts o;
+  fvc_opts_default(&o);
+  o.precision = (k == 1) ? B->precision : B->precision_u;
+  o.init = 1;
+  return o;
+}
+
+// Plans every stage's launch (hints: the iterations each system took in the
+// last outer iteration, else sqrt(rows)) and captures one outer iteration.
+int32_t batch_build(fvc_simple_batch *B) {
+  batch_drop_graph(B);
+  const int nst = B->gas ? 3 : 2;
+  int32_t rc;
+  for (int k = 0; k < nst; ++k) {
+    fvc_simple_batch::Stage &S = B->st[k];
+    fvc::context_free_batched(S.ctx, S.plan);
+    // the value path's buffers exist before the capture
+    if ((rc = fvc_matrix_update_values_async(S.ctx, S.ad, S.au, S.au)) != FVC_OK) return rc;
+    if ((rc = fvc::context_plan_batched(S.ctx, S.nsys, S.row_start.data(), S.codes.data(),
+                                        S.tols.data(), S.hints.empty() ? nullptr : S.hints.data(),
+                                        S.inits.data(), S.run, 0.0, batch_opts(B, k),
+                                        S.plan)) != FVC_OK)
+      return rc;
+  }
+  if (cudaStreamSynchronize(B->stream) != cudaSuccess) return FVC_ERR_CUDA;
+  cudaStream_t st = B->stream;
+  const int64_t l0 = fvc_kernel_launches();
+  if (!cap_ok(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed), "cudaStreamBeginCapture"))
+    return FVC_ERR_CUDA;
+  rc = FVC_OK;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaGraph_t g = nullptr;
+  const int nc = B->ncases;
+  const int ncond = (B->gas ? 2 : 1) * nc;
+  if (!cap_ok(cudaStreamGetCaptureInfo(st, &cs, nullptr, &g), "cudaStreamGetCaptureInfo"))
+    rc = FVC_ERR_CUDA;
+  for (int k = 0; k < ncond && rc == FVC_OK; ++k)
+    if (!cap_ok(cudaGraphConditionalHandleCreate(&B->h_handles[k], g, 0,
+                                                 cudaGraphCondAssignDefault),
+                "cudaGraphConditionalHandleCreate"))
+      rc = FVC_ERR_CUDA;
+  if (rc == FVC_OK &&
+      !cap_ok(cudaMemcpyAsync(B->d_handles, B->h_handles,
+                              sizeof(cudaGraphConditionalHandle) * ncond, cudaMemcpyHostToDevice,
+                              st),
+              "cudaMemcpyAsync (handles)"))
+    rc = FVC_ERR_CUDA;
+  auto solve_stage = [&](int k) -> int32_t {
+    fvc_simple_batch::Stage &S = B->st[k];
+    const unsigned gx = (unsigned)((S.maxlen + fvc::kT - 1) / fvc::kT);
+    fvc::stage_pack<<<dim3(gx, (unsigned)S.nsys), fvc::kT, 0, st>>>(S.segs, S.ad, S.au, S.b, S.x,
+                                                                    S.run);
+    fvc::count_launch();
+    int32_t r = fvc_matrix_update_values_async(S.ctx, S.ad, S.au, S.au);
+    if (r != FVC_OK) return r;
+    const fvc_opts o = batch_opts(B, k);
+    if ((r = fvc::context_enqueue_batched(S.ctx, S.plan, S.b, S.x, B->cs[0]->o.maxit, o)) !=
+        FVC_OK)
+      return r;
+    fvc::rec_stage<<<(S.nsys + 127) / 128, 128, 0, st>>>(
+        S.run, S.plan.ires, S.nsys, o.precision == FVC_PREC_MIXED ? 1 : 0, S.rec);
+    fvc::count_launch();
+    fvc::stage_unpack<<<dim3(gx, (unsigned)S.nsys), fvc::kT, 0, st>>>(S.segs, S.x);
+    fvc::count_launch();
+    return FVC_OK;
+  };
+  // IF(the case's solve ran and ended FVC_OK) { after(case) } for every case
+  auto after_stage = [&](int k, int hoff, int which) -> int32_t {
+    fvc_simple_batch::Stage &S = B->st[k];
+    fvc::CondSet a{B->d_handles + hoff, S.run, S.plan.ires, nc};
+    fvc::stage_conds<<<(nc + 127) / 128, 128, 0, st>>>(a);
+    fvc::count_launch();
+    for (int c = 0; c < nc; ++c) {
+      fvc_simple *s = B->cs[c];
+      // cap_if captures into the case's own body stream: point it at ours
+      cudaStream_t keep_stream = s->stream, keep_body = s->body;
+      s->stream = st;
+      s->body = B->body;
+      int64_t nl = 0;
+      const int32_t r = cap_if(s, B->h_handles[hoff + c], &nl, [&](cudaStream_t bs) {
+        return which == 3 ? after_pressure(s, bs) : after_energy(s, bs);
+      });
+      s->stream = keep_stream;
+      s->body = keep_body;
+      B->launches_body[which == 3 ? 0 : 1][c] = nl;
+      if (r != FVC_OK) return r;
+    }
+    return FVC_OK;
+  };
+  for (int c = 0; c < nc && rc == FVC_OK; ++c) rc = stage_momentum(B->cs[c], st);
+  if (rc == FVC_OK) rc = solve_stage(0);
+  for (int c = 0; c < nc && rc == FVC_OK; ++c) rc = stage_pressure(B->cs[c], st);
+  if (rc == FVC_OK) {
+    fvc::rec_case_dots<<<(nc + 127) / 128, 128, 0, st>>>(B->d_dots, nc, 3, 0, B->rec_dots);
+    fvc::count_launch();
+    rc = solve_stage(1);
+  }
+  if (rc == FVC_OK) rc = after_stage(1, 0, 3);
+  if (B->gas) {
+    for (int c = 0; c < nc && rc == FVC_OK; ++c) rc = stage_energy(B->cs[c], st);
+    if (rc == FVC_OK) {
+      fvc::rec_case_dots<<<(nc + 127) / 128, 128, 0, st>>>(B->d_dots, nc, 2, 3, B->rec_dots);
+      fvc::count_launch();
+      rc = solve_stage(2);
+    }
+    if (rc == FVC_OK) rc = after_stage(2, nc, 4);
+  }
+  if (rc == FVC_OK) {
+    cudaMemsetAsync(B->rec_err, 0, sizeof(int32_t), st);
+    fvc::rec_errs<<<(nc + 127) / 128, 128, 0, st>>>(B->d_errs, nc, B->rec_err);
+    fvc::count_launch();
+  }
+  cudaGraph_t out = nullptr;
+  const bool ended = cap_ok(cudaStreamEndCapture(st, &out), "cudaStreamEndCapture");
+  int64_t body = 0;
+  for (int q = 0; q < 2; ++q)
+    for (int64_t v : B->launches_body[q]) body += v;
+  B->launches_top = fvc_kernel_launches() - l0 - body;
+  fvc::count_launch(l0 - fvc_kernel_launches());  // counted per replay instead
+  if (rc == FVC_OK && !ended) rc = FVC_ERR_CUDA;
+  if (rc == FVC_OK) {
+    cudaGraphInstantiateParams ip;
+    memset(&ip, 0, sizeof(ip));
+    if (!cap_ok(cudaGraphInstantiateWithParams(&B->gexec, out, &ip),
+                "cudaGraphInstantiateWithParams"))
+      rc = FVC_ERR_CUDA;
+  }
+  if (rc != FVC_OK) {
+    if (out) cudaGraphDestroy(out);
+    cudaGetLastError();
+    fprintf(stderr, "fvcgpu: the batched SIMPLE iteration could not be captured (status %d)\n",
+            rc);
+    return rc;
+  }
+  B->graph = out;
+  return FVC_OK;
+}
+
+const char *const kBatchSys[4] = {"u1", "u2", "p'", "energy"};
+
+// one outer iteration of every case: the graph launch, then its record
+int32_t batch_step(fvc_simple_batch *B, int it, double *res, int32_t *its) {
+  cudaStream_t st = B->stream;
+  const int nc = B->ncases, nrep = B->gas ? 4 : 3, nst = B->gas ? 3 : 2;
+  if (cudaGraphLaunch(B->gexec, st) != cudaSuccess) return FVC_ERR_CUDA;
+  cudaMemcpyAsync(B->h_dots, B->rec_dots, sizeof(double) * 5 * nc, cudaMemcpyDeviceToHost, st);
+  size_t off = 0;
+  for (int k = 0; k < nst; ++k) {
+    cudaMemcpyAsync(B->h_sys + off, B->st[k].rec, sizeof(int32_t) * 4 * B->st[k].nsys,
+                    cudaMemcpyDeviceToHost, st);
+    off += 4 * (size_t)B->st[k].nsys;
+  }
+  cudaMemcpyAsync(B->h_err, B->rec_err, sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+  if (cudaStreamSynchronize(st) != cudaSuccess) return FVC_ERR_CUDA;
+  if (*B->h_err) return FVC_ERR_UNSUPPORTED;  // a velocity boundary code outside 0..4
+  int64_t launched = B->launches_top;
+  int32_t status = FVC_OK;
+  off = 0;
+  for (int k = 0; k < nst; ++k) {
+    fvc_simple_batch::Stage &S = B->st[k];
+    for (int sy = 0; sy < S.nsys; ++sy) {
+      const int32_t *r = B->h_sys + off + 4 * (size_t)sy;
+      const int c = S.sys_case[sy], which = S.sys_which[sy];
+      if (its) its[((size_t)it * nc + c) * nrep + (which - 1)] = r[0] ? r[2] : 0;
+      if (r[0] && r[1] == FVC_OK && which >= 3) launched += B->launches_body[which - 3][c];
+      if (r[0] && r[1] != FVC_OK && status == FVC_OK) {
+        fprintf(stderr, "fvcgpu: SIMPLE batch: case %d, %s solve ended with status %d after %d "
+                        "iterations\n", c, kBatchSys[which - 1], r[1], r[2]);
+        status = r[1];
+      }
+      // the next plan's share of blocks follows the iterations it took
+      if (r[0] && r[2] > 0) S.hints[sy] = (double)r[2];
+    }
+    off += 4 * (size_t)S.nsys;
+  }
+  fvc::count_launch(launched);
+  if (res)
+    for (int c = 0; c < nc; ++c) {
+      const double *d = B->h_dots + 5 * (size_t)c;
+      double *rr = res + ((size_t)it * nc + c) * nrep;
+      rr[0] = std::sqrt(d[0]);
+      rr[1] = std::sqrt(d[1]);
+      rr[2] = std::sqrt(d[2]);
+      if (nrep == 4) rr[3] = (std::sqrt(d[3]) >= 1.0e-32) ? std::sqrt(d[4]) : std::sqrt(d[3]);
+    }
+  return status;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t fvc_simple_batch_create(fvc_simple_batch **out, int32_t ncases,
+                                fvc_simple *const *cases, int32_t precision,
+                                int32_t precision_u) {
+  if (!out || ncases < 1 || !cases) return FVC_ERR_ARG;
+  if (precision_u < 0) precision_u = precision;
+  if ((precision != FVC_PREC_FP64 && precision != FVC_PREC_MIXED) ||
+      (precision_u != FVC_PREC_FP64 && precision_u != FVC_PREC_MIXED))
+    return FVC_ERR_UNSUPPORTED;
+  *out = nullptr;
+  fvc_simple *c0 = cases[0];
+  if (!c0) return FVC_ERR_ARG;
+  for (int c = 0; c < ncases; ++c) {
+    const fvc_simple *s = cases[c];
+    if (!s || s->device != c0->device || s->gas != c0->gas || s->o.matriz_u != 1 ||
+        s->o.matriz_pc != 1 || s->o.maxit != c0->o.maxit)
+      return FVC_ERR_ARG;
+  }
+  auto *B = new (std::nothrow) fvc_simple_batch();
+  if (!B) return FVC_ERR_CUDA;
+  B->device = c0->device;
+  B->ncases = ncases;
+  B->gas = c0->gas;
+  B->precision = precision;
+  B->precision_u = precision_u;
+  B->cs.assign(cases, cases + ncases);
+  cudaSetDevice(B->device);
+  int32_t rc = FVC_OK;
+  if (cudaStreamCreateWithFlags(&B->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&B->body, cudaStreamNonBlocking) != cudaSuccess)
+    rc = FVC_ERR_CUDA;
+  // every case's CSRD structure on the host (the one all its systems share)
+  std::vector<std::vector<int32_t>> ia_c(ncases), ja_c(ncases);
+  for (int c = 0; c < ncases && rc == FVC_OK; ++c) {
+    fvc_simple *s = cases[c];
+    if (cudaStreamSynchronize(s->stream) != cudaSuccess) rc = FVC_ERR_CUDA;
+    ia_c[c].resize(s->numel + 1);
+    int32_t nad = 0;
+    int64_t len = 0;
+    if (rc == FVC_OK)
+      rc = fvc_mesh_datastruc(s->ident.data(), s->numel, s->nshared, 1, 1, ia_c[c].data(),
+                              nullptr, &nad, &len);
+    ja_c[c].resize((size_t)std::max<int64_t>(len, 1));
+    if (rc == FVC_OK)
+      rc = fvc_mesh_datastruc(s->ident.data(), s->numel, s->nshared, 1, 1, ia_c[c].data(),
+                              ja_c[c].data(), &nad, &len);
+  }
+  const int nst = B->gas ? 3 : 2;
+  for (int k = 0; k < nst && rc == FVC_OK; ++k) rc = batch_stage(B, k, ia_c, ja_c);
+  const int ncond = (B->gas ? 2 : 1) * ncases;
+  size_t nsys_all = 0;
+  for (int k = 0; k < nst; ++k) nsys_all += (size_t)B->st[k].nsys;
+  if (rc == FVC_OK) {
+    std::vector<double *> dots(ncases);
+    std::vector<int32_t *> errs(ncases);
+    for (int c = 0; c < ncases; ++c) {
+      dots[c] = cases[c]->dots;
+      errs[c] = cases[c]->d_err;
+    }
+    if ((rc = balloc(B, B->d_dots, ncases)) == FVC_OK && (rc = balloc(B, B->d_errs, ncases)) ==
+        FVC_OK && (rc = balloc(B, B->rec_dots, 5 * (size_t)ncases)) == FVC_OK &&
+        (rc = balloc(B, B->rec_err, 1)) == FVC_OK && (rc = balloc(B, B->d_handles, ncond)) == FVC_OK) {
+      if (cudaMemcpy(B->d_dots, dots.data(), sizeof(double *) * ncases, cudaMemcpyHostToDevice) !=
+              cudaSuccess ||
+          cudaMemcpy(B->d_errs, errs.data(), sizeof(int32_t *) * ncases,
+                     cudaMemcpyHostToDevice) != cudaSuccess)
+        rc = FVC_ERR_CUDA;
+    }
+  }
+  if (rc == FVC_OK &&
+      (cudaMallocHost(&B->h_dots, sizeof(double) * 5 * ncases) != cudaSuccess ||
+       cudaMallocHost(&B->h_sys, sizeof(int32_t) * 4 * nsys_all) != cudaSuccess ||
+       cudaMallocHost(&B->h_err, sizeof(int32_t)) != cudaSuccess ||
+       cudaMallocHost(&B->h_handles, sizeof(cudaGraphConditionalHandle) * ncond) != cudaSuccess))
+    rc = FVC_ERR_CUDA;
+  if (rc == FVC_OK) {
+    for (int q = 0; q < 2; ++q) B->launches_body[q].assign(ncases, 0);
+    for (int k = 0; k < nst; ++k) {
+      B->st[k].hints.resize(B->st[k].nsys);
+      for (int sy = 0; sy < B->st[k].nsys; ++sy)  // until measured: sqrt(rows)
+        B->st[k].hints[sy] =
+            std::sqrt((double)(B->st[k].row_start[sy + 1] - B->st[k].row_start[sy]));
+    }
+  }
+  if (rc != FVC_OK) {
+    batch_release(B);
+    delete B;
+    return rc;
+  }
+  *out = B;
+  return FVC_OK;
+}
+
+int32_t fvc_simple_batch_iterate(fvc_simple_batch *B, int32_t nit, double *res, int32_t *its) {
+  if (!B || nit < 0) return FVC_ERR_ARG;
+  cudaSetDevice(B->device);
+  for (int it = 0; it < nit; ++it) {
+    // the first outer iteration runs on sqrt(rows) shares; the graph is
+    // captured again once, with the iterations it took as the shares
+    if (!B->gexec || (B->iterations_done >= 1 && !B->hinted)) {
+      if (B->iterations_done >= 1) B->hinted = true;
+      const int32_t rc = batch_build(B);
+      if (rc != FVC_OK) return rc;
+    }
+    const int32_t rc = batch_step(B, it, res, its);
+    ++B->iterations_done;
+    if (rc != FVC_OK) return rc;
+  }
+  return FVC_OK;
+}
+
+int32_t fvc_simple_batch_destroy(fvc_simple_batch *B) {
+  if (!B) return FVC_ERR_ARG;
+  cudaSetDevice(B->device);
+  cudaStreamSynchronize(B->stream);
+  batch_release(B);
+  delete B;
+  return FVC_OK;
+}
+
+}  // extern "C"

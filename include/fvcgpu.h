@@ -679,6 +679,44 @@ int32_t fvc_simple_set_fields(fvc_simple *s, const double *w, const double *p);
 
 int32_t fvc_simple_destroy(fvc_simple *s);
 
+/* ---- many SIMPLE cases together ------------------------------------------ */
+/* No single counterpart in the reference, which runs one case per process
+ * (src/Simple.f:317-801 per case).  The outer iterations of ncases
+ * independent loops (each an fvc_simple from fvc_simple_create, with
+ * fvc_simple_energy for all of them or for none; CSRD systems, matriz_u =
+ * matriz_pc = 1; one device; one maxit), with the linear solves of every
+ * stage in one persistent launch: all u1 and u2 systems, then all p'
+ * systems, then all enthalpy systems, each system with its own convergence
+ * test, tolerance (its case's tol_u / tol_pc), method (code_u / code_pc;
+ * BiCGSTAB for the enthalpy) and status.  precision (the p' systems) and
+ * precision_u (u, v and the enthalpy; < 0: as precision): FVC_PREC_FP64 or
+ * FVC_PREC_MIXED (FP32 iterations, FP64 refinement to the same tolerances
+ * on ||b - Ax||2 / ||b||2).  A mixed BiCGSTAB whose FP32 sweeps stall is not
+ * finished in FP64 inside a batch: the call ends with FVC_ERR_NOCONV, so
+ * systems prone to that (the enthalpy of a natural-convection or heated
+ * flow) keep precision_u FP64.  The reference's tests before a
+ * solve skip that system inside the launch (a per-system mask), and the work
+ * after a skipped p' or enthalpy solve is skipped with it.  Each outer
+ * iteration of all cases is one CUDA graph launch (captured at the first
+ * call, and again after the first outer iteration with each system's
+ * iteration count as its share of the launch's blocks).  The batch borrows
+ * the cases, which must outlive it; their fields are those of the loops
+ * (fvc_simple_fields etc.).  ncases is limited by the co-resident blocks of
+ * one launch (1216 on this GPU at 128 threads: 608 cases). */
+typedef struct fvc_simple_batch fvc_simple_batch;
+int32_t fvc_simple_batch_create(fvc_simple_batch **out, int32_t ncases,
+                                fvc_simple *const *cases, int32_t precision,
+                                int32_t precision_u);
+/* nit outer iterations of every case.  res (may be NULL) receives, per
+ * iteration and case, the norms fvc_simple_iterate (3: u1, u2, p') or
+ * fvc_simple_iterate_energy (4: and the enthalpy) return, at
+ * res[(it * ncases + case) * nres + k]; its likewise the solver iterations
+ * (FP32 ones for mixed, 0 where a solve was skipped).  A failed solve ends
+ * the call with its status after the outer iteration it failed in. */
+int32_t fvc_simple_batch_iterate(fvc_simple_batch *b, int32_t nit, double *res,
+                                 int32_t *its);
+int32_t fvc_simple_batch_destroy(fvc_simple_batch *b);
+
 #ifdef __cplusplus
 }
 #endif
