@@ -45,6 +45,7 @@ class FvcOpts(C.Structure):
         ("update_beta", I32),
         ("staging", I32),
         ("max_blocks", I32),
+        ("fp32_layout", I32),
     ]
 
 

@@ -540,7 +540,8 @@ int32_t fvc_spmv_fast(fvc_context *c, const double *d_x, double *d_y) {
 
 int32_t fvc_spmv_f32(fvc_context *c, const float *d_x, float *d_y) {
   if (!c || !c->has_matrix || !d_x || !d_y) return FVC_ERR_ARG;
-  int32_t rc = fvc::build_f32_copy(c->A, c->stream);
+  // the operator as the context's last mixed solve laid it out
+  int32_t rc = fvc::build_f32_copy(c->A, c->stream, c->A.layout32 ? c->A.layout_mode : 0);
   if (rc != FVC_OK) return rc;
   return fvc::launch_spmv_f32(c->A, d_x, d_y, c->stream);
 }
@@ -712,6 +713,21 @@ int32_t fvc_autotune(fvc_context *c, int32_t code, int32_t precision, int32_t tr
       o.staging = stg;
       cand.push_back(o);
     }
+  }
+  if (precision == FVC_PREC_MIXED) {
+    // the FP32 operator's slice widths: each slice its own width (no
+    // padding slots) against the uniform padded width of the shapes above,
+    // with the automatic shape and, for CG, both load forms
+    fvc_opts o = base;
+    o.fp32_layout = 1;
+    cand.push_back(o);
+    if (code == 1)
+      for (int stg : {1, 2}) {
+        fvc_opts q = o;
+        q.block_threads = 1024;
+        q.staging = stg;
+        cand.push_back(q);
+      }
   }
   int32_t rc = FVC_OK;
   double best_t = 0.0;

@@ -40,6 +40,7 @@ struct DeviceMatrix {
   int ell_w = 0;             // FP32 copy padded to this uniform slice width (0: SELL)
   bool have32 = false;
   bool layout32 = false;     // the FP32 layout (col16_ok, ell_w, buffers) is decided
+  int layout_mode = 0;       // ... for this fvc_opts.fp32_layout
   int cl_smax = -1;          // cluster PCG: most slots of one CTA's rows (-1: unknown)
   int *mirror = nullptr;     // per slot: the slot of the transposed entry (built on demand)
   // a mixed BiCGSTAB on this structure stalled: its later mixed BiCGSTAB
@@ -148,6 +149,7 @@ struct BatchPlan {
   BatchSys *dsys = nullptr;
   int *dsob = nullptr;
   double tol = 0.0;
+  int fp32_layout = 0;
 };
 int32_t plan_batched(DeviceMatrix &A, Scratch &S, int nsys, const int32_t *row_start,
                      const int32_t *codes, const double *tols, const double *its_hint,
@@ -169,7 +171,8 @@ int32_t launch_spmv(const DeviceMatrix &A, const double *x, double *y,
 int32_t launch_reciprocal(const DeviceMatrix &A, cudaStream_t stream);
 int32_t launch_spmv_f32(const DeviceMatrix &A, const float *x, float *y,
                         cudaStream_t stream);
-int32_t build_f32_copy(DeviceMatrix &A, cudaStream_t stream);
+// mode: fvc_opts.fp32_layout (0 uniform width where possible, 1 own widths)
+int32_t build_f32_copy(DeviceMatrix &A, cudaStream_t stream, int mode);
 int32_t ensure_f32_vectors(Scratch &S, size_t n);
 // batched mixed-precision solves (fvc_mixed.cu): the kernel for the block
 // size (for occupancy queries) and its cooperative launch over the batch

@@ -963,7 +963,7 @@ int32_t plan_batched(DeviceMatrix &A, Scratch &S, int nsys, const int32_t *row_s
   const int threads = (o.block_threads > 0) ? block_threads_for(o.block_threads, 0, 1) : 128;
   const bool mixed = o.precision == FVC_PREC_MIXED;
   if (mixed) {
-    int32_t rc = build_f32_copy(A, stream);
+    int32_t rc = build_f32_copy(A, stream, o.fp32_layout);
     if (rc == FVC_OK) rc = ensure_f32_vectors(S, (size_t)A.n);
     if (rc != FVC_OK) return rc;
   }
@@ -1128,6 +1128,7 @@ int32_t plan_batched(DeviceMatrix &A, Scratch &S, int nsys, const int32_t *row_s
   P.dsys = dsys;
   P.dsob = dsob;
   P.tol = tol;
+  P.fp32_layout = o.fp32_layout;
   return FVC_OK;
 }
 
@@ -1140,7 +1141,7 @@ int32_t enqueue_batched(DeviceMatrix &A, Scratch &S, const BatchPlan &P, const d
   if (P.mixed) {
     // the FP32 operator of the current values (stream-ordered once its
     // layout is decided, which planning did)
-    int32_t rc = build_f32_copy(A, stream);
+    int32_t rc = build_f32_copy(A, stream, P.fp32_layout);
     if (rc != FVC_OK) return rc;
     return launch_mixed_batched(A, S, P.dsys, P.dsob, P.total, P.threads, b, x, maxit, o, stream);
   }

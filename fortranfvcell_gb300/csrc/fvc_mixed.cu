@@ -1527,7 +1527,18 @@ int32_t launch_mixed_batched(const DeviceMatrix &A, const Scratch &S, const Batc
 // The FP32 operator: its layout (16-bit offsets, uniform width) once per
 // structure, with a host wait; then, after every value upload, the values
 // alone, stream-ordered (so that a captured graph can rebuild them).
-int32_t build_f32_copy(DeviceMatrix &A, cudaStream_t stream) {
+int32_t build_f32_copy(DeviceMatrix &A, cudaStream_t stream, int mode) {
+  if (A.layout32 && A.layout_mode != mode) {
+    // the other slice-width choice: the operator is laid out anew (its
+    // slot arrays have another size)
+    if (cudaStreamSynchronize(stream) != cudaSuccess) return FVC_ERR_CUDA;
+    cudaFree(A.val32);
+    cudaFree(A.col16);
+    A.val32 = nullptr;
+    A.col16 = nullptr;
+    A.layout32 = false;
+    A.have32 = false;
+  }
   if (A.have32) return FVC_OK;
   int blocks = std::max(1, std::min((A.nslices + 7) / 8, sm_count_m() * 8));
   if (A.layout32) {
@@ -1555,7 +1566,8 @@ int32_t build_f32_copy(DeviceMatrix &A, cudaStream_t stream) {
   A.col16_ok = (hf[0] == 0);
   // slices at most 4 wide (the cells of triangle / quadrilateral meshes):
   // pad them all to the widest, so the staged kernel needs no slice pointers
-  A.ell_w = (A.col16_ok && A.nslices > 0 && hf[2] >= 3 && hf[2] <= 4) ? hf[2] : 0;
+  A.ell_w = (mode == 0 && A.col16_ok && A.nslices > 0 && hf[2] >= 3 && hf[2] <= 4) ? hf[2] : 0;
+  A.layout_mode = mode;
   const size_t sl = std::max<size_t>(
       1, A.ell_w > 0 ? (size_t)A.nslices * kSlice * A.ell_w : (size_t)A.slots);
   if (!A.val32 && cudaMalloc(&A.val32, sizeof(float) * sl) != cudaSuccess) return FVC_ERR_CUDA;
@@ -1585,7 +1597,7 @@ int32_t enqueue_mixed(const DeviceMatrix &A0, Scratch &S, int code, const double
                       bool launch) {
   DeviceMatrix &A = const_cast<DeviceMatrix &>(A0);
   if (code != 1 && code != 2) return FVC_ERR_UNSUPPORTED;
-  int32_t rc = build_f32_copy(A, stream);
+  int32_t rc = build_f32_copy(A, stream, o.fp32_layout);
   if (rc != FVC_OK) return rc;
   if ((rc = ensure_f32_vectors(S, (size_t)A.n)) != FVC_OK) return rc;
   const int threads = block_threads_for(o.block_threads, A.nslices, sm_count_m());

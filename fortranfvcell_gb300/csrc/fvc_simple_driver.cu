@@ -9,6 +9,7 @@
 // (momentum, p'), whose values are refreshed from the device each time.
 // Only the few norms that steer the reference's control flow cross to the
 // host.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -1110,13 +1111,13 @@ __global__ void stage_unpack(const StageSeg *segs, const double *x) {
 struct CondSet {
   const cudaGraphConditionalHandle *h;
   const int32_t *run;
-  const int *ires;
+  const int32_t *status;  // per system, after an FP64 finish where one ran
   int ncases;
 };
 __global__ void stage_conds(CondSet a) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= a.ncases) return;
-  const unsigned int go = (a.run[c] != 0 && a.ires[16 * c + 1] == FVC_OK) ? 1u : 0u;
+  const unsigned int go = (a.run[c] != 0 && a.status[c] == FVC_OK) ? 1u : 0u;
   cudaGraphSetConditional(a.h[c], go);
 }
 
@@ -1128,15 +1129,38 @@ __global__ void rec_case_dots(const double *const *dots, int ncases, int k, int 
   for (int i = 0; i < k; ++i) rec[5 * (size_t)c + off + i] = dots[c][i];
 }
 
-// each system of a stage: run, status, iterations (mixed: the FP32 ones)
-__global__ void rec_stage(const int32_t *run, const int *ires, int nsys, int mixed,
-                          int32_t *rec) {
+// a mixed stage's systems to finish in FP64: BiCGSTAB systems that ran and
+// whose FP32 sweeps stalled (FVC_ERR_NOCONV before max_refine sweeps and
+// maxit iterations: the kernel's stall rule), as a synchronous mixed solve
+// finishes them
+__global__ void stall_mask(const int32_t *run, const int32_t *codes, const int *ires, int nsys,
+                           int max_refine, int maxit, int32_t *run2) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= nsys) return;
+  const int *r = ires + 16 * s;
+  run2[s] = (run[s] && codes[s] == 2 && r[1] == FVC_ERR_NOCONV && r[0] < max_refine &&
+             r[2] < maxit)
+                ? 1
+                : 0;
+}
+
+// each system of a stage: its status (after an FP64 finish where one ran)
+// for the conditional nodes, and its record: run, status, iterations (FP32
+// plus FP64 for mixed), FP32 iterations
+__global__ void stage_result(const int32_t *run, const int *ires, const int32_t *run2,
+                             const int *ires64, int nsys, int mixed, int32_t *status,
+                             int32_t *rec) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nsys) return;
+  const bool fin = run2 && run2[s];
+  const int st = !run[s] ? FVC_OK : (fin ? ires64[16 * s + 1] : ires[16 * s + 1]);
+  const int inner = run[s] ? (mixed ? ires[16 * s + 2] : 0) : 0;
+  const int its = !run[s] ? 0 : (mixed ? inner + (fin ? ires64[16 * s] : 0) : ires[16 * s]);
+  status[s] = st;
   rec[4 * (size_t)s] = run[s];
-  rec[4 * (size_t)s + 1] = run[s] ? ires[16 * s + 1] : FVC_OK;
-  rec[4 * (size_t)s + 2] = run[s] ? (mixed ? ires[16 * s + 2] : ires[16 * s]) : 0;
-  rec[4 * (size_t)s + 3] = run[s] ? ires[16 * s + 2] : 0;
+  rec[4 * (size_t)s + 1] = st;
+  rec[4 * (size_t)s + 2] = its;
+  rec[4 * (size_t)s + 3] = inner;
 }
 
 // the cases' gradient error words, or-ed
@@ -1164,7 +1188,12 @@ struct fvc_simple_batch {
     double *ad = nullptr, *au = nullptr, *b = nullptr, *x = nullptr;
     int32_t *run = nullptr;
     fvc::BatchPlan plan;
-    int32_t *rec = nullptr;  // device: 4 per system
+    int32_t *rec = nullptr;     // device: 4 per system
+    int32_t *status = nullptr;  // device: per system, the final status
+    // mixed stages with BiCGSTAB systems: the FP64 finish of stalled ones
+    bool finish = false;
+    fvc::BatchPlan plan64;
+    int32_t *run2 = nullptr, *codes_d = nullptr;
   } st[3];                   // 0 u1+u2, 1 p', 2 enthalpy
   double **d_dots = nullptr;    // device array of the cases' dots pointers
   int32_t **d_errs = nullptr;   // and of their gradient error words
@@ -1205,6 +1234,7 @@ void batch_release(fvc_simple_batch *B) {
   for (auto &S : B->st) {
     if (S.ctx) {
       fvc::context_free_batched(S.ctx, S.plan);
+      fvc::context_free_batched(S.ctx, S.plan64);
       fvc_context_destroy(S.ctx);
     }
   }
@@ -1277,8 +1307,14 @@ int32_t batch_stage(fvc_simple_batch *B, int k, const std::vector<std::vector<in
   if ((rc = balloc(B, S.segs, (size_t)S.nsys)) != FVC_OK || (rc = balloc(B, S.ad, N)) != FVC_OK ||
       (rc = balloc(B, S.au, (size_t)NAD)) != FVC_OK || (rc = balloc(B, S.b, N)) != FVC_OK ||
       (rc = balloc(B, S.x, N)) != FVC_OK || (rc = balloc(B, S.run, (size_t)S.nsys)) != FVC_OK ||
-      (rc = balloc(B, S.rec, 4 * (size_t)S.nsys)) != FVC_OK)
+      (rc = balloc(B, S.rec, 4 * (size_t)S.nsys)) != FVC_OK ||
+      (rc = balloc(B, S.status, (size_t)S.nsys)) != FVC_OK ||
+      (rc = balloc(B, S.run2, (size_t)S.nsys)) != FVC_OK ||
+      (rc = balloc(B, S.codes_d, (size_t)S.nsys)) != FVC_OK)
     return rc;
+  if (cudaMemcpy(S.codes_d, S.codes.data(), sizeof(int32_t) * S.nsys, cudaMemcpyHostToDevice) !=
+      cudaSuccess)
+    return FVC_ERR_CUDA;
   if (cudaMemcpy(S.segs, h.data(), sizeof(fvc::StageSeg) * S.nsys, cudaMemcpyHostToDevice) !=
       cudaSuccess)
     return FVC_ERR_CUDA;
@@ -1318,6 +1354,21 @@ int32_t batch_build(fvc_simple_batch *B) {
                                         S.inits.data(), S.run, 0.0, batch_opts(B, k),
                                         S.plan)) != FVC_OK)
       return rc;
+    // a mixed stage with BiCGSTAB systems: the FP64 plan that finishes the
+    // stalled ones from their FP32 iterate (warm start), on ||r|| <= tol ||b||
+    fvc::context_free_batched(S.ctx, S.plan64);
+    S.finish = batch_opts(B, k).precision == FVC_PREC_MIXED &&
+               std::find(S.codes.begin(), S.codes.end(), 2) != S.codes.end();
+    if (S.finish) {
+      fvc_opts f = batch_opts(B, k);
+      f.precision = FVC_PREC_FP64;
+      f.stop_rule = 1;
+      const std::vector<int32_t> warm((size_t)S.nsys, 0);
+      if ((rc = fvc::context_plan_batched(S.ctx, S.nsys, S.row_start.data(), S.codes.data(),
+                                          S.tols.data(), nullptr, warm.data(), S.run2, 0.0, f,
+                                          S.plan64)) != FVC_OK)
+        return rc;
+    }
   }
   if (cudaStreamSynchronize(B->stream) != cudaSuccess) return FVC_ERR_CUDA;
   cudaStream_t st = B->stream;
@@ -1351,11 +1402,21 @@ int32_t batch_build(fvc_simple_batch *B) {
     int32_t r = fvc_matrix_update_values_async(S.ctx, S.ad, S.au, S.au);
     if (r != FVC_OK) return r;
     const fvc_opts o = batch_opts(B, k);
-    if ((r = fvc::context_enqueue_batched(S.ctx, S.plan, S.b, S.x, B->cs[0]->o.maxit, o)) !=
-        FVC_OK)
-      return r;
-    fvc::rec_stage<<<(S.nsys + 127) / 128, 128, 0, st>>>(
-        S.run, S.plan.ires, S.nsys, o.precision == FVC_PREC_MIXED ? 1 : 0, S.rec);
+    const int maxit = B->cs[0]->o.maxit;
+    if ((r = fvc::context_enqueue_batched(S.ctx, S.plan, S.b, S.x, maxit, o)) != FVC_OK) return r;
+    if (S.finish) {
+      fvc::stall_mask<<<(S.nsys + 127) / 128, 128, 0, st>>>(S.run, S.codes_d, S.plan.ires,
+                                                            S.nsys, 30, maxit, S.run2);
+      fvc::count_launch();
+      fvc_opts f = o;
+      f.precision = FVC_PREC_FP64;
+      f.stop_rule = 1;
+      if ((r = fvc::context_enqueue_batched(S.ctx, S.plan64, S.b, S.x, maxit, f)) != FVC_OK)
+        return r;
+    }
+    fvc::stage_result<<<(S.nsys + 127) / 128, 128, 0, st>>>(
+        S.run, S.plan.ires, S.finish ? S.run2 : nullptr, S.finish ? S.plan64.ires : nullptr,
+        S.nsys, o.precision == FVC_PREC_MIXED ? 1 : 0, S.status, S.rec);
     fvc::count_launch();
     fvc::stage_unpack<<<dim3(gx, (unsigned)S.nsys), fvc::kT, 0, st>>>(S.segs, S.x);
     fvc::count_launch();
@@ -1364,7 +1425,7 @@ int32_t batch_build(fvc_simple_batch *B) {
   // IF(the case's solve ran and ended FVC_OK) { after(case) } for every case
   auto after_stage = [&](int k, int hoff, int which) -> int32_t {
     fvc_simple_batch::Stage &S = B->st[k];
-    fvc::CondSet a{B->d_handles + hoff, S.run, S.plan.ires, nc};
+    fvc::CondSet a{B->d_handles + hoff, S.run, S.status, nc};
     fvc::stage_conds<<<(nc + 127) / 128, 128, 0, st>>>(a);
     fvc::count_launch();
     for (int c = 0; c < nc; ++c) {

@@ -34,6 +34,7 @@ module fvcgpu
      integer(c_int32_t) :: update_beta
      integer(c_int32_t) :: staging
      integer(c_int32_t) :: max_blocks
+     integer(c_int32_t) :: fp32_layout
   end type fvc_opts
 
   ! options of the SIMPLE outer iteration (fvc_simple_opts in fvcgpu.h)

@@ -76,8 +76,11 @@ enum {
    * drop-in then finish in FP64 BiCGSTAB from that iterate (stats: the
    * iterations of both parts, the FP32 ones in inner_iterations), and the
    * context's later mixed BiCGSTAB solves run in FP64 from the start until
-   * fvc_matrix_set gives it another structure.  The enqueued and batched
-   * solves report that stall as FVC_ERR_NOCONV. */
+   * fvc_matrix_set gives it another structure.  fvc_solve_async reports
+   * that stall as FVC_ERR_NOCONV and, after one in an fvc_solve of the
+   * context, routes later ones to FP64 too; fvc_solve_batched reports it as
+   * FVC_ERR_NOCONV; the SIMPLE batch (fvc_simple_batch_*) finishes it in
+   * FP64 inside its graph. */
 };
 
 typedef struct {
@@ -103,6 +106,15 @@ typedef struct {
                           1: plain loads; 2: staged whenever the layout
                           allows                                           */
   int32_t max_blocks;  /* cap on the persistent grid (0 -> automatic)      */
+  int32_t fp32_layout; /* MIXED: the FP32 operator's slice widths.  0: when
+                          no row has more than 4 off-diagonals, every slice
+                          padded to the widest (width 3 or 4: no slice
+                          pointers, the staged kernels' uniform form), else
+                          each slice its own width; 1: each slice its own
+                          width (SELL-32: no padding slots, slice pointers).
+                          A solve that asks for the other choice than the
+                          context's operator has lays it out anew (a host
+                          wait), so graphs captured before then are stale */
 } fvc_opts;
 
 typedef struct {
@@ -203,13 +215,17 @@ int32_t fvc_solve_async(fvc_context *ctx, int32_t code, const double *d_b,
  * over the shapes the kernels support -- the automatic choice (a thread-
  * block cluster for a PCG system of at most 8192 rows, else one block per
  * SM with the fewest warps that cover the rows), 128..1024 threads per
- * block, a cap of 16/38/76 blocks, and for mixed CG plain loads or the
- * staged copies at 1024 threads -- and writes the fastest per iteration to *best (init
- * -1, the rest as fvc_opts_default) and its time to *best_us (may be NULL).
- * Pass *best to fvc_solve for later solves of this matrix and method.  The
- * shape changes only the summation order of the reductions, so results
- * move at rounding level.  Rows are one lane each in 32-row slices, the
- * form every kernel is written for; that is not tuned.  Returns FVC_OK, or
+ * block, a cap of 16/38/76 blocks, for mixed CG plain loads or the
+ * staged copies at 1024 threads, and for mixed solves the FP32 operator's
+ * slice widths (fvc_opts.fp32_layout: every slice padded to the widest row,
+ * or each slice its own width) -- and writes the fastest per iteration to
+ * *best (init -1, the rest as fvc_opts_default) and its time to *best_us
+ * (may be NULL).  Pass *best to fvc_solve for later solves of this matrix
+ * and method.  The shape changes only the summation order of the
+ * reductions, so results move at rounding level; the slice width changes
+ * nothing (padding slots add exactly 0).  Rows are one lane each in 32-row
+ * slices: with 3 or 4 off-diagonals per row, two lanes per row would leave
+ * half of every load on padding, so that is not tuned.  Returns FVC_OK, or
  * an FVC_* error; FVC_ERR_UNSUPPORTED for the (code, matriz) pairs
  * fvc_solve rejects and for mixed GMRES. */
 int32_t fvc_autotune(fvc_context *ctx, int32_t code, int32_t precision,
@@ -691,10 +707,10 @@ int32_t fvc_simple_destroy(fvc_simple *s);
  * BiCGSTAB for the enthalpy) and status.  precision (the p' systems) and
  * precision_u (u, v and the enthalpy; < 0: as precision): FVC_PREC_FP64 or
  * FVC_PREC_MIXED (FP32 iterations, FP64 refinement to the same tolerances
- * on ||b - Ax||2 / ||b||2).  A mixed BiCGSTAB whose FP32 sweeps stall is not
- * finished in FP64 inside a batch: the call ends with FVC_ERR_NOCONV, so
- * systems prone to that (the enthalpy of a natural-convection or heated
- * flow) keep precision_u FP64.  The reference's tests before a
+ * on ||b - Ax||2 / ||b||2).  A mixed BiCGSTAB whose FP32 sweeps stall is
+ * finished in FP64 from its FP32 iterate inside the same graph, as fvc_solve
+ * finishes one (a second, FP64 launch of the stage in which every other
+ * system is masked out).  The reference's tests before a
  * solve skip that system inside the launch (a per-system mask), and the work
  * after a skipped p' or enthalpy solve is skipped with it.  Each outer
  * iteration of all cases is one CUDA graph launch (captured at the first

@@ -144,3 +144,27 @@ def test_mixed_on_ellpack_input_with_padding(kind, nx):
     rel = np.linalg.norm(b - A @ x2) / np.linalg.norm(b)
     print(f"{kind} ELLPACK {n} rows, {pads} pad slots: its {s2.inner_iterations} rel {rel:.2e}")
     assert rel <= 1e-8
+
+
+@pytest.mark.parametrize("staging", [1, 2])
+def test_fp32_slice_widths_give_the_same_bits(staging):
+    # fvc_opts.fp32_layout: every slice padded to the widest row (width 4 on
+    # the mixed mesh) or each slice its own width (SELL-32).  The true terms
+    # are summed in the same order and the padding slots add exactly 0, so
+    # the two layouts give the same iterates; switching lays the operator out
+    # anew on the same context
+    from fortranfvcell_gb300 import Context, make_opts, mesh
+    s = mesh.pressure_system(mesh.square_mesh(300, kind="mixed", jitter=0.2, seed=8), matriz=1,
+                             unsym=True, pin_cell=1)
+    n = s.neq
+    b = np.random.default_rng(2).uniform(-1, 1, n)
+    ctx = Context()
+    ctx.set_matrix(1, True, n, s.nad, s.ad, s.au, s.au, s.ia, s.ja)
+    out = []
+    for layout in (0, 1, 0):
+        bd, xd = torch_dev(b), torch_dev(np.zeros(n))
+        st = ctx.solve(1, bd, xd, 1e-8, 200000,
+                       make_opts("mixed", init=1, staging=staging, fp32_layout=layout))
+        out.append((st.inner_iterations, xd.cpu().numpy()))
+    assert out[0][0] == out[1][0] == out[2][0]
+    assert np.array_equal(out[0][1], out[1][1]) and np.array_equal(out[0][1], out[2][1])
