@@ -865,19 +865,30 @@ def run_batched_c4(args):
         tot += r["ms"]
     sysout["reference_tests"] = {"per_stage_ms": per, "total_ms": round(tot, 3)}
     rule = {}
-    for prec in ("fp64", "mixed"):
-        o = make_opts(prec, init=1, stop_rule=1)
-        per, tot, wr, ok = {}, 0.0, 0.0, True
+    # the automatic forms (FP64: groups of blocks sharing one cooperative
+    # launch; mixed: one thread-block cluster of 8 per system), and each
+    # precision in the other form
+    variants = (("fp64", "fp64", 0), ("mixed", "mixed", 0), ("mixed_groups", "mixed", 1),
+                ("fp64_clusters", "fp64", 8))
+    for key, prec, csize in variants:
+        o = make_opts(prec, init=1, stop_rule=1, cluster_size=csize)
+        per, tot, wr, ok, fin = {}, 0.0, 0.0, True, 0
         for name, bt in stages:
             r = run(bt, o)
             per[name] = round(r["ms"], 3)
             tot += r["ms"]
             wr = max(wr, max(t.rel_residual for t in r["st"]))
             ok = ok and r["rc"] == 0
-        rule[prec] = dict(per_stage_ms=per, total_ms=round(tot, 3),
-                          worst_rel_residual=float(f"{wr:.3e}"), all_converged=ok)
+            if prec == "mixed":
+                fin += sum(1 for t in r["st"] if t.iterations > t.inner_iterations)
+        rule[key] = dict(per_stage_ms=per, total_ms=round(tot, 3),
+                         worst_rel_residual=float(f"{wr:.3e}"), all_converged=ok,
+                         form="groups" if (csize == 1 or (csize == 0 and prec == "fp64"))
+                         else "clusters of 8")
+        if prec == "mixed":
+            rule[key]["fp64_finished_systems"] = fin
     sysout["relres_rule"] = dict(rule="||b - Ax|| <= 1e-8 ||b|| for every system, per stage",
-                                 fp64=rule["fp64"], mixed=rule["mixed"],
+                                 **rule,
                                  mixed_over_fp64=round(rule["fp64"]["total_ms"]
                                                        / rule["mixed"]["total_ms"], 2))
     for _, bt in stages:

@@ -46,6 +46,7 @@ class FvcOpts(C.Structure):
         ("staging", I32),
         ("max_blocks", I32),
         ("fp32_layout", I32),
+        ("cluster_size", I32),
     ]
 
 

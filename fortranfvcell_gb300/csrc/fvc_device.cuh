@@ -12,6 +12,7 @@
 // FP64 SpMV is bit-identical to the reference routine (no FMA contraction:
 // products and sums are rounded separately, as the Fortran loops do).
 #pragma once
+#include <cooperative_groups.h>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -79,9 +80,50 @@ struct GridSync {
   double *totals;          // 4 slots x kMaxNV
   unsigned int nblocks;    // blocks that synchronise through this state
   unsigned int base;       // blockIdx.x of the first of them (0 for a whole grid)
+  // nonzero: the nblocks blocks are one thread-block cluster; the waits
+  // and reductions below then use the cluster barrier and distributed
+  // shared memory instead of global memory (cluster_exchange)
+  int cluster = 0;
 };
 
 constexpr int kMaxNV = 4;
+
+// The cluster form of a reduction.  Lane 0 of warp 0 of every CTA has
+// stored its block's NV partials in its own slot (mine); every thread of
+// every CTA then meets at the cluster barrier (arrive.release /
+// wait.acquire at cluster scope: the slots, and every global-memory write
+// made before it, are visible to the whole cluster after it); warp 0 reads
+// the CTAs' slots in rank order through distributed shared memory and sums
+// them in a fixed shuffle tree, so every CTA holds identical totals (in lane
+// 0 of warp 0).  There is no spin-wait: the barrier is the hardware's, and
+// every CTA reaches it the same number of times because every branch
+// around it depends only on those identical totals.  Two slots alternate
+// (a slot is written again only after a later barrier, so never while a
+// CTA still reads it), and the kernel ends with one more barrier so that
+// no CTA's shared memory goes away while another reads it.
+template <int NV>
+__device__ __forceinline__ void cluster_exchange(double (*slots)[kMaxNV], unsigned int ep,
+                                                 double (&t)[NV > 0 ? NV : 1]) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cl = cg::this_cluster();
+  cl.sync();
+  if (NV > 0 && threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+    const int nb = (int)cl.num_blocks();
+#pragma unroll
+    for (int q = 0; q < NV; ++q) {
+      double u = (lane < nb) ? *cl.map_shared_rank(&slots[ep & 1u][q], lane) : 0.0;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) u = __dadd_rn(u, __shfl_down_sync(0xffffffffu, u, o));
+      t[q] = u;
+    }
+  }
+}
+
+// the closing barrier of a kernel whose blocks reduce through cluster_exchange
+__device__ __forceinline__ void cluster_close(const GridSync &gs) {
+  if (gs.cluster) cooperative_groups::this_cluster().sync();
+}
 
 __device__ __forceinline__ uint64_t global_ns() {
   uint64_t t;
@@ -152,6 +194,25 @@ __device__ __forceinline__ bool grid_allreduce(const GridSync &gs, unsigned int 
     block_sum<(NV > 0 ? NV : 1)>(v, red);
   } else {
     __syncthreads();
+  }
+  if (gs.cluster) {
+    __shared__ double s_slot[2][kMaxNV];
+    const unsigned int ep = ++episode;
+    if (NV > 0 && threadIdx.x == 0)
+#pragma unroll
+      for (int q = 0; q < NV; ++q) s_slot[ep & 1u][q] = v[q];
+    double t[NV > 0 ? NV : 1];
+    cluster_exchange<NV>(s_slot, ep, t);
+    if (NV > 0) {
+      if (threadIdx.x == 0)
+#pragma unroll
+        for (int q = 0; q < NV; ++q) red[q] = t[q];
+      __syncthreads();
+#pragma unroll
+      for (int q = 0; q < NV; ++q) v[q] = red[q];
+      __syncthreads();
+    }
+    return true;
   }
   if (gs.nblocks == 1) {  // one block: its sum is the total (same value)
     ++episode;
@@ -246,6 +307,24 @@ __device__ __forceinline__ bool grid_allreduce_d(const GridSync &gs, unsigned in
   }
   __syncthreads();
   const unsigned int ep = ++episode;
+  if (gs.cluster) {
+    __shared__ double s_slot[2][kMaxNV];
+    if (warp == 0) {
+#pragma unroll
+      for (int q = 0; q < NV; ++q) {
+        double u = s_part[q][lane];
+#pragma unroll
+        for (int k = 1; k < 4; ++k) u = __dadd_rn(u, s_part[q][32 * k + lane]);
+        u = warp_sum(u);
+        if (lane == 0) s_slot[ep & 1u][q] = u;
+      }
+    }
+    double t[NV];
+    cluster_exchange<NV>(s_slot, ep, t);
+    if (threadIdx.x == 0) f(t);
+    __syncthreads();
+    return true;
+  }
   if (warp == 0) {
     const unsigned int nb = gs.nblocks;
     double *part = gs.partials + (size_t)(ep & 3u) * kMaxNV * nb;

@@ -150,6 +150,7 @@ struct BatchPlan {
   int *dsob = nullptr;
   double tol = 0.0;
   int fp32_layout = 0;
+  int cluster = 0;  // > 0: one cluster of this many blocks per system
 };
 int32_t plan_batched(DeviceMatrix &A, Scratch &S, int nsys, const int32_t *row_start,
                      const int32_t *codes, const double *tols, const double *its_hint,
@@ -179,9 +180,19 @@ int32_t ensure_f32_vectors(Scratch &S, size_t n);
 // descriptors (device BatchSys array) and the block-to-system map
 struct BatchSys;
 const void *mixed_batched_kernel(int threads);
+const void *krylov_batched_kernel(int threads);
+// A batched launch: groups of blocks of one cooperative launch (csize 0),
+// or an ordinary launch of clusters of csize blocks
+cudaError_t launch_groups(const void *kern, int blocks, int threads, int csize, void **args,
+                          cudaStream_t stream);
+void cluster_config(cudaLaunchConfig_t &cfg, cudaLaunchAttribute *at, int csize, int threads,
+                    cudaStream_t stream);
+// CTAs per cluster of a mixed batch when fvc_opts.cluster_size is 0
+constexpr int kBatchClusterDefault = 8;
 int32_t launch_mixed_batched(const DeviceMatrix &A, const Scratch &S, const BatchSys *dsys,
-                             const int *dsob, int blocks, int threads, const double *b, double *x,
-                             int maxit, const fvc_opts &o, cudaStream_t stream);
+                             const int *dsob, int blocks, int threads, int cluster,
+                             const double *b, double *x, int maxit, const fvc_opts &o,
+                             cudaStream_t stream);
 
 // Threads per block of a persistent solver launch when the caller sets
 // none (or a multiple of 128 it asked for, clamped to 128..1024).  The

@@ -20,6 +20,10 @@
 // roughly halve the FP64 instructions per row; they move results only at
 // rounding level, like the dot products, which are tree sums in a fixed
 // (deterministic) order instead of the reference's sequential sums.
+// BiCGSTAB adds one thing the reference lacks: where one of its
+// denominators is exactly zero (the reference goes on with Inf/NaN), the
+// recurrence restarts from the current residual, or the solve ends with
+// FVC_ERR_BREAKDOWN when it has just restarted (bicgstab_run).
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -298,7 +302,10 @@ __device__ __forceinline__ void bicgstab_run(const KArgs &a, const Part &P, cons
   __shared__ double buf[3 * kMaxT];
   __shared__ struct {
     double d, conv, rr0, alpha, w, beta, crit;
-    int stop;  // 0 go on, 1 converged, 2 NaN/Inf
+    int stop;     // 0 go on, 1 converged, 2 NaN/Inf, 3 breakdown
+    int restart;  // a breakdown: the next iteration restarts from s
+    int fresh;    // this iteration started from r0 = s (the start or a restart)
+    int brk;      // r.v = 0 or r.s = 0 in phase 1 (alpha = 0 this iteration)
   } sh;
   double *r = a.v0, *t = a.v7, *x = a.x;
   double *scur = a.v1, *snxt = a.v2, *pold = a.v3, *pnew = a.v4, *vold = a.v5, *vnew = a.v6;
@@ -328,10 +335,13 @@ __device__ __forceinline__ void bicgstab_run(const KArgs &a, const Part &P, cons
         sh.conv = rule0 ? a.tol * sqrt(fabs(q[0])) : a.tol * sqrt(q[1]);
         sh.crit = 0.0;
         sh.stop = 0;
+        sh.restart = 0;
+        sh.fresh = 1;
       }))
     return;
   int j, status = FVC_OK;
   double alpha = 0.0, w = 0.0, beta = 0.0;
+  bool restart = false;
   for (j = 1; j <= a.maxit; ++j) {
     // phase 1: v = A z with z = p/m, p formed from the previous p, v, s
     acc[0] = 0.0;
@@ -349,6 +359,9 @@ __device__ __forceinline__ void bicgstab_run(const KArgs &a, const Part &P, cons
     } else {
       FOR_ROWS(P) {
         const double *po = pold, *vo = vold, *sc = scur;
+        // after a breakdown beta = 0 (p = s) and the shadow residual is s:
+        // each row rewrites its own r before it reads it
+        if (restart) r[row] = sc[row];
         auto pf = [&](int k) { return fma(beta, fma(-w, vo[k], po[k]), sc[k]); };
         pnew[row] = pf(row);
         const double vi =
@@ -359,9 +372,13 @@ __device__ __forceinline__ void bicgstab_run(const KArgs &a, const Part &P, cons
         acc[1] = fma(vi, ri, acc[1]);
       }
     }
+    // r.v = 0 (the reference's alpha = r.s/0) or r.s = 0 (alpha = 0, no
+    // progress): alpha = 0, the iteration takes only its w step, and the
+    // next one restarts
     if (!grid_allreduce_d<2>(gs, ep, acc, buf, [&](const double *q) {
           sh.rr0 = q[0];
-          sh.alpha = q[0] / q[1];
+          sh.brk = (q[0] == 0.0 || q[1] == 0.0) ? 1 : 0;
+          sh.alpha = sh.brk ? 0.0 : q[0] / q[1];
         }))
       return;
     alpha = sh.alpha;
@@ -378,8 +395,10 @@ __device__ __forceinline__ void bicgstab_run(const KArgs &a, const Part &P, cons
       acc[0] = fma(ti, snxt[row], acc[0]);
       acc[1] = fma(ti, ti, acc[1]);
     }
+    // t = 0 exactly: s' = 0, the alpha step solved the system (the
+    // reference's 0/0 there gives NaN); w = 0 keeps x and s' as they are
     if (!grid_allreduce_d<2>(gs, ep, acc, buf,
-                             [&](const double *q) { sh.w = q[0] / q[1]; }))
+                             [&](const double *q) { sh.w = (q[1] != 0.0) ? q[0] / q[1] : 0.0; }))
       return;
     w = sh.w;
     // phase 3: x += alpha z ; x += w z' ; s'' = s' - w t ; s''.z' ; r.s'' ; s''.s''
@@ -403,14 +422,31 @@ __device__ __forceinline__ void bicgstab_run(const KArgs &a, const Part &P, cons
           sh.crit = rule0 ? sqrt(fabs(b0)) : sqrt(q[2]);
           sh.stop = (!(sh.crit == sh.crit) || !(sh.w == sh.w)) ? 2 : (sh.crit < sh.conv ? 1 : 0);
           sh.beta = (q[1] / sh.rr0) * (sh.alpha / sh.w);
+          // breakdown guard (where the reference's recurrence divides by
+          // zero and goes on with Inf/NaN): w = 0, r.s'' = 0 or a beta that
+          // is not finite restart the iteration from the current residual
+          // (shadow residual and p := s''); a breakdown in an iteration that
+          // itself started from its residual ends the solve (FVC_ERR_BREAKDOWN).
+          // Iterations without a breakdown are unchanged.
+          const bool broke = sh.stop == 0 &&
+                             (sh.brk || sh.w == 0.0 || q[1] == 0.0 || !isfinite(sh.beta));
+          sh.restart = 0;
+          if (broke && sh.fresh) {
+            sh.stop = 3;
+          } else if (broke) {
+            sh.restart = 1;
+            sh.beta = 0.0;
+          }
+          sh.fresh = sh.restart;
         }))
       return;
-    if (sh.stop == 2) {
-      status = FVC_ERR_NAN;
+    if (sh.stop >= 2) {
+      status = (sh.stop == 2) ? FVC_ERR_NAN : FVC_ERR_BREAKDOWN;
       break;
     }
     if (sh.stop == 1) break;
     beta = sh.beta;
+    restart = sh.restart != 0;
     double *tmp = scur;
     scur = snxt;
     snxt = tmp;
@@ -444,7 +480,9 @@ __global__ void __launch_bounds__(1024, 1) bicgstab_f64_t(KArgs a) {
 // (sys_of_block) and synchronises only with that system's blocks, so each
 // system iterates with its own solver and stops on its own inside one
 // cooperative launch.  PCG stores p (most groups are one block, where
-// publishing p is a __syncthreads).
+// publishing p is a __syncthreads).  With d.gs.cluster each system's blocks
+// are one thread-block cluster (an ordinary launch of many clusters: no
+// co-residency needed, the hardware starts clusters as SMs free up).
 template <int kMaxT>
 __global__ void __launch_bounds__(kMaxT, 1024 / kMaxT) krylov_batched(KArgs a, const BatchSys *__restrict__ sys,
                                                         const int *__restrict__ sys_of_block) {
@@ -459,6 +497,7 @@ __global__ void __launch_bounds__(kMaxT, 1024 / kMaxT) krylov_batched(KArgs a, c
     bicgstab_run<kMaxT>(ak, P, d.gs, d.result, d.iresult, rank == 0);
   else
     pcg_run<true, kMaxT>(ak, P, d.gs, d.result, d.iresult, rank == 0);
+  cluster_close(d.gs);
 }
 
 // ---------------------------------------------------------------------
@@ -944,6 +983,38 @@ int32_t launch_solve_status(const Scratch &S, int32_t *out, cudaStream_t stream,
   return cudaPeekAtLastError() == cudaSuccess ? FVC_OK : FVC_ERR_CUDA;
 }
 
+const void *krylov_batched_kernel(int threads) {
+  return threads <= 128   ? (const void *)krylov_batched<128>
+         : threads <= 256 ? (const void *)krylov_batched<256>
+                          : (const void *)krylov_batched<1024>;
+}
+
+void cluster_config(cudaLaunchConfig_t &cfg, cudaLaunchAttribute *at, int csize, int threads,
+                    cudaStream_t stream) {
+  cfg = cudaLaunchConfig_t{};
+  cfg.blockDim = dim3((unsigned)threads);
+  cfg.gridDim = dim3((unsigned)csize);
+  cfg.stream = stream;
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = (unsigned)csize;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+}
+
+cudaError_t launch_groups(const void *kern, int blocks, int threads, int csize, void **args,
+                          cudaStream_t stream) {
+  if (csize <= 0)
+    return cudaLaunchCooperativeKernel(kern, dim3((unsigned)blocks), dim3((unsigned)threads),
+                                       args, 0, stream);
+  cudaLaunchConfig_t cfg;
+  cudaLaunchAttribute at[1];
+  cluster_config(cfg, at, csize, threads, stream);
+  cfg.gridDim = dim3((unsigned)blocks);
+  return cudaLaunchKernelExC(&cfg, kern, args);
+}
+
 int32_t plan_batched(DeviceMatrix &A, Scratch &S, int nsys, const int32_t *row_start,
                      const int32_t *codes, const double *tols, const double *its_hint,
                      const int32_t *inits, const int32_t *run, double tol, const fvc_opts &o,
@@ -957,11 +1028,20 @@ int32_t plan_batched(DeviceMatrix &A, Scratch &S, int nsys, const int32_t *row_s
     if (code != 1 && code != 2) return FVC_ERR_UNSUPPORTED;
     any_bicg = any_bicg || code == 2;
   }
-  // 128-thread blocks by default: twice the co-resident blocks of 256, so the
-  // one-block minimum of the small systems takes a smaller share (C4 batch of
-  // 256 cavities: 184 ms at 128 threads, 215 at 256, 386 at 512)
-  const int threads = (o.block_threads > 0) ? block_threads_for(o.block_threads, 0, 1) : 128;
   const bool mixed = o.precision == FVC_PREC_MIXED;
+  // one thread-block cluster of csize CTAs per system (mixed batches by
+  // default), or groups of blocks of one cooperative launch (csize 0)
+  if (o.cluster_size < 0 || o.cluster_size > 16) return FVC_ERR_ARG;
+  const int csize = (o.cluster_size == 1)   ? 0
+                    : (o.cluster_size >= 2) ? o.cluster_size
+                    : (mixed ? kBatchClusterDefault : 0);
+  // groups: 128-thread blocks by default, twice the co-resident blocks of
+  // 256, so the one-block minimum of the small systems takes a smaller share
+  // (C4 batch of 256 cavities: 184 ms at 128 threads, 215 at 256, 386 at
+  // 512); clusters: 256
+  const int threads = (o.block_threads > 0) ? block_threads_for(o.block_threads, 0, 1)
+                      : csize > 0          ? 256
+                                           : 128;
   if (mixed) {
     int32_t rc = build_f32_copy(A, stream, o.fp32_layout);
     if (rc == FVC_OK) rc = ensure_f32_vectors(S, (size_t)A.n);
@@ -970,18 +1050,38 @@ int32_t plan_batched(DeviceMatrix &A, Scratch &S, int nsys, const int32_t *row_s
   int occ = 0;
   // PCG stores p: most groups of a batch are one block, where publishing p
   // is a __syncthreads (C4 batch of 256 cavities: 159 ms vs 184 ms)
-  const void *kern = mixed ? mixed_batched_kernel(threads)
-                           : (threads <= 128 ? (const void *)krylov_batched<128>
-                                             : (const void *)krylov_batched<1024>);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, threads, 0);
-  if (occ <= 0) occ = 1;
-  if (o.blocks_per_sm > 0 && o.blocks_per_sm < occ) occ = o.blocks_per_sm;
-  int cap = occ * sm_count();
-  if (o.max_blocks > 0) cap = std::min(cap, o.max_blocks);
-  if (nsys > cap) {
-    fprintf(stderr, "fvcgpu: %d systems exceed the %d co-resident blocks of one launch\n", nsys,
-            cap);
-    return FVC_ERR_ARG;
+  const void *kern = mixed ? mixed_batched_kernel(threads) : krylov_batched_kernel(threads);
+  int cap = 0;
+  if (csize > 0) {
+    // an ordinary launch of one cluster per system: no co-residency bound,
+    // but one cluster must fit on the device
+    if (csize > 8 &&
+        cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+            cudaSuccess) {
+      cudaGetLastError();
+      return FVC_ERR_UNSUPPORTED;
+    }
+    cudaLaunchConfig_t cfg{};
+    cudaLaunchAttribute at[1];
+    cluster_config(cfg, at, csize, threads, stream);
+    int ncl = 0;
+    if (cudaOccupancyMaxActiveClusters(&ncl, kern, &cfg) != cudaSuccess || ncl < 1) {
+      cudaGetLastError();
+      fprintf(stderr, "fvcgpu: no cluster of %d blocks of %d threads fits the device\n", csize,
+              threads);
+      return FVC_ERR_UNSUPPORTED;
+    }
+  } else {
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, threads, 0);
+    if (occ <= 0) occ = 1;
+    if (o.blocks_per_sm > 0 && o.blocks_per_sm < occ) occ = o.blocks_per_sm;
+    cap = occ * sm_count();
+    if (o.max_blocks > 0) cap = std::min(cap, o.max_blocks);
+    if (nsys > cap) {
+      fprintf(stderr, "fvcgpu: %d systems exceed the %d co-resident blocks of one launch\n", nsys,
+              cap);
+      return FVC_ERR_ARG;
+    }
   }
   // blocks per system in proportion to its work: slices x the expected
   // iterations (the caller's hint, else sqrt(rows), the growth of the
@@ -1002,8 +1102,18 @@ int32_t plan_batched(DeviceMatrix &A, Scratch &S, int nsys, const int32_t *row_s
     wt[s] = slices[s] * its * ((codes && codes[s] == 2) ? 2.0 : 1.0);
     wleft += wt[s];
   }
+  // clusters: csize blocks each, the heaviest systems first (the hardware
+  // starts clusters roughly in launch order, so the long solves begin at once)
+  std::vector<int> order(nsys);
+  for (int s = 0; s < nsys; ++s) order[s] = s;
+  if (csize > 0) {
+    std::stable_sort(order.begin(), order.end(), [&](int p, int q) { return wt[p] > wt[q]; });
+    std::fill(nb.begin(), nb.end(), csize);
+    std::fill(fixed.begin(), fixed.end(), 1);
+    wleft = 0.0;
+  }
   long capleft = cap;
-  for (bool changed = true; changed;) {
+  for (bool changed = csize == 0; changed;) {
     changed = false;
     for (int s = 0; s < nsys; ++s) {
       if (fixed[s]) continue;
@@ -1027,7 +1137,7 @@ int32_t plan_batched(DeviceMatrix &A, Scratch &S, int nsys, const int32_t *row_s
     }
     total += nb[s];
   }
-  while (total < cap) {  // rounding leftovers: largest remainder first
+  while (csize == 0 && total < cap) {  // rounding leftovers: largest remainder first
     int k = -1;
     for (int s = 0; s < nsys; ++s)
       if (!fixed[s] && nb[s] < most[s] && (k < 0 || frac[s] > frac[k])) k = s;
@@ -1036,7 +1146,7 @@ int32_t plan_batched(DeviceMatrix &A, Scratch &S, int nsys, const int32_t *row_s
     frac[k] = 0.0;
     ++total;
   }
-  while (total > cap) {  // trim the largest shares (nsys <= cap keeps one each)
+  while (csize == 0 && total > cap) {  // trim the largest shares (nsys <= cap keeps one each)
     int k = 0;
     for (int s = 1; s < nsys; ++s)
       if (nb[s] > nb[k]) k = s;
@@ -1069,7 +1179,8 @@ int32_t plan_batched(DeviceMatrix &A, Scratch &S, int nsys, const int32_t *row_s
   std::vector<int> hsob((size_t)total);
   size_t poff = 0;
   int b0 = 0;
-  for (int s = 0; s < nsys; ++s) {
+  for (int i = 0; i < nsys; ++i) {
+    const int s = order[i];
     BatchSys &d = hsys[s];
     d.s0 = row_start[s] / 32;
     d.s1 = d.s0 + slices[s];
@@ -1086,6 +1197,7 @@ int32_t plan_batched(DeviceMatrix &A, Scratch &S, int nsys, const int32_t *row_s
     d.gs.totals = part + poff + (size_t)4 * kMaxNV * nb[s];
     d.gs.nblocks = (unsigned int)nb[s];
     d.gs.base = (unsigned int)b0;
+    d.gs.cluster = csize > 0 ? 1 : 0;
     d.result = res + (size_t)s * 16;
     d.iresult = ires + (size_t)s * 16;
     d.run = run ? run + s : nullptr;
@@ -1115,6 +1227,7 @@ int32_t plan_batched(DeviceMatrix &A, Scratch &S, int nsys, const int32_t *row_s
   P.nsys = nsys;
   P.total = (int)total;
   P.threads = threads;
+  P.cluster = csize;
   P.mixed = mixed;
   P.kern = kern;
   P.buf = buf;
@@ -1143,7 +1256,8 @@ int32_t enqueue_batched(DeviceMatrix &A, Scratch &S, const BatchPlan &P, const d
     // layout is decided, which planning did)
     int32_t rc = build_f32_copy(A, stream, P.fp32_layout);
     if (rc != FVC_OK) return rc;
-    return launch_mixed_batched(A, S, P.dsys, P.dsob, P.total, P.threads, b, x, maxit, o, stream);
+    return launch_mixed_batched(A, S, P.dsys, P.dsob, P.total, P.threads, P.cluster, b, x, maxit,
+                                o, stream);
   }
   KArgs a{};
   a.A = view64(A);
@@ -1167,8 +1281,7 @@ int32_t enqueue_batched(DeviceMatrix &A, Scratch &S, const BatchPlan &P, const d
   const BatchSys *psys = P.dsys;
   const int *psob = P.dsob;
   void *args[] = {&a, &psys, &psob};
-  const cudaError_t ce =
-      cudaLaunchCooperativeKernel(P.kern, dim3((unsigned)P.total), dim3(P.threads), args, 0, stream);
+  const cudaError_t ce = launch_groups(P.kern, P.total, P.threads, P.cluster, args, stream);
   count_launch();
   if (ce != cudaSuccess) {
     fprintf(stderr, "fvcgpu: batched launch failed: %s\n", cudaGetErrorString(ce));
@@ -1221,18 +1334,90 @@ int32_t run_krylov_batched(DeviceMatrix &A, Scratch &S, int nsys,
   if (ce2 != cudaSuccess) return FVC_ERR_CUDA;
   if (herr != 0) return FVC_ERR_TIMEOUT;
   if (const int32_t c = check_word_status(S, stream); c != FVC_OK) return c;
+  // mixed BiCGSTAB systems whose FP32 sweeps stalled (the kernel's stall
+  // rule: FVC_ERR_NOCONV below max_refine sweeps and maxit iterations) are
+  // finished in FP64 from their iterate, on ||r|| <= tol ||b||, in one more
+  // batched launch over those systems alone -- as a single mixed solve does
+  std::vector<char> fin((size_t)nsys, 0);
+  std::vector<double> hres64;
+  std::vector<int> hires64;
+  if (mixed) {
+    const int max_refine = (o.max_refine > 0) ? o.max_refine : 30;
+    std::vector<int32_t> run2((size_t)nsys, 0);
+    int nfin = 0;
+    for (int s = 0; s < nsys; ++s) {
+      const int *ir = &hires[(size_t)s * 16];
+      if (codes && codes[s] == 2 && ir[1] == FVC_ERR_NOCONV && ir[0] < max_refine &&
+          ir[2] < maxit) {
+        run2[s] = 1;
+        fin[s] = 1;
+        ++nfin;
+      }
+    }
+    if (nfin > 0) {
+      fvc_opts f = o;
+      f.precision = FVC_PREC_FP64;
+      f.stop_rule = 1;
+      const std::vector<int32_t> warm((size_t)nsys, 0);
+      int32_t *run2_d = nullptr;
+      if (cudaMallocAsync((void **)&run2_d, sizeof(int32_t) * nsys, stream) != cudaSuccess)
+        return FVC_ERR_CUDA;
+      cudaMemcpyAsync(run2_d, run2.data(), sizeof(int32_t) * nsys, cudaMemcpyHostToDevice,
+                      stream);
+      BatchPlan P64;
+      rc = plan_batched(A, S, nsys, row_start, codes, tols, nullptr, warm.data(), run2_d, tol, f,
+                        stream, false, P64);
+      if (rc == FVC_OK) {
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        cudaEventRecord(e0, stream);
+        rc = enqueue_batched(A, S, P64, b, x, maxit, f, stream);
+        cudaEventRecord(e1, stream);
+        hres64.resize((size_t)nsys * 16);
+        hires64.resize((size_t)nsys * 16);
+        if (rc == FVC_OK) {
+          cudaMemcpyAsync(hres64.data(), P64.res, P64.res_bytes, cudaMemcpyDeviceToHost, stream);
+          cudaMemcpyAsync(hires64.data(), P64.ires, P64.ires_bytes, cudaMemcpyDeviceToHost,
+                          stream);
+          cudaMemcpyAsync(&herr, P64.err, sizeof(int), cudaMemcpyDeviceToHost, stream);
+        }
+        free_batched(P64, stream);
+        cudaFreeAsync(run2_d, stream);
+        ce2 = cudaStreamSynchronize(stream);
+        float ms2 = 0.f;
+        cudaEventElapsedTime(&ms2, e0, e1);
+        ms += ms2;
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        if (rc == FVC_OK && ce2 != cudaSuccess) rc = FVC_ERR_CUDA;
+        if (rc == FVC_OK && herr != 0) rc = FVC_ERR_TIMEOUT;
+      } else {
+        cudaFreeAsync(run2_d, stream);
+      }
+      if (rc != FVC_OK) return rc;
+    }
+  }
   int32_t worst = FVC_OK;
   for (int s = 0; s < nsys; ++s) {
     const double *r = &hres[(size_t)s * 16];
     const int *ir = &hires[(size_t)s * 16];
+    int its64 = 0;
+    if (fin[s]) {  // the FP64 finish's status and residual, its iterations
+      const int *i2 = &hires64[(size_t)s * 16];
+      hires[(size_t)s * 16 + 1] = i2[1];
+      its64 = i2[0];
+      hres[(size_t)s * 16 + 3] = hres64[(size_t)s * 16 + 3];
+      hres[(size_t)s * 16 + 4] = hres64[(size_t)s * 16 + 4];
+    }
     if (ir[1] == FVC_ERR_NAN) worst = FVC_ERR_NAN;
     else if (ir[1] != FVC_OK && worst == FVC_OK) worst = ir[1];
     if (st) {
       fvc_stats &t = st[s];
       memset(&t, 0, sizeof(t));
       t.status = ir[1];
-      // mixed: inner FP32 iterations, and reliable updates / sweeps
-      t.iterations = mixed ? ir[2] : ir[0];
+      // mixed: FP32 iterations (plus those of an FP64 finish), FP32
+      // iterations, and reliable updates / sweeps
+      t.iterations = mixed ? ir[2] + its64 : ir[0];
       t.inner_iterations = mixed ? ir[2] : 0;
       t.refinements = mixed ? ir[0] : 0;
       t.energy = mixed ? 0.0 : r[0];

@@ -105,6 +105,28 @@ __device__ __forceinline__ bool grid_allreduce_ff(const GridSync &gs, unsigned i
   if (threadIdx.x == 0) s_ok = 1;
   __syncthreads();
   const unsigned int ep = ++episode;
+  if (gs.cluster) {  // one thread-block cluster: cluster_exchange
+    __shared__ double s_slot[2][kMaxNV];
+    if (warp == 0) {
+#pragma unroll
+      for (int q = 0; q < NV; ++q) {
+        const float2 w = (lane < nwarps) ? red2[q * 32 + lane] : make_float2(0.0f, 0.0f);
+        float s = w.x, c = w.y;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          const float s2 = __shfl_xor_sync(0xffffffffu, s, o);
+          const float c2 = __shfl_xor_sync(0xffffffffu, c, o);
+          ff_add(s, c, s2, c2);
+        }
+        if (lane == 0) s_slot[ep & 1u][q] = (double)s + (double)c;
+      }
+    }
+    double t[NV];
+    cluster_exchange<NV>(s_slot, ep, t);
+    if (threadIdx.x == 0) f(t);
+    __syncthreads();
+    return true;
+  }
   if (warp == 0) {
     const unsigned int nb = gs.nblocks;
     double *part = gs.partials + (size_t)(ep & 3u) * kMaxNV * nb;
@@ -1407,7 +1429,9 @@ __global__ void __launch_bounds__(1024, 1) mixed_bicgstab(MArgs a) { mixed_bicgs
 
 // Batched mixed-precision solves: every block runs the mixed CG (code 1)
 // or the mixed BiCGSTAB (code 2) of its system of the block-diagonal
-// matrix, on that system's slices and synchronisation state.
+// matrix, on that system's slices and synchronisation state: a group of
+// blocks of one cooperative launch, or (d.gs.cluster) one thread-block
+// cluster of an ordinary launch.
 template <int kMaxT>
 __global__ void __launch_bounds__(kMaxT, 1024 / kMaxT)
     mixed_batched(MArgs a, const BatchSys *__restrict__ sys, const int *__restrict__ sob) {
@@ -1432,6 +1456,7 @@ __global__ void __launch_bounds__(kMaxT, 1024 / kMaxT)
   } else {
     mixed_cg_body<false, 0>(am);
   }
+  cluster_close(d.gs);
 }
 
 // The launch-wide arguments of the mixed kernels over matrix A and the
@@ -1499,12 +1524,15 @@ int32_t ensure_f32_vectors(Scratch &S, size_t n) {
 }
 
 const void *mixed_batched_kernel(int threads) {
-  return threads <= 128 ? (const void *)mixed_batched<128> : (const void *)mixed_batched<1024>;
+  return threads <= 128   ? (const void *)mixed_batched<128>
+         : threads <= 256 ? (const void *)mixed_batched<256>
+                          : (const void *)mixed_batched<1024>;
 }
 
 int32_t launch_mixed_batched(const DeviceMatrix &A, const Scratch &S, const BatchSys *dsys,
-                             const int *dsob, int blocks, int threads, const double *b, double *x,
-                             int maxit, const fvc_opts &o, cudaStream_t stream) {
+                             const int *dsob, int blocks, int threads, int cluster,
+                             const double *b, double *x, int maxit, const fvc_opts &o,
+                             cudaStream_t stream) {
   MArgs a = mixed_args(A, S, b, x);
   a.max_refine = (o.max_refine > 0) ? o.max_refine : 30;
   a.update_beta = o.update_beta;
@@ -1513,9 +1541,7 @@ int32_t launch_mixed_batched(const DeviceMatrix &A, const Scratch &S, const Batc
   // grid by the occupancy under it)
   const void *kern = mixed_batched_kernel(threads);
   void *args[] = {&a, &dsys, &dsob};
-  const cudaError_t ce =
-      cudaLaunchCooperativeKernel(kern, dim3((unsigned)blocks), dim3((unsigned)threads), args, 0,
-                                  stream);
+  const cudaError_t ce = launch_groups(kern, blocks, threads, cluster, args, stream);
   count_launch();
   if (ce != cudaSuccess) {
     fprintf(stderr, "fvcgpu: batched mixed launch failed: %s\n", cudaGetErrorString(ce));

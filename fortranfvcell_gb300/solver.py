@@ -32,7 +32,7 @@ def make_opts(precision: str = "fp64", init: int = -1, stop_rule: int = 0,
               refine_tol: float = 0.0, inner_tol: float = 0.0, max_refine: int = 0,
               block_threads: int = 0, blocks_per_sm: int = 0,
               update_beta: int = 0, staging: int = 0, max_blocks: int = 0,
-              fp32_layout: int = 0) -> FvcOpts:
+              fp32_layout: int = 0, cluster_size: int = 0) -> FvcOpts:
     o = FvcOpts()
     _lib.load().fvc_opts_default(C.byref(o))
     o.precision = {"fp64": _lib.FVC_PREC_FP64, "mixed": _lib.FVC_PREC_MIXED}[precision]
@@ -47,6 +47,7 @@ def make_opts(precision: str = "fp64", init: int = -1, stop_rule: int = 0,
     o.staging = staging
     o.max_blocks = max_blocks
     o.fp32_layout = fp32_layout
+    o.cluster_size = cluster_size
     return o
 
 

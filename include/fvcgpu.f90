@@ -35,6 +35,7 @@ module fvcgpu
      integer(c_int32_t) :: staging
      integer(c_int32_t) :: max_blocks
      integer(c_int32_t) :: fp32_layout
+     integer(c_int32_t) :: cluster_size
   end type fvc_opts
 
   ! options of the SIMPLE outer iteration (fvc_simple_opts in fvcgpu.h)

@@ -115,6 +115,17 @@ typedef struct {
                           A solve that asks for the other choice than the
                           context's operator has lays it out anew (a host
                           wait), so graphs captured before then are stale */
+  int32_t cluster_size; /* batched solves: how each system's blocks work
+                          together.  1: a group of blocks of one cooperative
+                          launch, synchronised through global memory, the
+                          share of blocks by expected work; k in 2..16: one
+                          thread-block cluster of k blocks per system
+                          (cluster barrier and distributed shared memory;
+                          an ordinary launch whose clusters start as SMs
+                          free up, heaviest systems first; above 8 needs
+                          the non-portable cluster sizes); 0: automatic --
+                          clusters of 8 for mixed precision, groups for
+                          FP64.  Single solves ignore it              */
 } fvc_opts;
 
 typedef struct {
@@ -239,16 +250,23 @@ int32_t fvc_autotune(fvc_context *ctx, int32_t code, int32_t precision,
  * be identity rows with b = 0 and x = 0.  Each system runs on its own group
  * of blocks with its own reductions and stopping test (tol, maxit and the
  * warm-start rule as in fvc_solve with code 1), so the iteration counts of
- * the systems are independent.  nsys is limited to the co-resident blocks of
- * one launch (FVC_ERR_ARG beyond).  st (host, nsys entries, may be NULL)
- * receives each system's statistics; solve_ms is the launch's time.
+ * the systems are independent.  opts->cluster_size chooses the groups: one
+ * thread-block cluster per system (mixed precision by default), or blocks
+ * of one cooperative launch sharing the device by expected work (FP64 by
+ * default), where nsys is limited to the co-resident blocks of the launch
+ * (FVC_ERR_ARG beyond).  st (host, nsys entries, may be NULL) receives
+ * each system's statistics; solve_ms is the device time of the solve.
  * Returns FVC_OK when every system converged, else FVC_ERR_NAN if one broke
  * down or the first other failure.  With FVC_PREC_MIXED each system runs
  * the mixed-precision solve of fvc_solve (FP32 iterations inside FP64
  * residual replacement or defect correction, stopping on the FP64
  * ||b-Ax||/||b|| <= tol); its statistics then count the FP32 iterations
- * and the refinements.  No counterpart in the reference, which solves one
- * system per call (src/Solver.f:28-346). */
+ * and the refinements.  A mixed BiCGSTAB system whose FP32 sweeps stall is
+ * finished in FP64 from its iterate (on ||r||2 <= tol ||b||2), as in
+ * fvc_solve, in a second launch over the stalled systems alone; its
+ * iterations then add the FP64 ones to inner_iterations (the FP32 ones).
+ * No counterpart in the reference, which solves one system per call
+ * (src/Solver.f:28-346). */
 int32_t fvc_solve_batched(fvc_context *ctx, int32_t nsys, const int32_t *row_start,
                           const double *d_b, double *d_x, double tol,
                           int32_t maxit, const fvc_opts *opts, fvc_stats *st);
