@@ -150,7 +150,16 @@ struct BatchPlan {
   int *dsob = nullptr;
   double tol = 0.0;
   int fp32_layout = 0;
-  int cluster = 0;  // > 0: one cluster of this many blocks per system
+  int cluster = 0;  // > 0: one cluster per system (cluster launches)
+  // cluster launches: one per cluster size, systems of the same size
+  // together; segment k covers blocks [sob_off, sob_off + blocks) of the
+  // block-to-system map.  Segments after the first run on their own
+  // streams, forked from and joined back to the caller's.
+  static constexpr int kMaxSeg = 5;
+  int nseg = 0;
+  int seg_csize[kMaxSeg] = {}, seg_blocks[kMaxSeg] = {}, seg_off[kMaxSeg] = {};
+  cudaStream_t aux[kMaxSeg] = {};
+  cudaEvent_t fork = nullptr, join[kMaxSeg] = {};
 };
 int32_t plan_batched(DeviceMatrix &A, Scratch &S, int nsys, const int32_t *row_start,
                      const int32_t *codes, const double *tols, const double *its_hint,

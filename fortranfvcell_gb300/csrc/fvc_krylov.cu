@@ -1031,10 +1031,15 @@ int32_t plan_batched(DeviceMatrix &A, Scratch &S, int nsys, const int32_t *row_s
   const bool mixed = o.precision == FVC_PREC_MIXED;
   // one thread-block cluster of csize CTAs per system (mixed batches by
   // default), or groups of blocks of one cooperative launch (csize 0)
-  if (o.cluster_size < 0 || o.cluster_size > 16) return FVC_ERR_ARG;
+  if (o.cluster_size < -1 || o.cluster_size > 16) return FVC_ERR_ARG;
+  // csize: the largest cluster (fixed sizes: all of them); adaptive (-1, and
+  // mixed precision's automatic choice): each system's cluster sized to it,
+  // about the largest system's rows / 16 rows per block, powers of two
+  const bool adaptive = o.cluster_size == -1 || (o.cluster_size == 0 && mixed);
   const int csize = (o.cluster_size == 1)   ? 0
                     : (o.cluster_size >= 2) ? o.cluster_size
-                    : (mixed ? kBatchClusterDefault : 0);
+                    : adaptive              ? 16
+                                            : 0;
   // groups: 128-thread blocks by default, twice the co-resident blocks of
   // 256, so the one-block minimum of the small systems takes a smaller share
   // (C4 batch of 256 cavities: 184 ms at 128 threads, 215 at 256, 386 at
@@ -1053,8 +1058,8 @@ int32_t plan_batched(DeviceMatrix &A, Scratch &S, int nsys, const int32_t *row_s
   const void *kern = mixed ? mixed_batched_kernel(threads) : krylov_batched_kernel(threads);
   int cap = 0;
   if (csize > 0) {
-    // an ordinary launch of one cluster per system: no co-residency bound,
-    // but one cluster must fit on the device
+    // ordinary launches of one cluster per system: no co-residency bound,
+    // but one cluster of the largest size must fit on the device
     if (csize > 8 &&
         cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
             cudaSuccess) {
@@ -1102,13 +1107,39 @@ int32_t plan_batched(DeviceMatrix &A, Scratch &S, int nsys, const int32_t *row_s
     wt[s] = slices[s] * its * ((codes && codes[s] == 2) ? 2.0 : 1.0);
     wleft += wt[s];
   }
-  // clusters: csize blocks each, the heaviest systems first (the hardware
+  // clusters: csize blocks each (adaptive: each system's own size), one
+  // launch per size, the heaviest systems first within it (the hardware
   // starts clusters roughly in launch order, so the long solves begin at once)
   std::vector<int> order(nsys);
   for (int s = 0; s < nsys; ++s) order[s] = s;
+  int nseg = 0, seg_csize[BatchPlan::kMaxSeg] = {}, seg_blocks[BatchPlan::kMaxSeg] = {},
+      seg_off[BatchPlan::kMaxSeg] = {};
   if (csize > 0) {
-    std::stable_sort(order.begin(), order.end(), [&](int p, int q) { return wt[p] > wt[q]; });
-    std::fill(nb.begin(), nb.end(), csize);
+    if (adaptive) {
+      int most_rows = 0;
+      for (int s = 0; s < nsys; ++s) most_rows = std::max(most_rows, slices[s] * 32);
+      const int per = std::max(1024, (most_rows + 15) / 16);
+      for (int s = 0; s < nsys; ++s) {
+        int c = 1;
+        while (c < 16 && (long)c * per < (long)slices[s] * 32) c *= 2;
+        nb[s] = c;
+      }
+    } else {
+      std::fill(nb.begin(), nb.end(), csize);
+    }
+    // segments by cluster size, largest first; within one, heaviest first
+    std::stable_sort(order.begin(), order.end(), [&](int p, int q) {
+      return nb[p] != nb[q] ? nb[p] > nb[q] : wt[p] > wt[q];
+    });
+    for (int i = 0; i < nsys; ++i) {
+      const int c = nb[order[i]];
+      if (nseg == 0 || seg_csize[nseg - 1] != c) {
+        seg_csize[nseg] = c;
+        seg_off[nseg] = (nseg == 0) ? 0 : seg_off[nseg - 1] + seg_blocks[nseg - 1];
+        ++nseg;
+      }
+      seg_blocks[nseg - 1] += c;
+    }
     std::fill(fixed.begin(), fixed.end(), 1);
     wleft = 0.0;
   }
@@ -1178,10 +1209,11 @@ int32_t plan_batched(DeviceMatrix &A, Scratch &S, int nsys, const int32_t *row_s
   std::vector<BatchSys> hsys(nsys);
   std::vector<int> hsob((size_t)total);
   size_t poff = 0;
-  int b0 = 0;
+  int b0 = 0, seg = 0;
   for (int i = 0; i < nsys; ++i) {
     const int s = order[i];
     BatchSys &d = hsys[s];
+    while (csize > 0 && seg + 1 < nseg && b0 >= seg_off[seg + 1]) ++seg;
     d.s0 = row_start[s] / 32;
     d.s1 = d.s0 + slices[s];
     d.code = codes ? codes[s] : 1;
@@ -1196,8 +1228,10 @@ int32_t plan_batched(DeviceMatrix &A, Scratch &S, int nsys, const int32_t *row_s
     d.gs.partials = part + poff;
     d.gs.totals = part + poff + (size_t)4 * kMaxNV * nb[s];
     d.gs.nblocks = (unsigned int)nb[s];
-    d.gs.base = (unsigned int)b0;
-    d.gs.cluster = csize > 0 ? 1 : 0;
+    // a cluster launch numbers its blocks from 0: the base within the segment
+    d.gs.base = (unsigned int)(csize > 0 ? b0 - seg_off[seg] : b0);
+    // a one-block cluster needs no cluster barrier: the block's own sums
+    d.gs.cluster = (csize > 0 && nb[s] > 1) ? 1 : 0;
     d.result = res + (size_t)s * 16;
     d.iresult = ires + (size_t)s * 16;
     d.run = run ? run + s : nullptr;
@@ -1228,6 +1262,18 @@ int32_t plan_batched(DeviceMatrix &A, Scratch &S, int nsys, const int32_t *row_s
   P.total = (int)total;
   P.threads = threads;
   P.cluster = csize;
+  if (csize == 0) {  // groups: one cooperative launch of every block
+    nseg = 1;
+    seg_csize[0] = 0;
+    seg_blocks[0] = (int)total;
+    seg_off[0] = 0;
+  }
+  P.nseg = nseg;
+  for (int k = 0; k < nseg; ++k) {
+    P.seg_csize[k] = seg_csize[k];
+    P.seg_blocks[k] = seg_blocks[k];
+    P.seg_off[k] = seg_off[k];
+  }
   P.mixed = mixed;
   P.kern = kern;
   P.buf = buf;
@@ -1242,7 +1288,41 @@ int32_t plan_batched(DeviceMatrix &A, Scratch &S, int nsys, const int32_t *row_s
   P.dsob = dsob;
   P.tol = tol;
   P.fp32_layout = o.fp32_layout;
+  // the segments after the first run on their own streams
+  if (nseg > 1) {
+    bool ok = cudaEventCreateWithFlags(&P.fork, cudaEventDisableTiming) == cudaSuccess;
+    for (int k = 1; k < nseg && ok; ++k)
+      ok = cudaStreamCreateWithFlags(&P.aux[k], cudaStreamNonBlocking) == cudaSuccess &&
+           cudaEventCreateWithFlags(&P.join[k], cudaEventDisableTiming) == cudaSuccess;
+    if (!ok) {
+      free_batched(P, stream);
+      return FVC_ERR_CUDA;
+    }
+  }
   return FVC_OK;
+}
+
+// The plan's launches: one (groups, or clusters of one size), or one per
+// cluster size, the first on the caller's stream and the others on the
+// plan's streams, forked from it after everything enqueued so far and
+// joined back into it (event waits: stream-ordered and capturable).
+template <typename L>
+int32_t launch_segments(const BatchPlan &P, cudaStream_t stream, L &&launch) {
+  if (P.nseg <= 1) return launch(0, stream);
+  if (cudaEventRecord(P.fork, stream) != cudaSuccess) return FVC_ERR_CUDA;
+  for (int k = 1; k < P.nseg; ++k)
+    if (cudaStreamWaitEvent(P.aux[k], P.fork, 0) != cudaSuccess) return FVC_ERR_CUDA;
+  int32_t rc = FVC_OK;
+  for (int k = 0; k < P.nseg; ++k) {
+    const int32_t r = launch(k, k == 0 ? stream : P.aux[k]);
+    if (r != FVC_OK && rc == FVC_OK) rc = r;
+  }
+  for (int k = 1; k < P.nseg; ++k) {
+    if (cudaEventRecord(P.join[k], P.aux[k]) != cudaSuccess ||
+        cudaStreamWaitEvent(stream, P.join[k], 0) != cudaSuccess)
+      rc = FVC_ERR_CUDA;
+  }
+  return rc;
 }
 
 int32_t enqueue_batched(DeviceMatrix &A, Scratch &S, const BatchPlan &P, const double *b,
@@ -1256,8 +1336,10 @@ int32_t enqueue_batched(DeviceMatrix &A, Scratch &S, const BatchPlan &P, const d
     // layout is decided, which planning did)
     int32_t rc = build_f32_copy(A, stream, P.fp32_layout);
     if (rc != FVC_OK) return rc;
-    return launch_mixed_batched(A, S, P.dsys, P.dsob, P.total, P.threads, P.cluster, b, x, maxit,
-                                o, stream);
+    return launch_segments(P, stream, [&](int k, cudaStream_t st) {
+      return launch_mixed_batched(A, S, P.dsys, P.dsob + P.seg_off[k], P.seg_blocks[k],
+                                  P.threads, P.seg_csize[k], b, x, maxit, o, st);
+    });
   }
   KArgs a{};
   a.A = view64(A);
@@ -1278,16 +1360,19 @@ int32_t enqueue_batched(DeviceMatrix &A, Scratch &S, const BatchPlan &P, const d
   a.maxit = maxit;
   a.init = 1;
   a.stop_rule = o.stop_rule;
-  const BatchSys *psys = P.dsys;
-  const int *psob = P.dsob;
-  void *args[] = {&a, &psys, &psob};
-  const cudaError_t ce = launch_groups(P.kern, P.total, P.threads, P.cluster, args, stream);
-  count_launch();
-  if (ce != cudaSuccess) {
-    fprintf(stderr, "fvcgpu: batched launch failed: %s\n", cudaGetErrorString(ce));
-    return FVC_ERR_CUDA;
-  }
-  return FVC_OK;
+  return launch_segments(P, stream, [&](int k, cudaStream_t st) {
+    const BatchSys *psys = P.dsys;
+    const int *psob = P.dsob + P.seg_off[k];
+    void *args[] = {&a, &psys, &psob};
+    const cudaError_t ce =
+        launch_groups(P.kern, P.seg_blocks[k], P.threads, P.seg_csize[k], args, st);
+    count_launch();
+    if (ce != cudaSuccess) {
+      fprintf(stderr, "fvcgpu: batched launch failed: %s\n", cudaGetErrorString(ce));
+      return FVC_ERR_CUDA;
+    }
+    return FVC_OK;
+  });
 }
 
 void free_batched(BatchPlan &P, cudaStream_t stream) {
@@ -1297,6 +1382,12 @@ void free_batched(BatchPlan &P, cudaStream_t stream) {
     else
       cudaFreeAsync(P.buf, stream);
   }
+  // (a stream destroyed with work pending finishes that work first)
+  for (int k = 0; k < BatchPlan::kMaxSeg; ++k) {
+    if (P.aux[k]) cudaStreamDestroy(P.aux[k]);
+    if (P.join[k]) cudaEventDestroy(P.join[k]);
+  }
+  if (P.fork) cudaEventDestroy(P.fork);
   P = BatchPlan();
 }
 

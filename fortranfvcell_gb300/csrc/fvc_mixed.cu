@@ -424,6 +424,28 @@ struct MPart {
   for (int s_ = (P).sb + (P).warp; s_ < (P).se; s_ += (P).nwarps) \
     for (int row = s_ * 32 + (P).lane, once_ = 1; once_ && row < (P).n; once_ = 0)
 
+// The same rows two slices per warp step: f(s, row, ok) gets this step's
+// two slices (s, s + nwarps), so a body that loads both rows' operands
+// before it stores either result keeps two rows' gathers in flight (the
+// warp's loads of one row otherwise wait on the stores of the one before,
+// which the compiler cannot move past them).  A missing second slice, or a
+// row at or beyond n, comes with ok = false and the slice's first row
+// (always valid) as its row: its loads are harmless and its results are
+// dropped.  The rows are visited in the order of MFOR_ROWS, so sums over
+// them are the same.
+template <typename F>
+__device__ __forceinline__ void mfor_rows2(const MPart &P, F &&f) {
+  for (int s = P.sb + P.warp; s < P.se; s += 2 * P.nwarps) {
+    const int s1 = s + P.nwarps;
+    const bool has1 = s1 < P.se;
+    const int ra = s * 32 + P.lane, rb = (has1 ? s1 : s) * 32 + P.lane;
+    const int sl[2] = {s, has1 ? s1 : s};
+    const bool ok[2] = {ra < P.n, has1 && rb < P.n};
+    const int rw[2] = {ok[0] ? ra : s * 32, ok[1] ? rb : s * 32};
+    f(sl, rw, ok);
+  }
+}
+
 // FP64 residual sweep: rs = b - A x rounded to FP32.  Returns ||b-Ax||^2,
 // ||b||^2, rs.(rs/m) and ||b-Ax||^2 over the rows the FP32 iteration moves
 // (FP64 sums).
@@ -508,7 +530,8 @@ __device__ __forceinline__ float2 p_update(float z, float bh, float bl, float ph
 }
 
 // CG phase A with plain loads: p = z + beta p_prev (formed at each gathered
-// neighbour), q = A p_hi, returns p_hi.q.  One slice per warp step.
+// neighbour), q = A p_hi, returns p_hi.q.  Two slices per warp step
+// (mfor_rows2).
 template <bool kFirst>
 __device__ __forceinline__ CSum cg_phase_a(const MArgs &a, const MPart &P, float bh, float bl,
                                            const Dir &d) {
@@ -517,17 +540,24 @@ __device__ __forceinline__ CSum cg_phase_a(const MArgs &a, const MPart &P, float
   auto pf = [&](int k) -> float2 {
     return kFirst ? make_float2(z[k], 0.0f) : p_update(z[k], bh, bl, d.ph[k], d.pl[k]);
   };
-  for (int s = P.sb + P.warp; s < P.se; s += P.nwarps) {
-    const int row = s * kSlice + P.lane;
-    if (row >= P.n) continue;
-    const float2 pi = pf(row);
-    const float t = arow32(a, s, P.lane, row, [&](int k) { return pf(k).x; });
-    d.ch[row] = pi.x;
-    d.cl[row] = pi.y;
-    a.q[row] = t;
-    if (kFirst) a.e[row] = make_float2(0.0f, 0.0f);
-    cpq.add(pi.x * t);
-  }
+  mfor_rows2(P, [&](const int(&sl)[2], const int(&rw)[2], const bool(&ok)[2]) {
+    float2 pi[2];
+    float t[2];
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      pi[u] = pf(rw[u]);
+      t[u] = arow32(a, sl[u], P.lane, rw[u], [&](int k) { return pf(k).x; });
+    }
+#pragma unroll
+    for (int u = 0; u < 2; ++u)
+      if (ok[u]) {
+        d.ch[rw[u]] = pi[u].x;
+        d.cl[rw[u]] = pi[u].y;
+        a.q[rw[u]] = t[u];
+        if (kFirst) a.e[rw[u]] = make_float2(0.0f, 0.0f);
+        cpq.add(pi[u].x * t[u]);
+      }
+  });
   return cpq;
 }
 
@@ -572,19 +602,36 @@ template <bool kPair, bool kUpdE>
 __device__ __forceinline__ void cg_phase_b(const MArgs &a, const MPart &P, float a1, float a1_lo,
                                            float alpha, float alpha_lo, const Dir &d, CSum &crz,
                                            CSum &crr) {
-  MFOR_ROWS(P) {
-    float2 eo;
-    float ro, rlo = 0.0f, zo;
-    cg_row_b<kPair, kUpdE>(a1, a1_lo, alpha, alpha_lo, a.q[row], a.rs[row],
-                           kPair ? a.rsl[row] : 0.0f, a.minv[row],
-                           kUpdE ? a.e[row] : make_float2(0.0f, 0.0f), kUpdE ? d.ph[row] : 0.0f,
-                           kUpdE ? d.pl[row] : 0.0f, kUpdE ? d.ch[row] : 0.0f,
-                           kUpdE ? d.cl[row] : 0.0f, eo, ro, rlo, zo, crz, crr);
-    if (kUpdE) a.e[row] = eo;
-    a.rs[row] = ro;
-    if (kPair) a.rsl[row] = rlo;
-    a.z[row] = zo;
-  }
+  mfor_rows2(P, [&](const int(&sl)[2], const int(&rw)[2], const bool(&ok)[2]) {
+    float qv[2], rv[2], rl[2], mv[2], p1h[2], p1l[2], pvh[2], pvl[2];
+    float2 ev[2];
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const int row = rw[u];
+      qv[u] = a.q[row];
+      rv[u] = a.rs[row];
+      rl[u] = kPair ? a.rsl[row] : 0.0f;
+      mv[u] = a.minv[row];
+      ev[u] = kUpdE ? a.e[row] : make_float2(0.0f, 0.0f);
+      p1h[u] = kUpdE ? d.ph[row] : 0.0f;
+      p1l[u] = kUpdE ? d.pl[row] : 0.0f;
+      pvh[u] = kUpdE ? d.ch[row] : 0.0f;
+      pvl[u] = kUpdE ? d.cl[row] : 0.0f;
+    }
+#pragma unroll
+    for (int u = 0; u < 2; ++u)
+      if (ok[u]) {
+        const int row = rw[u];
+        float2 eo;
+        float ro, rlo = 0.0f, zo;
+        cg_row_b<kPair, kUpdE>(a1, a1_lo, alpha, alpha_lo, qv[u], rv[u], rl[u], mv[u], ev[u],
+                               p1h[u], p1l[u], pvh[u], pvl[u], eo, ro, rlo, zo, crz, crr);
+        if (kUpdE) a.e[row] = eo;
+        a.rs[row] = ro;
+        if (kPair) a.rsl[row] = rlo;
+        a.z[row] = zo;
+      }
+  });
 }
 
 // ---------------------------------------------------------------------
@@ -1293,6 +1340,16 @@ constexpr int kSweepStall = 3;
 
 __device__ __forceinline__ void mixed_bicgstab_body(const MArgs &a) {
   __shared__ double red[kMaxNV * 32];
+  __shared__ float2 red2[kMaxNV * 32];
+  // the inner iteration's scalars: FP64 work of lane 0 of warp 0 inside the
+  // all-reduces (GB300 runs FP64 at ~1/64 of the FP32 rate: three FP64
+  // divisions in every thread of every iteration kept the FP64 pipe 40%
+  // busy), handed to the block as FP32 through shared memory
+  __shared__ struct {
+    double rr0, best;
+    float alpha, omega, beta;
+    int it_best, go;
+  } bs;
   if (f32_refused(a)) return;
   const MPart P(a);
   unsigned int ep = 0;
@@ -1338,71 +1395,131 @@ __device__ __forceinline__ void mixed_bicgstab_body(const MArgs &a) {
       e[row] = make_float2(0.0f, 0.0f);
     }
     if (!grid_barrier(a.gs, ep)) return;
-    int it = 0, it_best = 0;
-    double best = fabs(d);
+    if (threadIdx.x == 0) {
+      bs.best = fabs(d);
+      bs.it_best = 0;
+    }
+    int it = 0;
     for (;;) {
       ++it;
       // v = A z ; rr0 = s.r0 ; v.r0
-      CSum c0, c1;
-      MFOR_ROWS(P) {
-        const float vi = arow32(a, s_, P.lane, row, [&](int k) { return z[k]; });
-        v[row] = vi;
-        const float r0i = r0[row];
-        c0.add(sv[row] * r0i);
-        c1.add(vi * r0i);
-      }
-      double acc[2] = {c0.value(), c1.value()};
-      if (!grid_allreduce<2>(a.gs, ep, acc, red)) return;
-      const double rr0 = acc[0];
-      const float alpha = (float)(rr0 / acc[1]);
+      CSum c01[2];
+      mfor_rows2(P, [&](const int(&sl)[2], const int(&rw)[2], const bool(&ok)[2]) {
+        float vi[2], r0i[2], si[2];
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+          vi[u] = arow32(a, sl[u], P.lane, rw[u], [&](int k) { return z[k]; });
+          r0i[u] = r0[rw[u]];
+          si[u] = sv[rw[u]];
+        }
+#pragma unroll
+        for (int u = 0; u < 2; ++u)
+          if (ok[u]) {
+            v[rw[u]] = vi[u];
+            c01[0].add(si[u] * r0i[u]);
+            c01[1].add(vi[u] * r0i[u]);
+          }
+      });
       // breakdown (v.r0 or r0.s vanished in FP32): leave the correction as it
       // is and restart from an FP64 residual in the next sweep
-      if (!isfinite(alpha) || alpha == 0.0f) break;
+      if (!grid_allreduce_ff<2>(a.gs, ep, c01, red2, [&](const double *q) {
+            bs.rr0 = q[0];
+            bs.alpha = (float)(q[0] / q[1]);
+            bs.go = (isfinite(bs.alpha) && bs.alpha != 0.0f) ? 1 : 0;
+          }))
+        return;
+      if (!bs.go) break;
+      const float alpha = bs.alpha;
       // e += alpha z ; s -= alpha v ; z = s/m
-      MFOR_ROWS(P) {
-        e[row] = df_axpy(e[row], alpha, 0.0f, z[row]);
-        const float si = fmaf(-alpha, v[row], sv[row]);
-        sv[row] = si;
-        z[row] = si * minv[row];
-      }
+      mfor_rows2(P, [&](const int(&sl)[2], const int(&rw)[2], const bool(&ok)[2]) {
+        float2 ev[2];
+        float zi[2], vv[2], si[2], mi[2];
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+          ev[u] = e[rw[u]];
+          zi[u] = z[rw[u]];
+          vv[u] = v[rw[u]];
+          si[u] = sv[rw[u]];
+          mi[u] = minv[rw[u]];
+        }
+#pragma unroll
+        for (int u = 0; u < 2; ++u)
+          if (ok[u]) {
+            e[rw[u]] = df_axpy(ev[u], alpha, 0.0f, zi[u]);
+            const float sn = fmaf(-alpha, vv[u], si[u]);
+            sv[rw[u]] = sn;
+            z[rw[u]] = sn * mi[u];
+          }
+      });
       if (!grid_barrier(a.gs, ep)) return;
       // t = A z ; t.s ; t.t
-      CSum c2, c3;
-      MFOR_ROWS(P) {
-        const float ti = arow32(a, s_, P.lane, row, [&](int k) { return z[k]; });
-        t[row] = ti;
-        c2.add(ti * sv[row]);
-        c3.add(ti * ti);
-      }
-      acc[0] = c2.value();
-      acc[1] = c3.value();
-      if (!grid_allreduce<2>(a.gs, ep, acc, red)) return;
-      const float omega = (acc[1] > 0.0) ? (float)(acc[0] / acc[1]) : 0.0f;
-      if (!isfinite(omega)) break;
+      CSum c23[2];
+      mfor_rows2(P, [&](const int(&sl)[2], const int(&rw)[2], const bool(&ok)[2]) {
+        float ti[2], si[2];
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+          ti[u] = arow32(a, sl[u], P.lane, rw[u], [&](int k) { return z[k]; });
+          si[u] = sv[rw[u]];
+        }
+#pragma unroll
+        for (int u = 0; u < 2; ++u)
+          if (ok[u]) {
+            t[rw[u]] = ti[u];
+            c23[0].add(ti[u] * si[u]);
+            c23[1].add(ti[u] * ti[u]);
+          }
+      });
+      if (!grid_allreduce_ff<2>(a.gs, ep, c23, red2, [&](const double *q) {
+            bs.omega = (q[1] > 0.0) ? (float)(q[0] / q[1]) : 0.0f;
+            bs.go = isfinite(bs.omega) ? 1 : 0;
+          }))
+        return;
+      if (!bs.go) break;
+      const float omega = bs.omega;
       // e += w z ; s -= w t ; s.z ; r0.s
-      CSum c4, c5;
-      MFOR_ROWS(P) {
-        const float zi = z[row];
-        e[row] = df_axpy(e[row], omega, 0.0f, zi);
-        const float sn = fmaf(-omega, t[row], sv[row]);
-        sv[row] = sn;
-        c4.add(sn * zi);
-        c5.add(r0[row] * sn);
-      }
-      double acc2[2] = {c4.value(), c5.value()};
-      if (!grid_allreduce<2>(a.gs, ep, acc2, red)) return;
-      if (!(acc2[0] == acc2[0]) || fabs(acc2[0]) <= stop2 || inner_total + it >= a.maxit ||
-          omega == 0.0f)
-        break;
-      // restarted BiCGSTAB: an inner solve whose residual has not improved
-      // for kBcgStall iterations (FP32 stagnation) restarts from an FP64 one
-      if (fabs(acc2[0]) < 0.99 * best) {
-        best = fabs(acc2[0]);
-        it_best = it;
-      } else if (it - it_best > kBcgStall) {
-        break;
-      }
-      const float beta = (float)((acc2[1] / rr0) * ((double)alpha / (double)omega));
+      CSum c45[2];
+      mfor_rows2(P, [&](const int(&sl)[2], const int(&rw)[2], const bool(&ok)[2]) {
+        float2 ev[2];
+        float zi[2], ti[2], si[2], r0i[2];
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+          ev[u] = e[rw[u]];
+          zi[u] = z[rw[u]];
+          ti[u] = t[rw[u]];
+          si[u] = sv[rw[u]];
+          r0i[u] = r0[rw[u]];
+        }
+#pragma unroll
+        for (int u = 0; u < 2; ++u)
+          if (ok[u]) {
+            e[rw[u]] = df_axpy(ev[u], omega, 0.0f, zi[u]);
+            const float sn = fmaf(-omega, ti[u], si[u]);
+            sv[rw[u]] = sn;
+            c45[0].add(sn * zi[u]);
+            c45[1].add(r0i[u] * sn);
+          }
+      });
+      // stop on the inner reduction, a NaN, maxit or w = 0; restarted
+      // BiCGSTAB: an inner solve whose residual has not improved for
+      // kBcgStall iterations (FP32 stagnation) restarts from an FP64 one
+      if (!grid_allreduce_ff<2>(a.gs, ep, c45, red2, [&](const double *q) {
+            const double sz = fabs(q[0]);
+            int go = 1;
+            if (!(q[0] == q[0]) || sz <= stop2 || inner_total + it >= a.maxit ||
+                bs.omega == 0.0f) {
+              go = 0;
+            } else if (sz < 0.99 * bs.best) {
+              bs.best = sz;
+              bs.it_best = it;
+            } else if (it - bs.it_best > kBcgStall) {
+              go = 0;
+            }
+            bs.beta = (float)((q[1] / bs.rr0) * ((double)bs.alpha / (double)bs.omega));
+            bs.go = go;
+          }))
+        return;
+      if (!bs.go) break;
+      const float beta = bs.beta;
       // p = s + beta (p - w v) ; z = p/m
       MFOR_ROWS(P) {
         const float pi = fmaf(beta, fmaf(-omega, v[row], p[row]), sv[row]);

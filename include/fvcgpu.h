@@ -78,9 +78,9 @@ enum {
    * context's later mixed BiCGSTAB solves run in FP64 from the start until
    * fvc_matrix_set gives it another structure.  fvc_solve_async reports
    * that stall as FVC_ERR_NOCONV and, after one in an fvc_solve of the
-   * context, routes later ones to FP64 too; fvc_solve_batched reports it as
-   * FVC_ERR_NOCONV; the SIMPLE batch (fvc_simple_batch_*) finishes it in
-   * FP64 inside its graph. */
+   * context, routes later ones to FP64 too; fvc_solve_batched finishes the
+   * stalled systems in FP64 in a second launch; the SIMPLE batch
+   * (fvc_simple_batch_*) finishes them in FP64 inside its graph. */
 };
 
 typedef struct {
@@ -123,9 +123,13 @@ typedef struct {
                           (cluster barrier and distributed shared memory;
                           an ordinary launch whose clusters start as SMs
                           free up, heaviest systems first; above 8 needs
-                          the non-portable cluster sizes); 0: automatic --
-                          clusters of 8 for mixed precision, groups for
-                          FP64.  Single solves ignore it              */
+                          the non-portable cluster sizes); -1: one cluster
+                          per system sized to it (about the largest
+                          system's rows / 16 rows per block, powers of two
+                          up to 16; one launch per size, the launches side
+                          by side on forked streams); 0: automatic -- -1
+                          for mixed precision, groups for FP64.  Single
+                          solves ignore it                               */
 } fvc_opts;
 
 typedef struct {

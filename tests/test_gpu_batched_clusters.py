@@ -46,7 +46,7 @@ def _mixed_codes(systems):
     return codes, tols
 
 
-@pytest.mark.parametrize("csize", [2, 8, 16])
+@pytest.mark.parametrize("csize", [2, 8, 16, -1])
 def test_fp64_clusters_match_reference_per_system(orc, csize):
     # PCG beside BiCGSTAB, systems of 1 to ~2000 rows (some with fewer
     # slices than the cluster has blocks)
@@ -72,7 +72,8 @@ def test_fp64_clusters_match_reference_per_system(orc, csize):
 
 @pytest.mark.parametrize("csize", [0, 4, 16])
 def test_mixed_clusters_reach_tolerance(orc, csize):
-    # mixed precision (0: the automatic choice, clusters of 8): every system
+    # mixed precision (0: the automatic choice, one cluster per system sized
+    # to it, one launch per size on forked streams): every system
     # to ||b - Ax|| <= 1e-8 ||b|| recomputed in FP64, within 1e-4 of the
     # FP64 solution
     from fortranfvcell_gb300 import make_opts
@@ -90,24 +91,27 @@ def test_mixed_clusters_reach_tolerance(orc, csize):
 
 
 def test_clusters_and_groups_agree_and_repeat(orc):
-    # groups (cluster_size 1) and clusters partition a system's rows
-    # differently, so only the dot products' summation order differs: the
-    # same solutions to rounding; two cluster runs are bit-identical
+    # groups (cluster_size 1) and clusters (8, and sized per system: these
+    # systems fall into several sizes, so several launches on forked
+    # streams) partition a system's rows differently, so only the dot
+    # products' summation order differs: the same solutions to rounding;
+    # two runs of one form are bit-identical
     from fortranfvcell_gb300 import make_opts
     systems = batch(orc)
     codes, tols = _mixed_codes(systems)
     runs = [_solve(systems, 0.0, 20000, make_opts("fp64", init=1, cluster_size=c), codes, tols)
-            for c in (1, 8, 8)]
-    for (_, _, xg), (_, _, xc) in zip(runs[:1], runs[1:2]):
-        for a, b in zip(xg, xc):
+            for c in (1, 8, 8, -1, -1)]
+    for _, _, xc in (runs[1], runs[3]):
+        for a, b in zip(runs[0][2], xc):
             assert np.linalg.norm(a - b) <= 1e-9 * max(np.linalg.norm(a), 1e-300)
-    for a, b in zip(runs[1][2], runs[2][2]):
-        np.testing.assert_array_equal(a, b)
+    for i, j in ((1, 2), (3, 4)):
+        for a, b in zip(runs[i][2], runs[j][2]):
+            np.testing.assert_array_equal(a, b)
 
 
 def test_cluster_size_outside_the_range_is_refused(orc):
     from fortranfvcell_gb300 import _lib, make_opts
     systems = batch(orc)[:3]
-    for bad in (-1, 17):
+    for bad in (-2, 17):
         rc, _, _ = _solve(systems, 1e-8, 100, make_opts("fp64", init=1, cluster_size=bad))
         assert rc == _lib.FVC_ERR_ARG
