@@ -155,7 +155,7 @@ struct BatchPlan {
   // together; segment k covers blocks [sob_off, sob_off + blocks) of the
   // block-to-system map.  Segments after the first run on their own
   // streams, forked from and joined back to the caller's.
-  static constexpr int kMaxSeg = 5;
+  static constexpr int kMaxSeg = 16;
   int nseg = 0;
   int seg_csize[kMaxSeg] = {}, seg_blocks[kMaxSeg] = {}, seg_off[kMaxSeg] = {};
   cudaStream_t aux[kMaxSeg] = {};
@@ -196,8 +196,6 @@ cudaError_t launch_groups(const void *kern, int blocks, int threads, int csize, 
                           cudaStream_t stream);
 void cluster_config(cudaLaunchConfig_t &cfg, cudaLaunchAttribute *at, int csize, int threads,
                     cudaStream_t stream);
-// CTAs per cluster of a mixed batch when fvc_opts.cluster_size is 0
-constexpr int kBatchClusterDefault = 8;
 int32_t launch_mixed_batched(const DeviceMatrix &A, const Scratch &S, const BatchSys *dsys,
                              const int *dsob, int blocks, int threads, int cluster,
                              const double *b, double *x, int maxit, const fvc_opts &o,

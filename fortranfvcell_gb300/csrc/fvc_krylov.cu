@@ -1029,13 +1029,16 @@ int32_t plan_batched(DeviceMatrix &A, Scratch &S, int nsys, const int32_t *row_s
     any_bicg = any_bicg || code == 2;
   }
   const bool mixed = o.precision == FVC_PREC_MIXED;
-  // one thread-block cluster of csize CTAs per system (mixed batches by
-  // default), or groups of blocks of one cooperative launch (csize 0)
+  // one thread-block cluster per system (by default), or groups of blocks of
+  // one cooperative launch (csize 0).  C4 (256 cases, frozen p' and enthalpy
+  // systems, ||r|| <= 1e-8 ||b||): FP64 p' 152 ms in groups, 129 ms on
+  // clusters sized per system; enthalpy 219 / 176 ms
   if (o.cluster_size < -1 || o.cluster_size > 16) return FVC_ERR_ARG;
-  // csize: the largest cluster (fixed sizes: all of them); adaptive (-1, and
-  // mixed precision's automatic choice): each system's cluster sized to it,
-  // about the largest system's rows / 16 rows per block, powers of two
-  const bool adaptive = o.cluster_size == -1 || (o.cluster_size == 0 && mixed);
+  // csize: the largest cluster (fixed sizes: all of them); adaptive (-1, the
+  // automatic choice): each system's cluster sized to it,
+  // ceil(rows / (the largest system's rows / 16)) blocks, so that every block
+  // has about as many rows and the per-iteration times line up
+  const bool adaptive = o.cluster_size <= 0;
   const int csize = (o.cluster_size == 1)   ? 0
                     : (o.cluster_size >= 2) ? o.cluster_size
                     : adaptive              ? 16
@@ -1119,11 +1122,8 @@ int32_t plan_batched(DeviceMatrix &A, Scratch &S, int nsys, const int32_t *row_s
       int most_rows = 0;
       for (int s = 0; s < nsys; ++s) most_rows = std::max(most_rows, slices[s] * 32);
       const int per = std::max(1024, (most_rows + 15) / 16);
-      for (int s = 0; s < nsys; ++s) {
-        int c = 1;
-        while (c < 16 && (long)c * per < (long)slices[s] * 32) c *= 2;
-        nb[s] = c;
-      }
+      for (int s = 0; s < nsys; ++s)
+        nb[s] = (int)std::min<long>(16, std::max<long>(1, ((long)slices[s] * 32 + per - 1) / per));
     } else {
       std::fill(nb.begin(), nb.end(), csize);
     }

@@ -124,11 +124,10 @@ typedef struct {
                           an ordinary launch whose clusters start as SMs
                           free up, heaviest systems first; above 8 needs
                           the non-portable cluster sizes); -1: one cluster
-                          per system sized to it (about the largest
-                          system's rows / 16 rows per block, powers of two
-                          up to 16; one launch per size, the launches side
-                          by side on forked streams); 0: automatic -- -1
-                          for mixed precision, groups for FP64.  Single
+                          per system sized to it (ceil(rows / r) blocks, r
+                          the largest system's rows / 16, at least 1024;
+                          one launch per size, the launches side by side on
+                          forked streams); 0: automatic, -1.  Single
                           solves ignore it                               */
 } fvc_opts;
 
