@@ -1175,6 +1175,13 @@ __global__ void rec_errs(const int32_t *const *errs, int ncases, int32_t *out) {
 struct fvc_simple_batch {
   int device = 0, ncases = 0;
   cudaStream_t stream = nullptr, body = nullptr;
+  // the cases' cell kernels and conditional nodes run on kBranches
+  // streams side by side (case c on branch c mod kBranches), forked from
+  // and joined back into stream: each case's kernels are small, so one
+  // stream would leave most of the device idle between them
+  static constexpr int kBranches = 16;
+  cudaStream_t branch[kBranches] = {};
+  cudaEvent_t fork = nullptr, join[kBranches] = {};
   bool gas = false;
   int precision = FVC_PREC_FP64;    // p'
   int precision_u = FVC_PREC_FP64;  // u, v and the enthalpy
@@ -1244,6 +1251,11 @@ void batch_release(fvc_simple_batch *B) {
   if (B->h_err) cudaFreeHost(B->h_err);
   if (B->h_handles) cudaFreeHost(B->h_handles);
   if (B->body) cudaStreamDestroy(B->body);
+  for (int k = 0; k < fvc_simple_batch::kBranches; ++k) {
+    if (B->branch[k]) cudaStreamDestroy(B->branch[k]);
+    if (B->join[k]) cudaEventDestroy(B->join[k]);
+  }
+  if (B->fork) cudaEventDestroy(B->fork);
   if (B->stream) cudaStreamDestroy(B->stream);
 }
 
@@ -1422,17 +1434,35 @@ int32_t batch_build(fvc_simple_batch *B) {
     fvc::count_launch();
     return FVC_OK;
   };
+  // every case's part of a stage, case c on branch c mod kBranches: fork
+  // the branches from st, enqueue, join them back (event waits; in the
+  // capture these are the graph's parallel branches)
+  constexpr int kB = fvc_simple_batch::kBranches;
+  auto per_case = [&](auto &&f) -> int32_t {
+    if (!cap_ok(cudaEventRecord(B->fork, st), "cudaEventRecord (fork)")) return FVC_ERR_CUDA;
+    for (int k = 0; k < kB; ++k)
+      if (!cap_ok(cudaStreamWaitEvent(B->branch[k], B->fork, 0), "cudaStreamWaitEvent (fork)"))
+        return FVC_ERR_CUDA;
+    int32_t r = FVC_OK;
+    for (int c = 0; c < nc && r == FVC_OK; ++c) r = f(c, B->branch[c % kB]);
+    for (int k = 0; k < kB; ++k)
+      if (!cap_ok(cudaEventRecord(B->join[k], B->branch[k]), "cudaEventRecord (join)") ||
+          !cap_ok(cudaStreamWaitEvent(st, B->join[k], 0), "cudaStreamWaitEvent (join)"))
+        r = FVC_ERR_CUDA;
+    return r;
+  };
   // IF(the case's solve ran and ended FVC_OK) { after(case) } for every case
   auto after_stage = [&](int k, int hoff, int which) -> int32_t {
     fvc_simple_batch::Stage &S = B->st[k];
     fvc::CondSet a{B->d_handles + hoff, S.run, S.status, nc};
     fvc::stage_conds<<<(nc + 127) / 128, 128, 0, st>>>(a);
     fvc::count_launch();
-    for (int c = 0; c < nc; ++c) {
+    return per_case([&](int c, cudaStream_t bst) -> int32_t {
       fvc_simple *s = B->cs[c];
-      // cap_if captures into the case's own body stream: point it at ours
+      // cap_if adds the node on the case's stream and captures the body
+      // into the case's body stream: point them at the branch and ours
       cudaStream_t keep_stream = s->stream, keep_body = s->body;
-      s->stream = st;
+      s->stream = bst;
       s->body = B->body;
       int64_t nl = 0;
       const int32_t r = cap_if(s, B->h_handles[hoff + c], &nl, [&](cudaStream_t bs) {
@@ -1441,13 +1471,14 @@ int32_t batch_build(fvc_simple_batch *B) {
       s->stream = keep_stream;
       s->body = keep_body;
       B->launches_body[which == 3 ? 0 : 1][c] = nl;
-      if (r != FVC_OK) return r;
-    }
-    return FVC_OK;
+      return r;
+    });
   };
-  for (int c = 0; c < nc && rc == FVC_OK; ++c) rc = stage_momentum(B->cs[c], st);
+  if (rc == FVC_OK)
+    rc = per_case([&](int c, cudaStream_t bst) { return stage_momentum(B->cs[c], bst); });
   if (rc == FVC_OK) rc = solve_stage(0);
-  for (int c = 0; c < nc && rc == FVC_OK; ++c) rc = stage_pressure(B->cs[c], st);
+  if (rc == FVC_OK)
+    rc = per_case([&](int c, cudaStream_t bst) { return stage_pressure(B->cs[c], bst); });
   if (rc == FVC_OK) {
     fvc::rec_case_dots<<<(nc + 127) / 128, 128, 0, st>>>(B->d_dots, nc, 3, 0, B->rec_dots);
     fvc::count_launch();
@@ -1455,7 +1486,8 @@ int32_t batch_build(fvc_simple_batch *B) {
   }
   if (rc == FVC_OK) rc = after_stage(1, 0, 3);
   if (B->gas) {
-    for (int c = 0; c < nc && rc == FVC_OK; ++c) rc = stage_energy(B->cs[c], st);
+    if (rc == FVC_OK)
+      rc = per_case([&](int c, cudaStream_t bst) { return stage_energy(B->cs[c], bst); });
     if (rc == FVC_OK) {
       fvc::rec_case_dots<<<(nc + 127) / 128, 128, 0, st>>>(B->d_dots, nc, 2, 3, B->rec_dots);
       fvc::count_launch();
@@ -1576,8 +1608,13 @@ int32_t fvc_simple_batch_create(fvc_simple_batch **out, int32_t ncases,
   cudaSetDevice(B->device);
   int32_t rc = FVC_OK;
   if (cudaStreamCreateWithFlags(&B->stream, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaStreamCreateWithFlags(&B->body, cudaStreamNonBlocking) != cudaSuccess)
+      cudaStreamCreateWithFlags(&B->body, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&B->fork, cudaEventDisableTiming) != cudaSuccess)
     rc = FVC_ERR_CUDA;
+  for (int k = 0; k < fvc_simple_batch::kBranches && rc == FVC_OK; ++k)
+    if (cudaStreamCreateWithFlags(&B->branch[k], cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&B->join[k], cudaEventDisableTiming) != cudaSuccess)
+      rc = FVC_ERR_CUDA;
   // every case's CSRD structure on the host (the one all its systems share)
   std::vector<std::vector<int32_t>> ia_c(ncases), ja_c(ncases);
   for (int c = 0; c < ncases && rc == FVC_OK; ++c) {
