@@ -733,13 +733,14 @@ def run_batched_c4(args):
     the ideal-gas loop with the energy equation, from rest, tolerances 1e-8.
 
     batch: the outer iterations of all cases together (fvc_simple_batch):
-    each stage's solves of every case in one persistent launch (u and v,
-    then p', then the enthalpy) with per-system convergence and masks, one
-    outer iteration of all cases one CUDA graph; two untimed outer
-    iterations (the first captures the graph, the second captures it again
-    with each system's iteration count as its share of blocks), then
-    c4_its timed, FP64 and mixed precision (FP32 iterations, FP64
-    refinement) from rest each.  sequential: one more outer iteration of
+    each stage's solves of every case together (u and v, then p', then the
+    enthalpy; one thread-block cluster per system, one launch per cluster
+    size) with per-system convergence and masks, the cases' cell kernels
+    side by side on 16 branches, one outer iteration of all cases one CUDA
+    graph; two untimed outer iterations (the first captures the graph, the
+    second captures it again with each system's iteration count as its
+    weight), then c4_its timed, FP64 and mixed precision (FP32 iterations,
+    FP64 refinement) from rest each.  sequential: one more outer iteration of
     every case alone (its own CUDA graph loop) after the FP64 batch.
     systems: the u, v, T, p' systems of the FP64 batch's last outer
     iteration, frozen, solved again per stage in one launch each -- on the
