@@ -1174,6 +1174,54 @@ def run_reference(args):
     }
 
 
+def run_c4_profile_case(args):
+    """One frozen C4 stage solved twice, the second solve inside a profiler
+    range: the workload of the C4 stage profiles."""
+    import torch
+    from fortranfvcell_gb300 import Context, make_opts, pack_block_diagonal, mesh
+    from fortranfvcell_gb300.cells import SimpleBatch
+    stage, prec, csize = args.c4_profile.split(":")
+    which, code = {"p": (3, 1), "T": (4, 2)}[stage]
+    _, _, _, cases = c4_cases(args.c4_cases)
+    loops = c4_loops(cases)
+    bt = SimpleBatch(loops, "fp64")
+    bt.iterate(3, 4)
+    bt.close()
+    systems = []
+    for c, lp in zip(cases, loops):
+        ia, ja, nad = mesh.datastruc(c["ident"], 1, True)
+        ad, au, b = lp.system(which)
+        systems.append(dict(ad=ad, au=au, ia=ia, ja=ja, n=ad.size, nad=nad, b=b))
+    for lp in loops:
+        lp.close()
+    pk = pack_block_diagonal(systems)
+    ctx = Context(device=0)
+    ctx.set_matrix(1, True, pk["neq"], pk["nad"], pk["ad"], pk["au"], pk["au"], pk["ia"],
+                   pk["ja"])
+    bv = np.zeros(pk["neq"])
+    for sy, r in zip(systems, pk["rows"]):
+        bv[r] = sy["b"]
+    bd = torch.from_numpy(bv).cuda()
+    xd = torch.zeros(pk["neq"], dtype=torch.float64, device="cuda")
+    o = make_opts(prec, init=1, stop_rule=1, cluster_size=int(csize))
+    codes = np.full(len(systems), code, np.int32)
+    out = {"stage": stage, "precision": prec, "cluster_size": int(csize),
+           "systems": len(systems), "rows": int(pk["neq"])}
+    for rep in range(2):
+        if rep == 1:
+            torch.cuda.synchronize()
+            torch.cuda.profiler.start()
+        rc, st = ctx.solve_batched(pk["row_start"], bd, xd, C4_TOL, 50000, o,
+                                   raise_on_error=False, codes=codes)
+        if rep == 1:
+            torch.cuda.synchronize()
+            torch.cuda.profiler.stop()
+        out[f"solve{rep}"] = {"status": int(rc), "ms": round(st[0].solve_ms, 3),
+                              "iterations": int(sum(t.iterations for t in st))}
+    ctx.close()
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -1214,9 +1262,18 @@ def main():
                     help="profiling: run only this leg (no CPU side) and print its JSON")
     ap.add_argument("--profile-its", type=int, default=0,
                     help="profiling case: run each solver once for this many iterations")
+    ap.add_argument("--c4-profile", default=None, metavar="STAGE:PREC:CLUSTER",
+                    help="profiling case: one C4 stage (p or T) of --c4-cases cases, frozen "
+                         "after 3 FP64 batch outer iterations, solved twice to ||r|| <= 1e-8 "
+                         "||b|| in precision PREC (fp64 / mixed) with fvc_opts.cluster_size "
+                         "CLUSTER; the second solve between cudaProfilerStart and Stop (for "
+                         "ncu --profile-from-start off)")
     args = ap.parse_args()
     if args.profile_its > 0:
         print(json.dumps(run_profile_case(args)), flush=True)
+        return
+    if args.c4_profile:
+        print(json.dumps(run_c4_profile_case(args)), flush=True)
         return
     if args.profile_leg:
         args.no_cpu = True
