@@ -1029,8 +1029,8 @@ int32_t plan_batched(DeviceMatrix &A, Scratch &S, int nsys, const int32_t *row_s
     any_bicg = any_bicg || code == 2;
   }
   const bool mixed = o.precision == FVC_PREC_MIXED;
-  // one thread-block cluster per system (by default), or groups of blocks of
-  // one cooperative launch (csize 0).  C4 (256 cases, frozen p' and enthalpy
+  // one thread-block cluster per system, or groups of blocks of one
+  // cooperative launch (csize 0).  C4 (256 cases, frozen p' and enthalpy
   // systems, ||r|| <= 1e-8 ||b||): FP64 p' 152 ms in groups, 129 ms on
   // clusters sized per system; enthalpy 219 / 176 ms
   if (o.cluster_size < -1 || o.cluster_size > 16) return FVC_ERR_ARG;
@@ -1038,7 +1038,24 @@ int32_t plan_batched(DeviceMatrix &A, Scratch &S, int nsys, const int32_t *row_s
   // automatic choice): each system's cluster sized to it,
   // ceil(rows / (the largest system's rows / 16)) blocks, so that every block
   // has about as many rows and the per-iteration times line up
-  const bool adaptive = o.cluster_size <= 0;
+  bool adaptive = o.cluster_size <= 0;
+  if (o.cluster_size == 0) {
+    // automatic: clusters sized per system when their blocks fill the
+    // device, else groups, where a large system can spread over more than
+    // 16 blocks (C4's enthalpy systems in FP64: 256 cases 184 ms on
+    // clusters against 233 ms in groups; 64 cases 83 against 52 ms)
+    int most_rows = 0;
+    for (int s = 0; s < nsys; ++s)
+      most_rows = std::max(most_rows, row_start[s + 1] - row_start[s]);
+    const long per = std::max(1024, (most_rows + 15) / 16);
+    long want = 0;
+    for (int s = 0; s < nsys; ++s)
+      want += std::min<long>(16, std::max<long>(1, (row_start[s + 1] - row_start[s] + per - 1) / per));
+    int occ256 = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &occ256, mixed ? mixed_batched_kernel(256) : krylov_batched_kernel(256), 256, 0);
+    if (want < (long)std::max(occ256, 1) * sm_count()) adaptive = false;
+  }
   const int csize = (o.cluster_size == 1)   ? 0
                     : (o.cluster_size >= 2) ? o.cluster_size
                     : adaptive              ? 16

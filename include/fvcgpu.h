@@ -127,8 +127,10 @@ typedef struct {
                           per system sized to it (ceil(rows / r) blocks, r
                           the largest system's rows / 16, at least 1024;
                           one launch per size, the launches side by side on
-                          forked streams); 0: automatic, -1.  Single
-                          solves ignore it                               */
+                          forked streams); 0: automatic -- -1 when the
+                          systems' clusters would fill the device (their
+                          blocks at least its resident 256-thread
+                          blocks), else 1.  Single solves ignore it     */
 } fvc_opts;
 
 typedef struct {
