@@ -81,6 +81,7 @@ class FvcCellMesh(C.Structure):
         ("pedge", C.c_void_p),
         ("sedge", C.c_void_p),
         ("e", C.c_void_p),
+        ("geometry", C.c_void_p),
     ]
 
 
@@ -143,6 +144,8 @@ SIGNATURES = {
     "fvc_assemble_pressure": ([P, I32, P, I32, I32, I32, P, P, P, P, I32, I32, I32, I32, P, P,
                                P, P], I32),
     "fvc_cells_gradient": ([C.POINTER(FvcCellMesh), I32, I32, P, P, P], I32),
+    "fvc_cells_geometry_create": ([C.POINTER(FvcCellMesh), C.POINTER(C.c_void_p)], I32),
+    "fvc_cells_geometry_destroy": ([P], I32),
     "fvc_cells_momentum": ([C.POINTER(FvcCellMesh), I32, I32, P, P, P, P, P, P, F64, I32, F64,
                             I32, I32, P, P, P, P, P, P, P, P, P], I32),
     "fvc_cells_momentum_ideal_gas": ([C.POINTER(FvcCellMesh), I32, I32, P, P, P, P, P, P, P, P,

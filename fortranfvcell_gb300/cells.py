@@ -45,6 +45,32 @@ class CellMesh:
                                   int(np.asarray(e).shape[0]),
                                   *[self.t[k].data_ptr() for k in
                                     ("coor", "ix", "nelcon", "num", "pedge", "sedge", "e")])
+        self._geo = None
+
+    def cache_geometry(self, on: bool = True) -> None:
+        """Compute every cell's geometry once (fvc_cells_geometry_create) for
+        the cell routines to read instead of recomputing it; the same bits
+        either way.  on=False drops the cache."""
+        import torch
+        L = _lib.load()
+        if self._geo is not None:
+            L.fvc_cells_geometry_destroy(self._geo)
+            self._geo = None
+            self.s.geometry = None
+        if on:
+            torch.cuda.synchronize()
+            g = C.c_void_p()
+            _lib.check(L.fvc_cells_geometry_create(C.byref(self.s), C.byref(g)),
+                       "fvc_cells_geometry_create")
+            self._geo = g
+            self.s.geometry = g.value
+
+    def __del__(self):
+        if getattr(self, "_geo", None) is not None:
+            try:
+                _lib.load().fvc_cells_geometry_destroy(self._geo)
+            except Exception:
+                pass
 
     @property
     def num(self):

@@ -37,11 +37,13 @@ namespace {
 
 constexpr int MS = 4;
 
+struct Geom;
 struct Mesh {
   int numel, nshared, ld;  // ld = nshared + 1 (ix rows: nodes, then material)
   const double *coor;
   const int32_t *ix, *nelcon, *num, *pedge;
   const double *sedge, *e;
+  const Geom *geo;  // the cells' geometry computed once (null: per kernel)
 };
 
 __device__ __forceinline__ int ixa(const Mesh &m, int i, int c) {  // ix(i, c), 1-based
@@ -122,6 +124,14 @@ __device__ double areacell(const double eta[2][MS], int ns) {
   a = a + half_cross(eta[0][0], eta[1][0], eta[0][3], eta[1][3]);
   a = a + half_cross(eta[0][1], eta[1][1], eta[0][2], eta[1][2]);
   return 0.5 * a;
+}
+
+// the neighbour links alone (what the kernels use of the stencil when the
+// geometry comes from the mesh's cache)
+__device__ void gather_links(Stencil &S, const Mesh &m, int nel) {
+  S.ns = nsides(m, nel);
+  for (int j = 1; j <= m.nshared; ++j)
+    S.viz[j - 1] = m.nelcon[(j - 1) + (size_t)(nel - 1) * m.nshared];
 }
 
 // cellGeom2D + ghost centroids + vectorKm2d for the central cell
@@ -208,6 +218,30 @@ __device__ void geom(Geom &G, const Stencil &S) {
   }
 }
 
+// A cell's links and geometry: from the mesh's geometry cache when it has
+// one (geom() of the same stencil, stored once: the same bits), else
+// computed here as the reference's cell routines do
+__device__ __forceinline__ void cell_setup(Stencil &S, Geom &G, const Mesh &m, int nel) {
+  if (m.geo) {
+    gather_links(S, m, nel);
+    G = m.geo[nel - 1];
+  } else {
+    gather(S, m, nel);
+    geom(G, S);
+  }
+}
+
+// every cell's geometry into the cache
+__global__ void geometry_kernel(Mesh m, Geom *out) {
+  const int nel = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  if (nel > m.numel) return;
+  Stencil S;
+  Geom G;
+  gather(S, m, nel);
+  geom(G, S);
+  out[nel - 1] = G;
+}
+
 __device__ double limit(double r, int icod) {
   switch (icod) {
     case 1: return 0.0;
@@ -288,8 +322,7 @@ __global__ void gradient_kernel(Mesh m, int kind, int comp, const double *__rest
   if (nel > m.numel) return;
   Stencil S;
   Geom G;
-  gather(S, m, nel);
-  geom(G, S);
+  cell_setup(S, G, m, nel);
   const double uP = u[nel - 1];
   const double go1 = v2(grad, 1, nel), go2 = v2(grad, 2, nel);
   double ug[MS];
@@ -352,8 +385,7 @@ __global__ void momentum_kernel(Mesh m, MomArgs a) {
   const double ZERO = 1.0e-7, eps = 1.0e-14, cnst = 1.0e60;
   Stencil S;
   Geom G;
-  gather(S, m, nel);
-  geom(G, S);
+  cell_setup(S, G, m, nel);
   const int ns = S.ns, nsh = m.nshared, comp = a.comp;
   const double viscosity = prop(m, nel, 1);
   const double rhoA = prop(m, nel, 2);
@@ -556,8 +588,7 @@ __global__ void pc_kernel(Mesh m, PcArgs a) {
   const double cnst = 1.0e60;
   Stencil S;
   Geom G;
-  gather(S, m, nel);
-  geom(G, S);
+  cell_setup(S, G, m, nel);
   const int ns = S.ns, nsh = m.nshared;
   const double rhoA = prop(m, nel, 2);
   const double *w = a.w, *d = a.d;
@@ -654,8 +685,7 @@ __global__ void pc_idg_kernel(Mesh m, PcIdgArgs a) {
   const double cnst = 1.0e60, ZERO = 1.0e-7;
   Stencil S;
   Geom G;
-  gather(S, m, nel);
-  geom(G, S);
+  cell_setup(S, G, m, nel);
   const int ns = S.ns, nsh = m.nshared;
   const double *w = a.w, *d = a.d, *ro = a.ro;
   const double rhoP = ro3(ro, 3, nel), rhoA = prop(m, nel, 2);
@@ -791,8 +821,7 @@ __global__ void energy_gradient_kernel(Mesh m, int lib, const int32_t *__restric
   if (nel > m.numel) return;
   Stencil S;
   Geom G;
-  gather(S, m, nel);
-  geom(G, S);
+  cell_setup(S, G, m, nel);
   const double uP = u[nel - 1];
   const double go1 = v2(grad, 1, nel), go2 = v2(grad, 2, nel);
   const double cesp = prop(m, nel, 4), tref = prop(m, nel, 5);
@@ -829,8 +858,7 @@ __global__ void energy_kernel(Mesh m, EnArgs a) {
   const double ZERO = 1.0e-14, eps = 1.0e-14;
   Stencil S;
   Geom G;
-  gather(S, m, nel);
-  geom(G, S);
+  cell_setup(S, G, m, nel);
   const int ns = S.ns, nsh = m.nshared, lib = a.lib;
   const double kc = prop(m, nel, 3);
   const double cesp = prop(m, nel, 4);
@@ -988,6 +1016,7 @@ Mesh view(const fvc_cell_mesh *m) {
   v.pedge = m->pedge;
   v.sedge = m->sedge;
   v.e = m->e;
+  v.geo = static_cast<const Geom *>(m->geometry);
   return v;
 }
 
@@ -1299,6 +1328,31 @@ int32_t fvc_getres(int32_t numel, const int32_t *num, double *u, double *x, int3
                                                               to_equations ? 1 : 0);
   fvc::count_launch();
   return cudaPeekAtLastError() == cudaSuccess ? FVC_OK : FVC_ERR_CUDA;
+}
+
+int32_t fvc_cells_geometry_create(const fvc_cell_mesh *m, void **geometry) {
+  if (!geometry || !m || m->numel <= 0 || (m->nshared != 3 && m->nshared != 4) || !m->coor ||
+      !m->ix || !m->nelcon)
+    return FVC_ERR_ARG;
+  *geometry = nullptr;
+  fvc::cells::Geom *g = nullptr;
+  if (cudaMalloc(&g, sizeof(fvc::cells::Geom) * (size_t)m->numel) != cudaSuccess)
+    return FVC_ERR_CUDA;
+  fvc::cells::Mesh v = fvc::cells::view(m);
+  v.geo = nullptr;
+  fvc::cells::geometry_kernel<<<fvc::cells::grid(m->numel), fvc::cells::kThreads>>>(v, g);
+  fvc::count_launch();
+  if (cudaDeviceSynchronize() != cudaSuccess) {
+    cudaFree(g);
+    return FVC_ERR_CUDA;
+  }
+  *geometry = g;
+  return FVC_OK;
+}
+
+int32_t fvc_cells_geometry_destroy(void *geometry) {
+  if (geometry) cudaFree(geometry);
+  return FVC_OK;
 }
 
 }  // extern "C"

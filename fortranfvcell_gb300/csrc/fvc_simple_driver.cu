@@ -122,6 +122,7 @@ struct fvc_simple {
   fvc_simple_opts o{};
   int numel = 0, nshared = 0, nnode = 0, nmat = 0;
   fvc_cell_mesh m{};
+  void *geo = nullptr;  // the cells' geometry, computed once (m.geometry)
   // device mesh storage
   double *coor = nullptr, *sedge = nullptr, *e = nullptr;
   int32_t *ix = nullptr, *nelcon = nullptr, *num = nullptr, *pedge = nullptr;
@@ -191,6 +192,7 @@ void release(fvc_simple *s) {
   if (s->h_dots) cudaFreeHost(s->h_dots);
   if (s->h_err) cudaFreeHost(s->h_err);
   if (s->h_rec) cudaFreeHost(s->h_rec);
+  if (s->geo) fvc_cells_geometry_destroy(s->geo);
   if (s->stream) cudaStreamDestroy(s->stream);
 }
 
@@ -397,6 +399,12 @@ int32_t fvc_simple_create(fvc_simple **out, int32_t device, int32_t numel, int32
   s->m.pedge = s->pedge;
   s->m.sedge = s->sedge;
   s->m.e = s->e;
+  // the cell geometry once (the cell kernels would otherwise recompute it,
+  // in FP64, in every kernel of every outer iteration), once the mesh
+  // arrays have landed
+  if (cudaStreamSynchronize(s->stream) != cudaSuccess) return fail(FVC_ERR_CUDA);
+  if ((rc = fvc_cells_geometry_create(&s->m, &s->geo)) != FVC_OK) return fail(rc);
+  s->m.geometry = s->geo;
   std::vector<int32_t> &ident = s->ident;
   ident.resize((size_t)nshared * n);
   if ((rc = fvc_mesh_numeq(num, nelcon, numel, nshared, ident.data())) != FVC_OK) return fail(rc);

@@ -444,7 +444,22 @@ typedef struct {
   const double *sedge;    /* (3, nshared+1, numel): boundary values u, v, p  */
   const double *e;        /* (10, nmat): e(1) viscosity, e(2) density,
                              e(6) time coefficient, e(7) TVD limiter 1..7    */
+  const void *geometry;   /* optional: the mesh's cell geometry from
+                             fvc_cells_geometry_create (NULL: each cell kernel
+                             computes its cell's geometry from coor, as the
+                             reference's cell routines do; both give the same
+                             bits, the cache saves the FP64 work)            */
 } fvc_cell_mesh;
+
+/* The geometry of every cell of m (centroids, face normals, lengths and
+ * midpoints, ghost centroids, the reference's cellGeom2D / vectorKm2d
+ * quantities) computed once into a DEVICE buffer (*geometry, 600 bytes per
+ * cell), for fvc_cell_mesh.geometry.  It depends only on coor, ix and
+ * nelcon, which must hold their values when it is called (it runs on the
+ * default stream and waits for the device).  Free it with
+ * fvc_cells_geometry_destroy. */
+int32_t fvc_cells_geometry_create(const fvc_cell_mesh *m, void **geometry);
+int32_t fvc_cells_geometry_destroy(void *geometry);
 
 /* Green-Gauss cell gradient over the polygon of neighbour / ghost-cell
  * centroids (gform, src/Pform.f:466-646).  kind 1: velocity component comp

@@ -1,12 +1,25 @@
 """The GPU cell kernels of the SIMPLE iteration against the restated
 reference (oracle/fvc_oracle_simple.c), bit for bit, on random states with
-every boundary code the cells handle."""
+every boundary code the cells handle -- each test twice: with the cell
+geometry computed in every kernel, as the reference's cell routines do, and
+read from the mesh's geometry cache (fvc_cells_geometry_create), which the
+SIMPLE loops use."""
 import numpy as np
 import pytest
 
 from _simple_ref import cavity
 
 pytestmark = pytest.mark.gpu
+
+CACHE_GEOMETRY = False
+
+
+@pytest.fixture(autouse=True, params=[False, True], ids=["geometry-per-kernel", "geometry-cached"])
+def _geometry(request):
+    global CACHE_GEOMETRY
+    CACHE_GEOMETRY = request.param
+    yield
+    CACHE_GEOMETRY = False
 
 
 def dev(a, dtype=None):
@@ -45,8 +58,11 @@ def fields(rng, n):
 
 def mesh_on_gpu(case):
     from fortranfvcell_gb300 import cells
-    return cells.CellMesh(case["coor"], case["ix"], case["nelcon"], case["num"], case["pedge"],
-                          case["sedge"], case["e"])
+    m = cells.CellMesh(case["coor"], case["ix"], case["nelcon"], case["num"], case["pedge"],
+                       case["sedge"], case["e"])
+    if CACHE_GEOMETRY:
+        m.cache_geometry()
+    return m
 
 
 @pytest.mark.parametrize("kind,nx,seed", [("quad", 9, 1), ("tri", 7, 2), ("mixed", 8, 3)])

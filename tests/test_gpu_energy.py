@@ -2,13 +2,24 @@
 gradient) against the restated reference cells of src/CellibTrans.f
 (oracle/fvc_oracle_simple.c), bit for bit: both cell libraries, CSRD and
 ELLPACK, quadrilateral, triangle and mixed meshes, two materials, every
-boundary code, volume sources and random states."""
+boundary code, volume sources and random states; each test with the cell
+geometry computed in the kernels and read from the mesh's geometry cache."""
 import numpy as np
 import pytest
 
 from _simple_ref import cavity
 
 pytestmark = pytest.mark.gpu
+
+CACHE_GEOMETRY = False
+
+
+@pytest.fixture(autouse=True, params=[False, True], ids=["geometry-per-kernel", "geometry-cached"])
+def _geometry(request):
+    global CACHE_GEOMETRY
+    CACHE_GEOMETRY = request.param
+    yield
+    CACHE_GEOMETRY = False
 
 
 def dev(a, dtype=None):
@@ -45,8 +56,11 @@ def energy_case(orc, kind, nx, seed):
 
 def mesh_on_gpu(case):
     from fortranfvcell_gb300 import cells
-    return cells.CellMesh(case["coor"], case["ix"], case["nelcon"], case["num"], case["pedge"],
-                          case["sedge"], case["e"])
+    m = cells.CellMesh(case["coor"], case["ix"], case["nelcon"], case["num"], case["pedge"],
+                       case["sedge"], case["e"])
+    if CACHE_GEOMETRY:
+        m.cache_geometry()
+    return m
 
 
 def state(rng, n, lib):
