@@ -362,7 +362,7 @@ int32_t fvc_context_destroy(fvc_context *c) {
   if (!c) return FVC_ERR_ARG;
   cudaSetDevice(c->device);
   free_matrix(c);
-  for (int i = 0; i < 8; ++i) cudaFree(c->S.v[i]);
+  for (int i = 0; i < fvc::Scratch::kVec; ++i) cudaFree(c->S.v[i]);
   for (int i = 0; i < 10; ++i) cudaFree(c->S.f[i]);
   cudaFree(c->S.g);
   cudaFree(c->S.partials);

@@ -54,7 +54,8 @@ struct DeviceMatrix {
 
 struct Scratch {
   size_t n = 0, nf = 0, ngmres = 0;  // capacities of v[], f[], g
-  double *v[8] = {nullptr};     // Krylov vectors
+  static constexpr int kVec = 10;
+  double *v[kVec] = {nullptr};  // Krylov vectors
   float *f[10] = {nullptr};     // FP32 vectors (mixed precision)
   double *g = nullptr;          // GMRES basis (k+1) x n
   double *partials = nullptr;   // reduction partials

@@ -44,6 +44,7 @@ struct KArgs {
   const double *b;
   double *x;
   double *v0, *v1, *v2, *v3, *v4, *v5, *v6, *v7;
+  double *v8, *v9;  // batched BiCGSTAB: z = p/m and z' = s'/m stored once per row
   double *g;  // GMRES basis
   GridSync gs;
   double tol;
@@ -294,8 +295,14 @@ __global__ void __launch_bounds__(1024, 1) pcg_f64(KArgs a) {
 //            s''.(s'/m) ; r.s'' ; s''.s''                       -> beta, stop
 // v0 = r (shadow r0), v1/v2 = s, v3/v4 = p, v5/v6 = v, v7 = t.
 // ---------------------------------------------------------------------
-// kT: solve A^T x = b through the transposed row sums (sell_row_fma_t)
-template <int kMaxT = 1024, bool kT = false>
+// kT: solve A^T x = b through the transposed row sums (sell_row_fma_t).
+// kStoreZ (batched solves, bound by GB300's FP64 rate rather than by their
+// barriers): p and s' are formed once per row with z = p/m and z' = s'/m
+// (a.v8, a.v9) and published by a barrier before the SpMV that gathers
+// them -- five synchronisations per iteration instead of three, about half
+// the FP64 instructions (a gathered neighbour costs one FMA instead of
+// three or two), the same bits.
+template <int kMaxT = 1024, bool kT = false, bool kStoreZ = false>
 __device__ __forceinline__ void bicgstab_run(const KArgs &a, const Part &P, const GridSync &gs,
                                              double *result, int *iresult, bool lead) {
   __shared__ double red[kMaxNV * 32];
@@ -346,7 +353,24 @@ __device__ __forceinline__ void bicgstab_run(const KArgs &a, const Part &P, cons
     // phase 1: v = A z with z = p/m, p formed from the previous p, v, s
     acc[0] = 0.0;
     acc[1] = 0.0;
-    if (j == 1) {
+    if (kStoreZ) {
+      double *zp = a.v8;
+      FOR_ROWS(P) {
+        if (restart) r[row] = scur[row];
+        const double pi =
+            (j == 1) ? pnew[row] : fma(beta, fma(-w, vold[row], pold[row]), scur[row]);
+        pnew[row] = pi;
+        zp[row] = pi * minv[row];
+      }
+      if (!grid_barrier(gs, ep)) return;
+      FOR_ROWS(P) {
+        const double vi = row_fma<kT>(a.A, s_, P.lane, row, [&](int k) { return zp[k]; });
+        vnew[row] = vi;
+        const double ri = r[row];
+        acc[0] = fma(scur[row], ri, acc[0]);
+        acc[1] = fma(vi, ri, acc[1]);
+      }
+    } else if (j == 1) {
       FOR_ROWS(P) {
         const double *pc = pnew;
         const double vi =
@@ -385,15 +409,31 @@ __device__ __forceinline__ void bicgstab_run(const KArgs &a, const Part &P, cons
     // phase 2: s' = s - alpha v ; t = A z with z = s'/m
     acc[0] = 0.0;
     acc[1] = 0.0;
-    FOR_ROWS(P) {
-      const double *sc = scur, *vn = vnew;
-      auto sf = [&](int k) { return fma(-alpha, vn[k], sc[k]); };
-      snxt[row] = sf(row);
-      const double ti =
-          row_fma<kT>(a.A, s_, P.lane, row, [&](int k) { return sf(k) * minv[k]; });
-      t[row] = ti;
-      acc[0] = fma(ti, snxt[row], acc[0]);
-      acc[1] = fma(ti, ti, acc[1]);
+    if (kStoreZ) {
+      double *zs = a.v9;
+      FOR_ROWS(P) {
+        const double s1 = fma(-alpha, vnew[row], scur[row]);
+        snxt[row] = s1;
+        zs[row] = s1 * minv[row];
+      }
+      if (!grid_barrier(gs, ep)) return;
+      FOR_ROWS(P) {
+        const double ti = row_fma<kT>(a.A, s_, P.lane, row, [&](int k) { return zs[k]; });
+        t[row] = ti;
+        acc[0] = fma(ti, snxt[row], acc[0]);
+        acc[1] = fma(ti, ti, acc[1]);
+      }
+    } else {
+      FOR_ROWS(P) {
+        const double *sc = scur, *vn = vnew;
+        auto sf = [&](int k) { return fma(-alpha, vn[k], sc[k]); };
+        snxt[row] = sf(row);
+        const double ti =
+            row_fma<kT>(a.A, s_, P.lane, row, [&](int k) { return sf(k) * minv[k]; });
+        t[row] = ti;
+        acc[0] = fma(ti, snxt[row], acc[0]);
+        acc[1] = fma(ti, ti, acc[1]);
+      }
     }
     // t = 0 exactly: s' = 0, the alpha step solved the system (the
     // reference's 0/0 there gives NaN); w = 0 keeps x and s' as they are
@@ -408,8 +448,8 @@ __device__ __forceinline__ void bicgstab_run(const KArgs &a, const Part &P, cons
     FOR_ROWS(P) {
       const double mi = minv[row];
       const double s1 = snxt[row];
-      const double z1 = s1 * mi;
-      double xi = fma(alpha, pnew[row] * mi, x[row]);
+      const double z1 = kStoreZ ? a.v9[row] : s1 * mi;
+      double xi = fma(alpha, kStoreZ ? a.v8[row] : pnew[row] * mi, x[row]);
       x[row] = fma(w, z1, xi);
       const double si = fma(-w, t[row], s1);
       snxt[row] = si;
@@ -494,7 +534,7 @@ __global__ void __launch_bounds__(kMaxT, 1024 / kMaxT) krylov_batched(KArgs a, c
   ak.tol = d.tol;
   ak.init = d.init;
   if (d.code == 2)
-    bicgstab_run<kMaxT>(ak, P, d.gs, d.result, d.iresult, rank == 0);
+    bicgstab_run<kMaxT, false, true>(ak, P, d.gs, d.result, d.iresult, rank == 0);
   else
     pcg_run<true, kMaxT>(ak, P, d.gs, d.result, d.iresult, rank == 0);
   cluster_close(d.gs);
@@ -759,7 +799,7 @@ Launch persistent_launch(K kernel, const DeviceMatrix &A, const fvc_opts &o) {
 
 int32_t ensure_vectors(Scratch &S, size_t n, int nvec, size_t nblocks, bool gmres) {
   if (S.n < n) {
-    for (int i = 0; i < 8; ++i) {
+    for (int i = 0; i < Scratch::kVec; ++i) {
       if (S.v[i]) cudaFree(S.v[i]);
       S.v[i] = nullptr;
     }
@@ -1256,7 +1296,7 @@ int32_t plan_batched(DeviceMatrix &A, Scratch &S, int nsys, const int32_t *row_s
     for (int k = 0; k < nb[s]; ++k) hsob[(size_t)b0 + k] = s;
     b0 += nb[s];
   }
-  int32_t rc = mixed ? FVC_OK : ensure_vectors(S, (size_t)A.n, any_bicg ? 8 : 5, 1, false);
+  int32_t rc = mixed ? FVC_OK : ensure_vectors(S, (size_t)A.n, any_bicg ? 10 : 5, 1, false);
 #ifdef FVC_CHECK
   // the check word lives in the scratch's error block (check builds)
   if (rc == FVC_OK) rc = ensure_sync(S, 1);
@@ -1373,6 +1413,8 @@ int32_t enqueue_batched(DeviceMatrix &A, Scratch &S, const BatchPlan &P, const d
   a.v5 = S.v[5];
   a.v6 = S.v[6];
   a.v7 = S.v[7];
+  a.v8 = S.v[8];
+  a.v9 = S.v[9];
   a.tol = P.tol;
   a.maxit = maxit;
   a.init = 1;
