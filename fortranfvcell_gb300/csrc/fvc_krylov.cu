@@ -509,6 +509,14 @@ __global__ void __launch_bounds__(1024, 1) bicgstab_f64(KArgs a) {
   bicgstab_run(a, Part(a.A.nslices, a.A.n), a.gs, a.result, a.iresult, blockIdx.x == 0);
 }
 
+// The same with z = p/m and z' = s'/m stored once per row (kStoreZ): for
+// systems large enough that the FP64 rate, not the barriers, bounds the
+// iteration
+__global__ void __launch_bounds__(1024, 1) bicgstab_f64_z(KArgs a) {
+  bicgstab_run<1024, false, true>(a, Part(a.A.nslices, a.A.n), a.gs, a.result, a.iresult,
+                                  blockIdx.x == 0);
+}
+
 // BiCGSTAB on A^T x = b over A's storage (a.A.mirror set)
 __global__ void __launch_bounds__(1024, 1) bicgstab_f64_t(KArgs a) {
   bicgstab_run<1024, true>(a, Part(a.A.nslices, a.A.n), a.gs, a.result, a.iresult,
@@ -844,6 +852,8 @@ int32_t enqueue_persistent(K kernel, const DeviceMatrix &A, Scratch &S, const do
   a.v5 = S.v[5];
   a.v6 = S.v[6];
   a.v7 = S.v[7];
+  a.v8 = S.v[8];
+  a.v9 = S.v[9];
   a.g = S.g;
   a.gs = make_sync(S, L.blocks);
   a.tol = tol;
@@ -977,8 +987,14 @@ int32_t run_pcg(const DeviceMatrix &A, Scratch &S, const double *b, double *x, d
   return run_persistent(pcg_f64<false>, A, S, b, x, tol, maxit, init, o, stream, st, 5, false);
 }
 
+// FP64 BiCGSTAB with z stored once per row from this many rows on (below,
+// the two extra grid barriers cost more than the FP64 they save)
+constexpr int kStoreZRows = 524288;
+
 int32_t run_bicgstab(const DeviceMatrix &A, Scratch &S, const double *b, double *x, double tol,
                      int maxit, int init, const fvc_opts &o, cudaStream_t stream, fvc_stats *st) {
+  if (A.n >= kStoreZRows)
+    return run_persistent(bicgstab_f64_z, A, S, b, x, tol, maxit, init, o, stream, st, 10, false);
   return run_persistent(bicgstab_f64, A, S, b, x, tol, maxit, init, o, stream, st, 8, false);
 }
 
@@ -1009,8 +1025,11 @@ int32_t enqueue_solve(const DeviceMatrix &A, Scratch &S, int code, const double 
                               launch);
   }
   if (code == 2)
-    return enqueue_persistent(bicgstab_f64, A, S, b, x, tol, maxit, init, o, stream, 8, false,
-                              launch);
+    return A.n >= kStoreZRows
+               ? enqueue_persistent(bicgstab_f64_z, A, S, b, x, tol, maxit, init, o, stream, 10,
+                                    false, launch)
+               : enqueue_persistent(bicgstab_f64, A, S, b, x, tol, maxit, init, o, stream, 8,
+                                    false, launch);
   if (code == 3)
     return enqueue_persistent(gmres_f64, A, S, b, x, tol, maxit, 1, o, stream, 0, true, launch);
   return FVC_ERR_UNSUPPORTED;
