@@ -990,7 +990,8 @@ int32_t run_pcg(const DeviceMatrix &A, Scratch &S, const double *b, double *x, d
 // FP64 BiCGSTAB with z stored once per row from this many rows on (below,
 // the two extra grid barriers cost more than the FP64 they save; the 262k-
 // row enthalpy solves of a 512^2 natural-convection loop gain: 30 outer
-// iterations 2.93 -> 2.77 s)
+// iterations 2.93 -> 2.77 s; the 65k-row ones of a 256^2 loop lose: 200
+// outer iterations 6.26 -> 6.55 s)
 constexpr int kStoreZRows = 131072;
 
 int32_t run_bicgstab(const DeviceMatrix &A, Scratch &S, const double *b, double *x, double tol,
