@@ -73,8 +73,8 @@ constexpr int kTraceMax = 256;
 // between two FP64 recomputations (CG: a reliable update; BiCGSTAB: a
 // defect-correction sweep).  For BiCGSTAB, 0.1 rather than a deep inner
 // solve: a restarted FP32 BiCGSTAB stalls near FP32's limit on the
-// enthalpy systems (C4 enthalpy batch, 256 systems: 198 ms at 0.1, 291 ms
-// at 1e-2, 693 ms at 1e-4; FP64 251 ms).
+// enthalpy systems (the enthalpy systems of 256 heated cavities, batched:
+// 198 ms at 0.1, 291 ms at 1e-2, 693 ms at 1e-4; FP64 251 ms).
 constexpr double kInnerTolDefault = 0.1;
 constexpr int kHistoryMax = 16384;
 

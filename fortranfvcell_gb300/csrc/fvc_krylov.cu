@@ -1092,9 +1092,10 @@ int32_t plan_batched(DeviceMatrix &A, Scratch &S, int nsys, const int32_t *row_s
   }
   const bool mixed = o.precision == FVC_PREC_MIXED;
   // one thread-block cluster per system, or groups of blocks of one
-  // cooperative launch (csize 0).  C4 (256 cases, frozen p' and enthalpy
-  // systems, ||r|| <= 1e-8 ||b||): FP64 p' 152 ms in groups, 129 ms on
-  // clusters sized per system; enthalpy 219 / 176 ms
+  // cooperative launch (csize 0).  The p' and enthalpy systems of 256
+  // SIMPLE cases (32^2 to 254^2 cells, 4.0M rows a stage), frozen, to
+  // ||r|| <= 1e-8 ||b||: FP64 p' 152 ms in groups, 129 ms on clusters sized
+  // per system; enthalpy 219 / 176 ms
   if (o.cluster_size < -1 || o.cluster_size > 16) return FVC_ERR_ARG;
   // csize: the largest cluster (fixed sizes: all of them); adaptive (-1, the
   // automatic choice): each system's cluster sized to it,
@@ -1104,8 +1105,9 @@ int32_t plan_batched(DeviceMatrix &A, Scratch &S, int nsys, const int32_t *row_s
   if (o.cluster_size == 0) {
     // automatic: clusters sized per system when their blocks fill the
     // device, else groups, where a large system can spread over more than
-    // 16 blocks (C4's enthalpy systems in FP64: 256 cases 184 ms on
-    // clusters against 233 ms in groups; 64 cases 83 against 52 ms)
+    // 16 blocks (the enthalpy systems of those SIMPLE cases in FP64: 256
+    // cases 184 ms on clusters against 233 ms in groups; 64 cases 83
+    // against 52 ms)
     int most_rows = 0;
     for (int s = 0; s < nsys; ++s)
       most_rows = std::max(most_rows, row_start[s + 1] - row_start[s]);
@@ -1124,8 +1126,8 @@ int32_t plan_batched(DeviceMatrix &A, Scratch &S, int nsys, const int32_t *row_s
                                             : 0;
   // groups: 128-thread blocks by default, twice the co-resident blocks of
   // 256, so the one-block minimum of the small systems takes a smaller share
-  // (C4 batch of 256 cavities: 184 ms at 128 threads, 215 at 256, 386 at
-  // 512); clusters: 256
+  // (the u, v, T and p' systems of 256 heated cavities, 1024 systems: 184 ms
+  // at 128 threads, 215 at 256, 386 at 512); clusters: 256
   const int threads = (o.block_threads > 0) ? block_threads_for(o.block_threads, 0, 1)
                       : csize > 0          ? 256
                                            : 128;
@@ -1136,7 +1138,7 @@ int32_t plan_batched(DeviceMatrix &A, Scratch &S, int nsys, const int32_t *row_s
   }
   int occ = 0;
   // PCG stores p: most groups of a batch are one block, where publishing p
-  // is a __syncthreads (C4 batch of 256 cavities: 159 ms vs 184 ms)
+  // is a __syncthreads (the same 1024 systems: 159 ms vs 184 ms)
   const void *kern = mixed ? mixed_batched_kernel(threads) : krylov_batched_kernel(threads);
   int cap = 0;
   if (csize > 0) {
