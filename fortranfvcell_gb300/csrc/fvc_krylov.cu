@@ -1120,17 +1120,18 @@ int32_t plan_batched(DeviceMatrix &A, Scratch &S, int nsys, const int32_t *row_s
         &occ256, mixed ? mixed_batched_kernel(256) : krylov_batched_kernel(256), 256, 0);
     if (want < (long)std::max(occ256, 1) * sm_count()) adaptive = false;
   }
-  const int csize = (o.cluster_size == 1)   ? 0
-                    : (o.cluster_size >= 2) ? o.cluster_size
-                    : adaptive              ? 16
-                                            : 0;
+  int csize = (o.cluster_size == 1)   ? 0
+              : (o.cluster_size >= 2) ? o.cluster_size
+              : adaptive              ? 16
+                                      : 0;
   // groups: 128-thread blocks by default, twice the co-resident blocks of
   // 256, so the one-block minimum of the small systems takes a smaller share
   // (the u, v, T and p' systems of 256 heated cavities, 1024 systems: 184 ms
   // at 128 threads, 215 at 256, 386 at 512); clusters: 256
-  const int threads = (o.block_threads > 0) ? block_threads_for(o.block_threads, 0, 1)
-                      : csize > 0          ? 256
-                                           : 128;
+  auto threads_for = [&](int cs) {
+    return (o.block_threads > 0) ? block_threads_for(o.block_threads, 0, 1) : cs > 0 ? 256 : 128;
+  };
+  int threads = threads_for(csize);
   if (mixed) {
     int32_t rc = build_f32_copy(A, stream, o.fp32_layout);
     if (rc == FVC_OK) rc = ensure_f32_vectors(S, (size_t)A.n);
@@ -1144,23 +1145,31 @@ int32_t plan_batched(DeviceMatrix &A, Scratch &S, int nsys, const int32_t *row_s
   if (csize > 0) {
     // ordinary launches of one cluster per system: no co-residency bound,
     // but one cluster of the largest size must fit on the device
-    if (csize > 8 &&
-        cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
-            cudaSuccess) {
-      cudaGetLastError();
-      return FVC_ERR_UNSUPPORTED;
-    }
-    cudaLaunchConfig_t cfg{};
-    cudaLaunchAttribute at[1];
-    cluster_config(cfg, at, csize, threads, stream);
+    bool fits = csize <= 8 ||
+                cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
+                    cudaSuccess;
     int ncl = 0;
-    if (cudaOccupancyMaxActiveClusters(&ncl, kern, &cfg) != cudaSuccess || ncl < 1) {
-      cudaGetLastError();
-      fprintf(stderr, "fvcgpu: no cluster of %d blocks of %d threads fits the device\n", csize,
-              threads);
-      return FVC_ERR_UNSUPPORTED;
+    if (fits) {
+      cudaLaunchConfig_t cfg{};
+      cudaLaunchAttribute at[1];
+      cluster_config(cfg, at, csize, threads, stream);
+      fits = cudaOccupancyMaxActiveClusters(&ncl, kern, &cfg) == cudaSuccess && ncl >= 1;
     }
-  } else {
+    if (!fits) {
+      cudaGetLastError();
+      if (o.cluster_size != 0) {
+        fprintf(stderr, "fvcgpu: no cluster of %d blocks of %d threads fits the device\n",
+                csize, threads);
+        return FVC_ERR_UNSUPPORTED;
+      }
+      // the automatic choice falls back to groups
+      csize = 0;
+      adaptive = false;
+      threads = threads_for(0);
+      kern = mixed ? mixed_batched_kernel(threads) : krylov_batched_kernel(threads);
+    }
+  }
+  if (csize == 0) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, threads, 0);
     if (occ <= 0) occ = 1;
     if (o.blocks_per_sm > 0 && o.blocks_per_sm < occ) occ = o.blocks_per_sm;
