@@ -937,7 +937,9 @@ void dropin(double *ad, double *au, double *al, double *x, double *b, const int3
   fvc_stats st;
   int32_t rc = fvc_solver_ex(ad, au, al, x, b, iax, ja, *neq, *nad, *unsym != 0, *tol, *maxit, cd,
                              mz, &o, &st);
-  if (rc == FVC_ERR_NOCONV || rc == FVC_ERR_NAN) {
+  // a breakdown too: where the reference divides by zero it goes on with
+  // NaN to maxit and prints this warning before its STOP
+  if (rc == FVC_ERR_NOCONV || rc == FVC_ERR_NAN || rc == FVC_ERR_BREAKDOWN) {
     if (cd == 1)
       printf(" *** WARNING:  PCG no convergence reached after %9d iterations !%s Res %s Conv\n\n",
              *maxit, fortran_d(st.final_crit, 20, 6).c_str(), fortran_d(st.conv, 20, 6).c_str());
