@@ -103,3 +103,35 @@ def test_breakdowns_stay_in_their_system_of_a_batch(orc):
         assert rc_o == 0
         err = np.linalg.norm(x[pk["rows"][k]] - x_ref) / np.linalg.norm(x_ref)
         assert err <= 1e-8, (k, err)
+
+
+def test_dropin_breakdown_stops_like_the_reference(fvc, tmp_path):
+    # through solver_ (the drop-in): the reference would run its NaN to
+    # maxit, print its BiCGSTAB warning and STOP; so does the drop-in, in a
+    # child process so that the test runner survives
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    script = tmp_path / "breakdown.py"
+    script.write_text(f"""
+import sys, ctypes as C, numpy as np
+sys.path.insert(0, {root!r})
+import fortranfvcell_gb300 as f
+L = f.load()
+ad = np.ones(2); au = np.array([-1.25, -1.25]); b = np.array([2.0, 1.0]); x = np.zeros(2)
+ia = np.array([1, 2, 3], np.int32); ja = np.array([2, 1], np.int32)
+i32 = lambda v: C.byref(C.c_int32(v)); f64 = lambda v: C.byref(C.c_double(v))
+p = lambda a: a.ctypes.data_as(C.c_void_p)
+L.fvc_solver(p(ad), p(au), p(au), p(x), p(b), C.cast(p(ia), C.POINTER(C.c_int32)),
+             C.cast(p(ja), C.POINTER(C.c_int32)), i32(2), i32(2), i32(1), f64(1e-8),
+             i32(50), i32(2), i32(1), i32(0))
+print("RETURNED", bool(np.isfinite(x).all()))
+""")
+    r = subprocess.run([sys.executable, str(script)], capture_output=True, text=True, timeout=300)
+    assert "BiPCGSTAB no convergence reached after" in r.stdout
+    assert "RETURNED" not in r.stdout and r.returncode == 0
+    env = dict(os.environ, FVC_STOP_ON_ERROR="0")
+    r = subprocess.run([sys.executable, str(script)], capture_output=True, text=True, timeout=300,
+                       env=env)
+    assert "RETURNED True" in r.stdout
