@@ -429,19 +429,22 @@ struct MPart {
 // before it stores either result keeps two rows' gathers in flight (the
 // warp's loads of one row otherwise wait on the stores of the one before,
 // which the compiler cannot move past them).  A missing second slice, or a
-// row at or beyond n, comes with ok = false and the slice's first row
-// (always valid) as its row: its loads are harmless and its results are
-// dropped.  The rows are visited in the order of MFOR_ROWS, so sums over
-// them are the same.
+// second row at or beyond n, comes as a copy of the first (the same slice,
+// lane and row, so every load it makes is the first row's own, in bounds)
+// with ok = false: its results are dropped.  A lane whose first row is at
+// or beyond n (the last slice's padding) has nothing left to do.  The rows
+// are visited in the order of MFOR_ROWS, so sums over them are the same.
 template <typename F>
 __device__ __forceinline__ void mfor_rows2(const MPart &P, F &&f) {
   for (int s = P.sb + P.warp; s < P.se; s += 2 * P.nwarps) {
+    const int ra = s * 32 + P.lane;
+    if (ra >= P.n) break;  // later slices of this warp are further on
     const int s1 = s + P.nwarps;
-    const bool has1 = s1 < P.se;
-    const int ra = s * 32 + P.lane, rb = (has1 ? s1 : s) * 32 + P.lane;
-    const int sl[2] = {s, has1 ? s1 : s};
-    const bool ok[2] = {ra < P.n, has1 && rb < P.n};
-    const int rw[2] = {ok[0] ? ra : s * 32, ok[1] ? rb : s * 32};
+    const int rb = s1 * 32 + P.lane;
+    const bool second = s1 < P.se && rb < P.n;
+    const int sl[2] = {s, second ? s1 : s};
+    const int rw[2] = {ra, second ? rb : ra};
+    const bool ok[2] = {true, second};
     f(sl, rw, ok);
   }
 }
