@@ -509,6 +509,14 @@ __global__ void __launch_bounds__(1024, 1) bicgstab_f64(KArgs a) {
   bicgstab_run(a, Part(a.A.nslices, a.A.n), a.gs, a.result, a.iresult, blockIdx.x == 0);
 }
 
+// A small system's BiCGSTAB on one thread-block cluster: the same body, its
+// reductions and barriers through the cluster (GridSync.cluster), its
+// vectors in global memory (L2-resident at these sizes)
+__global__ void __launch_bounds__(256) bicgstab_cl(KArgs a) {
+  bicgstab_run<256>(a, Part(a.A.nslices, a.A.n), a.gs, a.result, a.iresult, blockIdx.x == 0);
+  cluster_close(a.gs);
+}
+
 // The same with z = p/m and z' = s'/m stored once per row (kStoreZ): for
 // systems large enough that the FP64 rate, not the barriers, bounds the
 // iteration
@@ -994,8 +1002,94 @@ int32_t run_pcg(const DeviceMatrix &A, Scratch &S, const double *b, double *x, d
 // outer iterations 6.26 -> 6.55 s)
 constexpr int kStoreZRows = 131072;
 
+// BiCGSTAB on one cluster up to this many rows (a block of 256 threads per
+// eight slices, at most 16 blocks): the grid-wide kernel's grid waits cost
+// more than a cluster's FP64 throughput there
+constexpr int kBcgClusterRows = 16384;
+
+// Enqueues the cluster BiCGSTAB when the system is small enough, the caller
+// left the launch shape automatic and one cluster fits; FVC_ERR_UNSUPPORTED,
+// with nothing enqueued, otherwise.  launch = false only prepares the scratch.
+int32_t enqueue_bicgstab_cluster(const DeviceMatrix &A, Scratch &S, const double *b, double *x,
+                                 double tol, int maxit, int init, const fvc_opts &o,
+                                 cudaStream_t stream, bool launch) {
+  if (A.n <= 0 || A.n > kBcgClusterRows || o.block_threads != 0 || o.blocks_per_sm != 0 ||
+      o.max_blocks != 0)
+    return FVC_ERR_UNSUPPORTED;
+  constexpr int threads = 256;
+  const int csize = std::min(16, std::max(1, (A.nslices + 7) / 8));
+  static bool attrs_set = false;
+  if (!attrs_set) {
+    cudaFuncSetAttribute((const void *)bicgstab_cl,
+                         cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    attrs_set = true;
+  }
+  cudaLaunchConfig_t cfg;
+  cudaLaunchAttribute at[1];
+  cluster_config(cfg, at, csize, threads, stream);
+  int ncl = 0;
+  if (cudaOccupancyMaxActiveClusters(&ncl, (const void *)bicgstab_cl, &cfg) != cudaSuccess ||
+      ncl < 1) {
+    cudaGetLastError();
+    return FVC_ERR_UNSUPPORTED;
+  }
+  int32_t rc = ensure_vectors(S, (size_t)A.n, 8, 1, false);
+  if (rc != FVC_OK || !launch) return rc;
+  // the error block (wait and check words) and the result slots start at zero
+  cudaMemsetAsync(S.err, 0, 64, stream);
+  cudaMemsetAsync(S.iresult, 0, 16 * sizeof(int), stream);
+  cudaMemsetAsync(S.result, 0, 16 * sizeof(double), stream);
+  KArgs a{};
+  a.A = view64(A);
+  a.A.chk = check_word(S);
+  a.m = A.jac;
+  a.minv = A.jinv;
+  a.b = b;
+  a.x = x;
+  a.v0 = S.v[0];
+  a.v1 = S.v[1];
+  a.v2 = S.v[2];
+  a.v3 = S.v[3];
+  a.v4 = S.v[4];
+  a.v5 = S.v[5];
+  a.v6 = S.v[6];
+  a.v7 = S.v[7];
+  a.gs = make_sync(S, 1);
+  a.gs.nblocks = (unsigned int)csize;
+  a.gs.cluster = csize > 1 ? 1 : 0;
+  a.tol = tol;
+  a.maxit = maxit;
+  a.init = init;
+  a.stop_rule = o.stop_rule;
+  a.result = S.result;
+  a.iresult = S.iresult;
+  void *args[] = {&a};
+  const cudaError_t ce = launch_groups((const void *)bicgstab_cl, csize, threads, csize, args, stream);
+  count_launch();
+  if (ce != cudaSuccess) {
+    fprintf(stderr, "fvcgpu: cluster BiCGSTAB launch failed: %s\n", cudaGetErrorString(ce));
+    cudaGetLastError();
+    return FVC_ERR_CUDA;
+  }
+  return FVC_OK;
+}
+
 int32_t run_bicgstab(const DeviceMatrix &A, Scratch &S, const double *b, double *x, double tol,
                      int maxit, int init, const fvc_opts &o, cudaStream_t stream, fvc_stats *st) {
+  if (enqueue_bicgstab_cluster(A, S, b, x, tol, maxit, init, o, stream, false) == FVC_OK) {
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, stream);
+    const int32_t rc = enqueue_bicgstab_cluster(A, S, b, x, tol, maxit, init, o, stream, true);
+    cudaEventRecord(e1, stream);
+    if (rc != FVC_OK) {
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      return rc;
+    }
+    return read_stats(S, stream, e0, e1, true, st);
+  }
   if (A.n >= kStoreZRows)
     return run_persistent(bicgstab_f64_z, A, S, b, x, tol, maxit, init, o, stream, st, 10, false);
   return run_persistent(bicgstab_f64, A, S, b, x, tol, maxit, init, o, stream, st, 8, false);
@@ -1026,6 +1120,10 @@ int32_t enqueue_solve(const DeviceMatrix &A, Scratch &S, int code, const double 
                                 launch);
     return enqueue_persistent(pcg_f64<false>, A, S, b, x, tol, maxit, init, o, stream, 5, false,
                               launch);
+  }
+  if (code == 2) {
+    const int32_t rc = enqueue_bicgstab_cluster(A, S, b, x, tol, maxit, init, o, stream, launch);
+    if (rc != FVC_ERR_UNSUPPORTED) return rc;
   }
   if (code == 2)
     return A.n >= kStoreZRows
