@@ -39,7 +39,10 @@ constexpr int kClMaxRows = 2048;  // rows per CTA
 // Largest system run on a cluster: measured per PCG iteration on GB300 (16
 // CTAs, 256 rows each) against the grid-wide kernel: 4096 rows 6.65 vs
 // 8.41 us, 6124 rows 7.59 vs 8.41 us, 10000 rows 9.59 vs 8.95 us.  Forming
-// p at every read instead of the p barrier was slower at every size.
+// p at every read instead of the p barrier was slower at every size.  The
+// FP64 rate of the cluster's SMs bounds it: 512 or 1024 rows per CTA
+// instead of 256 (8 or 4 CTAs for 4096 rows) took a 64^2 cavity's 200
+// outer iterations from 0.67 s to 0.81 and 1.13 s.
 constexpr int kClMaxN = 8192;
 
 struct ClArgs {
